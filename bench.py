@@ -1,0 +1,403 @@
+#!/usr/bin/env python
+"""Benchmark: seconds per implicit time step (assembly + Krylov) of the
+neo-Hookean elastodynamics workload (4x1x1 beam, 176x44x44 hexes -> 2,044,416
+tet4, 358,425 nodes, 5,233,801 3x3 CSR blocks; CG + diagonal preconditioner),
+mixed precision (FP32 tangent + FP32 inner CG, FP64 residual/Newton) beside
+the plain FP64 GPU path, with the relative L2 distance between the two.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gsls|reference]
+
+--impl reference times the CPU restatement of the reference's algorithm
+(oracle/, OpenMP over all host cores) on the same workload.  N > 1 runs
+independent replicas (the path does not shard across GPUs), one per rank.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "s/implicit step (assembly+Krylov), mixed vs FP64 GPU at <=1e-8 rel L2; HBM GB/s"
+WORKLOAD = dict(nx=176, ny=44, nz=44)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gsls", choices=["gsls", "reference"])
+    ap.add_argument("--small", action="store_true", help="small mesh (debugging only)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def workload(args):
+    from svfsi_gb300 import problems
+    if args.small:
+        return problems.struct_beam(24, 6, 6, nsteps=args.steps)
+    return problems.struct_beam(**WORKLOAD, nsteps=args.steps)
+
+
+def workload_desc(p):
+    return (f"{p.name}: neo-Hookean+ST91 elastodynamics, {p.nEl:,} tet4, {p.nNo:,} nodes, "
+            f"nnz {p.nnz:,} 3x3 blocks, CG+diag, dt 1e-3, Newton tol 1e-8")
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower() in ("active", "1"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel_key: str):
+    f = ROOT / "profiles" / "traffic.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        v = d.get(kernel_key)
+        if v is not None:
+            return float(v)
+    return None
+
+
+# ---------------------------------------------------------------------------
+def run_gsls(args):
+    import torch
+    from svfsi_gb300 import _lib, build, fsils, problems
+    rank, local, world = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    build.build()
+    L = _lib.load()
+    _lib.check(L.gsls_init(local), "gsls_init")
+    p = workload(args)
+    K, W = args.steps, args.warmup
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed_run(precision, profile=False):
+        lhs, mesh, eq = problems.build_equation(p, precision=precision)
+        stream = torch.cuda.ExternalStream(L.gsls_get_stream(lhs.h))
+        infos = []
+        for _ in range(W):
+            infos.append(eq.step())
+        barrier()
+        torch.cuda.synchronize()
+        if profile:
+            L.gsls_profile_reset()
+            L.gsls_profile_enable(1)
+        n0 = L.gsls_launch_count()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        timed = []
+        for _ in range(K):
+            timed.append(eq.step())
+        ev1.record(stream)
+        ev1.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        launches = L.gsls_launch_count() - n0
+        ms = ev0.elapsed_time(ev1)
+        prof = None
+        if profile:
+            L.gsls_profile_enable(0)
+            cnt, tot = C.c_longlong(), C.c_double()
+            L.gsls_profile_read(b"cg_spmv", C.byref(cnt), C.byref(tot))
+            acnt, atot = C.c_longlong(), C.c_double()
+            L.gsls_profile_read(b"assembly", C.byref(acnt), C.byref(atot))
+            prof = {"cg_spmv": (cnt.value, tot.value), "assembly": (acnt.value, atot.value)}
+        state = eq.get_state()
+        res = dict(ms=ms, launches=launches, prof=prof, state=state,
+                   newton=np.mean([i.newton_itr for i in timed]),
+                   cg=np.mean([i.ls_itr_total for i in timed]),
+                   asm_ms=np.mean([i.t_assembly_ms for i in timed]),
+                   suc=all(i.last_suc for i in timed))
+        eq.free()
+        mesh.free()
+        lhs.free()
+        return res
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    mixed = timed_run(fsils.PREC_MIXED, profile=True)
+    clk = clocks.stop()
+    fp64 = timed_run(fsils.PREC_FP64)
+    ms_mixed = max_over_ranks(mixed["ms"]) / K
+    ms_fp64 = max_over_ranks(fp64["ms"]) / K
+    D_m, D_f = mixed["state"][2], fp64["state"][2]
+    rel_l2 = float(np.linalg.norm(D_m - D_f) / np.linalg.norm(D_f))
+
+    # e2e through the public API with host buffers (pinned), H2D + D2H per step
+    lhs, mesh, eq = problems.build_equation(p, precision=fsils.PREC_MIXED)
+    shp = (p.nNo, p.tDof)
+    host = [torch.zeros(shp, dtype=torch.float64).pin_memory() for _ in range(3)]
+    hv = [h.numpy() for h in host]
+    for _ in range(W):
+        eq.set_state(*hv)
+        eq.step()
+        hv[0][:], hv[1][:], hv[2][:] = eq.get_state()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        eq.set_state(*hv)
+        eq.step()
+        Ao, Yo, Do = eq.get_state()
+        hv[0][:], hv[1][:], hv[2][:] = Ao, Yo, Do
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0) / K
+    eq.free()
+    mesh.free()
+    lhs.free()
+    state_bytes = 3 * p.nNo * p.tDof * 8
+
+    # roofline of the dominant kernel (CG SpMV + fused dot, FP32 values)
+    cnt, tot_ms = mixed["prof"]["cg_spmv"]
+    peak, peak_kind = peaks()
+    B = p.algorithmic_bytes(4, 4)["spmv"]
+    avg_s = (tot_ms / max(cnt, 1)) / 1e3
+    achieved = B / avg_s / 1e9 if cnt else None
+    roof = {"kernel": "k_cg_spmv<3,float,float> (block-CSR SpMV + fused P.KP)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None,
+            "peak_source": f"{peak_kind} hbm_gbs", "bytes_per_launch": B,
+            "avg_launch_us": avg_s * 1e6, "launches": cnt,
+            "traffic": traffic_from_profiles("cg_spmv_d3_f32_struct_beam_176x44x44")}
+
+    out = {
+        "metric": METRIC, "value": ms_mixed / 1e3 / world, "unit": "s/step",
+        "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": ms_mixed,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 tangent+inner CG / f64 residual,Newton,reductions",
+        "data": "synthetic: seeded Kuhn-split beam mesh, no external data",
+        "config": {"workload": workload_desc(p), "precision": "mixed",
+                   "l2": "inputs larger than L2 (FP32 Val 188 MB, FP64 Val 377 MB)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "fp64": {"value": ms_fp64 / 1e3 / world, "ms_per_step": ms_fp64,
+                 "newton_itr_per_step": fp64["newton"], "cg_itr_per_step": fp64["cg"],
+                 "assembly_ms_per_newton": fp64["asm_ms"] / max(fp64["newton"], 1)},
+        "mixed": {"newton_itr_per_step": mixed["newton"], "cg_itr_per_step": mixed["cg"],
+                  "assembly_ms_per_newton": mixed["asm_ms"] / max(mixed["newton"], 1),
+                  "all_solves_converged": bool(mixed["suc"])},
+        "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "rel_l2_mixed_vs_fp64": rel_l2,
+        "roofline": roof,
+        "e2e": {"value": e2e_s / world, "unit": "s/step", "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes},
+        "gpu_launches": int(mixed["launches"]),
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(p, fp64["newton"], fp64["cg"])
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+def _colouring(p):
+    """Conflict-free element colouring of a Kuhn beam: hex parity (8) x tet
+    type (6); hexes of equal parity share no node."""
+    h = np.arange(p.nEl) // 6
+    t6 = np.arange(p.nEl) % 6
+    xs = np.unique(p.x[:, 0]).size - 1
+    ys = np.unique(p.x[:, 1]).size - 1
+    i, j, k = h % xs, (h // xs) % ys, h // (xs * ys)
+    col = ((i % 2) + 2 * (j % 2) + 4 * (k % 2)) * 6 + t6
+    order = np.argsort(col, kind="stable").astype(np.int32)
+    off = np.concatenate([[0], np.cumsum(np.bincount(col, minlength=48))]).astype(np.int32)
+    return 48, off, order
+
+
+def cpu_sample(p, threads):
+    """Time, on the host cores with the oracle: one assembly, one diagonal
+    preconditioning and CG iterations (slope between 5 and 25 iterations)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    L = O.load()
+    L.orc_assemble_colored.argtypes = [C.POINTER(O.EqP), C.c_int, C.c_int, O.c_int_p,
+                                       O.c_double_p, O.c_double_p, O.c_double_p, O.c_double_p,
+                                       O.c_int_p, O.c_int_p, O.c_double_p, O.c_double_p, C.c_int,
+                                       O.c_int_p, O.c_int_p]
+    O.set_threads(threads)
+    ncol, off, order = _colouring(p)
+    rng = np.random.default_rng(0)
+    A = 1e-3 * rng.standard_normal((p.nNo, 3))
+    Y = 1e-3 * rng.standard_normal((p.nNo, 3))
+    D = 1e-3 * rng.standard_normal((p.nNo, 3))
+    R = np.zeros((p.nNo, 3))
+    Val = np.zeros((p.nnz, 9))
+    eqp = O.eqp_from(p)
+    ien, x, rp, cp = O.i32(p.ien), O.f64(p.x), O.i32(p.rowPtr), O.i32(p.colPtr)
+    t0 = time.perf_counter()
+    L.orc_assemble_colored(C.byref(eqp), p.nNo, p.nEl, O.ip(ien), O.dp(x), O.dp(A), O.dp(Y),
+                           O.dp(D), O.ip(rp), O.ip(cp), O.dp(R), O.dp(Val), ncol, O.ip(off),
+                           O.ip(order))
+    t_asm = time.perf_counter() - t0
+    s = O.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
+    s.bc_create(1, p.dirichlet[0].nodes, 3, 0, np.zeros((p.dirichlet[0].nodes.size, 3)))
+    times = {}
+    for m in (5, 25):
+        ls = O.ls_create(O.LS_TYPE_CG, relTol=1e-30, mItr=m)
+        Rc, Vc = R.copy(), Val.copy()
+        t0 = time.perf_counter()
+        s.solve(ls, 3, Rc, Vc, O.PRECOND_FSILS)
+        times[m] = time.perf_counter() - t0
+    t_it = (times[25] - times[5]) / 20.0
+    t_pre = max(times[5] - 5 * t_it, 0.0)
+    return t_asm, t_pre, t_it
+
+
+def cpu_baseline(p, newton, cg):
+    threads = os.cpu_count() or 1
+    t_asm, t_pre, t_it = cpu_sample(p, threads)
+    per_step = newton * (t_asm + t_pre) + cg * t_it
+    return {"value": per_step, "unit": "s/step", "cores": threads, "kind": "port",
+            "sample": (f"oracle (C restatement, FP64, OpenMP {threads} threads) on the full mesh: "
+                       f"1 assembly {t_asm:.3f}s, 1 diag precond {t_pre:.3f}s, CG {t_it * 1e3:.2f} "
+                       f"ms/iter (5->25 iter slope); per step = {newton:.2f} Newton x (asm+precond) "
+                       f"+ {cg:.1f} CG iters, the counts of the FP64 GPU run of the same algorithm")}
+
+
+def run_reference(args):
+    rank, local, world = dist_env()
+    if rank != 0:
+        return
+    p = workload(args)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    # Newton / CG counts of this workload's first step, by the CPU oracle itself
+    if args.small:
+        eq = O.OracleEquation(p)
+        info = eq.step()
+        newton, cg = info.newton_itr, info.ls_itr_total
+        src = "first step run in full by the oracle"
+    else:
+        newton, cg = REF_COUNTS
+        src = ("Newton/CG counts per step of this workload (first steps, identical algorithm, "
+               "recorded from the parity-checked GPU FP64 run)")
+    vals = []
+    for k in range(args.warmup + args.steps):
+        t_asm, t_pre, t_it = cpu_sample(p, threads)
+        if k >= args.warmup:
+            vals.append(newton * (t_asm + t_pre) + cg * t_it)
+    v = statistics.median(vals)
+    out = {"metric": METRIC, "value": v, "unit": "s/step", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+           "data": "synthetic: seeded Kuhn-split beam mesh, no external data",
+           "config": {"workload": workload_desc(p), "precision": "fp64 (reference CPU)"},
+           "cpu_baseline": {"value": v, "unit": "s/step", "cores": threads, "kind": "port",
+                            "sample": (f"per step: 1 colored OpenMP assembly + 1 diag precond + "
+                                       f"CG per-iteration time from 5->25 iterations, scaled by "
+                                       f"{newton} Newton and {cg} CG iterations per step ({src})")},
+           "e2e": {"value": v, "unit": "s/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# Newton iterations and total CG iterations per step of the full-size beam
+# (FP64 path), used to scale the CPU sample in the reference arm.
+REF_COUNTS = (5.0, 500.0)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gsls(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,261 @@
+/*
+ * gsls -- GB300-native implicit-step engine for svFSI-style finite-element
+ * solves: element residual/tangent assembly + svFSILS-compatible Krylov
+ * solve, hand-written CUDA for sm_103a, one process on one GPU.
+ *
+ * Plain C ABI: plain pointers and sizes, no C++ or torch types.  Every
+ * function returns an int status (GSLS_OK = 0).  The svFSILS-shaped calls
+ * keep the argument order of the reference's Fortran interface
+ * (Code/Source/svFSILS/FSILS_API.h:51-135, C mirror FSILS_api_c.h:52-64) so
+ * a Fortran BIND(C) interface maps 1:1; indices are 1-based there as in the
+ * reference.  Reference paths below are relative to the svFSI project root.
+ *
+ * Array layouts are the reference's column-major ones:
+ *   Val[j*dof*dof + r*dof + c]  block j (CSR order), row r, column c
+ *   R[a*dof + i]                node a, component i
+ *   state[a*tDof + i]           node a, unknown i (An/Yn/Dn, Ag/Yg/Dg)
+ *   IEN[e*eNoN + a]             node (1-based) of local vertex a of element e
+ *   x[a*nsd + i]                coordinate i of node a
+ */
+#ifndef GSLS_H
+#define GSLS_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GSLS_VERSION 1
+
+/* ---- status codes ---- */
+#define GSLS_OK 0
+#define GSLS_ERR_ARG (-1)      /* bad argument (the reference STOPs instead) */
+#define GSLS_ERR_CUDA (-2)     /* CUDA runtime error */
+#define GSLS_ERR_STATE (-3)    /* object not created / already created */
+#define GSLS_ERR_NAN (-4)      /* NaN/Inf met in the residual or Krylov scalars */
+#define GSLS_ERR_JAC (-5)      /* non-positive element Jacobian */
+#define GSLS_ERR_UNSUPPORTED (-6)
+#define GSLS_ERR_NOMEM (-7)
+
+/* ---- constants identical to Code/Source/svFSILS/FSILS_STRUCT.h:53-62 ---- */
+#define GSLS_LS_TYPE_CG 798
+#define GSLS_LS_TYPE_GMRES 797
+#define GSLS_LS_TYPE_NS 796
+#define GSLS_LS_TYPE_BICGS 795
+#define GSLS_PRECOND_FSILS 701
+#define GSLS_PRECOND_RCS 709
+#define GSLS_BC_TYPE_DIR 0
+#define GSLS_BC_TYPE_NEU 1
+
+/* ---- arithmetic modes ---- */
+#define GSLS_PREC_FP64 0  /* plain FP64 everywhere (the drop-in) */
+#define GSLS_PREC_MIXED 1 /* FP32 tangent + FP32 inner Krylov; FP64 residual,
+                             det F, Newton update, reductions, Gram-Schmidt */
+
+/* ---- physics ids for assembly ---- */
+#define GSLS_PHYS_HEATS 1
+#define GSLS_PHYS_STRUCT 2
+#define GSLS_PHYS_CEP 3
+#define GSLS_PHYS_FLUID 4
+
+/* Mirrors FSILS_subLsType, Code/Source/svFSILS/FSILS_STRUCT.h:162-191
+   (Fortran LOGICAL stored as int32). */
+typedef struct {
+  int suc, mItr, sD, itr, cM, cN, cD, reserve;
+  double absTol, relTol, iNorm, fNorm, dB, callD;
+} gsls_sub_ls;
+
+/* Mirrors FSILS_lsType, Code/Source/svFSILS/FSILS_STRUCT.h:193-204. */
+typedef struct {
+  int foC, LS_type, Resm, Resc;
+  gsls_sub_ls GM, CG, RI;
+} gsls_ls;
+
+typedef struct gsls_lhs gsls_lhs;   /* replaces FSILS_lhsType */
+typedef struct gsls_mesh gsls_mesh; /* element data for assembly */
+typedef struct gsls_eq gsls_eq;     /* one equation's time integrator */
+
+/* ------------------------------------------------------------------------ */
+/* Library */
+
+/* Select the CUDA device for this process. */
+int gsls_init(int device);
+/* Library version (GSLS_VERSION). */
+int gsls_version(void);
+/* Human-readable text for the last error of this thread. */
+const char *gsls_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* svFSILS-shaped linear-solver API */
+
+/* Replaces FSILS_LHS_CREATE, Code/Source/svFSILS/LHS.f:51-111 (serial
+   branch): rowPtr[nNo+1] and colPtr[nnz] are 1-based, columns sorted per
+   row; gNodes is accepted for interface parity (map = identity on 1 GPU). */
+int gsls_lhs_create(gsls_lhs **lhs, int gnNo, int nNo, int nnz,
+                    const int *gNodes, const int *rowPtr, const int *colPtr,
+                    int nFaces);
+/* Replaces FSILS_LHS_FREE, Code/Source/svFSILS/LHS.f:295-325. */
+int gsls_lhs_free(gsls_lhs *lhs);
+
+/* Replaces FSILS_BC_CREATE, Code/Source/svFSILS/BC.f:50-121: faIn 1-based,
+   gNodes 1-based, val(dof,nNo) nullable (NULL = zeros). */
+int gsls_bc_create(gsls_lhs *lhs, int faIn, int nNo, int dof, int BC_type,
+                   const int *gNodes, const double *val);
+
+/* Replaces FSILS_LS_CREATE, Code/Source/svFSILS/LS.f:50-119: defaults per
+   LS_type, then every non-NULL optional argument overrides. */
+int gsls_ls_create(gsls_ls *ls, int LS_type, const double *relTol,
+                   const double *absTol, const int *maxItr, const int *dimKry,
+                   const double *relTolIn, const double *absTolIn,
+                   const int *maxItrIn);
+
+/* Replaces FSILS_SOLVE, Code/Source/svFSILS/SOLVE.f:51-143, host arrays:
+   Ri(dof,nNo) is overwritten with the solution and Val(dof*dof,nnz) is left
+   scaled by the preconditioner, exactly as the reference does.  incL and res
+   (length nFaces) are nullable.  Non-convergence is reported through
+   ls->RI.suc = 0 with GSLS_OK, as in the reference. */
+int gsls_solve(gsls_lhs *lhs, gsls_ls *ls, int dof, double *Ri, double *Val,
+               int prec, const int *incL, const double *res);
+
+/* Same as gsls_solve on device arrays.  val_prec selects the element type of
+   dVal (GSLS_PREC_FP64: double, GSLS_PREC_MIXED: float, inner Krylov in
+   FP32).  dRi is always double. */
+int gsls_solve_dev(gsls_lhs *lhs, gsls_ls *ls, int dof, double *dRi,
+                   void *dVal, int val_prec, int prec, const int *incL,
+                   const double *res);
+
+/* y = K x for block-CSR K (FSILS_SPARMULVV, Code/Source/svFSILS/SPARMUL.f:
+   51-133) on device arrays; val_prec as above, x and y double. */
+int gsls_spmv_dev(gsls_lhs *lhs, int dof, const void *dVal, int val_prec,
+                  const double *dx, double *dy);
+
+/* Dot product and 2-norm on device arrays (FSILS_DOTV / FSILS_NORMV,
+   Code/Source/svFSILS/DOT.f:56-110, NORM.f:55-110); result on the host. */
+int gsls_dot_dev(gsls_lhs *lhs, int dof, const double *du, const double *dv,
+                 double *result);
+int gsls_norm_dev(gsls_lhs *lhs, int dof, const double *du, double *result);
+
+/* CUDA stream used by every call on this lhs (cudaStream_t as void*;
+   NULL = the library's own stream). */
+int gsls_set_stream(gsls_lhs *lhs, void *stream);
+void *gsls_get_stream(gsls_lhs *lhs);
+
+/* ------------------------------------------------------------------------ */
+/* Assembly (replaces GLOBALEQASSEM -> CONSTRUCT_* -> DOASSEM,
+   Code/Source/svFSI/EQASSEM.f:38-87 and LHSA.f:266-298) */
+
+/* Upload a tet4 mesh (IEN 1-based, eNoN = 4, nsd = 3) bound to lhs's CSR.
+   Builds the element -> CSR position map and a conflict-free element
+   colouring (deterministic scatter). */
+int gsls_mesh_create(gsls_mesh **mesh, gsls_lhs *lhs, int nEl, int eNoN,
+                     const int *IEN, int nsd, const double *x);
+int gsls_mesh_free(gsls_mesh *mesh);
+/* Number of colours of the element colouring. */
+int gsls_mesh_ncolors(const gsls_mesh *mesh);
+
+/* Parameters of one equation/domain (constant properties, optional
+   per-element parameter). */
+typedef struct {
+  int phys;         /* GSLS_PHYS_* */
+  int dof;          /* unknowns of this equation */
+  int tDof;         /* total unknowns per node in the state arrays */
+  int s;            /* 0-based first unknown of this equation */
+  double am, af, beta, gam, dt;   /* generalized-alpha */
+  double rho;       /* density (solid_density / fluid_density) */
+  double cond;      /* HEATS conductivity */
+  double src;       /* HEATS source term */
+  double C10;       /* STRUCT neo-Hookean C10 = mu/2 */
+  double Kpen;      /* STRUCT ST91 penalty (bulk modulus) */
+  double visc;      /* STRUCT solid viscosity */
+  double dmp;       /* STRUCT damping */
+  double fb[3];     /* body force */
+  double Diso;      /* CEP isotropic diffusivity */
+  double mu_f;      /* FLUID viscosity */
+  double ctM, ctC;  /* FLUID stabilisation constants */
+  const double *eparam; /* host, per element (original order) or NULL:
+                           STRUCT C10, CEP Diso, HEATS conductivity */
+} gsls_eq_params;
+
+/* Assemble R(dof,nNo) (double) and Val(dof*dof,nnz) (double or float per
+   val_prec) on device arrays from device state arrays Ag/Yg/Dg(tDof,nNo).
+   R and Val are overwritten (LSALLOC zeroing included). */
+int gsls_assemble_dev(gsls_mesh *mesh, const gsls_eq_params *p,
+                      const double *dAg, const double *dYg, const double *dDg,
+                      double *dR, void *dVal, int val_prec);
+/* Same on host arrays (copies in and out). */
+int gsls_assemble(gsls_mesh *mesh, const gsls_eq_params *p, const double *Ag,
+                  const double *Yg, const double *Dg, double *R, double *Val);
+
+/* ------------------------------------------------------------------------ */
+/* Time integration of one equation (replaces the per-step work of
+   Code/Source/svFSI/MAIN.f:89-281 for one equation: PICP, SETBCDIR, Newton
+   loop of PICI / LSALLOC / assembly / SETBCNEU / LSSOLVE / PICC). */
+
+typedef struct {
+  int LS_type, prec;            /* GSLS_LS_TYPE_*, GSLS_PRECOND_* */
+  double ls_relTol, ls_absTol;  /* <= 0: library default */
+  int ls_mItr, ls_sD;           /* <= 0: library default */
+  double ls_relTolIn[2];        /* NS GM/CG relTol, <= 0: default */
+  int ls_mItrIn[2];             /* NS GM/CG mItr, <= 0: default */
+  int minItr, maxItr;           /* Newton limits (defaults 1, 5) */
+  double tol;                   /* Newton relative tolerance */
+  double absTol;                /* Newton absolute tolerance (eq%absTol) */
+  int precision;                /* GSLS_PREC_FP64 or GSLS_PREC_MIXED */
+} gsls_eq_solver;
+
+int gsls_eq_create(gsls_eq **eq, gsls_mesh *mesh, const gsls_eq_params *p,
+                   const gsls_eq_solver *sv);
+int gsls_eq_free(gsls_eq *eq);
+
+/* Strong Dirichlet BC on a node list (1-based): component c of the
+   equation is set to g*gx[a] (Yn) with An = 0 when bit c of mask is set
+   (mask = 0: all components); the face also enters the linear solver as a
+   BC_TYPE_DIR face.  gx nullable (= 1). */
+int gsls_eq_add_dirichlet(gsls_eq *eq, int nNo, const int *gNodes,
+                          const double *gx, double g, int mask);
+/* Constant traction h on tri3 faces (fIEN 1-based, 3 x nFel), integrated
+   as SETBCTRACL does (Code/Source/svFSI/SETBC.f:319-416). */
+int gsls_eq_add_traction(gsls_eq *eq, int nFel, const int *fIEN,
+                         const double h[3]);
+
+/* Old-step state (tDof x nNo, host) in and current state out. */
+int gsls_eq_set_state(gsls_eq *eq, const double *Ao, const double *Yo,
+                      const double *Do);
+int gsls_eq_get_state(gsls_eq *eq, double *Ao, double *Yo, double *Do);
+/* Device pointers of the resident old-step state (valid until the next
+   step); for callers that keep the state on the GPU. */
+int gsls_eq_state_dev(gsls_eq *eq, double **dAo, double **dYo, double **dDo);
+
+typedef struct {
+  int newton_itr;       /* Newton iterations taken */
+  int ls_itr_total;     /* Krylov iterations summed over Newton iterations */
+  double last_iNorm;    /* RI%iNorm of the last linear solve */
+  double r1_last;       /* RI%iNorm / eq%iNorm at exit */
+  int last_suc;         /* RI%suc of the last linear solve */
+  double t_assembly_ms; /* device time in assembly (CUDA events) */
+  double t_solve_ms;    /* device time in the linear solve */
+} gsls_step_info;
+
+/* Advance one time step. */
+int gsls_eq_step(gsls_eq *eq, gsls_step_info *info);
+/* Per-element parameter update (host, original element order). */
+int gsls_eq_set_eparam(gsls_eq *eq, const double *eparam);
+
+/* Count of this library's kernel launches so far (for launch accounting). */
+long long gsls_launch_count(void);
+
+/* Kernel timing (no counterpart in the reference, which only keeps wall
+   clock per call in ls%callD).  When enabled, the library brackets its
+   dominant launches with CUDA events on its own stream and accumulates,
+   per name, the number of launches that did work and their device time:
+   "cg_spmv" (SpMV + fused dot of one CG iteration), "assembly" (all colour
+   launches of one assembly).  Off by default. */
+int gsls_profile_enable(int on);
+int gsls_profile_reset(void);
+int gsls_profile_read(const char *name, long long *count, double *total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

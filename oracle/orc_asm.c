@@ -1,0 +1,637 @@
+/*
+ * Oracle (test infrastructure only): restatement of the svFSI driver-side
+ * hot path -- sparsity (LHSA), element assembly (HEATS3D, STRUCT3D with the
+ * neo-Hookean + ST91 material), scatter (DOASSEM), traction loads, and the
+ * generalized-alpha predictor / initiator / corrector with the Newton loop.
+ * F/ = Code/Source/svFSI in the svFSI project.  All arithmetic is FP64.
+ */
+#include "orc.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+static void *xcalloc(size_t n, size_t s) {
+  void *p = calloc(n ? n : 1, s);
+  if (!p) {
+    fprintf(stderr, "oracle: out of memory\n");
+    abort();
+  }
+  return p;
+}
+
+/* ---------------------------------------------------------------------- */
+/* LHSA + ADDCOL, F/LHSA.f:38-241: per row a sorted list of unique columns */
+typedef struct {
+  int n, cap;
+  int *c;
+} rowlist;
+
+static void addcol(rowlist *r, int col) {
+  int i = 0;
+  while (i < r->n && r->c[i] < col) i++;
+  if (i < r->n && r->c[i] == col) return;
+  if (r->n == r->cap) {
+    r->cap = r->cap ? r->cap + (r->cap / 5 > 5 ? r->cap / 5 : 5) : 40;
+    r->c = (int *)realloc(r->c, sizeof(int) * (size_t)r->cap);
+  }
+  memmove(r->c + i + 1, r->c + i, sizeof(int) * (size_t)(r->n - i));
+  r->c[i] = col;
+  r->n++;
+}
+
+static rowlist *lhsa_rows(int nNo, int nEl, int eNoN, const int *IEN) {
+  rowlist *rows = (rowlist *)xcalloc(nNo, sizeof(rowlist));
+  for (int e = 0; e < nEl; e++)
+    for (int a = 0; a < eNoN; a++) {
+      const int rowN = IEN[(size_t)e * eNoN + a];
+      for (int b = 0; b < eNoN; b++) addcol(&rows[rowN], IEN[(size_t)e * eNoN + b]);
+    }
+  return rows;
+}
+
+int orc_lhsa_count(int nNo, int nEl, int eNoN, const int *IEN) {
+  rowlist *rows = lhsa_rows(nNo, nEl, eNoN, IEN);
+  long long nnz = 0;
+  for (int i = 0; i < nNo; i++) {
+    nnz += rows[i].n;
+    free(rows[i].c);
+  }
+  free(rows);
+  return (int)nnz;
+}
+
+int orc_lhsa(int nNo, int nEl, int eNoN, const int *IEN, int *rowPtr,
+             int *colPtr, int nnzCap) {
+  rowlist *rows = lhsa_rows(nNo, nEl, eNoN, IEN);
+  int j = 0, rc = 0;
+  rowPtr[0] = 0;
+  for (int i = 0; i < nNo; i++) {
+    if (rows[i].n == 0) rc = -1; /* "Node is isolated" */
+    for (int k = 0; k < rows[i].n; k++) {
+      if (j < nnzCap) colPtr[j] = rows[i].c[k];
+      j++;
+    }
+    rowPtr[i + 1] = j;
+    free(rows[i].c);
+  }
+  free(rows);
+  if (j > nnzCap) return -2;
+  return rc ? rc : j;
+}
+
+/* DOASSEM, F/LHSA.f:266-298: bisection for the column inside the row. */
+void orc_doassem(int dof, int eNoN, const int *ptr, const double *lK,
+                 const double *lR, const int *rowPtr, const int *colPtr,
+                 double *R, double *Val) {
+  const int dd = dof * dof;
+  for (int a = 0; a < eNoN; a++) {
+    const int rowN = ptr[a];
+    for (int k = 0; k < dof; k++) R[(size_t)rowN * dof + k] += lR[a * dof + k];
+    for (int b = 0; b < eNoN; b++) {
+      const int colN = ptr[b];
+      /* the Fortran bisection runs on 1-based [left,right]; same search in
+         0-based form: left = rowPtr(rowN), right = rowPtr(rowN+1) */
+      int left = rowPtr[rowN] + 1, right = rowPtr[rowN + 1] + 1;
+      int p = (right + left) / 2;
+      while (colN != colPtr[p - 1]) {
+        if (colN > colPtr[p - 1])
+          left = p;
+        else
+          right = p;
+        p = (right + left) / 2;
+      }
+      for (int k = 0; k < dd; k++)
+        Val[(size_t)(p - 1) * dd + k] += lK[(size_t)(a * eNoN + b) * dd + k];
+    }
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* tet4 quadrature and shape functions, F/NN.f:268-275 and F/NN.f:654-671 */
+static void tet4_gauss(double w[4], double N[4][4]) {
+  const double s = (5.0 + 3.0 * sqrt(5.0)) / 20.0;
+  const double t = (5.0 - sqrt(5.0)) / 20.0;
+  const double xi[4][3] = {{s, t, t}, {t, s, t}, {t, t, s}, {t, t, t}};
+  for (int g = 0; g < 4; g++) {
+    w[g] = 1.0 / 24.0;
+    N[g][0] = xi[g][0];
+    N[g][1] = xi[g][1];
+    N[g][2] = xi[g][2];
+    N[g][3] = 1.0 - xi[g][0] - xi[g][1] - xi[g][2];
+  }
+}
+static const double TET4_NXI[3][4] = {{1, 0, 0, -1}, {0, 1, 0, -1}, {0, 0, 1, -1}};
+
+/* GNN (insd = 3), F/NN.f:1469-1565 */
+static void gnn3(const double xl[12], double Nx[3][4], double *Jac) {
+  double xXi[3][3] = {{0}}, xiX[3][3];
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++)
+      for (int k = 0; k < 3; k++) xXi[i][k] += xl[a * 3 + i] * TET4_NXI[k][a];
+  const double J = xXi[0][0] * xXi[1][1] * xXi[2][2] + xXi[0][1] * xXi[1][2] * xXi[2][0] +
+                   xXi[0][2] * xXi[1][0] * xXi[2][1] - xXi[0][0] * xXi[1][2] * xXi[2][1] -
+                   xXi[0][1] * xXi[1][0] * xXi[2][2] - xXi[0][2] * xXi[1][1] * xXi[2][0];
+  xiX[0][0] = (xXi[1][1] * xXi[2][2] - xXi[1][2] * xXi[2][1]) / J;
+  xiX[0][1] = (xXi[2][1] * xXi[0][2] - xXi[2][2] * xXi[0][1]) / J;
+  xiX[0][2] = (xXi[0][1] * xXi[1][2] - xXi[0][2] * xXi[1][1]) / J;
+  xiX[1][0] = (xXi[1][2] * xXi[2][0] - xXi[1][0] * xXi[2][2]) / J;
+  xiX[1][1] = (xXi[2][2] * xXi[0][0] - xXi[2][0] * xXi[0][2]) / J;
+  xiX[1][2] = (xXi[0][2] * xXi[1][0] - xXi[0][0] * xXi[1][2]) / J;
+  xiX[2][0] = (xXi[1][0] * xXi[2][1] - xXi[1][1] * xXi[2][0]) / J;
+  xiX[2][1] = (xXi[2][0] * xXi[0][1] - xXi[2][1] * xXi[0][0]) / J;
+  xiX[2][2] = (xXi[0][0] * xXi[1][1] - xXi[0][1] * xXi[1][0]) / J;
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++)
+      Nx[i][a] = 0.0 + TET4_NXI[0][a] * xiX[0][i] + TET4_NXI[1][a] * xiX[1][i] +
+                 TET4_NXI[2][a] * xiX[2][i];
+  *Jac = J;
+}
+
+/* ---------------------------------------------------------------------- */
+/* CONSTRUCT_HEATS / HEATS3D, F/HEATS.f:39-159 for one tet4 element.
+   al, yl: tDof x 4 local copies; uses component p->s. */
+void orc_elem_heats(const orc_eqp *p, const double xl[12], const double *al,
+                    const double *yl, double lR[4], double lK[16]) {
+  double w4[4], N4[4][4], Nx[3][4], Jac;
+  tet4_gauss(w4, N4);
+  gnn3(xl, Nx, &Jac);
+  for (int a = 0; a < 4; a++) lR[a] = 0.0;
+  for (int k = 0; k < 16; k++) lK[k] = 0.0;
+  const double nu = p->cond, s = p->src, rho = p->rho;
+  const double T1 = p->af * p->gam * p->dt;
+  const double amd = p->am * rho / T1;
+  const int i = p->s, tD = p->tDof;
+  for (int g = 0; g < 4; g++) {
+    const double w = w4[g] * Jac;
+    const double *N = N4[g];
+    const double wl = w * T1;
+    double Td = -s, Tx[3] = {0, 0, 0};
+    for (int a = 0; a < 4; a++) {
+      Td = Td + N[a] * al[a * tD + i];
+      Tx[0] = Tx[0] + Nx[0][a] * yl[a * tD + i];
+      Tx[1] = Tx[1] + Nx[1][a] * yl[a * tD + i];
+      Tx[2] = Tx[2] + Nx[2][a] * yl[a * tD + i];
+    }
+    Td = Td * rho;
+    for (int a = 0; a < 4; a++) {
+      lR[a] = lR[a] + w * (N[a] * Td + (Nx[0][a] * Tx[0] + Nx[1][a] * Tx[1] + Nx[2][a] * Tx[2]) * nu);
+      for (int b = 0; b < 4; b++)
+        lK[a * 4 + b] = lK[a * 4 + b] +
+                        wl * (N[a] * N[b] * amd +
+                              nu * (Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b]));
+    }
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* 3x3 helpers, F/MATFUN.f (MAT_DET:177, MAT_INV:238, TEN_*:419-478) */
+#define M3(A, i, j) A[(i)*3 + (j)]
+static double det3(const double *A) {
+  return M3(A, 0, 0) * (M3(A, 1, 1) * M3(A, 2, 2) - M3(A, 1, 2) * M3(A, 2, 1)) -
+         M3(A, 0, 1) * (M3(A, 1, 0) * M3(A, 2, 2) - M3(A, 1, 2) * M3(A, 2, 0)) +
+         M3(A, 0, 2) * (M3(A, 1, 0) * M3(A, 2, 1) - M3(A, 1, 1) * M3(A, 2, 0));
+}
+static void inv3(const double *A, double *B) {
+  const double d = det3(A);
+  M3(B, 0, 0) = (M3(A, 1, 1) * M3(A, 2, 2) - M3(A, 1, 2) * M3(A, 2, 1)) / d;
+  M3(B, 0, 1) = (M3(A, 0, 2) * M3(A, 2, 1) - M3(A, 0, 1) * M3(A, 2, 2)) / d;
+  M3(B, 0, 2) = (M3(A, 0, 1) * M3(A, 1, 2) - M3(A, 0, 2) * M3(A, 1, 1)) / d;
+  M3(B, 1, 0) = (M3(A, 1, 2) * M3(A, 2, 0) - M3(A, 1, 0) * M3(A, 2, 2)) / d;
+  M3(B, 1, 1) = (M3(A, 0, 0) * M3(A, 2, 2) - M3(A, 0, 2) * M3(A, 2, 0)) / d;
+  M3(B, 1, 2) = (M3(A, 0, 2) * M3(A, 1, 0) - M3(A, 0, 0) * M3(A, 1, 2)) / d;
+  M3(B, 2, 0) = (M3(A, 1, 0) * M3(A, 2, 1) - M3(A, 1, 1) * M3(A, 2, 0)) / d;
+  M3(B, 2, 1) = (M3(A, 0, 1) * M3(A, 2, 0) - M3(A, 0, 0) * M3(A, 2, 1)) / d;
+  M3(B, 2, 2) = (M3(A, 0, 0) * M3(A, 1, 1) - M3(A, 0, 1) * M3(A, 1, 0)) / d;
+}
+static void matmul3(const double *A, const double *B, double *C) {
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0.0;
+      for (int k = 0; k < 3; k++) s += M3(A, i, k) * M3(B, k, j);
+      M3(C, i, j) = s;
+    }
+}
+
+/* GETPK2CC, neo-Hookean branch + ST91 volumetric penalty (GETSVOLP) and
+   CCTOVOIGT: F/MATMODELS.f:41-150, 539-564, 1588-1647.  No fibres, no
+   active stress/strain.  Dm is 6x6 row-major, Voigt order 11,22,33,12,23,31. */
+void orc_pk2cc_nhk(double C10, double Kpen, const double F[9], double S[9],
+                   double Dm[36]) {
+  const double nd = 3.0;
+  const double J = det3(F);
+  const double J2d = pow(J, -2.0 / nd);
+  double C[9], Ci[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0.0;
+      for (int k = 0; k < 3; k++) s += M3(F, k, i) * M3(F, k, j);
+      M3(C, i, j) = s;
+    }
+  inv3(C, Ci);
+  double p = 0.0, pl = 0.0;
+  if (Kpen != 0.0) {
+    p = 0.5 * Kpen * (J - 1.0 / J);
+    pl = Kpen * J;
+  }
+  const double g1 = 2.0 * C10;
+  double Sb[9] = {g1, 0, 0, 0, g1, 0, 0, 0, g1};
+  double CSb = 0.0;
+  for (int k = 0; k < 9; k++) CSb += C[k] * Sb[k];
+  const double r1 = J2d * CSb / nd;
+  for (int k = 0; k < 9; k++) S[k] = J2d * Sb[k] - r1 * Ci[k];
+  double CC[81];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++)
+          CC[((i * 3 + j) * 3 + k) * 3 + l] =
+              (-2.0 / nd) * (M3(Ci, i, j) * M3(S, k, l) + M3(S, i, j) * M3(Ci, k, l));
+  for (int k = 0; k < 9; k++) S[k] = S[k] + p * J * Ci[k];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++) {
+          const double sym = 0.5 * (M3(Ci, i, k) * M3(Ci, j, l) + M3(Ci, i, l) * M3(Ci, j, k));
+          const double dy = M3(Ci, i, j) * M3(Ci, k, l);
+          CC[((i * 3 + j) * 3 + k) * 3 + l] += 2.0 * (r1 - p * J) * sym + (pl * J - 2.0 * r1 / nd) * dy;
+        }
+  static const int vi[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {2, 0}};
+  for (int I = 0; I < 6; I++)
+    for (int Jv = I; Jv < 6; Jv++) {
+      const double v = CC[((vi[I][0] * 3 + vi[I][1]) * 3 + vi[Jv][0]) * 3 + vi[Jv][1]];
+      Dm[I * 6 + Jv] = v;
+      Dm[Jv * 6 + I] = v;
+    }
+}
+
+/* CONSTRUCT_dSOLID / STRUCT3D for one tet4 element, F/STRUCT.f:39-496.
+   mu_e: per-element C10 override if > 0 (else p->C10). */
+void orc_elem_struct(const orc_eqp *p, double C10_e, const double xl[12],
+                     const double *al, const double *yl, const double *dl,
+                     double lR[12], double lK[144]) {
+  double w4[4], N4[4][4], Nx[3][4], Jac;
+  tet4_gauss(w4, N4);
+  gnn3(xl, Nx, &Jac);
+  for (int k = 0; k < 12; k++) lR[k] = 0.0;
+  for (int k = 0; k < 144; k++) lK[k] = 0.0;
+  const int dof = 3, tD = p->tDof;
+  const double rho = p->rho, mu = p->visc, dmp = p->dmp;
+  const double afu = p->af * p->beta * p->dt * p->dt;
+  const double afv = p->af * p->gam * p->dt;
+  const double amd = p->am * rho + afv * dmp;
+  const int i0 = p->s, j0 = i0 + 1, k0 = j0 + 1;
+  const double C10 = C10_e > 0.0 ? C10_e : p->C10;
+  for (int g = 0; g < 4; g++) {
+    const double w = w4[g] * Jac;
+    const double *N = N4[g];
+    double ud[3], vx[9] = {0}, F[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int c = 0; c < 3; c++) ud[c] = -rho * p->fb[c];
+    for (int a = 0; a < 4; a++) {
+      const int ids[3] = {i0, j0, k0};
+      for (int c = 0; c < 3; c++) {
+        ud[c] = ud[c] + N[a] * (rho * (al[a * tD + ids[c]] - 0.0) + dmp * yl[a * tD + ids[c]]);
+        for (int m = 0; m < 3; m++) {
+          M3(vx, c, m) = M3(vx, c, m) + Nx[m][a] * yl[a * tD + ids[c]];
+          M3(F, c, m) = M3(F, c, m) + Nx[m][a] * dl[a * tD + ids[c]];
+        }
+      }
+    }
+    const double J = det3(F);
+    double Fi[9];
+    inv3(F, Fi);
+    /* viscous contribution */
+    double VxFi[9], ddev[9], Svis[9], tmp[9], FiT[9];
+    matmul3(vx, Fi, VxFi);
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) M3(ddev, a, b) = 0.5 * (M3(VxFi, a, b) + M3(VxFi, b, a));
+    const double trd = (M3(ddev, 0, 0) + M3(ddev, 1, 1) + M3(ddev, 2, 2)) / 3.0;
+    for (int a = 0; a < 3; a++) M3(ddev, a, a) -= trd;
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) M3(FiT, a, b) = M3(Fi, b, a);
+    matmul3(ddev, FiT, tmp);
+    matmul3(Fi, tmp, Svis);
+    for (int k = 0; k < 9; k++) Svis[k] *= 2.0 * mu * J;
+    double S[9], Dm[36], P[9];
+    orc_pk2cc_nhk(C10, p->Kpen, F, S, Dm);
+    for (int k = 0; k < 9; k++) S[k] += Svis[k];
+    matmul3(F, S, P);
+    for (int a = 0; a < 4; a++)
+      for (int c = 0; c < 3; c++)
+        lR[a * dof + c] += w * (N[a] * ud[c] + Nx[0][a] * M3(P, c, 0) + Nx[1][a] * M3(P, c, 1) +
+                                Nx[2][a] * M3(P, c, 2));
+    double Bm[4][6][3], NxFi[4][3], DdNx[4][3], VxNx[4][3];
+    for (int a = 0; a < 4; a++) {
+      for (int c = 0; c < 3; c++) {
+        Bm[a][0][c] = Nx[0][a] * M3(F, c, 0);
+        Bm[a][1][c] = Nx[1][a] * M3(F, c, 1);
+        Bm[a][2][c] = Nx[2][a] * M3(F, c, 2);
+        Bm[a][3][c] = Nx[0][a] * M3(F, c, 1) + M3(F, c, 0) * Nx[1][a];
+        Bm[a][4][c] = Nx[1][a] * M3(F, c, 2) + M3(F, c, 1) * Nx[2][a];
+        Bm[a][5][c] = Nx[2][a] * M3(F, c, 0) + M3(F, c, 2) * Nx[0][a];
+      }
+      for (int c = 0; c < 3; c++)
+        NxFi[a][c] = Nx[0][a] * M3(Fi, 0, c) + Nx[1][a] * M3(Fi, 1, c) + Nx[2][a] * M3(Fi, 2, c);
+      for (int c = 0; c < 3; c++) {
+        DdNx[a][c] = M3(ddev, c, 0) * NxFi[a][0] + M3(ddev, c, 1) * NxFi[a][1] + M3(ddev, c, 2) * NxFi[a][2];
+        VxNx[a][c] = M3(VxFi, 0, c) * NxFi[a][0] + M3(VxFi, 1, c) * NxFi[a][1] + M3(VxFi, 2, c) * NxFi[a][2];
+      }
+    }
+    const double r13 = 1.0 / 3.0, r23 = 2.0 / 3.0;
+    const double rmu = afu * mu * J, rmv = afv * mu * J;
+    for (int b = 0; b < 4; b++)
+      for (int a = 0; a < 4; a++) {
+        double NxSNx = 0.0;
+        for (int m = 0; m < 3; m++)
+          for (int q = 0; q < 3; q++) NxSNx += Nx[m][a] * M3(S, m, q) * Nx[q][b];
+        const double T1 = amd * N[a] * N[b] + afu * NxSNx;
+        double DBm[6][3];
+        for (int I = 0; I < 6; I++)
+          for (int c = 0; c < 3; c++) {
+            double s = 0.0;
+            for (int K = 0; K < 6; K++) s += Dm[I * 6 + K] * Bm[b][K][c];
+            DBm[I][c] = s;
+          }
+        const double NxNx = NxFi[a][0] * NxFi[b][0] + NxFi[a][1] * NxFi[b][1] + NxFi[a][2] * NxFi[b][2];
+        for (int r = 0; r < 3; r++)
+          for (int c = 0; c < 3; c++) {
+            double BmDBm = 0.0;
+            for (int I = 0; I < 6; I++) BmDBm += Bm[a][I][r] * DBm[I][c];
+            double Tv = (2.0 * (DdNx[a][r] * NxFi[b][c] - DdNx[b][r] * NxFi[a][c]) -
+                         (NxNx * M3(VxFi, r, c) + NxFi[b][r] * VxNx[a][c] - r23 * NxFi[a][r] * VxNx[b][c])) *
+                        rmu;
+            if (r == c)
+              Tv += (r13 * NxFi[a][r] * NxFi[b][r] + NxNx) * rmv;
+            else
+              Tv += (NxFi[a][c] * NxFi[b][r] - r23 * NxFi[a][r] * NxFi[b][c]) * rmv;
+            const double diag = (r == c) ? T1 : 0.0;
+            lK[(size_t)(a * 4 + b) * 9 + r * 3 + c] += w * (diag + afu * BmDBm + Tv);
+          }
+      }
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* GLOBALEQASSEM -> CONSTRUCT_* -> DOASSEM over all elements (one domain),
+   F/EQASSEM.f:38-87. */
+int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
+                 const double *x, const double *Ag, const double *Yg,
+                 const double *Dg, const int *rowPtr, const int *colPtr,
+                 double *R, double *Val) {
+  (void)nNo;
+  const int tD = p->tDof;
+  double xl[12], al[4 * 16], yl[4 * 16], dl[4 * 16];
+  int ptr[4];
+  if (tD > 16) return -1;
+  for (int e = 0; e < nEl; e++) {
+    for (int a = 0; a < 4; a++) {
+      const int Ac = IEN[(size_t)e * 4 + a];
+      ptr[a] = Ac;
+      for (int i = 0; i < 3; i++) xl[a * 3 + i] = x[(size_t)Ac * 3 + i];
+      for (int i = 0; i < tD; i++) {
+        al[a * tD + i] = Ag[(size_t)Ac * tD + i];
+        yl[a * tD + i] = Yg[(size_t)Ac * tD + i];
+        dl[a * tD + i] = Dg ? Dg[(size_t)Ac * tD + i] : 0.0;
+      }
+    }
+    if (p->phys == 1) {
+      double lR[4], lK[16];
+      orc_elem_heats(p, xl, al, yl, lR, lK);
+      orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+    } else if (p->phys == 2) {
+      double lR[12], lK[144];
+      const double C10e = p->eparam ? p->eparam[e] : 0.0;
+      orc_elem_struct(p, C10e, xl, al, yl, dl, lR, lK);
+      orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+    } else {
+      return -2;
+    }
+  }
+  return 0;
+}
+
+/* Same as orc_assemble with the element loop split by a conflict-free
+   colouring (elements of one colour share no node) and run with OpenMP
+   inside each colour -- the multi-core CPU baseline.  order[] lists element
+   ids colour by colour, color_off[ncolor+1] delimits the colours. */
+int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
+                         const double *x, const double *Ag, const double *Yg,
+                         const double *Dg, const int *rowPtr, const int *colPtr,
+                         double *R, double *Val, int ncolor, const int *color_off,
+                         const int *order) {
+  (void)nNo;
+  (void)nEl;
+  const int tD = p->tDof;
+  if (tD > 16) return -1;
+  for (int c = 0; c < ncolor; c++) {
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int k = color_off[c]; k < color_off[c + 1]; k++) {
+      const int e = order[k];
+      double xl[12], al[4 * 16], yl[4 * 16], dl[4 * 16];
+      int ptr[4];
+      for (int a = 0; a < 4; a++) {
+        const int Ac = IEN[(size_t)e * 4 + a];
+        ptr[a] = Ac;
+        for (int i = 0; i < 3; i++) xl[a * 3 + i] = x[(size_t)Ac * 3 + i];
+        for (int i = 0; i < tD; i++) {
+          al[a * tD + i] = Ag[(size_t)Ac * tD + i];
+          yl[a * tD + i] = Yg[(size_t)Ac * tD + i];
+          dl[a * tD + i] = Dg ? Dg[(size_t)Ac * tD + i] : 0.0;
+        }
+      }
+      if (p->phys == 1) {
+        double lR[4], lK[16];
+        orc_elem_heats(p, xl, al, yl, lR, lK);
+        orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+      } else if (p->phys == 2) {
+        double lR[12], lK[144];
+        orc_elem_struct(p, p->eparam ? p->eparam[e] : 0.0, xl, al, yl, dl, lR, lK);
+        orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+      }
+    }
+  }
+  return 0;
+}
+
+/* SETBCTRACL for tri3 faces with a constant traction vector h,
+   F/SETBC.f:319-416; 3-point rule F/NN.f:416-422, w = 1/6. */
+void orc_traction(int dof, int nFel, const int *fIEN, const double *x,
+                  const double h[3], double *R) {
+  const double s = 2.0 / 3.0, t = 1.0 / 6.0;
+  const double xi[3][2] = {{t, t}, {s, t}, {t, s}};
+  for (int e = 0; e < nFel; e++) {
+    const int *n = fIEN + (size_t)e * 3;
+    double v1[3], v2[3], nV[3];
+    for (int i = 0; i < 3; i++) {
+      v1[i] = x[(size_t)n[0] * 3 + i] - x[(size_t)n[2] * 3 + i];
+      v2[i] = x[(size_t)n[1] * 3 + i] - x[(size_t)n[2] * 3 + i];
+    }
+    nV[0] = v1[1] * v2[2] - v1[2] * v2[1];
+    nV[1] = v1[2] * v2[0] - v1[0] * v2[2];
+    nV[2] = v1[0] * v2[1] - v1[1] * v2[0];
+    const double Jac = sqrt(nV[0] * nV[0] + nV[1] * nV[1] + nV[2] * nV[2]);
+    double lR[3][3] = {{0}};
+    for (int g = 0; g < 3; g++) {
+      const double w = Jac / 6.0;
+      const double N[3] = {xi[g][0], xi[g][1], 1.0 - xi[g][0] - xi[g][1]};
+      double hh[3] = {0, 0, 0};
+      for (int a = 0; a < 3; a++)
+        for (int i = 0; i < 3; i++) hh[i] += N[a] * h[i];
+      for (int a = 0; a < 3; a++)
+        for (int i = 0; i < 3; i++) lR[a][i] -= w * N[a] * hh[i];
+    }
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < 3 && i < dof; i++) R[(size_t)n[a] * dof + i] += lR[a][i];
+  }
+}
+
+/* gen-alpha coefficients, F/INITIALIZE.f:76-139 */
+void orc_genalpha(double roInf, int second_order, double *am, double *af,
+                  double *beta, double *gam) {
+  *am = second_order ? (2.0 - roInf) / (1.0 + roInf)
+                     : 0.5 * (3.0 - roInf) / (1.0 + roInf);
+  *af = 1.0 / (1.0 + roInf);
+  *beta = 0.25 * pow(1.0 + *am - *af, 2.0);
+  *gam = 0.5 + *am - *af;
+}
+
+/* ---------------------------------------------------------------------- */
+/* One time step of one equation: PICP (F/PIC.f:40-130), SETBCDIR
+   (F/SETBC.f:39-228), then the Newton loop of F/MAIN.f:116-215 with
+   PICI (F/PIC.f:133-166), LSALLOC, assembly, SETBCNEU, LSSOLVE and PICC
+   (F/PIC.f:169-297).  At the end An/Yn/Dn are copied to Ao/Yo/Do
+   (F/MAIN.f:277-279).  eq->p.s must be 0 (single equation). */
+static void apply_dir(orc_eq *eq, double *lA, double *lY) {
+  const int tD = eq->p.tDof, s = eq->p.s, dof = eq->p.dof;
+  for (int ib = 0; ib < eq->nDir; ib++) {
+    const orc_dirbc *bc = &eq->dir[ib];
+    for (int a = 0; a < bc->nNo; a++) {
+      const int Ac = bc->nodes[a];
+      const double gx = bc->gx ? bc->gx[a] : 1.0;
+      for (int c = 0; c < dof; c++) {
+        if (bc->mask && !((bc->mask >> c) & 1)) continue;
+        lA[(size_t)Ac * tD + s + c] = 0.0 * gx;
+        lY[(size_t)Ac * tD + s + c] = bc->g * gx;
+      }
+    }
+  }
+}
+
+int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
+  const int nNo = eq->nNo, tD = eq->p.tDof, dof = eq->p.dof;
+  const size_t nS = (size_t)nNo * tD;
+  const double dt = eq->p.dt, gam = eq->p.gam, beta = eq->p.beta;
+  const int dFlag = (eq->p.phys == 2);
+  memset(info, 0, sizeof(*info));
+  /* PICP */
+  const double coef = (gam - 1.0) / gam;
+  for (size_t k = 0; k < nS; k++) eq->An[k] = eq->Ao[k] * coef;
+  for (size_t k = 0; k < nS; k++) eq->Yn[k] = eq->Yo[k];
+  if (dFlag) {
+    const double c2 = dt * dt * (0.5 * gam - beta) / (gam - 1.0);
+    for (size_t k = 0; k < nS; k++) eq->Dn[k] = eq->Do[k] + eq->Yn[k] * dt + eq->An[k] * c2;
+  } else {
+    for (size_t k = 0; k < nS; k++) eq->Dn[k] = eq->Do[k];
+  }
+  /* SETBCDIR */
+  apply_dir(eq, eq->An, eq->Yn);
+
+  /* LS structures: one face per Dirichlet BC (FSILSINI, F/BAFINI.f:468-513) */
+  orc_lhs *lhs = orc_lhs_create(nNo, eq->nnz, eq->rowPtr, eq->colPtr, eq->nDir);
+  for (int ib = 0; ib < eq->nDir; ib++) {
+    const orc_dirbc *bc = &eq->dir[ib];
+    double *sv = (double *)xcalloc((size_t)3 * bc->nNo, sizeof(double));
+    if (bc->mask)
+      for (int a = 0; a < bc->nNo; a++)
+        for (int c = 0; c < 3; c++) sv[a * 3 + c] = ((bc->mask >> c) & 1) ? 0.0 : 1.0;
+    orc_bc_create(lhs, ib + 1, bc->nNo, 3, ORC_BC_TYPE_Dir, bc->nodes, sv);
+    free(sv);
+  }
+  orc_ls ls;
+  orc_ls_create(&ls, eq->LS_type);
+  if (eq->ls_relTol > 0) ls.RI.relTol = eq->ls_relTol;
+  if (eq->ls_absTol > 0) ls.RI.absTol = eq->ls_absTol;
+  if (eq->ls_mItr > 0) ls.RI.mItr = eq->ls_mItr;
+  if (eq->ls_sD > 0) {
+    ls.RI.sD = eq->ls_sD;
+    ls.GM.sD = eq->ls_sD;
+  }
+  if (eq->ls_relTolIn[0] > 0) {
+    ls.GM.relTol = eq->ls_relTolIn[0];
+    ls.CG.relTol = eq->ls_relTolIn[1];
+  }
+  if (eq->ls_mItrIn[0] > 0) {
+    ls.GM.mItr = eq->ls_mItrIn[0];
+    ls.CG.mItr = eq->ls_mItrIn[1];
+  }
+
+  double *Ag = (double *)xcalloc(nS, sizeof(double));
+  double *Yg = (double *)xcalloc(nS, sizeof(double));
+  double *Dg = (double *)xcalloc(nS, sizeof(double));
+  double *R = (double *)xcalloc((size_t)nNo * dof, sizeof(double));
+  double *Val = (double *)xcalloc((size_t)eq->nnz * dof * dof, sizeof(double));
+  int *incL = (int *)xcalloc(eq->nDir > 0 ? eq->nDir : 1, sizeof(int));
+  double *res = (double *)xcalloc(eq->nDir > 0 ? eq->nDir : 1, sizeof(double));
+  for (int f = 0; f < eq->nDir; f++) incL[f] = 1;
+
+  int itr = 0, ok = 0, rc = 0;
+  const double am = eq->p.am, af = eq->p.af;
+  while (!ok) {
+    /* PICI */
+    itr++;
+    for (size_t k = 0; k < nS; k++) {
+      Ag[k] = eq->Ao[k] * (1.0 - am) + eq->An[k] * am;
+      Yg[k] = eq->Yo[k] * (1.0 - af) + eq->Yn[k] * af;
+      Dg[k] = eq->Do[k] * (1.0 - af) + eq->Dn[k] * af;
+    }
+    /* LSALLOC */
+    memset(R, 0, sizeof(double) * (size_t)nNo * dof);
+    memset(Val, 0, sizeof(double) * (size_t)eq->nnz * dof * dof);
+    rc = orc_assemble(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr, eq->colPtr, R, Val);
+    if (rc) break;
+    /* SETBCNEU (traction) */
+    for (int t = 0; t < eq->nTrac; t++)
+      orc_traction(dof, eq->trac[t].nFel, eq->trac[t].fIEN, eq->x, eq->trac[t].h, R);
+    /* LSSOLVE */
+    rc = orc_solve(lhs, &ls, dof, R, Val, eq->prec, incL, res);
+    if (rc) break;
+    info->ls_itr_total += ls.RI.itr;
+    info->last_suc = ls.RI.suc;
+    /* PICC */
+    const double c1 = gam * dt, c2 = beta * dt * dt;
+    for (int a = 0; a < nNo; a++)
+      for (int c = 0; c < dof; c++) {
+        const double r = R[(size_t)a * dof + c];
+        const size_t k = (size_t)a * tD + eq->p.s + c;
+        eq->An[k] = eq->An[k] - r;
+        eq->Yn[k] = eq->Yn[k] - r * c1;
+        eq->Dn[k] = eq->Dn[k] - r * c2;
+      }
+    if (ls.RI.iNorm == 0.0) ls.RI.iNorm = 2.220446049250313e-16;
+    if (eq->eq_iNorm == 0.0) eq->eq_iNorm = ls.RI.iNorm;
+    if (itr == 1) eq->eq_pNorm = ls.RI.iNorm / eq->eq_iNorm;
+    const double r1 = ls.RI.iNorm / eq->eq_iNorm;
+    const int l1 = eq->eq_iNorm <= eq->eqAbsTol;
+    const int l2 = itr >= eq->maxItr;
+    const int l3 = r1 <= eq->tol;
+    const int l4 = r1 <= eq->tol * eq->eq_pNorm;
+    const int l5 = itr >= eq->minItr;
+    if (l1 || l2 || ((l3 || l4) && l5)) ok = 1;
+    info->last_iNorm = ls.RI.iNorm;
+    info->r1_last = r1;
+  }
+  info->newton_itr = itr;
+  memcpy(eq->Ao, eq->An, nS * sizeof(double));
+  memcpy(eq->Yo, eq->Yn, nS * sizeof(double));
+  if (dFlag) memcpy(eq->Do, eq->Dn, nS * sizeof(double));
+  orc_lhs_free(lhs);
+  free(Ag);
+  free(Yg);
+  free(Dg);
+  free(R);
+  free(Val);
+  free(incL);
+  free(res);
+  return rc;
+}

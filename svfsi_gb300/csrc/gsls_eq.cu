@@ -1,0 +1,408 @@
+// Device-resident time integration of one equation: the per-step work of
+// Code/Source/svFSI/MAIN.f:89-281 -- PICP (PIC.f:40-130), SETBCDIR
+// (SETBC.f:39-228), and the Newton loop PICI (PIC.f:133-166) -> LSALLOC +
+// assembly -> SETBCNEU traction (SETBC.f:319-416) -> FSILS_SOLVE -> PICC
+// (PIC.f:169-297).  State arrays stay in HBM between steps; the host reads
+// one scalar (RI%iNorm) per Newton iteration for the stopping test.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gsls_internal.cuh"
+
+namespace gsls {
+int assemble_dev(gsls_mesh *m, const gsls_eq_params *p, const double *Ag, const double *Yg,
+                 const double *Dg, double *R, void *Val, int val_prec);
+int mesh_set_eparam(gsls_mesh *m, const double *eparam);
+int mesh_check_error(gsls_mesh *m);
+gsls_lhs *mesh_lhs(gsls_mesh *m);
+int mesh_coords_host(gsls_mesh *m, double *x);
+}  // namespace gsls
+
+struct gsls_eq {
+  gsls_mesh *mesh = nullptr;
+  gsls_lhs *lhs = nullptr;
+  gsls_eq_params p;
+  gsls_eq_solver sv;
+  gsls_ls ls;
+  bool dFlag = false;
+  int nNo = 0, nnz = 0;
+  gsls::DevBuf st[9];  // Ao Yo Do An Yn Dn Ag Yg Dg
+  gsls::DevBuf R, Val, Ftrac;
+  bool has_trac = false;
+  struct Dir {
+    gsls::DevBuf nodes, gx;
+    int n = 0;
+    double g = 0.0;
+    int mask = 0;
+  };
+  std::vector<Dir *> dirs;
+  int nextFace = 0;
+  double eq_iNorm = 0.0, eq_pNorm = 0.0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ~gsls_eq() {
+    for (auto *d : dirs) delete d;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+};
+
+namespace gsls {
+
+constexpr int kT = 256;
+
+static inline int nblk(size_t n) {
+  size_t b = (n + kT - 1) / kT;
+  const size_t cap = (size_t)num_sms() * 16;
+  if (b > cap) b = cap;
+  return b < 1 ? 1 : (int)b;
+}
+
+// PICP for one equation occupying unknowns [s, s+dof) of tDof
+__global__ void k_picp(int nNo, int tDof, int s, int dof, double coef, int dFlag, double dt,
+                       double c2, const double *__restrict__ Ao, const double *__restrict__ Yo,
+                       const double *__restrict__ Do, double *__restrict__ An,
+                       double *__restrict__ Yn, double *__restrict__ Dn) {
+  const size_t n = (size_t)nNo * dof;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t a = t / dof, c = t - a * dof;
+    const size_t k = a * tDof + s + c;
+    const double an = Ao[k] * coef;
+    An[k] = an;
+    const double yn = Yo[k];
+    Yn[k] = yn;
+    Dn[k] = dFlag ? Do[k] + yn * dt + an * c2 : Do[k];
+  }
+}
+
+// SETBCDIR with dirA = 0, dirY = g*gx on the masked components
+__global__ void k_setbcdir(int n, const int *__restrict__ nodes, const double *__restrict__ gx,
+                           double g, int mask, int tDof, int s, int dof, double *__restrict__ An,
+                           double *__restrict__ Yn) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    const size_t Ac = nodes[a];
+    const double v = gx ? gx[a] : 1.0;
+    for (int c = 0; c < dof; c++) {
+      if (mask && !((mask >> c) & 1)) continue;
+      An[Ac * tDof + s + c] = 0.0 * v;
+      Yn[Ac * tDof + s + c] = g * v;
+    }
+  }
+}
+
+// PICI: Ag = Ao(1-am) + An am; Yg, Dg with af
+__global__ void k_pici(size_t n, double am, double af, const double *__restrict__ Ao,
+                       const double *__restrict__ An, const double *__restrict__ Yo,
+                       const double *__restrict__ Yn, const double *__restrict__ Do,
+                       const double *__restrict__ Dn, double *__restrict__ Ag,
+                       double *__restrict__ Yg, double *__restrict__ Dg) {
+  const double c1 = 1.0 - am, c3 = 1.0 - af;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    Ag[k] = Ao[k] * c1 + An[k] * am;
+    Yg[k] = Yo[k] * c3 + Yn[k] * af;
+    Dg[k] = Do[k] * c3 + Dn[k] * af;
+  }
+}
+
+// PICC: An -= R; Yn -= R gam dt; Dn -= R beta dt^2
+__global__ void k_picc(int nNo, int tDof, int s, int dof, double c1, double c2,
+                       const double *__restrict__ R, double *__restrict__ An,
+                       double *__restrict__ Yn, double *__restrict__ Dn) {
+  const size_t n = (size_t)nNo * dof;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t a = t / dof, c = t - a * dof;
+    const size_t k = a * tDof + s + c;
+    const double r = R[t];
+    An[k] = An[k] - r;
+    Yn[k] = Yn[k] - r * c1;
+    Dn[k] = Dn[k] - r * c2;
+  }
+}
+
+__global__ void k_axpy1(size_t n, double *__restrict__ y, const double *__restrict__ x) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    y[k] += x[k];
+}
+
+}  // namespace gsls
+
+using namespace gsls;
+
+extern "C" {
+
+int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
+                   const gsls_eq_solver *sv) {
+  if (!out || !mesh || !p || !sv) return GSLS_ERR_ARG;
+  if (p->dof < 1 || p->dof > 4 || p->s < 0 || p->s + p->dof > p->tDof) return GSLS_ERR_ARG;
+  if (sv->precision != GSLS_PREC_FP64 && sv->precision != GSLS_PREC_MIXED) return GSLS_ERR_ARG;
+  gsls_eq *eq = new gsls_eq();
+  eq->mesh = mesh;
+  eq->lhs = mesh_lhs(mesh);
+  eq->p = *p;
+  eq->p.eparam = nullptr;
+  eq->sv = *sv;
+  if (eq->sv.maxItr <= 0) eq->sv.maxItr = 5;
+  if (eq->sv.minItr <= 0) eq->sv.minItr = 1;
+  eq->dFlag = (p->phys == GSLS_PHYS_STRUCT);
+  eq->nNo = eq->lhs->nNo;
+  eq->nnz = eq->lhs->nnz;
+  int rc = gsls_ls_create(&eq->ls, sv->LS_type, sv->ls_relTol > 0 ? &sv->ls_relTol : nullptr,
+                          sv->ls_absTol > 0 ? &sv->ls_absTol : nullptr,
+                          sv->ls_mItr > 0 ? &sv->ls_mItr : nullptr,
+                          sv->ls_sD > 0 ? &sv->ls_sD : nullptr,
+                          sv->ls_relTolIn[0] > 0 ? sv->ls_relTolIn : nullptr, nullptr,
+                          sv->ls_mItrIn[0] > 0 ? sv->ls_mItrIn : nullptr);
+  if (rc != GSLS_OK) {
+    delete eq;
+    return rc;
+  }
+  const size_t ns = (size_t)eq->nNo * p->tDof;
+  for (int k = 0; k < 9; k++) {
+    if ((rc = eq->st[k].alloc(sizeof(double) * ns)) != GSLS_OK) {
+      delete eq;
+      return rc;
+    }
+    cudaMemsetAsync(eq->st[k].p, 0, sizeof(double) * ns, eq->lhs->stream);
+  }
+  const size_t vb = (size_t)eq->nnz * p->dof * p->dof * (sv->precision == GSLS_PREC_MIXED ? 4 : 8);
+  if ((rc = eq->R.alloc(sizeof(double) * (size_t)eq->nNo * p->dof)) != GSLS_OK ||
+      (rc = eq->Val.alloc(vb)) != GSLS_OK) {
+    delete eq;
+    return rc;
+  }
+  if (p->eparam && (rc = mesh_set_eparam(mesh, p->eparam)) != GSLS_OK) {
+    delete eq;
+    return rc;
+  }
+  cudaEventCreate(&eq->e0);
+  cudaEventCreate(&eq->e1);
+  cudaStreamSynchronize(eq->lhs->stream);
+  *out = eq;
+  return GSLS_OK;
+}
+
+int gsls_eq_free(gsls_eq *eq) {
+  if (!eq) return GSLS_ERR_ARG;
+  cudaStreamSynchronize(eq->lhs->stream);
+  delete eq;
+  return GSLS_OK;
+}
+
+int gsls_eq_set_eparam(gsls_eq *eq, const double *eparam) {
+  if (!eq) return GSLS_ERR_ARG;
+  return mesh_set_eparam(eq->mesh, eparam);
+}
+
+int gsls_eq_add_dirichlet(gsls_eq *eq, int nNo, const int *gNodes, const double *gx, double g,
+                          int mask) {
+  if (!eq || nNo < 0 || (nNo > 0 && !gNodes)) return GSLS_ERR_ARG;
+  gsls_lhs *lhs = eq->lhs;
+  if (eq->nextFace >= lhs->nFaces) {
+    set_error("gsls_eq_add_dirichlet: no free LS face (raise nFaces in gsls_lhs_create)");
+    return GSLS_ERR_STATE;
+  }
+  // FSILSINI (Code/Source/svFSI/BAFINI.f:488-512): dof = nsd, val 0 on the
+  // constrained directions, 1 on the free ones when a direction mask is set
+  std::vector<double> sv((size_t)3 * nNo, 0.0);
+  if (mask)
+    for (int a = 0; a < nNo; a++)
+      for (int c = 0; c < 3; c++) sv[(size_t)a * 3 + c] = ((mask >> c) & 1) ? 0.0 : 1.0;
+  int rc = gsls_bc_create(lhs, eq->nextFace + 1, nNo, 3, GSLS_BC_TYPE_DIR, gNodes, sv.data());
+  if (rc != GSLS_OK) return rc;
+  eq->nextFace++;
+  auto *d = new gsls_eq::Dir();
+  d->n = nNo;
+  d->g = g;
+  d->mask = mask;
+  std::vector<int> nodes(nNo);
+  for (int a = 0; a < nNo; a++) nodes[a] = gNodes[a] - 1;
+  GSLS_TRY(d->nodes.alloc(sizeof(int) * (nNo > 0 ? nNo : 1)));
+  if (nNo)
+    GSLS_CUDA(cudaMemcpyAsync(d->nodes.p, nodes.data(), sizeof(int) * nNo, cudaMemcpyHostToDevice,
+                              lhs->stream));
+  if (gx) {
+    GSLS_TRY(d->gx.alloc(sizeof(double) * (nNo > 0 ? nNo : 1)));
+    GSLS_CUDA(cudaMemcpyAsync(d->gx.p, gx, sizeof(double) * nNo, cudaMemcpyHostToDevice,
+                              lhs->stream));
+  }
+  GSLS_CUDA(cudaStreamSynchronize(lhs->stream));
+  eq->dirs.push_back(d);
+  return GSLS_OK;
+}
+
+int gsls_eq_add_traction(gsls_eq *eq, int nFel, const int *fIEN, const double h[3]) {
+  if (!eq || nFel < 0 || (nFel > 0 && !fIEN) || !h) return GSLS_ERR_ARG;
+  gsls_lhs *lhs = eq->lhs;
+  const int dof = eq->p.dof;
+  const int nNo = eq->nNo;
+  // nodal load of SETBCTRACL's 3-point rule (w = 1/6, N = (t,t,s),(s,t,t),(t,s,t))
+  std::vector<double> F((size_t)nNo * dof, 0.0);
+  if (eq->has_trac)
+    GSLS_CUDA(cudaMemcpy(F.data(), eq->Ftrac.p, sizeof(double) * F.size(), cudaMemcpyDeviceToHost));
+  std::vector<double> x((size_t)nNo * 3);
+  GSLS_TRY(mesh_coords_host(eq->mesh, x.data()));
+  const double s = 2.0 / 3.0, t = 1.0 / 6.0;
+  const double xi[3][2] = {{t, t}, {s, t}, {t, s}};
+  for (int e = 0; e < nFel; e++) {
+    int n[3];
+    for (int a = 0; a < 3; a++) {
+      n[a] = fIEN[(size_t)e * 3 + a] - 1;
+      if (n[a] < 0 || n[a] >= nNo) return GSLS_ERR_ARG;
+    }
+    double v1[3], v2[3], nV[3];
+    for (int i = 0; i < 3; i++) {
+      v1[i] = x[(size_t)n[0] * 3 + i] - x[(size_t)n[2] * 3 + i];
+      v2[i] = x[(size_t)n[1] * 3 + i] - x[(size_t)n[2] * 3 + i];
+    }
+    nV[0] = v1[1] * v2[2] - v1[2] * v2[1];
+    nV[1] = v1[2] * v2[0] - v1[0] * v2[2];
+    nV[2] = v1[0] * v2[1] - v1[1] * v2[0];
+    const double Jac = sqrt(nV[0] * nV[0] + nV[1] * nV[1] + nV[2] * nV[2]);
+    double lR[3][3] = {{0}};
+    for (int g = 0; g < 3; g++) {
+      const double w = Jac / 6.0;
+      const double N[3] = {xi[g][0], xi[g][1], 1.0 - xi[g][0] - xi[g][1]};
+      double hh[3] = {0, 0, 0};
+      for (int a = 0; a < 3; a++)
+        for (int i = 0; i < 3; i++) hh[i] += N[a] * h[i];
+      for (int a = 0; a < 3; a++)
+        for (int i = 0; i < 3; i++) lR[a][i] -= w * N[a] * hh[i];
+    }
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < 3 && i < dof; i++) F[(size_t)n[a] * dof + i] += lR[a][i];
+  }
+  GSLS_TRY(eq->Ftrac.alloc(sizeof(double) * F.size()));
+  GSLS_CUDA(cudaMemcpyAsync(eq->Ftrac.p, F.data(), sizeof(double) * F.size(),
+                            cudaMemcpyHostToDevice, lhs->stream));
+  GSLS_CUDA(cudaStreamSynchronize(lhs->stream));
+  eq->has_trac = true;
+  return GSLS_OK;
+}
+
+int gsls_eq_set_state(gsls_eq *eq, const double *Ao, const double *Yo, const double *Do) {
+  if (!eq || !Ao || !Yo) return GSLS_ERR_ARG;
+  const size_t nb = sizeof(double) * (size_t)eq->nNo * eq->p.tDof;
+  cudaStream_t st = eq->lhs->stream;
+  GSLS_CUDA(cudaMemcpyAsync(eq->st[0].p, Ao, nb, cudaMemcpyHostToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(eq->st[1].p, Yo, nb, cudaMemcpyHostToDevice, st));
+  if (Do)
+    GSLS_CUDA(cudaMemcpyAsync(eq->st[2].p, Do, nb, cudaMemcpyHostToDevice, st));
+  else
+    GSLS_CUDA(cudaMemsetAsync(eq->st[2].p, 0, nb, st));
+  return GSLS_OK;
+}
+
+int gsls_eq_get_state(gsls_eq *eq, double *Ao, double *Yo, double *Do) {
+  if (!eq) return GSLS_ERR_ARG;
+  const size_t nb = sizeof(double) * (size_t)eq->nNo * eq->p.tDof;
+  cudaStream_t st = eq->lhs->stream;
+  if (Ao) GSLS_CUDA(cudaMemcpyAsync(Ao, eq->st[0].p, nb, cudaMemcpyDeviceToHost, st));
+  if (Yo) GSLS_CUDA(cudaMemcpyAsync(Yo, eq->st[1].p, nb, cudaMemcpyDeviceToHost, st));
+  if (Do) GSLS_CUDA(cudaMemcpyAsync(Do, eq->st[2].p, nb, cudaMemcpyDeviceToHost, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  return GSLS_OK;
+}
+
+int gsls_eq_state_dev(gsls_eq *eq, double **dAo, double **dYo, double **dDo) {
+  if (!eq) return GSLS_ERR_ARG;
+  if (dAo) *dAo = eq->st[0].as<double>();
+  if (dYo) *dYo = eq->st[1].as<double>();
+  if (dDo) *dDo = eq->st[2].as<double>();
+  return GSLS_OK;
+}
+
+int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
+  if (!eq) return GSLS_ERR_ARG;
+  gsls_step_info loc;
+  if (!info) info = &loc;
+  memset(info, 0, sizeof(*info));
+  gsls_lhs *lhs = eq->lhs;
+  cudaStream_t st = lhs->stream;
+  const gsls_eq_params &p = eq->p;
+  const int nNo = eq->nNo, tD = p.tDof, dof = p.dof;
+  const size_t ns = (size_t)nNo * tD, nr = (size_t)nNo * dof;
+  double *Ao = eq->st[0].as<double>(), *Yo = eq->st[1].as<double>(), *Do = eq->st[2].as<double>();
+  double *An = eq->st[3].as<double>(), *Yn = eq->st[4].as<double>(), *Dn = eq->st[5].as<double>();
+  double *Ag = eq->st[6].as<double>(), *Yg = eq->st[7].as<double>(), *Dg = eq->st[8].as<double>();
+  const int valp = eq->sv.precision;
+  // PICP: copy the whole state first so that unknowns of other equations
+  // carry over, then predict this equation's block
+  GSLS_CUDA(cudaMemcpyAsync(An, Ao, sizeof(double) * ns, cudaMemcpyDeviceToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(Yn, Yo, sizeof(double) * ns, cudaMemcpyDeviceToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(Dn, Do, sizeof(double) * ns, cudaMemcpyDeviceToDevice, st));
+  const double coef = (p.gam - 1.0) / p.gam;
+  const double c2p = p.dt * p.dt * (0.5 * p.gam - p.beta) / (p.gam - 1.0);
+  k_picp<<<nblk(nr), kT, 0, st>>>(nNo, tD, p.s, dof, coef, eq->dFlag ? 1 : 0, p.dt, c2p, Ao, Yo,
+                                  Do, An, Yn, Dn);
+  GSLS_CHECK_LAUNCH();
+  for (auto *d : eq->dirs) {
+    if (d->n == 0) continue;
+    k_setbcdir<<<nblk(d->n), kT, 0, st>>>(d->n, d->nodes.as<int>(), d->gx.as<double>(), d->g,
+                                          d->mask, tD, p.s, dof, An, Yn);
+    GSLS_CHECK_LAUNCH();
+  }
+  GSLS_TRY(lhs_update_faces(lhs, nullptr, nullptr));
+  int itr = 0;
+  bool ok = false;
+  float ms = 0.f;
+  while (!ok) {
+    itr++;
+    k_pici<<<nblk(ns), kT, 0, st>>>(ns, p.am, p.af, Ao, An, Yo, Yn, Do, Dn, Ag, Yg, Dg);
+    GSLS_CHECK_LAUNCH();
+    cudaEventRecord(eq->e0, st);
+    GSLS_TRY(assemble_dev(eq->mesh, &p, Ag, Yg, Dg, eq->R.as<double>(), eq->Val.p, valp));
+    if (eq->has_trac) {
+      k_axpy1<<<nblk(nr), kT, 0, st>>>(nr, eq->R.as<double>(), eq->Ftrac.as<double>());
+      GSLS_CHECK_LAUNCH();
+    }
+    cudaEventRecord(eq->e1, st);
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = solve_dev(lhs, &eq->ls, dof, eq->R.as<double>(), eq->Val.p, valp, eq->sv.prec);
+    info->t_solve_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    cudaEventElapsedTime(&ms, eq->e0, eq->e1);
+    info->t_assembly_ms += ms;
+    if (prof_on()) prof_add("assembly", 1, ms);
+    if (rc != GSLS_OK) return rc;
+    GSLS_TRY(mesh_check_error(eq->mesh));
+    info->ls_itr_total += eq->ls.RI.itr;
+    info->last_suc = eq->ls.RI.suc;
+    // PICC
+    k_picc<<<nblk(nr), kT, 0, st>>>(nNo, tD, p.s, dof, p.gam * p.dt, p.beta * p.dt * p.dt,
+                                    eq->R.as<double>(), An, Yn, Dn);
+    GSLS_CHECK_LAUNCH();
+    // Newton test, Code/Source/svFSI/PIC.f:263-275
+    double iN = eq->ls.RI.iNorm;
+    if (iN == 0.0) iN = 2.220446049250313e-16;
+    if (eq->eq_iNorm == 0.0) eq->eq_iNorm = iN;
+    if (itr == 1) eq->eq_pNorm = iN / eq->eq_iNorm;
+    const double r1 = iN / eq->eq_iNorm;
+    const bool l1 = eq->eq_iNorm <= eq->sv.absTol;
+    const bool l2 = itr >= eq->sv.maxItr;
+    const bool l3 = r1 <= eq->sv.tol;
+    const bool l4 = r1 <= eq->sv.tol * eq->eq_pNorm;
+    const bool l5 = itr >= eq->sv.minItr;
+    if (l1 || l2 || ((l3 || l4) && l5)) ok = true;
+    info->last_iNorm = iN;
+    info->r1_last = r1;
+    if (!std::isfinite(iN)) {
+      set_error("Newton: non-finite residual norm");
+      return GSLS_ERR_NAN;
+    }
+  }
+  info->newton_itr = itr;
+  // Ao = An, Yo = Yn and, for equations with displacement, Do = Dn
+  // (Code/Source/svFSI/MAIN.f:277-279): swap the buffers
+  for (int k = 0; k < (eq->dFlag ? 3 : 2); k++) {
+    std::swap(eq->st[k].p, eq->st[k + 3].p);
+    std::swap(eq->st[k].bytes, eq->st[k + 3].bytes);
+  }
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  return GSLS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,185 @@
+// Internal definitions shared by the gsls translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gsls.h"
+
+namespace gsls {
+
+// ---------------------------------------------------------------------------
+// error handling
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define GSLS_CUDA(...)                                                         \
+  do {                                                                         \
+    cudaError_t _e = (__VA_ARGS__);                                                 \
+    if (_e != cudaSuccess) return ::gsls::cuda_fail(_e, #__VA_ARGS__, __FILE__, __LINE__); \
+  } while (0)
+
+#define GSLS_CHECK_LAUNCH()                                                    \
+  do {                                                                         \
+    ::gsls::count_launch();                                                    \
+    cudaError_t _e = cudaGetLastError();                                       \
+    if (_e != cudaSuccess) return ::gsls::cuda_fail(_e, "kernel launch", __FILE__, __LINE__); \
+  } while (0)
+
+#define GSLS_TRY(...)                                                          \
+  do {                                                                         \
+    int _rc = (__VA_ARGS__);                                                        \
+    if (_rc != GSLS_OK) return _rc;                                            \
+  } while (0)
+
+void count_launch();
+int num_sms();
+
+// kernel timing registry (gsls_profile_*)
+bool prof_on();
+void prof_add(const char *name, long long count, double ms);
+// pool of reusable CUDA events
+cudaEvent_t prof_event(int i);
+
+// ---------------------------------------------------------------------------
+// device buffer (RAII, stream-ordered free)
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  int alloc(size_t n);              // no-op if already >= n bytes
+  void release();
+  template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+// ---------------------------------------------------------------------------
+// Krylov scalar block living in device memory (one per solve context).
+struct KrylovScalars {
+  double iNorm, eps, err, errO, alpha, dot, fNorm;
+  double pad0;
+  int done;   // 0 running, 1 converged, 2 max iterations, 3 breakdown/NaN
+  int itr;    // completed iterations
+  int mItr;
+  int suc;
+  // GMRES
+  double h_norm;
+  double pad1[3];
+};
+
+// Face (BC) description, FSILS_faceType.
+struct Face {
+  bool foC = false, coupledFlag = false, sharedFlag = false, incFlag = true;
+  int nNo = 0, dof = 0, bGrp = GSLS_BC_TYPE_DIR;
+  std::vector<int> glob;     // 0-based
+  std::vector<double> val;   // dof x nNo
+  double nS = 0.0, res = 0.0;
+};
+
+// Scratch for reductions and Krylov work vectors.
+struct Workspace {
+  DevBuf partials;    // double[grid * 64]
+  DevBuf ticket;      // unsigned[8]
+  DevBuf scal;        // KrylovScalars
+  DevBuf vec[6];      // Krylov work vectors (X, P, KP, R32...)
+  DevBuf W;           // diag preconditioner (double dof x nNo)
+  DevBuf W2;          // RCS second scaling
+  DevBuf mask;        // Dirichlet mask (double dof x nNo)
+  DevBuf basis;       // GMRES basis (sD+1) vectors
+  DevBuf hcol;        // GMRES Hessenberg column (double)
+  DevBuf io;          // host<->device staging for gsls_solve
+  DevBuf io2;
+  KrylovScalars *h_scal = nullptr;  // pinned host mirror
+  int mask_dof = -1;
+  std::vector<int> mask_key;
+};
+
+}  // namespace gsls
+
+struct gsls_lhs {
+  int gnNo = 0, nNo = 0, nnz = 0, nFaces = 0, mynNo = 0;
+  std::vector<int> h_rowPtr, h_colPtr, h_diagPtr;  // 0-based
+  gsls::DevBuf d_rowPtr, d_colPtr, d_diagPtr, d_rowOf;
+  std::vector<gsls::Face> faces;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int grid = 0;          // fixed reduction grid (deterministic sums)
+  gsls::Workspace ws;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace gsls {
+
+// ---------------------------------------------------------------------------
+// kernel-side helpers
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum; result valid in thread 0. blockDim.x multiple of 32, <= 1024.
+__device__ __forceinline__ double block_sum(double v, double *sh /*[32]*/) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (wid == 0) v = warp_sum(v);
+  return v;
+}
+
+// Deterministic grid reduction of NV values per block.  Every block calls it
+// with its block sums in thread 0 (vals[k]); returns true in exactly one
+// block (the last to arrive), whose thread 0 holds the totals in out[k].
+// The summation order depends only on gridDim.x, so results are bitwise
+// reproducible for a fixed grid.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce_last(const double *vals, double *partials,
+                                                 unsigned *ticket, double *out,
+                                                 double *sh) {
+  __shared__ bool amLast;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) partials[(size_t)k * gridDim.x + blockIdx.x] = vals[k];
+    __threadfence();
+    const unsigned t = atomicAdd(ticket, 1u);
+    amLast = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!amLast) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+      s += __ldcg(&partials[(size_t)k * gridDim.x + i]);
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) out[k] = s;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+  return true;
+}
+
+template <class T> struct VecOf;
+
+}  // namespace gsls
+
+// internal entry points across translation units
+namespace gsls {
+int lhs_prepare_ws(gsls_lhs *lhs, int dof);
+int lhs_update_faces(gsls_lhs *lhs, const int *incL, const double *res);
+int build_dir_mask(gsls_lhs *lhs, int dof);
+int solve_dev(gsls_lhs *lhs, gsls_ls *ls, int dof, double *dRi, void *dVal,
+              int val_prec, int prec);
+int spmv_launch(gsls_lhs *lhs, int dof, const void *dVal, int val_prec,
+                const void *dx, void *dy, int xprec);
+}  // namespace gsls

@@ -1,0 +1,203 @@
+"""Python host side mirroring the svFSILS call surface on top of the gsls
+C ABI (the names follow Code/Source/svFSILS/FSILS_API.h:51-135).
+
+Arrays are numpy; indices passed to the FSILS_* functions are 1-based as in
+the reference.  Every call goes through libgsls.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import (BC_TYPE_DIR, BC_TYPE_NEU, LS_TYPE_BICGS, LS_TYPE_CG, LS_TYPE_GMRES,
+                   LS_TYPE_NS, PREC_FP64, PREC_MIXED, PRECOND_FSILS, PRECOND_RCS, EqParams,
+                   EqSolver, Ls, StepInfo, check)
+
+__all__ = [
+    "FSILS_LHS_CREATE", "FSILS_BC_CREATE", "FSILS_LS_CREATE", "FSILS_SOLVE", "Lhs", "Mesh",
+    "Equation", "LS_TYPE_CG", "LS_TYPE_GMRES", "LS_TYPE_NS", "LS_TYPE_BICGS", "PRECOND_FSILS",
+    "PRECOND_RCS", "BC_TYPE_DIR", "BC_TYPE_NEU", "PREC_FP64", "PREC_MIXED",
+]
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(_lib.c_int_p)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_lib.c_double_p)
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Lhs:
+    """Handle of FSILS_lhsType (gsls_lhs)."""
+
+    def __init__(self, gnNo, nNo, nnz, gNodes, rowPtr, colPtr, nFaces):
+        L = _lib.load()
+        self._keep = [_i32(gNodes), _i32(rowPtr), _i32(colPtr)]
+        h = C.c_void_p()
+        check(L.gsls_lhs_create(C.byref(h), gnNo, nNo, nnz, _ip(self._keep[0]),
+                                _ip(self._keep[1]), _ip(self._keep[2]), nFaces),
+              "FSILS_LHS_CREATE")
+        self.h = h
+        self.nNo, self.nnz, self.nFaces = nNo, nnz, nFaces
+
+    def free(self):
+        if self.h:
+            _lib.load().gsls_lhs_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def FSILS_LHS_CREATE(gnNo, nNo, nnz, gNodes, rowPtr, colPtr, nFaces) -> Lhs:
+    """Code/Source/svFSILS/LHS.f:51 -- rowPtr/colPtr/gNodes 1-based."""
+    return Lhs(gnNo, nNo, nnz, gNodes, rowPtr, colPtr, nFaces)
+
+
+def FSILS_BC_CREATE(lhs: Lhs, faIn, nNo, dof, BC_type, gNodes, Val=None):
+    """Code/Source/svFSILS/BC.f:50 -- faIn and gNodes 1-based, Val(dof,nNo)."""
+    g = _i32(gNodes)
+    v = None if Val is None else _f64(Val)
+    check(_lib.load().gsls_bc_create(lhs.h, faIn, nNo, dof, BC_type, _ip(g),
+                                     _dp(v) if v is not None else None), "FSILS_BC_CREATE")
+
+
+def FSILS_LS_CREATE(LS_type, relTol=None, absTol=None, maxItr=None, dimKry=None,
+                    relTolIn=None, absTolIn=None, maxItrIn=None) -> Ls:
+    """Code/Source/svFSILS/LS.f:50 -- optional arguments as in the reference."""
+    ls = Ls()
+
+    def d(v):
+        return None if v is None else C.byref(C.c_double(v))
+
+    def i(v):
+        return None if v is None else C.byref(C.c_int(v))
+
+    def d2(v):
+        return None if v is None else (C.c_double * 2)(*v)
+
+    def i2(v):
+        return None if v is None else (C.c_int * 2)(*v)
+
+    check(_lib.load().gsls_ls_create(C.byref(ls), LS_type, d(relTol), d(absTol), i(maxItr),
+                                     i(dimKry), d2(relTolIn), d2(absTolIn), i2(maxItrIn)),
+          "FSILS_LS_CREATE")
+    return ls
+
+
+def FSILS_SOLVE(lhs: Lhs, ls: Ls, dof, Ri: np.ndarray, Val: np.ndarray, prec, incL=None,
+                res=None):
+    """Code/Source/svFSILS/SOLVE.f:51 -- Ri(dof,nNo) overwritten with the
+    solution, Val(dof*dof,nnz) left preconditioned (in place)."""
+    assert Ri.dtype == np.float64 and Ri.flags.c_contiguous
+    assert Val.dtype == np.float64 and Val.flags.c_contiguous
+    il = None if incL is None else _i32(incL)
+    rs = None if res is None else _f64(res)
+    check(_lib.load().gsls_solve(lhs.h, C.byref(ls), dof, _dp(Ri), _dp(Val), prec,
+                                 _ip(il) if il is not None else None,
+                                 _dp(rs) if rs is not None else None), "FSILS_SOLVE")
+
+
+class Mesh:
+    """tet4 mesh bound to an Lhs (element -> CSR map + colouring on device)."""
+
+    def __init__(self, lhs: Lhs, ien0: np.ndarray, x: np.ndarray):
+        ien1 = _i32(np.asarray(ien0) + 1)
+        xx = _f64(x)
+        h = C.c_void_p()
+        check(_lib.load().gsls_mesh_create(C.byref(h), lhs.h, ien1.shape[0], 4, _ip(ien1), 3,
+                                           _dp(xx)), "gsls_mesh_create")
+        self.h = h
+        self.lhs = lhs
+        self.nEl = ien1.shape[0]
+
+    @property
+    def ncolors(self) -> int:
+        return _lib.load().gsls_mesh_ncolors(self.h)
+
+    def assemble(self, params: EqParams, Ag, Yg, Dg, dof):
+        """Host-array assembly: returns (R[nNo,dof], Val[nnz,dof*dof])."""
+        nNo, nnz = self.lhs.nNo, self.lhs.nnz
+        R = np.zeros((nNo, dof))
+        Val = np.zeros((nnz, dof * dof))
+        a, y = _f64(Ag), _f64(Yg)
+        d = None if Dg is None else _f64(Dg)
+        check(_lib.load().gsls_assemble(self.h, C.byref(params), _dp(a), _dp(y),
+                                        _dp(d) if d is not None else None, _dp(R), _dp(Val)),
+              "gsls_assemble")
+        return R, Val
+
+    def free(self):
+        if self.h:
+            _lib.load().gsls_mesh_free(self.h)
+            self.h = None
+
+
+class Equation:
+    """Device-resident time integrator of one equation (gsls_eq)."""
+
+    def __init__(self, mesh: Mesh, params: EqParams, solver: EqSolver):
+        h = C.c_void_p()
+        check(_lib.load().gsls_eq_create(C.byref(h), mesh.h, C.byref(params), C.byref(solver)),
+              "gsls_eq_create")
+        self.h = h
+        self.mesh = mesh
+        self.params = params
+        self.nNo = mesh.lhs.nNo
+        self.tDof = params.tDof
+
+    def add_dirichlet(self, nodes0, g, gx=None, mask=0):
+        n1 = _i32(np.asarray(nodes0) + 1)
+        gxa = None if gx is None else _f64(gx)
+        check(_lib.load().gsls_eq_add_dirichlet(self.h, n1.size, _ip(n1),
+                                                _dp(gxa) if gxa is not None else None,
+                                                float(g), int(mask)), "gsls_eq_add_dirichlet")
+
+    def add_traction(self, faces0, h):
+        f1 = _i32(np.asarray(faces0) + 1)
+        hh = _f64(h)
+        check(_lib.load().gsls_eq_add_traction(self.h, f1.shape[0], _ip(f1), _dp(hh)),
+              "gsls_eq_add_traction")
+
+    def set_state(self, Ao, Yo, Do=None):
+        a, y = _f64(Ao), _f64(Yo)
+        d = None if Do is None else _f64(Do)
+        check(_lib.load().gsls_eq_set_state(self.h, _dp(a), _dp(y),
+                                            _dp(d) if d is not None else None),
+              "gsls_eq_set_state")
+
+    def get_state(self):
+        shp = (self.nNo, self.tDof)
+        Ao, Yo, Do = np.zeros(shp), np.zeros(shp), np.zeros(shp)
+        check(_lib.load().gsls_eq_get_state(self.h, _dp(Ao), _dp(Yo), _dp(Do)),
+              "gsls_eq_get_state")
+        return Ao, Yo, Do
+
+    def step(self) -> StepInfo:
+        info = StepInfo()
+        check(_lib.load().gsls_eq_step(self.h, C.byref(info)), "gsls_eq_step")
+        return info
+
+    def set_eparam(self, ep):
+        e = None if ep is None else _f64(ep)
+        check(_lib.load().gsls_eq_set_eparam(self.h, _dp(e) if e is not None else None),
+              "gsls_eq_set_eparam")
+
+    def free(self):
+        if self.h:
+            _lib.load().gsls_eq_free(self.h)
+            self.h = None

@@ -1,0 +1,184 @@
+"""Synthetic problem definitions (seeded; no external data).
+
+Each builder returns a ``Problem``: mesh, CSR, equation parameters,
+boundary conditions and solver settings for one equation, in the reference's
+conventions.  The workloads follow the five benchmark configurations:
+
+* ``heats_cube``   -- unsteady heat equation on a Kuhn-split unit cube
+                      (20^3 hexes -> 48,000 tets, 9,261 nodes at full size).
+* ``struct_beam``  -- neo-Hookean + ST91 elastodynamics of a 4x1x1 beam
+                      (176x44x44 hexes -> 2,044,416 tets, 358,425 nodes).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import meshgen
+from ._lib import (LS_TYPE_CG, PHYS_HEATS, PHYS_STRUCT, PREC_FP64, PRECOND_FSILS, EqParams,
+                   EqSolver)
+
+SEED = 20261203
+
+
+def genalpha(roInf: float, second_order: bool):
+    """F/INITIALIZE.f:76-139: (am, af, beta, gam)."""
+    am = (2.0 - roInf) / (1.0 + roInf) if second_order else 0.5 * (3.0 - roInf) / (1.0 + roInf)
+    af = 1.0 / (1.0 + roInf)
+    beta = 0.25 * (1.0 + am - af) ** 2
+    gam = 0.5 + am - af
+    return am, af, beta, gam
+
+
+@dataclass
+class DirBC:
+    nodes: np.ndarray   # 0-based
+    g: float
+    gx: np.ndarray | None = None
+    mask: int = 0       # 0 = all components
+
+
+@dataclass
+class TracBC:
+    faces: np.ndarray   # (nFel, 3) 0-based
+    h: tuple
+
+
+@dataclass
+class Problem:
+    name: str
+    x: np.ndarray
+    ien: np.ndarray          # (nEl, 4) 0-based
+    rowPtr: np.ndarray       # 0-based
+    colPtr: np.ndarray       # 0-based
+    phys: int
+    dof: int
+    tDof: int
+    params: dict
+    dirichlet: list = field(default_factory=list)
+    traction: list = field(default_factory=list)
+    LS_type: int = LS_TYPE_CG
+    prec: int = PRECOND_FSILS
+    ls_relTol: float = -1.0
+    ls_absTol: float = -1.0
+    ls_mItr: int = -1
+    ls_sD: int = -1
+    minItr: int = 1
+    maxItr: int = 5
+    tol: float = 1e-6
+    absTol: float = 1e-15
+    nsteps: int = 10
+    eparam: np.ndarray | None = None
+
+    @property
+    def nNo(self):
+        return self.x.shape[0]
+
+    @property
+    def nEl(self):
+        return self.ien.shape[0]
+
+    @property
+    def nnz(self):
+        return int(self.colPtr.size)
+
+    def eq_params(self) -> EqParams:
+        p = EqParams()
+        p.phys, p.dof, p.tDof, p.s = self.phys, self.dof, self.tDof, 0
+        for k, v in self.params.items():
+            if k == "fb":
+                for i in range(3):
+                    p.fb[i] = v[i]
+            else:
+                setattr(p, k, v)
+        return p
+
+    def eq_solver(self, precision=PREC_FP64) -> EqSolver:
+        s = EqSolver()
+        s.LS_type, s.prec = self.LS_type, self.prec
+        s.ls_relTol, s.ls_absTol = self.ls_relTol, self.ls_absTol
+        s.ls_mItr, s.ls_sD = self.ls_mItr, self.ls_sD
+        s.ls_relTolIn[0] = s.ls_relTolIn[1] = -1.0
+        s.ls_mItrIn[0] = s.ls_mItrIn[1] = -1
+        s.minItr, s.maxItr, s.tol, s.absTol = self.minItr, self.maxItr, self.tol, self.absTol
+        s.precision = precision
+        return s
+
+    def initial_state(self):
+        z = np.zeros((self.nNo, self.tDof))
+        return z.copy(), z.copy(), z.copy()
+
+    def algorithmic_bytes(self, s_A: int, s_v: int):
+        """Per-call algorithmic bytes of one CG iteration and one assembly
+        (B_cg and B_asm of the design notes)."""
+        nnz, nNo, d = self.nnz, self.nNo, self.dof
+        B_spmv = nnz * (d * d * s_A + 4) + 8 * nNo + 2 * nNo * d * s_v
+        B_cg = nnz * (d * d * s_A + 4) + 8 * nNo + 11 * nNo * d * s_v
+        fields = 3 if self.phys == PHYS_STRUCT else 2
+        B_asm = 16 * self.nEl + 24 * nNo + fields * nNo * self.tDof * 8 + nnz * d * d * s_A + 8 * nNo * d
+        return {"spmv": B_spmv, "cg_iter": B_cg, "assembly": B_asm}
+
+
+def heats_cube(n: int = 20, nsteps: int = 10) -> Problem:
+    """Config: unit cube, n^3 hexes x 6 tets, conductivity 1, source 0,
+    density 1, T=1 at x=0 and T=0 at x=1, T0=0, rho_inf 0.5, dt 0.01,
+    CG + diagonal preconditioner, LS tolerance 1e-10."""
+    x, ien = meshgen.kuhn_box(n, n, n)
+    rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
+    am, af, beta, gam = genalpha(0.5, second_order=False)
+    params = dict(am=am, af=af, beta=beta, gam=gam, dt=0.01, rho=1.0, cond=1.0, src=0.0)
+    left = meshgen.nodes_on_plane(x, 0, 0.0)
+    right = meshgen.nodes_on_plane(x, 0, 1.0)
+    return Problem(name=f"heats_cube_{n}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
+                   phys=PHYS_HEATS, dof=1, tDof=1, params=params,
+                   dirichlet=[DirBC(left, 1.0), DirBC(right, 0.0)],
+                   LS_type=LS_TYPE_CG, prec=PRECOND_FSILS, ls_relTol=1e-10,
+                   minItr=1, maxItr=5, tol=1e-6, nsteps=nsteps)
+
+
+def struct_beam(nx: int = 176, ny: int = 44, nz: int = 44, nsteps: int = 10,
+                E: float = 1e6, nu: float = 0.45, traction=(0.0, 0.0, -1e3),
+                eparam: np.ndarray | None = None) -> Problem:
+    """Config: 4x1x1 beam, nHK + ST91, E=1e6, nu=0.45, rho=1, x=0 clamped,
+    constant traction on x=4, dt=1e-3, Newton tolerance 1e-8, CG + diagonal
+    preconditioner (the reference's default for struct)."""
+    x, ien = meshgen.kuhn_box(nx, ny, nz, 4.0, 1.0, 1.0)
+    rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
+    am, af, beta, gam = genalpha(0.2, second_order=True)
+    mu = E * 0.5 / (1.0 + nu)                    # F/READFILES.f:2662
+    kap = E / (1.0 - 2.0 * nu) / 3.0             # F/READFILES.f:2670
+    params = dict(am=am, af=af, beta=beta, gam=gam, dt=1e-3, rho=1.0, C10=0.5 * mu, Kpen=kap,
+                  visc=0.0, dmp=0.0, fb=(0.0, 0.0, 0.0))
+    clamp = meshgen.nodes_on_plane(x, 0, 0.0)
+    tface = meshgen.faces_on_plane(x, ien, 0, 4.0)
+    return Problem(name=f"struct_beam_{nx}x{ny}x{nz}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
+                   phys=PHYS_STRUCT, dof=3, tDof=3, params=params,
+                   dirichlet=[DirBC(clamp, 0.0)], traction=[TracBC(tface, tuple(traction))],
+                   LS_type=LS_TYPE_CG, prec=PRECOND_FSILS, minItr=1, maxItr=10, tol=1e-8,
+                   nsteps=nsteps, eparam=eparam)
+
+
+def make_lhs_arrays(p: Problem):
+    """1-based rowPtr/colPtr/gNodes for FSILS_LHS_CREATE."""
+    return (np.arange(1, p.nNo + 1, dtype=np.int32), (p.rowPtr + 1).astype(np.int32),
+            (p.colPtr + 1).astype(np.int32))
+
+
+def build_equation(p: Problem, precision=PREC_FP64):
+    """LHS + mesh + equation on the GPU for a Problem."""
+    from .fsils import Equation, Mesh, FSILS_LHS_CREATE
+    g, rp1, cp1 = make_lhs_arrays(p)
+    lhs = FSILS_LHS_CREATE(p.nNo, p.nNo, p.nnz, g, rp1, cp1, max(1, len(p.dirichlet)))
+    mesh = Mesh(lhs, p.ien, p.x)
+    prm = p.eq_params()
+    eq = Equation(mesh, prm, p.eq_solver(precision))
+    if p.eparam is not None:
+        eq.set_eparam(p.eparam)
+    for d in p.dirichlet:
+        eq.add_dirichlet(d.nodes, d.g, d.gx, d.mask)
+    for t in p.traction:
+        eq.add_traction(t.faces, t.h)
+    Ao, Yo, Do = p.initial_state()
+    eq.set_state(Ao, Yo, Do)
+    return lhs, mesh, eq

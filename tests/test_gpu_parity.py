@@ -1,0 +1,193 @@
+"""GPU parity: every kernel path through the C ABI against the oracle on the
+same seeded inputs.
+
+Tolerances (FP64 path): SpMV and assembly 1e-12 relative; one linear solve
+1e-10 relative L2 on the solution; time steps 1e-10 relative L2 on the
+state after N steps.  Mixed path: solution within 1e-8 relative L2 of the
+FP64 oracle (the mixed-precision contract).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from svfsi_gb300 import _lib, fsils, problems
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float).ravel(), np.asarray(b, float).ravel()
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def torch_dev():
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    return torch
+
+
+def _lhs_for(p, nFaces=1):
+    g, rp1, cp1 = problems.make_lhs_arrays(p)
+    return fsils.FSILS_LHS_CREATE(p.nNo, p.nNo, p.nnz, g, rp1, cp1, nFaces)
+
+
+@pytest.mark.parametrize("dof", [1, 2, 3, 4])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_spmv_block_csr(gsls, orc, dof, mixed):
+    torch = torch_dev()
+    p = problems.heats_cube(6)
+    lhs = _lhs_for(p)
+    rng = np.random.default_rng(dof)
+    Val = rng.standard_normal((p.nnz, dof * dof))
+    U = rng.standard_normal((p.nNo, dof))
+    ref = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 0).spmv(dof, Val, U)
+    vt = torch.tensor(Val, dtype=torch.float32 if mixed else torch.float64, device="cuda")
+    ut = torch.tensor(U, dtype=torch.float64, device="cuda")
+    yt = torch.zeros_like(ut)
+    torch.cuda.synchronize()
+    _lib.check(gsls.gsls_spmv_dev(lhs.h, dof, C.c_void_p(vt.data_ptr()),
+                                  _lib.PREC_MIXED if mixed else _lib.PREC_FP64,
+                                  C.c_void_p(ut.data_ptr()), C.c_void_p(yt.data_ptr())))
+    y = yt.cpu().numpy()
+    assert rel(y, ref) < (1e-5 if mixed else 1e-14)
+
+
+def test_dot_norm(gsls, orc):
+    torch = torch_dev()
+    p = problems.heats_cube(5)
+    lhs = _lhs_for(p)
+    rng = np.random.default_rng(0)
+    u, v = rng.standard_normal((p.nNo, 3)), rng.standard_normal((p.nNo, 3))
+    ut = torch.tensor(u, device="cuda")
+    vt = torch.tensor(v, device="cuda")
+    out = C.c_double()
+    _lib.check(gsls.gsls_dot_dev(lhs.h, 3, C.c_void_p(ut.data_ptr()), C.c_void_p(vt.data_ptr()),
+                                 C.byref(out)))
+    assert abs(out.value - float(np.sum(u * v))) < 1e-12 * np.abs(u * v).sum()
+    _lib.check(gsls.gsls_norm_dev(lhs.h, 3, C.c_void_p(ut.data_ptr()), C.byref(out)))
+    assert abs(out.value - np.linalg.norm(u)) < 1e-13 * np.linalg.norm(u)
+
+
+def _assembled_system(p, seed=0):
+    import oracle as O
+    rng = np.random.default_rng(seed)
+    A = 1e-3 * rng.standard_normal((p.nNo, p.tDof))
+    Y = 1e-3 * rng.standard_normal((p.nNo, p.tDof))
+    D = 1e-2 * rng.standard_normal((p.nNo, p.tDof))
+    R, Val = O.assemble(p, A, Y, D)
+    return A, Y, D, R, Val
+
+
+@pytest.mark.parametrize("case", ["heats", "struct"])
+def test_assembly_fp64(gsls, orc, case):
+    p = problems.heats_cube(6) if case == "heats" else problems.struct_beam(8, 3, 3)
+    A, Y, D, R0, V0 = _assembled_system(p)
+    lhs = _lhs_for(p)
+    mesh = fsils.Mesh(lhs, p.ien, p.x)
+    assert mesh.ncolors >= 20
+    R, Val = mesh.assemble(p.eq_params(), A, Y, D, p.dof)
+    assert rel(R, R0) < 1e-12
+    assert rel(Val, V0) < 1e-12
+
+
+def test_assembly_per_element_parameter(gsls, orc):
+    p = problems.struct_beam(4, 2, 2)
+    rng = np.random.default_rng(11)
+    ep = p.params["C10"] * np.exp(0.2 * rng.standard_normal(p.nEl))
+    A, Y, D, _, _ = _assembled_system(p)
+    import oracle as O
+    R0, V0 = O.assemble(p, A, Y, D, eparam=ep)
+    lhs = _lhs_for(p)
+    mesh = fsils.Mesh(lhs, p.ien, p.x)
+    prm = p.eq_params()
+    e = np.ascontiguousarray(ep)
+    prm.eparam = e.ctypes.data_as(_lib.c_double_p)
+    R, Val = mesh.assemble(prm, A, Y, D, p.dof)
+    assert rel(R, R0) < 1e-12 and rel(Val, V0) < 1e-12
+
+
+@pytest.mark.parametrize("case,lstype", [("heats", "cg"), ("heats", "gmres"),
+                                         ("struct", "cg"), ("struct", "gmres")])
+def test_fsils_solve_matches_oracle(gsls, orc, case, lstype):
+    p = problems.heats_cube(6) if case == "heats" else problems.struct_beam(8, 3, 3)
+    _, _, _, R0, V0 = _assembled_system(p, seed=1)
+    d = p.dof
+    dirn = p.dirichlet[0].nodes
+    # product
+    lhs = _lhs_for(p, nFaces=1)
+    fsils.FSILS_BC_CREATE(lhs, 1, dirn.size, 3, fsils.BC_TYPE_DIR, dirn + 1, np.zeros((dirn.size, 3)))
+    t = fsils.LS_TYPE_CG if lstype == "cg" else fsils.LS_TYPE_GMRES
+    kw = dict(relTol=1e-8, maxItr=2000) if lstype == "cg" else dict(relTol=1e-8, maxItr=10, dimKry=40)
+    ls = fsils.FSILS_LS_CREATE(t, **kw)
+    R, Val = R0.copy(), V0.copy()
+    fsils.FSILS_SOLVE(lhs, ls, d, R, Val, fsils.PRECOND_FSILS)
+    # oracle
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
+    s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
+    ols = orc.ls_create(t, relTol=1e-8, mItr=kw["maxItr"], sD=kw.get("dimKry"))
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, d, Ro, Vo, orc.PRECOND_FSILS)
+    assert rel(Val, Vo) < 1e-15
+    assert ls.RI.suc == ols.RI.suc == 1
+    assert abs(ls.RI.iNorm - ols.RI.iNorm) <= 1e-12 * ols.RI.iNorm
+    assert abs(ls.RI.itr - ols.RI.itr) <= 2
+    assert rel(R, Ro) < 1e-7
+    # both satisfy the preconditioned system to the requested tolerance
+    assert ls.RI.fNorm <= 1e-8 * ls.RI.iNorm * 1.0001
+
+
+def test_heats_c1_ten_steps_fp64(gsls, orc):
+    p = problems.heats_cube(20, nsteps=10)
+    lhs, mesh, eq = problems.build_equation(p)
+    oeq = orc.OracleEquation(p)
+    for s in range(p.nsteps):
+        gi = eq.step()
+        oi = oeq.step()
+        assert gi.newton_itr == oi.newton_itr
+    A, Y, D = eq.get_state()
+    Ao, Yo, Do = oeq.state()
+    assert rel(Y, Yo) < 1e-10
+    assert rel(A, Ao) < 1e-8
+
+
+def test_heats_mixed_within_1e8(gsls, orc):
+    p = problems.heats_cube(12, nsteps=5)
+    p.tol = 1e-12
+    p.maxItr = 8
+    lhs, mesh, eq = problems.build_equation(p, precision=fsils.PREC_MIXED)
+    oeq = orc.OracleEquation(p)
+    for s in range(p.nsteps):
+        eq.step()
+        oeq.step()
+    _, Y, _ = eq.get_state()
+    _, Yo, _ = oeq.state()
+    assert rel(Y, Yo) < 1e-8
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_struct_steps(gsls, orc, precision):
+    p = problems.struct_beam(12, 3, 3, nsteps=3)
+    prec = fsils.PREC_FP64 if precision == "fp64" else fsils.PREC_MIXED
+    lhs, mesh, eq = problems.build_equation(p, precision=prec)
+    oeq = orc.OracleEquation(p)
+    for s in range(p.nsteps):
+        gi = eq.step()
+        oeq.step()
+        assert gi.last_suc == 1
+    A, Y, D = eq.get_state()
+    Ao, Yo, Do = oeq.state()
+    tol = 1e-9 if precision == "fp64" else 1e-8
+    assert rel(D, Do) < tol
+    assert rel(Y, Yo) < 10 * tol
+
+
+def test_assembly_and_solve_deterministic(gsls):
+    p = problems.struct_beam(8, 3, 3, nsteps=2)
+    outs = []
+    for _ in range(2):
+        lhs, mesh, eq = problems.build_equation(p)
+        for s in range(p.nsteps):
+            eq.step()
+        outs.append(eq.get_state()[2])
+    assert np.array_equal(outs[0], outs[1])

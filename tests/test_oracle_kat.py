@@ -1,0 +1,249 @@
+"""Known-answer tests pinning the oracle (CPU only).
+
+The reference ships no tests or golden data and cannot be compiled here, so
+the oracle is pinned by mathematics: exact P1 element matrices, the patch
+test, material identities and finite differences, Krylov solves against a
+dense solve, and the gen-alpha closed forms.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from svfsi_gb300 import meshgen, problems
+
+
+def test_kuhn_cube_counts():
+    p = problems.heats_cube(20)
+    assert (p.nNo, p.nEl, p.nnz) == (9261, 48000, 128581)
+    assert meshgen.tet_jacobians(p.x, p.ien).min() > 0
+
+
+def test_kuhn_beam_counts_small():
+    b = problems.struct_beam(8, 2, 2)
+    assert b.nNo == 9 * 3 * 3 and b.nEl == 8 * 2 * 2 * 6
+    assert meshgen.tet_jacobians(b.x, b.ien).min() > 0
+    # traction face covers the x=4 end exactly (area 1)
+    f = b.traction[0].faces
+    x = b.x
+    area = 0.5 * np.linalg.norm(np.cross(x[f[:, 1]] - x[f[:, 0]], x[f[:, 2]] - x[f[:, 0]]), axis=1)
+    assert abs(area.sum() - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("n", [(2, 2, 2), (3, 2, 4)])
+def test_lhsa_equals_sorted_unique(orc, n):
+    x, ien = meshgen.kuhn_box(*n)
+    rng = np.random.default_rng(1)
+    ien = ien[rng.permutation(ien.shape[0])]
+    rp, cp = orc.lhsa(x.shape[0], ien)
+    rp2, cp2 = meshgen.csr_from_ien(x.shape[0], ien)
+    assert np.array_equal(rp, rp2) and np.array_equal(cp, cp2)
+
+
+def _unit_tet():
+    # x1..x4 with det(x1-x4, x2-x4, x3-x4) = 1
+    return np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [0, 0, 0]], dtype=float)
+
+
+def test_p1_laplacian_and_mass_kat(orc):
+    p = problems.heats_cube(1)
+    eqp = orc.eqp_from(p)
+    xl = orc.f64(_unit_tet().ravel())
+    al = np.zeros(4)
+    yl = np.zeros(4)
+    lR = np.zeros(4)
+    lK = np.zeros(16)
+    # conductivity only
+    eqp.rho = 0.0
+    eqp.cond = 2.0
+    orc.load().orc_elem_heats(C.byref(eqp), orc.dp(xl), orc.dp(al), orc.dp(yl), orc.dp(lR), orc.dp(lK))
+    T1 = eqp.af * eqp.gam * eqp.dt
+    G = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [-1, -1, -1]], dtype=float)
+    K = (1.0 / 6.0) * 2.0 * G @ G.T
+    assert np.allclose(lK.reshape(4, 4) / T1, K, rtol=1e-14, atol=1e-15)
+    # mass only: amd * V/20 (1 + delta_ab), amd = am*rho/T1
+    eqp.rho = 1.0
+    eqp.cond = 0.0
+    orc.load().orc_elem_heats(C.byref(eqp), orc.dp(xl), orc.dp(al), orc.dp(yl), orc.dp(lR), orc.dp(lK))
+    M = (1.0 / 6.0) / 20.0 * (np.ones((4, 4)) + np.eye(4))
+    assert np.allclose(lK.reshape(4, 4), eqp.am * M, rtol=1e-13)
+
+
+def test_heats_patch_test(orc):
+    """Linear T = 1 - x with dT/dt = 0 is in the P1 space: the assembled
+    residual vanishes at interior nodes."""
+    p = problems.heats_cube(3)
+    Y = (1.0 - p.x[:, 0]).reshape(-1, 1)
+    A = np.zeros_like(Y)
+    R, Val = orc.assemble(p, A, Y)
+    interior = np.all((p.x > 1e-12) & (p.x < 1 - 1e-12), axis=1)
+    assert np.abs(R[interior]).max() < 1e-14
+    # Val is symmetric (the heat tangent is)
+    n = p.nNo
+    K = np.zeros((n, n))
+    for i in range(n):
+        for j in range(p.rowPtr[i], p.rowPtr[i + 1]):
+            K[i, p.colPtr[j]] = Val[j, 0]
+    assert np.allclose(K, K.T, rtol=0, atol=1e-15)
+
+
+def test_heats_steady_state_kept(orc):
+    """Starting from the steady profile, a time step keeps it (Newton + CG)."""
+    p = problems.heats_cube(4, nsteps=1)
+    eq = orc.OracleEquation(p)
+    Y0 = (1.0 - p.x[:, 0]).reshape(-1, 1)
+    eq.set_state(np.zeros_like(Y0), Y0, np.zeros_like(Y0))
+    eq.step()
+    _, Y, _ = eq.state()
+    assert np.abs(Y - Y0).max() < 1e-9
+
+
+def _pk2(orc, C10, K, F):
+    S = np.zeros(9)
+    Dm = np.zeros(36)
+    orc.load().orc_pk2cc_nhk(C10, K, orc.dp(orc.f64(F.ravel())), orc.dp(S), orc.dp(Dm))
+    return S.reshape(3, 3), Dm.reshape(6, 6)
+
+
+def test_nhk_stress_free_reference(orc):
+    S, Dm = _pk2(orc, 1.7e5, 3.3e6, np.eye(3))
+    assert np.abs(S).max() < 1e-9
+    assert np.allclose(Dm, Dm.T)
+    # small-strain limit: Dm = lambda 1x1 + 2 mu I (mu = 2 C10, lambda = K - 2mu/3)
+    mu, K = 3.4e5, 3.3e6
+    lam = K - 2 * mu / 3
+    ref = np.zeros((6, 6))
+    ref[:3, :3] = lam
+    ref[np.arange(3), np.arange(3)] += 2 * mu
+    ref[np.arange(3, 6), np.arange(3, 6)] = mu
+    assert np.allclose(Dm, ref, rtol=1e-12, atol=1e-6)
+
+
+def test_nhk_tangent_matches_fd(orc):
+    rng = np.random.default_rng(7)
+    C10, K = 1.7e5, 3.3e6
+    F = np.eye(3) + 0.15 * rng.standard_normal((3, 3))
+    _, Dm = _pk2(orc, C10, K, F)
+    voigt = [(0, 0), (1, 1), (2, 2), (0, 1), (1, 2), (2, 0)]
+    for trial in range(4):
+        dF = rng.standard_normal((3, 3))
+        h = 1e-6
+        Sp, _ = _pk2(orc, C10, K, F + h * dF)
+        Sm, _ = _pk2(orc, C10, K, F - h * dF)
+        dS = (Sp - Sm) / (2 * h)
+        dC = F.T @ dF + dF.T @ F
+        dCv = np.array([dC[i, j] * (1 if i == j else 2) for i, j in voigt])
+        pred = 0.5 * Dm @ dCv
+        got = np.array([dS[i, j] for i, j in voigt])
+        assert np.allclose(got, pred, rtol=1e-6, atol=1e-6 * np.abs(pred).max())
+
+
+def _laplace_1d(n):
+    rp = [0]
+    cp = []
+    vals = []
+    for i in range(n):
+        for j in (i - 1, i, i + 1):
+            if 0 <= j < n:
+                cp.append(j)
+                vals.append(2.0 if j == i else -1.0)
+        rp.append(len(cp))
+    return np.array(rp, np.int32), np.array(cp, np.int32), np.array(vals)
+
+
+@pytest.mark.parametrize("lstype", ["cg", "gmres"])
+def test_krylov_1d_laplacian_exact(orc, lstype):
+    n = 40
+    rp, cp, v = _laplace_1d(n)
+    A = np.zeros((n, n))
+    for i in range(n):
+        A[i, cp[rp[i]:rp[i + 1]]] = v[rp[i]:rp[i + 1]]
+    b = np.sin(np.arange(n) + 1.0)
+    s = orc.OracleSolver(n, rp, cp, 0)
+    if lstype == "cg":
+        ls = orc.ls_create(orc.LS_TYPE_CG, relTol=1e-12, mItr=200)
+    else:
+        ls = orc.ls_create(orc.LS_TYPE_GMRES, relTol=1e-12, mItr=4, sD=60)
+    R = b.copy().reshape(n, 1)
+    Val = v.copy().reshape(-1, 1)
+    s.solve(ls, 1, R, Val, orc.PRECOND_FSILS)
+    x = np.linalg.solve(A, b)
+    assert ls.RI.suc == 1
+    assert np.allclose(R.ravel(), x, rtol=1e-9, atol=1e-9)
+    if lstype == "cg":
+        assert ls.RI.itr <= n
+
+
+@pytest.mark.parametrize("roInf", [0.0, 0.2, 0.5, 1.0])
+def test_genalpha_closed_form(orc, roInf):
+    out = [C.c_double() for _ in range(4)]
+    for so in (0, 1):
+        orc.load().orc_genalpha(roInf, so, *[C.byref(o) for o in out])
+        am, af, beta, gam = (o.value for o in out)
+        assert np.allclose((am, af, beta, gam), problems.genalpha(roInf, bool(so)), rtol=1e-15)
+        assert abs(gam - (0.5 + am - af)) < 1e-15
+        assert abs(af - 1 / (1 + roInf)) < 1e-15
+
+
+def test_doassem_equals_dense_assembly(orc):
+    p = problems.struct_beam(2, 1, 1)
+    rng = np.random.default_rng(3)
+    A = 1e-3 * rng.standard_normal((p.nNo, 3))
+    Y = 1e-3 * rng.standard_normal((p.nNo, 3))
+    D = 1e-2 * rng.standard_normal((p.nNo, 3))
+    R, Val = orc.assemble(p, A, Y, D)
+    # dense re-assembly from element matrices
+    n = p.nNo
+    Kd = np.zeros((3 * n, 3 * n))
+    Rd = np.zeros(3 * n)
+    eqp = orc.eqp_from(p)
+    for e in range(p.nEl):
+        nd = p.ien[e]
+        lR = np.zeros(12)
+        lK = np.zeros(144)
+        xl = orc.f64(p.x[nd].ravel())
+        al, yl, dl = (orc.f64(M[nd].ravel()) for M in (A, Y, D))
+        orc.load().orc_elem_struct(C.byref(eqp), 0.0, orc.dp(xl), orc.dp(al), orc.dp(yl),
+                                   orc.dp(dl), orc.dp(lR), orc.dp(lK))
+        for a in range(4):
+            Rd[3 * nd[a]:3 * nd[a] + 3] += lR[3 * a:3 * a + 3]
+            for b in range(4):
+                Kd[3 * nd[a]:3 * nd[a] + 3, 3 * nd[b]:3 * nd[b] + 3] += \
+                    lK[(a * 4 + b) * 9:(a * 4 + b + 1) * 9].reshape(3, 3)
+    Kc = np.zeros_like(Kd)
+    for i in range(n):
+        for j in range(p.rowPtr[i], p.rowPtr[i + 1]):
+            c = p.colPtr[j]
+            Kc[3 * i:3 * i + 3, 3 * c:3 * c + 3] = Val[j].reshape(3, 3)
+    assert np.allclose(Kc, Kd, rtol=1e-13, atol=1e-9)
+    assert np.allclose(R.ravel(), Rd, rtol=1e-13, atol=1e-12)
+
+
+def test_struct_tangent_is_residual_derivative(orc):
+    """The assembled tangent is d(residual)/d(A) through the gen-alpha
+    chain (dD = af*beta*dt^2/am ...) -- checked by central differences."""
+    p = problems.struct_beam(2, 1, 1)
+    rng = np.random.default_rng(5)
+    A0 = 1e-3 * rng.standard_normal((p.nNo, 3))
+    Y0 = 1e-3 * rng.standard_normal((p.nNo, 3))
+    D0 = 1e-2 * rng.standard_normal((p.nNo, 3))
+    prm = p.params
+    am, af, beta, gam, dt = prm["am"], prm["af"], prm["beta"], prm["gam"], prm["dt"]
+    R0, Val = orc.assemble(p, A0, Y0, D0)
+    n = p.nNo
+    Kc = np.zeros((3 * n, 3 * n))
+    for i in range(n):
+        for j in range(p.rowPtr[i], p.rowPtr[i + 1]):
+            c = p.colPtr[j]
+            Kc[3 * i:3 * i + 3, 3 * c:3 * c + 3] = Val[j].reshape(3, 3)
+    dA = rng.standard_normal((p.nNo, 3))
+    h = 1e-4
+
+    def R_at(s):
+        # An += s dA -> Ag += am s dA, Yg += af gam dt s dA, Dg += af beta dt^2 s dA
+        return orc.assemble(p, A0 + am * s * dA, Y0 + af * gam * dt * s * dA,
+                            D0 + af * beta * dt * dt * s * dA)[0]
+
+    fd = (R_at(h) - R_at(-h)).ravel() / (2 * h)
+    pred = am * (Kc @ dA.ravel()) / am  # lK is scaled so that K dA = dR/dAn
+    assert np.allclose(fd, pred, rtol=1e-5, atol=1e-6 * np.abs(pred).max())
