@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--impl", default="gsls", choices=["gsls", "reference"])
     ap.add_argument("--small", action="store_true", help="small mesh (debugging only)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--only", choices=["all", "mixed", "fp64"], default="all",
+                    help="time one precision only (profiling runs)")
     return ap.parse_args()
 
 
@@ -204,6 +206,12 @@ def run_gsls(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    if args.only != "all":
+        r = timed_run(fsils.PREC_MIXED if args.only == "mixed" else fsils.PREC_FP64, profile=True)
+        if rank == 0:
+            print(json.dumps({"only": args.only, "ms_per_step": r["ms"] / K, "newton": r["newton"],
+                              "cg": r["cg"], "prof": r["prof"], "launches": r["launches"]}))
+        return
     clocks = ClockSampler(local)
     clocks.start()
     mixed = timed_run(fsils.PREC_MIXED, profile=True)

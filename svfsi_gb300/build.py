@@ -29,6 +29,7 @@ SOURCES = [
     "gsls_krylov.cu",
     "gsls_assemble.cu",
     "gsls_eq.cu",
+    "gsls_gmres.cu",
 ]
 
 

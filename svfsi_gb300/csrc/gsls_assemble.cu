@@ -41,6 +41,8 @@ constexpr int kAsmThreads = 128;
 struct Tet4Rule {
   double N[4][4];  // N[g][a]
   double w;
+  double M[4][4];  // sum_g N_a(g) N_b(g)
+  double Ns[4];    // sum_g N_a(g)
 };
 __constant__ Tet4Rule c_rule;
 
@@ -56,6 +58,14 @@ static Tet4Rule make_rule() {
     r.N[g][3] = 1.0 - xi[g][0] - xi[g][1] - xi[g][2];
   }
   r.w = 1.0 / 24.0;
+  for (int a = 0; a < 4; a++) {
+    r.Ns[a] = 0.0;
+    for (int b = 0; b < 4; b++) {
+      r.M[a][b] = 0.0;
+      for (int g = 0; g < 4; g++) r.M[a][b] += r.N[g][a] * r.N[g][b];
+    }
+    for (int g = 0; g < 4; g++) r.Ns[a] += r.N[g][a];
+  }
   return r;
 }
 
@@ -175,290 +185,11 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// STRUCT3D with neo-Hookean (GETPK2CC stIso_nHook) + ST91 (GETSVOLP).
-template <class T>
-__device__ __forceinline__ T det3(const T F[3][3]) {
-  return F[0][0] * (F[1][1] * F[2][2] - F[1][2] * F[2][1]) -
-         F[0][1] * (F[1][0] * F[2][2] - F[1][2] * F[2][0]) +
-         F[0][2] * (F[1][0] * F[2][1] - F[1][1] * F[2][0]);
-}
-template <class T>
-__device__ __forceinline__ void inv3(const T A[3][3], T B[3][3]) {
-  const T d = det3(A);
-  B[0][0] = (A[1][1] * A[2][2] - A[1][2] * A[2][1]) / d;
-  B[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) / d;
-  B[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) / d;
-  B[1][0] = (A[1][2] * A[2][0] - A[1][0] * A[2][2]) / d;
-  B[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) / d;
-  B[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) / d;
-  B[2][0] = (A[1][0] * A[2][1] - A[1][1] * A[2][0]) / d;
-  B[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) / d;
-  B[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) / d;
-}
+}  // namespace gsls
 
-__device__ __forceinline__ int vo(int I, int k) {
-  // Voigt pairs 11,22,33,12,23,31 (CCTOVOIGT)
-  const int p0[6] = {0, 1, 2, 0, 1, 2};
-  const int p1[6] = {0, 1, 2, 1, 2, 0};
-  return k == 0 ? p0[I] : p1[I];
-}
+#include "gsls_asm_struct.cuh"
 
-template <class VT>
-__global__ void __launch_bounds__(kAsmThreads) k_asm_struct(AsmArgs A) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= A.nColorEl) return;
-  using AT = VT;  // tangent precision
-  const int e = A.el0 + t;
-  const int4 nd = A.ien[e];
-  const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
-  const int tD = A.tDof, s0 = A.s;
-  double xl[4][3];
-#pragma unroll
-  for (int a = 0; a < 4; a++)
-#pragma unroll
-    for (int i = 0; i < 3; i++) xl[a][i] = A.x[(size_t)n4[a] * 3 + i];
-  double Nx[3][4], Jac;
-  gnn_tet4(xl, Nx, Jac);
-  if (!(Jac != 0.0) || !isfinite(Jac)) atomicOr(A.err, 1);
-
-  // F, velocity gradient, inertia (per Gauss point sums handled below)
-  double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-  double vx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  double ala[4][3], yla[4][3];
-#pragma unroll
-  for (int a = 0; a < 4; a++) {
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const size_t k = (size_t)n4[a] * tD + s0 + c;
-      const double d = A.Dg[k];
-      ala[a][c] = A.Ag[k];
-      yla[a][c] = A.Yg[k];
-#pragma unroll
-      for (int m = 0; m < 3; m++) {
-        F[c][m] += Nx[m][a] * d;
-        vx[c][m] += Nx[m][a] * yla[a][c];
-      }
-    }
-  }
-  const double rho = A.rho, mu = A.visc, dmp = A.dmp;
-  const double afu = A.af * A.beta * A.dt * A.dt;
-  const double afv = A.af * A.gam * A.dt;
-  const double amd = A.am * rho + afv * dmp;
-  const double C10 = A.eparam ? A.eparam[e] : A.C10;
-
-  // ---- material (FP64): J, C, Ci, S_iso, p, pl (GETPK2CC nHK + GETSVOLP)
-  const double J = det3(F);
-  double Fi[3][3];
-  inv3(F, Fi);
-  double C[3][3], Ci[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) C[i][j] = F[0][i] * F[0][j] + F[1][i] * F[1][j] + F[2][i] * F[2][j];
-  inv3(C, Ci);
-  const double J2d = pow(J, -2.0 / 3.0);
-  double p = 0.0, pl = 0.0;
-  if (A.Kpen != 0.0) {
-    p = 0.5 * A.Kpen * (J - 1.0 / J);
-    pl = A.Kpen * J;
-  }
-  const double g1 = 2.0 * C10;
-  const double r1 = J2d * (g1 * (C[0][0] + C[1][1] + C[2][2])) / 3.0;
-  double Siso[3][3], S[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      Siso[i][j] = J2d * (i == j ? g1 : 0.0) - r1 * Ci[i][j];
-      S[i][j] = Siso[i][j] + p * J * Ci[i][j];
-    }
-  // ---- viscous stress (Code/Source/svFSI/STRUCT.f:258-269)
-  double VxFi[3][3], ddev[3][3];
-  const bool visc = (mu != 0.0);
-  if (visc) {
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) VxFi[i][j] = vx[i][0] * Fi[0][j] + vx[i][1] * Fi[1][j] + vx[i][2] * Fi[2][j];
-    double tr = 0.0;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) ddev[i][j] = 0.5 * (VxFi[i][j] + VxFi[j][i]);
-    tr = (ddev[0][0] + ddev[1][1] + ddev[2][2]) / 3.0;
-#pragma unroll
-    for (int i = 0; i < 3; i++) ddev[i][i] -= tr;
-    double tmp[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) tmp[i][j] = ddev[i][0] * Fi[j][0] + ddev[i][1] * Fi[j][1] + ddev[i][2] * Fi[j][2];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++)
-        S[i][j] += 2.0 * mu * J * (Fi[i][0] * tmp[0][j] + Fi[i][1] * tmp[1][j] + Fi[i][2] * tmp[2][j]);
-  }
-  // ---- residual (FP64)
-  double P[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) P[i][j] = F[i][0] * S[0][j] + F[i][1] * S[1][j] + F[i][2] * S[2][j];
-  const double w = c_rule.w * Jac;
-  double lR[4][3];
-#pragma unroll
-  for (int a = 0; a < 4; a++)
-#pragma unroll
-    for (int c = 0; c < 3; c++) lR[a][c] = 0.0;
-#pragma unroll
-  for (int g = 0; g < 4; g++) {
-    double ud[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      ud[c] = -rho * A.fb[c];
-#pragma unroll
-      for (int a = 0; a < 4; a++) ud[c] += c_rule.N[g][a] * (rho * ala[a][c] + dmp * yla[a][c]);
-    }
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int c = 0; c < 3; c++)
-        lR[a][c] += w * (c_rule.N[g][a] * ud[c] + Nx[0][a] * P[c][0] + Nx[1][a] * P[c][1] +
-                         Nx[2][a] * P[c][2]);
-  }
-#pragma unroll
-  for (int a = 0; a < 4; a++)
-#pragma unroll
-    for (int c = 0; c < 3; c++) A.R[(size_t)n4[a] * 3 + c] += lR[a][c];
-
-  // ---- tangent (AT): Dm from CC in closed form
-  AT Cia[3][3], Sia[3][3], Sa[3][3], Fa[3][3], Nxa[3][4];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      Cia[i][j] = AT(Ci[i][j]);
-      Sia[i][j] = AT(Siso[i][j]);
-      Sa[i][j] = AT(S[i][j]);
-      Fa[i][j] = AT(F[i][j]);
-    }
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int a = 0; a < 4; a++) Nxa[i][a] = AT(Nx[i][a]);
-  const AT cA = AT(2.0 * (r1 - p * J));
-  const AT cB = AT(pl * J - 2.0 * r1 / 3.0);
-  const AT c23 = AT(-2.0 / 3.0);
-  AT Dm[6][6];
-#pragma unroll
-  for (int I = 0; I < 6; I++)
-#pragma unroll
-    for (int K = I; K < 6; K++) {
-      const int i = vo(I, 0), j = vo(I, 1), k = vo(K, 0), l = vo(K, 1);
-      const AT v = c23 * (Cia[i][j] * Sia[k][l] + Sia[i][j] * Cia[k][l]) +
-                   cA * (AT(0.5) * (Cia[i][k] * Cia[j][l] + Cia[i][l] * Cia[j][k])) +
-                   cB * (Cia[i][j] * Cia[k][l]);
-      Dm[I][K] = v;
-      Dm[K][I] = v;
-    }
-  const AT Wsum = AT(4.0 * w);            // sum_g w_g
-  const AT afuW = AT(afu) * Wsum;
-  // viscous tangent quantities
-  AT NxFi[4][3], DdNx[4][3], VxNx[4][3], VxFa[3][3];
-  const AT rmu = AT(afu * mu * J), rmv = AT(afv * mu * J);
-  if (visc) {
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-#pragma unroll
-      for (int c = 0; c < 3; c++)
-        NxFi[a][c] = AT(Nx[0][a] * Fi[0][c] + Nx[1][a] * Fi[1][c] + Nx[2][a] * Fi[2][c]);
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        DdNx[a][c] = AT(ddev[c][0]) * NxFi[a][0] + AT(ddev[c][1]) * NxFi[a][1] + AT(ddev[c][2]) * NxFi[a][2];
-        VxNx[a][c] = AT(VxFi[0][c]) * NxFi[a][0] + AT(VxFi[1][c]) * NxFi[a][1] + AT(VxFi[2][c]) * NxFi[a][2];
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) VxFa[i][j] = AT(VxFi[i][j]);
-  }
-  VT *Val = reinterpret_cast<VT *>(A.Val);
-#pragma unroll 1
-  for (int b = 0; b < 4; b++) {
-    // Bm(:,:,b) (Code/Source/svFSI/STRUCT.f:300-318) and DBm = Dm Bm_b
-    AT Bb[6][3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      Bb[0][c] = Nxa[0][b] * Fa[c][0];
-      Bb[1][c] = Nxa[1][b] * Fa[c][1];
-      Bb[2][c] = Nxa[2][b] * Fa[c][2];
-      Bb[3][c] = Nxa[0][b] * Fa[c][1] + Fa[c][0] * Nxa[1][b];
-      Bb[4][c] = Nxa[1][b] * Fa[c][2] + Fa[c][1] * Nxa[2][b];
-      Bb[5][c] = Nxa[2][b] * Fa[c][0] + Fa[c][2] * Nxa[0][b];
-    }
-    AT DB[6][3];
-#pragma unroll
-    for (int I = 0; I < 6; I++)
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        AT acc = AT(0);
-#pragma unroll
-        for (int K = 0; K < 6; K++) acc += Dm[I][K] * Bb[K][c];
-        DB[I][c] = acc;
-      }
-    AT SNxb[3];
-#pragma unroll
-    for (int m = 0; m < 3; m++) SNxb[m] = Sa[m][0] * Nxa[0][b] + Sa[m][1] * Nxa[1][b] + Sa[m][2] * Nxa[2][b];
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-      AT Ba[6][3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        Ba[0][c] = Nxa[0][a] * Fa[c][0];
-        Ba[1][c] = Nxa[1][a] * Fa[c][1];
-        Ba[2][c] = Nxa[2][a] * Fa[c][2];
-        Ba[3][c] = Nxa[0][a] * Fa[c][1] + Fa[c][0] * Nxa[1][a];
-        Ba[4][c] = Nxa[1][a] * Fa[c][2] + Fa[c][1] * Nxa[2][a];
-        Ba[5][c] = Nxa[2][a] * Fa[c][0] + Fa[c][2] * Nxa[0][a];
-      }
-      const AT NxSNx = Nxa[0][a] * SNxb[0] + Nxa[1][a] * SNxb[1] + Nxa[2][a] * SNxb[2];
-      double Mab = 0.0;
-#pragma unroll
-      for (int g = 0; g < 4; g++) Mab += w * c_rule.N[g][a] * c_rule.N[g][b];
-      const AT T1 = AT(amd * Mab) + afuW * NxSNx;
-      AT blk[9];
-#pragma unroll
-      for (int r = 0; r < 3; r++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          AT BmDBm = AT(0);
-#pragma unroll
-          for (int I = 0; I < 6; I++) BmDBm += Ba[I][r] * DB[I][c];
-          AT v = afuW * BmDBm + ((r == c) ? T1 : AT(0));
-          if (visc) {
-            const AT NxNx = NxFi[a][0] * NxFi[b][0] + NxFi[a][1] * NxFi[b][1] + NxFi[a][2] * NxFi[b][2];
-            AT Tv = (AT(2) * (DdNx[a][r] * NxFi[b][c] - DdNx[b][r] * NxFi[a][c]) -
-                     (NxNx * VxFa[r][c] + NxFi[b][r] * VxNx[a][c] - AT(2.0 / 3.0) * NxFi[a][r] * VxNx[b][c])) *
-                    rmu;
-            if (r == c)
-              Tv += (AT(1.0 / 3.0) * NxFi[a][r] * NxFi[b][r] + NxNx) * rmv;
-            else
-              Tv += (NxFi[a][c] * NxFi[b][r] - AT(2.0 / 3.0) * NxFi[a][r] * NxFi[b][c]) * rmv;
-            v += Wsum * Tv;
-          }
-          blk[r * 3 + c] = v;
-        }
-      const int4 m4 = A.map[(size_t)e * 4 + a];
-      const int pos = (b == 0) ? m4.x : (b == 1) ? m4.y : (b == 2) ? m4.z : m4.w;
-      VT *dst = Val + (size_t)pos * 9;
-#pragma unroll
-      for (int k = 0; k < 9; k++) dst[k] += VT(blk[k]);
-    }
-  }
-}
+namespace gsls {
 
 // ---------------------------------------------------------------------------
 static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *Ag,

@@ -1,0 +1,378 @@
+// Restarted GMRES (GMRESS/GMRESV, Code/Source/svFSILS/GMRES.f:171-431):
+// classical Gram-Schmidt with one batched multi-dot per Arnoldi step and the
+// Pythagorean norm (GMRES.f:116-126), Givens rotations (GMRES.f:130-141),
+// back-substitution (GMRES.f:149-155).  Basis vectors in the Krylov vector
+// type (FP32 in mixed mode); Hessenberg matrix, Givens data and every
+// cross-block sum in FP64.  The Arnoldi loop runs device-resident: the
+// Givens kernel sets a device flag and the host polls it once per batch.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "gsls_internal.cuh"
+#include "gsls_spmv.cuh"
+
+namespace gsls {
+
+constexpr int kT = 256;
+
+struct GmresCtl {
+  double eps;   // max(absTol, relTol*iNorm)
+  double pad;
+  int i;        // next Arnoldi column (1-based)
+  int done;     // inner loop finished
+  int conv;     // converged (suc)
+  int last_i;   // last column built in this restart
+  int nan;
+  int pad2;
+};
+
+// u1 = R - u1 (sub) or R, norm -> *outNorm
+template <class XT>
+__global__ void __launch_bounds__(kT) k_gm_residual(size_t n, const XT *__restrict__ R,
+                                                    XT *__restrict__ u1, int sub, double *partials,
+                                                    unsigned *ticket, double *outNorm) {
+  __shared__ double sh[32];
+  __shared__ XT sha[32];
+  XT acc = XT(0);
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const XT v = sub ? XT(R[k] - u1[k]) : R[k];
+    u1[k] = v;
+    acc = fma(v, v, acc);
+  }
+  double bs = double(block_sum_t<XT>(acc, sha));
+  double tot;
+  if (grid_reduce_last<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0)
+    *outNorm = sqrt(tot);
+}
+
+template <class XT>
+__global__ void k_gm_scale(size_t n, XT *__restrict__ u, const double *normp) {
+  const XT inv = XT(1.0 / *normp);
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    u[k] = u[k] * inv;
+}
+
+// SpMV that is skipped once the Arnoldi loop is done
+template <int D, class VT, class XT>
+__global__ void __launch_bounds__(kT) k_gm_spmv(int nNo, const int *__restrict__ rowPtr,
+                                                const int *__restrict__ colPtr,
+                                                const VT *__restrict__ Val,
+                                                const XT *__restrict__ x, XT *__restrict__ y,
+                                                const GmresCtl *ctl) {
+  if (*(volatile const int *)&ctl->done) return;
+  using AT = typename AccOf<VT>::T;
+  constexpr int RPW = 32 / D;
+  const int lane = threadIdx.x & 31, grp = lane / D, r = lane - grp * D;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  GatherX<D, XT, AT> g{x};
+  for (int base = warp * RPW; base < nNo; base += nwarps * RPW) {
+    const int i = base + grp;
+    if (grp < RPW && i < nNo)
+      y[(size_t)i * D + r] = XT(spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, g));
+  }
+}
+
+// h_j = u_j . v, j = 0..nvec-1; warp w of a block owns j = w, w+8, ...; one
+// FP64 partial per (j, block).
+template <class XT>
+__global__ void __launch_bounds__(kT) k_gm_multidot(size_t n, const XT *__restrict__ basis,
+                                                    size_t ld, int nvec, const XT *__restrict__ v,
+                                                    double *partials, const GmresCtl *ctl) {
+  if (*(volatile const int *)&ctl->done) return;
+  const size_t per = (n + gridDim.x - 1) / gridDim.x;
+  const size_t s = (size_t)blockIdx.x * per;
+  const size_t e = s + per < n ? s + per : n;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = wid; j < nvec; j += nw) {
+    const XT *__restrict__ u = basis + ld * j;
+    XT acc = XT(0);
+    for (size_t k = s + lane; k < e; k += 32) acc = fma(u[k], v[k], acc);
+    double a = double(acc);
+    a = warp_sum(a);
+    if (lane == 0) partials[(size_t)j * gridDim.x + blockIdx.x] = a;
+  }
+}
+
+// Column sums of the multi-dot partials: one block per j (deterministic).
+__global__ void k_gm_colsum(int grid, const double *partials, double *h, const GmresCtl *ctl) {
+  if (*(volatile const int *)&ctl->done) return;
+  __shared__ double sh[32];
+  const int j = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < grid; b += blockDim.x) s += partials[(size_t)j * grid + b];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) h[j] = s;
+}
+
+// Pythagorean norm + Givens rotation for column i (1-based), one thread.
+// hraw[0..i] receives the unrotated column for the Gram-Schmidt update.
+__global__ void k_gm_givens(int sD, double *H, const double *hcol, double *hraw, double *c,
+                            double *s, double *err, GmresCtl *ctl) {
+  if (ctl->done) return;
+  const int i = ctl->i;
+  double *h = H + (size_t)(i - 1) * (sD + 1);
+  for (int j = 0; j <= i; j++) h[j] = hcol[j];
+  for (int j = 0; j < i; j++) {
+    hraw[j] = h[j];
+    h[i] = h[i] - h[j] * h[j];
+  }
+  h[i] = sqrt(fabs(h[i]));
+  hraw[i] = h[i];
+  for (int j = 1; j <= i - 1; j++) {
+    const double tmp = c[j - 1] * h[j - 1] + s[j - 1] * h[j];
+    h[j] = -s[j - 1] * h[j - 1] + c[j - 1] * h[j];
+    h[j - 1] = tmp;
+  }
+  const double tmp = sqrt(h[i - 1] * h[i - 1] + h[i] * h[i]);
+  c[i - 1] = h[i - 1] / tmp;
+  s[i - 1] = h[i] / tmp;
+  h[i - 1] = tmp;
+  h[i] = 0.0;
+  err[i] = -s[i - 1] * err[i - 1];
+  err[i - 1] = c[i - 1] * err[i - 1];
+  ctl->last_i = i;
+  if (!isfinite(err[i]) || !isfinite(hraw[i]) || hraw[i] == 0.0) {
+    // breakdown: h(i+1,i) = 0 or non-finite
+    ctl->nan = (!isfinite(err[i]) || !isfinite(hraw[i])) ? 1 : 0;
+    ctl->conv = ctl->nan ? 0 : 1;
+    ctl->done = 1;
+  } else if (fabs(err[i]) < ctl->eps) {
+    ctl->conv = 1;
+    ctl->done = 1;
+  }
+  ctl->i = i + 1;
+  if (i >= sD) ctl->done = 1;
+}
+
+// u_{i+1} = (u_{i+1} - sum_j hraw_j u_j) / hraw_i
+template <class XT>
+__global__ void __launch_bounds__(kT) k_gm_orth(size_t n, XT *__restrict__ basis, size_t ld,
+                                                const double *__restrict__ hraw,
+                                                const GmresCtl *ctl, int i_expected) {
+  if (ctl->last_i != i_expected || ctl->nan || hraw[i_expected] == 0.0) return;
+  const int i = i_expected;
+  __shared__ XT hs[512];
+  for (int j = threadIdx.x; j < i && j < 512; j += blockDim.x) hs[j] = XT(hraw[j]);
+  __syncthreads();
+  XT *__restrict__ v = basis + ld * i;
+  const XT inv = XT(1.0 / hraw[i]);
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    XT acc = v[k];
+    for (int j = 0; j < i; j++) acc = fma(-hs[j], basis[ld * j + k], acc);
+    v[k] = acc * inv;
+  }
+}
+
+// Back substitution y = H(1:i,1:i)^-1 err(1:i), one thread.
+__global__ void k_gm_backsub(int sD, const double *H, const double *err, double *y,
+                             const GmresCtl *ctl) {
+  int i = ctl->last_i;
+  if (i > sD) i = sD;
+  for (int j = 0; j < i; j++) y[j] = err[j];
+  for (int j = i; j >= 1; j--) {
+    for (int k = j + 1; k <= i; k++) y[j - 1] -= H[(size_t)(k - 1) * (sD + 1) + (j - 1)] * y[k - 1];
+    y[j - 1] /= H[(size_t)(j - 1) * (sD + 1) + (j - 1)];
+  }
+}
+
+// X += sum_j y_j u_j
+template <class XT>
+__global__ void __launch_bounds__(kT) k_gm_update_x(size_t n, XT *__restrict__ X,
+                                                    const XT *__restrict__ basis, size_t ld,
+                                                    const double *__restrict__ y,
+                                                    const GmresCtl *ctl) {
+  const int i = ctl->last_i;
+  __shared__ XT ys[512];
+  for (int j = threadIdx.x; j < i && j < 512; j += blockDim.x) ys[j] = XT(y[j]);
+  __syncthreads();
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    XT acc = X[k];
+    for (int j = 0; j < i; j++) acc = fma(ys[j], basis[ld * j + k], acc);
+    X[k] = acc;
+  }
+}
+
+template <class XT>
+__global__ void k_to_xt(size_t n, const double *__restrict__ a, XT *__restrict__ b) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    b[k] = XT(a[k]);
+}
+
+template <class XT>
+__global__ void k_scale_out_g(size_t n, double *__restrict__ Rout, const XT *__restrict__ X,
+                              const double *__restrict__ W) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    Rout[k] = W[k] * double(X[k]);
+}
+
+__global__ void __launch_bounds__(kT) k_norm2(size_t n, const double *__restrict__ u,
+                                              double *out, double *partials, unsigned *ticket) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    acc += u[k] * u[k];
+  double bs = block_sum(acc, sh);
+  double tot;
+  if (grid_reduce_last<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) *out = tot;
+}
+
+__global__ void k_vmul(size_t n, double *__restrict__ R, const double *__restrict__ W) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    R[k] *= W[k];
+}
+
+template <int D, class VT, class XT>
+static int gmres_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const double *Wc) {
+  cudaStream_t st = lhs->stream;
+  Workspace &ws = lhs->ws;
+  const int nNo = lhs->nNo, sD = ls->sD;
+  if (sD < 1 || sD > 512) {
+    set_error("GMRES: Krylov space dimension must be in [1, 512]");
+    return GSLS_ERR_ARG;
+  }
+  const size_t nv = (size_t)nNo * D;
+  const size_t ld = (nv + 31) & ~(size_t)31;
+  GSLS_TRY(ws.basis.alloc(sizeof(XT) * ld * (size_t)(sD + 1)));
+  const int G = lhs->grid;
+  const int Gd = num_sms() * 2;
+  const size_t hbytes = sizeof(double) * ((size_t)(sD + 1) * sD + 6 * (sD + 2)) + 64;
+  GSLS_TRY(ws.hcol.alloc(hbytes + sizeof(GmresCtl) + 64));
+  GSLS_TRY(ws.partials.alloc(sizeof(double) * (size_t)(sD + 2) * (Gd > G ? Gd : G) + 64));
+  double *H = ws.hcol.as<double>();
+  double *hcol = H + (size_t)(sD + 1) * sD;
+  double *hraw = hcol + (sD + 2);
+  double *cc = hraw + (sD + 2);
+  double *ss = cc + (sD + 2);
+  double *err = ss + (sD + 2);
+  double *y = err + (sD + 2);
+  GmresCtl *ctl = reinterpret_cast<GmresCtl *>(y + (sD + 2));
+  XT *basis = ws.basis.as<XT>();
+  XT *X = ws.vec[0].as<XT>(), *Rk = ws.vec[3].as<XT>();
+  double *part = ws.partials.as<double>();
+  unsigned *tk = ws.ticket.as<unsigned>();
+  double *dnorm = ws.scal.as<double>();
+
+  auto t0 = std::chrono::steady_clock::now();
+  ls->suc = 0;
+  k_norm2<<<G, kT, 0, st>>>(nv, R, dnorm, part, tk);
+  GSLS_CHECK_LAUNCH();
+  double n2;
+  GSLS_CUDA(cudaMemcpyAsync(&n2, dnorm, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  double eps = sqrt(n2);
+  ls->iNorm = eps;
+  ls->fNorm = eps;
+  eps = fmax(ls->absTol, ls->relTol * eps);
+  ls->itr = 0;
+  if (!std::isfinite(n2)) {
+    set_error("GMRES: NaN/Inf in the right-hand side");
+    return GSLS_ERR_NAN;
+  }
+  if (ls->iNorm <= ls->absTol) {
+    // the reference returns with R untouched (GMRES.f:310-314); SOLVE then
+    // applies R = Wc*R
+    ls->callD = 2.220446049250313e-16;
+    ls->dB = 0.0;
+    k_vmul<<<G, kT, 0, st>>>(nv, R, Wc);
+    GSLS_CHECK_LAUNCH();
+    GSLS_CUDA(cudaStreamSynchronize(st));
+    return GSLS_OK;
+  }
+  k_to_xt<XT><<<G, kT, 0, st>>>(nv, R, Rk);
+  GSLS_CHECK_LAUNCH();
+  GSLS_CUDA(cudaMemsetAsync(X, 0, sizeof(XT) * nv, st));
+  GmresCtl hc;
+  for (int l = 1; l <= ls->mItr; l++) {
+    ls->dB = ls->fNorm;
+    ls->itr++;
+    XT *u1 = basis;
+    memset(&hc, 0, sizeof(hc));
+    hc.eps = eps;
+    hc.i = 1;
+    GSLS_CUDA(cudaMemcpyAsync(ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+    if (l > 1) {
+      k_gm_spmv<D, VT, XT><<<G, kT, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
+                                             lhs->d_colPtr.as<int>(), Val, X, u1, ctl);
+      GSLS_CHECK_LAUNCH();
+    }
+    k_gm_residual<XT><<<G, kT, 0, st>>>(nv, Rk, u1, l > 1 ? 1 : 0, part, tk, err);
+    GSLS_CHECK_LAUNCH();
+    k_gm_scale<XT><<<G, kT, 0, st>>>(nv, u1, err);
+    GSLS_CHECK_LAUNCH();
+    int i_next = 1, batch = 4;
+    bool inner_done = false;
+    while (!inner_done) {
+      for (int b = 0; b < batch && i_next <= sD; b++, i_next++) {
+        const int i = i_next;
+        XT *ui = basis + ld * (i - 1), *ui1 = basis + ld * i;
+        k_gm_spmv<D, VT, XT><<<G, kT, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
+                                               lhs->d_colPtr.as<int>(), Val, ui, ui1, ctl);
+        GSLS_CHECK_LAUNCH();
+        k_gm_multidot<XT><<<Gd, kT, 0, st>>>(nv, basis, ld, i + 1, ui1, part, ctl);
+        GSLS_CHECK_LAUNCH();
+        k_gm_colsum<<<i + 1, kT, 0, st>>>(Gd, part, hcol, ctl);
+        GSLS_CHECK_LAUNCH();
+        k_gm_givens<<<1, 1, 0, st>>>(sD, H, hcol, hraw, cc, ss, err, ctl);
+        GSLS_CHECK_LAUNCH();
+        k_gm_orth<XT><<<G, kT, 0, st>>>(nv, basis, ld, hraw, ctl, i);
+        GSLS_CHECK_LAUNCH();
+      }
+      GSLS_CUDA(cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, st));
+      GSLS_CUDA(cudaStreamSynchronize(st));
+      if (hc.done || i_next > sD) inner_done = true;
+      if (batch < 16) batch *= 2;
+    }
+    if (hc.nan) {
+      set_error("GMRES: NaN/Inf in the Arnoldi process");
+      return GSLS_ERR_NAN;
+    }
+    ls->itr += hc.last_i;
+    k_gm_backsub<<<1, 1, 0, st>>>(sD, H, err, y, ctl);
+    GSLS_CHECK_LAUNCH();
+    k_gm_update_x<XT><<<G, kT, 0, st>>>(nv, X, basis, ld, y, ctl);
+    GSLS_CHECK_LAUNCH();
+    double errv;
+    GSLS_CUDA(cudaMemcpyAsync(&errv, err + hc.last_i, sizeof(double), cudaMemcpyDeviceToHost, st));
+    GSLS_CUDA(cudaStreamSynchronize(st));
+    ls->fNorm = fabs(errv);
+    if (hc.conv) {
+      ls->suc = 1;
+      break;
+    }
+  }
+  k_scale_out_g<XT><<<G, kT, 0, st>>>(nv, R, X, Wc);
+  GSLS_CHECK_LAUNCH();
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  ls->dB = 10.0 * log(ls->fNorm / ls->dB);
+  ls->callD = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return GSLS_OK;
+}
+
+int gmres_run(gsls_lhs *lhs, gsls_sub_ls *ls, int D, bool mixed, const void *Val, double *R,
+              const double *Wc) {
+#define GSLS_GM_CASE(DV)                                                                   \
+  case DV:                                                                                 \
+    return mixed ? gmres_t<DV, float, float>(lhs, ls, (const float *)Val, R, Wc)           \
+                 : gmres_t<DV, double, double>(lhs, ls, (const double *)Val, R, Wc);
+  switch (D) {
+    GSLS_GM_CASE(1)
+    GSLS_GM_CASE(2)
+    GSLS_GM_CASE(3)
+    GSLS_GM_CASE(4)
+    default:
+      return GSLS_ERR_UNSUPPORTED;
+  }
+#undef GSLS_GM_CASE
+}
+
+}  // namespace gsls

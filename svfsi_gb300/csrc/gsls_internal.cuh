@@ -36,6 +36,7 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
   } while (0)
 
 void count_launch();
+void count_launch_n(int n);
 int num_sms();
 
 // kernel timing registry (gsls_profile_*)
@@ -62,7 +63,7 @@ struct DevBuf {
 // Krylov scalar block living in device memory (one per solve context).
 struct KrylovScalars {
   double iNorm, eps, err, errO, alpha, dot, fNorm;
-  double pad0;
+  double beta;
   int done;   // 0 running, 1 converged, 2 max iterations, 3 breakdown/NaN
   int itr;    // completed iterations
   int mItr;
@@ -81,8 +82,23 @@ struct Face {
   double nS = 0.0, res = 0.0;
 };
 
+// Identity of a captured CG batch graph (kernel arguments baked in).
+struct GraphKey {
+  int D, vsz, xsz;
+  const void *val;
+  const void *x;
+  int batch, nNo;
+  bool operator==(const GraphKey &o) const {
+    return D == o.D && vsz == o.vsz && xsz == o.xsz && val == o.val && x == o.x &&
+           batch == o.batch && nNo == o.nNo;
+  }
+};
+
 // Scratch for reductions and Krylov work vectors.
 struct Workspace {
+  DevBuf Wf;          // float copy of W (FP32 scaling pass)
+  cudaGraphExec_t cg_graph = nullptr;
+  GraphKey cg_key{};
   DevBuf partials;    // double[grid * 64]
   DevBuf ticket;      // unsigned[8]
   DevBuf scal;        // KrylovScalars
@@ -182,4 +198,7 @@ int solve_dev(gsls_lhs *lhs, gsls_ls *ls, int dof, double *dRi, void *dVal,
               int val_prec, int prec);
 int spmv_launch(gsls_lhs *lhs, int dof, const void *dVal, int val_prec,
                 const void *dx, void *dy, int xprec);
+// restarted GMRES on the preconditioned system (gsls_gmres.cu)
+int gmres_run(gsls_lhs *lhs, gsls_sub_ls *ls, int D, bool mixed, const void *Val,
+              double *R, const double *Wc);
 }  // namespace gsls

@@ -23,6 +23,7 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
 }
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launch_n(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 struct ProfEntry {
   long long count = 0;
@@ -113,6 +114,7 @@ int lhs_prepare_ws(gsls_lhs *lhs, int dof) {
   for (int k = 0; k < 6; k++) GSLS_TRY(ws.vec[k].alloc(sizeof(double) * nv));
   GSLS_TRY(ws.W.alloc(sizeof(double) * nv));
   GSLS_TRY(ws.W2.alloc(sizeof(double) * nv));
+  GSLS_TRY(ws.Wf.alloc(sizeof(float) * nv));
   GSLS_TRY(ws.mask.alloc(sizeof(double) * nv));
   if (!ws.h_scal) {
     GSLS_CUDA(cudaMallocHost(&ws.h_scal, sizeof(KrylovScalars)));
@@ -313,6 +315,7 @@ int gsls_lhs_free(gsls_lhs *lhs) {
   if (!lhs) return GSLS_ERR_ARG;
   if (lhs->stream) cudaStreamSynchronize(lhs->stream);
   if (lhs->ws.h_scal) cudaFreeHost(lhs->ws.h_scal);
+  if (lhs->ws.cg_graph) cudaGraphExecDestroy(lhs->ws.cg_graph);
   if (lhs->ev0) cudaEventDestroy(lhs->ev0);
   if (lhs->ev1) cudaEventDestroy(lhs->ev1);
   cudaStream_t s = lhs->own_stream ? lhs->stream : nullptr;

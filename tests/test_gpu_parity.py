@@ -191,3 +191,33 @@ def test_assembly_and_solve_deterministic(gsls):
             eq.step()
         outs.append(eq.get_state()[2])
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("lstype", ["cg", "gmres"])
+@pytest.mark.parametrize("case", ["heats", "struct"])
+def test_solve_dev_mixed_fp32_inner(gsls, orc, case, lstype):
+    """FP32 matrix values and FP32 inner Krylov through gsls_solve_dev: the
+    solution agrees with the FP64 oracle to the inner tolerance."""
+    torch = torch_dev()
+    p = problems.heats_cube(6) if case == "heats" else problems.struct_beam(8, 3, 3)
+    _, _, _, R0, V0 = _assembled_system(p, seed=2)
+    d = p.dof
+    dirn = p.dirichlet[0].nodes
+    lhs = _lhs_for(p, nFaces=1)
+    fsils.FSILS_BC_CREATE(lhs, 1, dirn.size, 3, fsils.BC_TYPE_DIR, dirn + 1, np.zeros((dirn.size, 3)))
+    t = fsils.LS_TYPE_CG if lstype == "cg" else fsils.LS_TYPE_GMRES
+    kw = dict(relTol=1e-5, maxItr=3000) if lstype == "cg" else dict(relTol=1e-5, maxItr=20, dimKry=50)
+    ls = fsils.FSILS_LS_CREATE(t, **kw)
+    Rt = torch.tensor(R0, dtype=torch.float64, device="cuda")
+    Vt = torch.tensor(V0, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    _lib.check(gsls.gsls_solve_dev(lhs.h, C.byref(ls), d, C.c_void_p(Rt.data_ptr()),
+                                   C.c_void_p(Vt.data_ptr()), _lib.PREC_MIXED,
+                                   fsils.PRECOND_FSILS, None, None))
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
+    s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
+    ols = orc.ls_create(orc.LS_TYPE_CG, relTol=1e-12, mItr=5000)
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, d, Ro, Vo, orc.PRECOND_FSILS)
+    assert ls.RI.suc == 1
+    assert rel(Rt.cpu().numpy(), Ro) < 1e-3
