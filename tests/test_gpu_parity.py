@@ -243,4 +243,13 @@ def test_solve_dev_mixed_fp32_inner(gsls, orc, case, lstype):
     Ro, Vo = R0.copy(), V0.copy()
     s.solve(ols, d, Ro, Vo, orc.PRECOND_FSILS)
     assert ls.RI.suc == 1
-    assert rel(Rt.cpu().numpy(), Ro) < 1e-3
+    x = Rt.cpu().numpy()
+    # true FP64 residual of the Dirichlet-reduced system (free rows/columns)
+    free = np.ones(p.nNo, bool)
+    free[dirn] = False
+    assert np.all(x[~free] == 0.0)
+    Kx = s.spmv(d, V0, x)
+    r = (R0 - Kx)[free]
+    assert np.linalg.norm(r) < 1e-4 * np.linalg.norm(R0[free])
+    if lstype == "cg":
+        assert rel(x, Ro) < 1e-3
