@@ -156,11 +156,13 @@ def run_gsls(args):
             import torch.distributed as dist
             dist.barrier()
 
-    def timed_run(precision, profile=False):
+    def timed_run(precision, profile=False, nsteps=None, nwarm=None):
+        nK = K if nsteps is None else nsteps
+        nW = W if nwarm is None else nwarm
         lhs, mesh, eq = problems.build_equation(p, precision=precision)
         stream = torch.cuda.ExternalStream(L.gsls_get_stream(lhs.h))
         infos = []
-        for _ in range(W):
+        for _ in range(nW):
             infos.append(eq.step())
         barrier()
         torch.cuda.synchronize()
@@ -171,7 +173,7 @@ def run_gsls(args):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
         timed = []
-        for _ in range(K):
+        for _ in range(nK):
             timed.append(eq.step())
         ev1.record(stream)
         ev1.synchronize()
@@ -214,9 +216,12 @@ def run_gsls(args):
         return
     clocks = ClockSampler(local)
     clocks.start()
-    mixed = timed_run(fsils.PREC_MIXED, profile=True)
+    mixed = timed_run(fsils.PREC_MIXED)
     clk = clocks.stop()
     fp64 = timed_run(fsils.PREC_FP64)
+    # kernel-level timing (CUDA events around every CG SpMV) in a separate,
+    # shorter run so that the headline numbers carry no event overhead
+    profd = timed_run(fsils.PREC_MIXED, profile=True, nsteps=2, nwarm=1)
     ms_mixed = max_over_ranks(mixed["ms"]) / K
     ms_fp64 = max_over_ranks(fp64["ms"]) / K
     D_m, D_f = mixed["state"][2], fp64["state"][2]
@@ -247,7 +252,7 @@ def run_gsls(args):
     state_bytes = 3 * p.nNo * p.tDof * 8
 
     # roofline of the dominant kernel (CG SpMV + fused dot, FP32 values)
-    cnt, tot_ms = mixed["prof"]["cg_spmv"]
+    cnt, tot_ms = profd["prof"]["cg_spmv"]
     peak, peak_kind = peaks()
     B = p.algorithmic_bytes(4, 4)["spmv"]
     avg_s = (tot_ms / max(cnt, 1)) / 1e3

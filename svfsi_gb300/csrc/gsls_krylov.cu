@@ -267,23 +267,38 @@ static int wait_scalars(gsls_lhs *lhs) {
   return GSLS_OK;
 }
 
+// Grid of a grid-stride kernel: exactly the resident blocks on all SMs (one
+// wave), capped by the lhs reduction grid; fixed per kernel and device, so
+// its reductions stay reproducible.
+template <class K>
+static int resident_grid(K kernel, int cap) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kThreads, 0);
+  if (nb < 1) nb = 1;
+  int g = nb * num_sms();
+  return g < cap ? g : cap;
+}
+
 template <int D, class VT, class XT>
 static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter, bool prof,
                       int ev_base) {
   cudaStream_t st = lhs->stream;
   Workspace &ws = lhs->ws;
-  const int nNo = lhs->nNo, G = lhs->grid;
+  const int nNo = lhs->nNo;
+  static const int Gs = resident_grid(k_cg_spmv<D, VT, XT>, 1 << 30);
+  static const int Gu = resident_grid(k_cg_update<XT>, 1 << 30);
+  const int G1 = Gs < lhs->grid ? Gs : lhs->grid, G2 = Gu < lhs->grid ? Gu : lhs->grid;
   const size_t nv = (size_t)nNo * D;
   KrylovScalars *S = ws.scal.as<KrylovScalars>();
   double *part = ws.partials.as<double>();
   unsigned *tk = ws.ticket.as<unsigned>();
   for (int b = 0; b < n_iter; b++) {
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b), st);
-    k_cg_spmv<D, VT, XT><<<G, kThreads, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
-                                                 lhs->d_colPtr.as<int>(), Val, v, S, part, tk);
+    k_cg_spmv<D, VT, XT><<<G1, kThreads, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
+                                                  lhs->d_colPtr.as<int>(), Val, v, S, part, tk);
     GSLS_CHECK_LAUNCH();
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b + 1), st);
-    k_cg_update<XT><<<G, kThreads, 0, st>>>(nv, v, S, part, tk);
+    k_cg_update<XT><<<G2, kThreads, 0, st>>>(nv, v, S, part, tk);
     GSLS_CHECK_LAUNCH();
   }
   return GSLS_OK;
