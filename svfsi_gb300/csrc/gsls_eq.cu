@@ -171,7 +171,7 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
   }
   const size_t vb = (size_t)eq->nnz * p->dof * p->dof * (sv->precision == GSLS_PREC_MIXED ? 4 : 8);
   if ((rc = eq->R.alloc(sizeof(double) * (size_t)eq->nNo * p->dof)) != GSLS_OK ||
-      (rc = eq->Val.alloc(vb)) != GSLS_OK) {
+      (rc = eq->Val.alloc(vb + 64)) != GSLS_OK) {
     delete eq;
     return rc;
   }
@@ -362,7 +362,7 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     }
     cudaEventRecord(eq->e1, st);
     auto t0 = std::chrono::steady_clock::now();
-    int rc = solve_dev(lhs, &eq->ls, dof, eq->R.as<double>(), eq->Val.p, valp, eq->sv.prec);
+    int rc = solve_dev(lhs, &eq->ls, dof, eq->R.as<double>(), eq->Val.p, valp, eq->sv.prec, true);
     info->t_solve_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     cudaEventElapsedTime(&ms, eq->e0, eq->e1);
     info->t_assembly_ms += ms;

@@ -88,15 +88,20 @@ struct GraphKey {
   const void *val;
   const void *x;
   int batch, nNo;
+  bool tma;
   bool operator==(const GraphKey &o) const {
     return D == o.D && vsz == o.vsz && xsz == o.xsz && val == o.val && x == o.x &&
-           batch == o.batch && nNo == o.nNo;
+           batch == o.batch && nNo == o.nNo && tma == o.tma;
   }
 };
 
 // Scratch for reductions and Krylov work vectors.
 struct Workspace {
   DevBuf Wf;          // float copy of W (FP32 scaling pass)
+  DevBuf err;         // device error word of staged kernels
+  int tma_key = -1, tma_smem = 0, tma_grid = 0;
+  bool tma_ok = false;
+  long long tma_info[3] = {0, 0, 0};  // TmaTiles of the cached geometry
   cudaGraphExec_t cg_graph = nullptr;
   GraphKey cg_key{};
   DevBuf partials;    // double[grid * 64]
@@ -194,8 +199,9 @@ namespace gsls {
 int lhs_prepare_ws(gsls_lhs *lhs, int dof);
 int lhs_update_faces(gsls_lhs *lhs, const int *incL, const double *res);
 int build_dir_mask(gsls_lhs *lhs, int dof);
+// padded: dVal has >= 16 bytes of slack after its end (enables staged copies)
 int solve_dev(gsls_lhs *lhs, gsls_ls *ls, int dof, double *dRi, void *dVal,
-              int val_prec, int prec);
+              int val_prec, int prec, bool padded);
 int spmv_launch(gsls_lhs *lhs, int dof, const void *dVal, int val_prec,
                 const void *dx, void *dy, int xprec);
 // restarted GMRES on the preconditioned system (gsls_gmres.cu)

@@ -113,6 +113,177 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
   }
 }
 
+// ---------------------------------------------------------------------------
+// TMA-staged variant of k_cg_spmv.  A tile is NW*(32/D) consecutive block
+// rows; its matrix values and column indices are one contiguous range each,
+// copied global -> shared by cp.async.bulk (one elected thread, completion on
+// an mbarrier), double-buffered so the copy of tile k+2 overlaps the math of
+// tile k.  Lanes then read values/columns from shared memory and only gather
+// the vector from L2.  Copies start on a 16-byte boundary (ranges rounded
+// outwards), so Val and colPtr must be allocated with >= 16 bytes of slack.
+struct TmaTiles {
+  int ntiles, tile_rows;
+  int val_buf, col_buf;  // bytes per buffer (multiples of 16)
+  int *err;              // device error word (bit 1: barrier wait timed out)
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Bounded wait on an mbarrier phase; false if the limit was hit.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); it++) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+template <int D, class VT>
+__device__ __forceinline__ void tma_issue_tile(int t, int nNo, const TmaTiles &tt,
+                                               const int *__restrict__ rowPtr,
+                                               const int *__restrict__ colPtr,
+                                               const VT *__restrict__ Val, unsigned char *buf,
+                                               uint64_t *bar) {
+  constexpr int DD = D * D, A = 16 / sizeof(VT);
+  const int r0 = t * tt.tile_rows;
+  const int r1 = min(r0 + tt.tile_rows, nNo);
+  const int c0 = __ldg(rowPtr + r0), c1 = __ldg(rowPtr + r1);
+  const long long e0 = (long long)c0 * DD, e1 = (long long)c1 * DD;
+  const long long e0a = e0 & ~(long long)(A - 1), e1a = (e1 + A - 1) & ~(long long)(A - 1);
+  const int c0a = c0 & ~3, c1a = (c1 + 3) & ~3;
+  const unsigned vb = (unsigned)((e1a - e0a) * sizeof(VT)), cb = (unsigned)((c1a - c0a) * 4);
+  mbar_expect_tx(bar, vb + cb);
+  bulk_g2s(buf, Val + e0a, vb, bar);
+  bulk_g2s(buf + tt.val_buf, colPtr + c0a, cb, bar);
+}
+
+template <int D, class VT, class XT, int NW>
+__global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__restrict__ rowPtr,
+                                                         const int *__restrict__ colPtr,
+                                                         const VT *__restrict__ Val, CgVecs v,
+                                                         KrylovScalars *S, double *partials,
+                                                         unsigned *ticket, TmaTiles tt) {
+  if (*(volatile int *)&S->done) return;
+  using AT = typename AccOf<VT>::T;
+  constexpr int RPW = 32 / D, DD = D * D, A = 16 / sizeof(VT);
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ double sh[32];
+  __shared__ AT sha[32];
+  const int bufsz = tt.val_buf + tt.col_buf;
+  unsigned char *buf0 = smem, *buf1 = smem + bufsz;
+  const int par = S->itr & 1;
+  const XT *__restrict__ Pold = (const XT *)(par ? v.P1 : v.P0);
+  XT *__restrict__ Pnew = (XT *)(par ? v.P0 : v.P1);
+  const XT *__restrict__ R = (const XT *)v.R;
+  XT *__restrict__ KP = (XT *)v.KP;
+  const AT beta = AT(S->beta);
+  GatherDir<D, XT, AT> g{R, Pold, beta};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, grp = lane / D, r = lane - grp * D;
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int t0 = blockIdx.x, stride = gridDim.x;
+  if (threadIdx.x == 0) {
+    if (t0 < tt.ntiles) tma_issue_tile<D, VT>(t0, nNo, tt, rowPtr, colPtr, Val, buf0, &bars[0]);
+    if (t0 + stride < tt.ntiles)
+      tma_issue_tile<D, VT>(t0 + stride, nNo, tt, rowPtr, colPtr, Val, buf1, &bars[1]);
+  }
+  AT dot = AT(0);
+  bool ok = true;
+  int k = 0;
+  for (int t = t0; t < tt.ntiles; t += stride, k++) {
+    const int b = k & 1;
+    unsigned char *buf = b ? buf1 : buf0;
+    const bool waited = mbar_wait(&bars[b], (k >> 1) & 1);
+    if (!__syncthreads_and(waited)) {
+      // a copy did not land: stop, drain what is in flight (bounded), flag
+      ok = false;
+      if (threadIdx.x == 0) {
+        mbar_wait(&bars[b], (k >> 1) & 1);
+        if (t + stride < tt.ntiles) mbar_wait(&bars[b ^ 1], ((k + 1) >> 1) & 1);
+      }
+      break;
+    }
+    const int r0 = t * tt.tile_rows;
+    const long long e0a = ((long long)__ldg(rowPtr + r0) * DD) & ~(long long)(A - 1);
+    const int c0a = __ldg(rowPtr + r0) & ~3;
+    const VT *__restrict__ sv = reinterpret_cast<const VT *>(buf);
+    const int *__restrict__ sc = reinterpret_cast<const int *>(buf + tt.val_buf);
+    const int i = r0 + wid * RPW + grp;
+    if (grp < RPW && i < nNo && i < r0 + tt.tile_rows) {
+      const int rs = __ldg(rowPtr + i), re = __ldg(rowPtr + i + 1);
+      const VT *vrow = sv + ((long long)rs * DD - e0a) + r * D;
+      const int *crow = sc + (rs - c0a);
+      AT acc0 = AT(0), acc1 = AT(0);
+      int j = 0;
+      const int nb = re - rs;
+      for (; j + 1 < nb; j += 2) {
+        const int cA = crow[j], cB = crow[j + 1];
+        AT xa[D], xb[D];
+        g.get(cA, xa);
+        g.get(cB, xb);
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+          acc0 = fma(AT(vrow[j * DD + c]), xa[c], acc0);
+          acc1 = fma(AT(vrow[(j + 1) * DD + c]), xb[c], acc1);
+        }
+      }
+      if (j < nb) {
+        const int cA = crow[j];
+        AT xa[D];
+        g.get(cA, xa);
+#pragma unroll
+        for (int c = 0; c < D; c++) acc0 = fma(AT(vrow[j * DD + c]), xa[c], acc0);
+      }
+      const AT y = acc0 + acc1;
+      const size_t kk = (size_t)i * D + r;
+      const AT pn = AT(R[kk]) + beta * AT(Pold[kk]);
+      Pnew[kk] = XT(pn);
+      KP[kk] = XT(y);
+      dot = fma(pn, y, dot);
+    }
+    __syncthreads();  // everyone is done with this buffer
+    if (threadIdx.x == 0 && t + 2 * stride < tt.ntiles)
+      tma_issue_tile<D, VT>(t + 2 * stride, nNo, tt, rowPtr, colPtr, Val, buf, &bars[b]);
+  }
+  if (!ok && threadIdx.x == 0) atomicOr(tt.err, 2);
+  const AT bsa = block_sum_t<AT>(dot, sha);
+  double bs = double(bsa);
+  double tot;
+  if (grid_reduce_last<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
+    S->errO = S->err;
+    S->dot = tot;
+    S->alpha = S->errO / tot;
+    if (!isfinite(S->alpha)) S->done = 3;
+    if (*(volatile int *)tt.err) S->done = 3;
+  }
+}
+
 // X += alpha P_new; R -= alpha KP; err = ||R||^2; beta; convergence test
 template <class XT>
 __global__ void __launch_bounds__(kThreads) k_cg_update(size_t n, CgVecs v, KrylovScalars *S,
@@ -279,9 +450,64 @@ static int resident_grid(K kernel, int cap) {
   return g < cap ? g : cap;
 }
 
+constexpr int kTmaWarps = 8;
+
+// Tile geometry of the staged SpMV for block size D and value type VT,
+// from the host copy of rowPtr; cached per lhs.  Returns false when the
+// staged kernel does not apply (tiles too large for shared memory).
+template <int D, class VT>
+static bool tma_setup(gsls_lhs *lhs, TmaTiles &tt, int &smem, int &grid) {
+  Workspace &ws = lhs->ws;
+  const int key = D * 16 + (int)sizeof(VT);
+  if (ws.tma_key == key) {
+    tt = *reinterpret_cast<TmaTiles *>(&ws.tma_info);
+    smem = ws.tma_smem;
+    grid = ws.tma_grid;
+    return ws.tma_ok;
+  }
+  constexpr int DD = D * D, A = 16 / sizeof(VT);
+  const int rows = kTmaWarps * (32 / D);
+  const int nNo = lhs->nNo;
+  const std::vector<int> &rp = lhs->h_rowPtr;
+  long long vmax = 0, cmax = 0;
+  const int ntiles = (nNo + rows - 1) / rows;
+  for (int t = 0; t < ntiles; t++) {
+    const int r0 = t * rows, r1 = std::min(r0 + rows, nNo);
+    const long long e0 = (long long)rp[r0] * DD, e1 = (long long)rp[r1] * DD;
+    const long long e0a = e0 & ~(long long)(A - 1), e1a = (e1 + A - 1) & ~(long long)(A - 1);
+    const long long c0a = rp[r0] & ~3, c1a = (rp[r1] + 3) & ~3;
+    vmax = std::max(vmax, (e1a - e0a) * (long long)sizeof(VT));
+    cmax = std::max(cmax, (c1a - c0a) * 4LL);
+  }
+  tt.ntiles = ntiles;
+  tt.tile_rows = rows;
+  tt.val_buf = (int)((vmax + 127) & ~127LL);
+  tt.col_buf = (int)((cmax + 127) & ~127LL);
+  tt.err = ws.err.as<int>();
+  smem = 2 * (tt.val_buf + tt.col_buf);
+  bool ok = smem <= 200 * 1024;
+  grid = 0;
+  if (ok) {
+    auto kern = k_cg_spmv_tma<D, VT, VT, kTmaWarps>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kTmaWarps * 32, smem);
+    if (nb < 1) ok = false;
+    grid = std::min(ntiles, nb * num_sms());
+    grid = std::min(grid, lhs->grid);
+  }
+  ws.tma_key = key;
+  *reinterpret_cast<TmaTiles *>(&ws.tma_info) = tt;
+  ws.tma_smem = smem;
+  ws.tma_grid = grid;
+  ws.tma_ok = ok;
+  return ok;
+}
+
 template <int D, class VT, class XT>
 static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter, bool prof,
-                      int ev_base) {
+                      int ev_base, const TmaTiles *tt = nullptr, int tma_smem = 0,
+                      int tma_grid = 0) {
   cudaStream_t st = lhs->stream;
   Workspace &ws = lhs->ws;
   const int nNo = lhs->nNo;
@@ -294,8 +520,12 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
   unsigned *tk = ws.ticket.as<unsigned>();
   for (int b = 0; b < n_iter; b++) {
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b), st);
-    k_cg_spmv<D, VT, XT><<<G1, kThreads, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
-                                                  lhs->d_colPtr.as<int>(), Val, v, S, part, tk);
+    if (tt)
+      k_cg_spmv_tma<D, VT, XT, kTmaWarps><<<tma_grid, kTmaWarps * 32, tma_smem, st>>>(
+          nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, v, S, part, tk, *tt);
+    else
+      k_cg_spmv<D, VT, XT><<<G1, kThreads, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
+                                                    lhs->d_colPtr.as<int>(), Val, v, S, part, tk);
     GSLS_CHECK_LAUNCH();
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b + 1), st);
     k_cg_update<XT><<<G2, kThreads, 0, st>>>(nv, v, S, part, tk);
@@ -306,7 +536,8 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
 
 // CG on the preconditioned system; R (double, device) in: rhs, out: W*X.
 template <int D, class VT, class XT>
-static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const double *Wc) {
+static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const double *Wc,
+                bool val_padded) {
   cudaStream_t st = lhs->stream;
   Workspace &ws = lhs->ws;
   const int nNo = lhs->nNo;
@@ -323,7 +554,13 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   const bool prof = prof_on();
   const int B = nv < (1u << 20) ? 8 : 16;
   // CUDA graph of B iterations, cached per (D, types, Val, workspace)
-  GraphKey key{D, (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo};
+  // TMA-staged SpMV for FP32 values in a buffer with copy slack
+  TmaTiles tt{};
+  int tsmem = 0, tgrid = 0;
+  const bool use_tma = val_padded && sizeof(VT) == 4 && tma_setup<D, VT>(lhs, tt, tsmem, tgrid);
+  const TmaTiles *ttp = use_tma ? &tt : nullptr;
+  if (use_tma) GSLS_CUDA(cudaMemsetAsync(ws.err.p, 0, sizeof(int), st));
+  GraphKey key{D, (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma};
   if (!prof && !(ws.cg_graph && ws.cg_key == key)) {
     if (ws.cg_graph) {
       cudaGraphExecDestroy(ws.cg_graph);
@@ -331,7 +568,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
     }
     cudaGraph_t g;
     GSLS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int rc = cg_enqueue<D, VT, XT>(lhs, Val, v, B, false, 0);
+    int rc = cg_enqueue<D, VT, XT>(lhs, Val, v, B, false, 0, ttp, tsmem, tgrid);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc != GSLS_OK) return rc;
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
@@ -342,7 +579,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   while (ws.h_scal->done == 0) {
     const int itr_before = ws.h_scal->itr;
     if (prof) {
-      GSLS_TRY(cg_enqueue<D, VT, XT>(lhs, Val, v, B, true, 0));
+      GSLS_TRY(cg_enqueue<D, VT, XT>(lhs, Val, v, B, true, 0, ttp, tsmem, tgrid));
     } else {
       GSLS_CUDA(cudaGraphLaunch(ws.cg_graph, st));
       count_launch_n(2 * B - 1);
@@ -370,6 +607,14 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   ls->fNorm = sqrt(h.err);
   ls->dB = (h.errO < 2.220446049250313e-16) ? 0.0 : 5.0 * log(h.err / h.errO);
   ls->callD = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (use_tma) {
+    int herr = 0;
+    GSLS_CUDA(cudaMemcpy(&herr, ws.err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+      set_error("CG: a staged copy did not complete (bounded mbarrier wait expired)");
+      return GSLS_ERR_CUDA;
+    }
+  }
   if (h.done == 3) {
     set_error("CG: NaN/Inf or breakdown in Krylov scalars");
     return GSLS_ERR_NAN;
@@ -378,7 +623,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
 }
 
 template <int D, class VT, class XT>
-static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec) {
+static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, bool padded) {
   Workspace &ws = lhs->ws;
   double *W = ws.W.as<double>();
   if (prec == GSLS_PRECOND_FSILS) {
@@ -392,7 +637,7 @@ static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec) {
   }
   switch (ls->LS_type) {
     case GSLS_LS_TYPE_CG:
-      return cg_t<D, VT, XT>(lhs, &ls->RI, Val, dRi, W);
+      return cg_t<D, VT, XT>(lhs, &ls->RI, Val, dRi, W, padded);
     case GSLS_LS_TYPE_GMRES:
       return gmres_run(lhs, &ls->RI, D, sizeof(VT) == 4, Val, dRi, W);
     case GSLS_LS_TYPE_NS:
@@ -405,14 +650,14 @@ static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec) {
 }
 
 int solve_dev(gsls_lhs *lhs, gsls_ls *ls, int dof, double *dRi, void *dVal, int val_prec,
-              int prec) {
+              int prec, bool padded) {
   GSLS_TRY(lhs_prepare_ws(lhs, dof));
   GSLS_TRY(build_dir_mask(lhs, dof));
   const bool mixed = (val_prec == GSLS_PREC_MIXED);
 #define GSLS_SOLVE_CASE(DV)                                                              \
   case DV:                                                                               \
-    return mixed ? solve_t<DV, float, float>(lhs, ls, dRi, (float *)dVal, prec)          \
-                 : solve_t<DV, double, double>(lhs, ls, dRi, (double *)dVal, prec);
+    return mixed ? solve_t<DV, float, float>(lhs, ls, dRi, (float *)dVal, prec, padded)  \
+                 : solve_t<DV, double, double>(lhs, ls, dRi, (double *)dVal, prec, padded);
   switch (dof) {
     GSLS_SOLVE_CASE(1)
     GSLS_SOLVE_CASE(2)
@@ -468,7 +713,7 @@ int gsls_solve_dev(gsls_lhs *lhs, gsls_ls *ls, int dof, double *dRi, void *dVal,
     return GSLS_ERR_ARG;
   }
   GSLS_TRY(lhs_update_faces(lhs, incL, res));
-  return solve_dev(lhs, ls, dof, dRi, dVal, val_prec, prec);
+  return solve_dev(lhs, ls, dof, dRi, dVal, val_prec, prec, false);
 }
 
 int gsls_solve(gsls_lhs *lhs, gsls_ls *ls, int dof, double *Ri, double *Val, int prec,
@@ -480,11 +725,12 @@ int gsls_solve(gsls_lhs *lhs, gsls_ls *ls, int dof, double *Ri, double *Val, int
   GSLS_TRY(lhs_update_faces(lhs, incL, res));
   const size_t nr = (size_t)lhs->nNo * dof, nval = (size_t)lhs->nnz * dof * dof;
   GSLS_TRY(lhs->ws.io.alloc(sizeof(double) * nr));
-  GSLS_TRY(lhs->ws.io2.alloc(sizeof(double) * nval));
+  GSLS_TRY(lhs->ws.io2.alloc(sizeof(double) * nval + 64));
   cudaStream_t st = lhs->stream;
   GSLS_CUDA(cudaMemcpyAsync(lhs->ws.io.p, Ri, sizeof(double) * nr, cudaMemcpyHostToDevice, st));
   GSLS_CUDA(cudaMemcpyAsync(lhs->ws.io2.p, Val, sizeof(double) * nval, cudaMemcpyHostToDevice, st));
-  int rc = solve_dev(lhs, ls, dof, lhs->ws.io.as<double>(), lhs->ws.io2.p, GSLS_PREC_FP64, prec);
+  int rc = solve_dev(lhs, ls, dof, lhs->ws.io.as<double>(), lhs->ws.io2.p, GSLS_PREC_FP64, prec,
+                     true);
   if (rc != GSLS_OK && rc != GSLS_ERR_NAN) return rc;
   GSLS_CUDA(cudaMemcpyAsync(Ri, lhs->ws.io.p, sizeof(double) * nr, cudaMemcpyDeviceToHost, st));
   GSLS_CUDA(cudaMemcpyAsync(Val, lhs->ws.io2.p, sizeof(double) * nval, cudaMemcpyDeviceToHost, st));

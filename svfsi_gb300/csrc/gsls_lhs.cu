@@ -115,6 +115,10 @@ int lhs_prepare_ws(gsls_lhs *lhs, int dof) {
   GSLS_TRY(ws.W.alloc(sizeof(double) * nv));
   GSLS_TRY(ws.W2.alloc(sizeof(double) * nv));
   GSLS_TRY(ws.Wf.alloc(sizeof(float) * nv));
+  if (!ws.err.p) {
+    GSLS_TRY(ws.err.alloc(64));
+    GSLS_CUDA(cudaMemsetAsync(ws.err.p, 0, 64, lhs->stream));
+  }
   GSLS_TRY(ws.mask.alloc(sizeof(double) * nv));
   if (!ws.h_scal) {
     GSLS_CUDA(cudaMallocHost(&ws.h_scal, sizeof(KrylovScalars)));
@@ -282,7 +286,7 @@ int gsls_lhs_create(gsls_lhs **out, int gnNo, int nNo, int nnz, const int *gNode
   cudaEventCreate(&lhs->ev0);
   cudaEventCreate(&lhs->ev1);
   if ((rc = lhs->d_rowPtr.alloc(sizeof(int) * (nNo + 1))) ||
-      (rc = lhs->d_colPtr.alloc(sizeof(int) * nnz)) ||
+      (rc = lhs->d_colPtr.alloc(sizeof(int) * nnz + 64)) ||
       (rc = lhs->d_diagPtr.alloc(sizeof(int) * nNo)) ||
       (rc = lhs->d_rowOf.alloc(sizeof(int) * nnz))) {
     gsls_lhs_free(lhs);
