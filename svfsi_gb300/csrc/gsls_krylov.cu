@@ -11,6 +11,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "gsls_internal.cuh"
@@ -26,21 +27,28 @@ struct CgVecs {
   void *X, *R, *P0, *P1, *KP;
 };
 
-// R_k = R; P0 = 0; X = 0; iNorm = ||R||; eps; errO = err = iNorm^2; beta = 0
-template <class XT>
-__global__ void __launch_bounds__(kThreads) k_cg_init(size_t n, const double *__restrict__ R,
+// R_k = R; P0 = P1 = KP = 0; X = 0; iNorm = ||R||; eps; errO = err =
+// iNorm^2; beta = 0.  Work vectors use node stride VD (pads stay zero).
+template <int D, class XT>
+__global__ void __launch_bounds__(kThreads) k_cg_init(int nNo, const double *__restrict__ R,
                                                       CgVecs v, KrylovScalars *S, double absTol,
                                                       double relTol, int mItr, double *partials,
                                                       unsigned *ticket) {
+  constexpr int VD = VStride<D, XT>::v;
   __shared__ double sh[32];
-  XT *Rk = (XT *)v.R, *P0 = (XT *)v.P0, *X = (XT *)v.X;
+  XT *Rk = (XT *)v.R, *P0 = (XT *)v.P0, *P1 = (XT *)v.P1, *X = (XT *)v.X, *KP = (XT *)v.KP;
   double acc = 0.0;
+  const size_t n = (size_t)nNo * VD;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (size_t)gridDim.x * blockDim.x) {
-    const double r = R[k];
+    const size_t a = k / VD;
+    const int c = (int)(k - a * VD);
+    const double r = (c < D) ? R[a * D + c] : 0.0;
     acc += r * r;
     Rk[k] = XT(r);
     P0[k] = XT(0);
+    P1[k] = XT(0);
+    KP[k] = XT(0);
     X[k] = XT(0);
   }
   double bs = block_sum(acc, sh);
@@ -77,6 +85,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
                                                       unsigned *ticket) {
   if (*(volatile int *)&S->done) return;
   using AT = typename AccOf<VT>::T;
+  constexpr int VD = VStride<D, XT>::v;
   __shared__ double sh[32];
   __shared__ AT sha[32];
   constexpr int RPW = 32 / D;
@@ -86,7 +95,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
   const XT *__restrict__ R = (const XT *)v.R;
   XT *__restrict__ KP = (XT *)v.KP;
   const AT beta = AT(S->beta);
-  GatherDir<D, XT, AT> g{R, Pold, beta};
+  GatherDir<D, XT, AT, VD> g{R, Pold, beta};
   const int lane = threadIdx.x & 31, grp = lane / D, r = lane - grp * D;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -95,7 +104,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
     const int i = base + grp;
     if (grp < RPW && i < nNo) {
       const AT y = spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, g);
-      const size_t k = (size_t)i * D + r;
+      const size_t k = (size_t)i * VD + r;
       const AT pn = AT(R[k]) + beta * AT(Pold[k]);
       Pnew[k] = XT(pn);
       KP[k] = XT(y);
@@ -186,6 +195,7 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
                                                          unsigned *ticket, TmaTiles tt) {
   if (*(volatile int *)&S->done) return;
   using AT = typename AccOf<VT>::T;
+  constexpr int VD = VStride<D, XT>::v;
   constexpr int RPW = 32 / D, DD = D * D, A = 16 / sizeof(VT);
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[2];
@@ -199,7 +209,7 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
   const XT *__restrict__ R = (const XT *)v.R;
   XT *__restrict__ KP = (XT *)v.KP;
   const AT beta = AT(S->beta);
-  GatherDir<D, XT, AT> g{R, Pold, beta};
+  GatherDir<D, XT, AT, VD> g{R, Pold, beta};
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, grp = lane / D, r = lane - grp * D;
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
@@ -261,7 +271,7 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
         for (int c = 0; c < D; c++) acc0 = fma(AT(vrow[j * DD + c]), xa[c], acc0);
       }
       const AT y = acc0 + acc1;
-      const size_t kk = (size_t)i * D + r;
+      const size_t kk = (size_t)i * VD + r;
       const AT pn = AT(R[kk]) + beta * AT(Pold[kk]);
       Pnew[kk] = XT(pn);
       KP[kk] = XT(y);
@@ -284,10 +294,13 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
   }
 }
 
-// X += alpha P_new; R -= alpha KP; err = ||R||^2; beta; convergence test
+// X += alpha P_new; R -= alpha KP; err = ||R||^2; beta; convergence test.
+// Fat blocks (kUpdThreads) keep the grid -- and the last-block ticket chain
+// -- short; FP32 vectors are streamed as float4.
+constexpr int kUpdThreads = 1024;
 template <class XT>
-__global__ void __launch_bounds__(kThreads) k_cg_update(size_t n, CgVecs v, KrylovScalars *S,
-                                                        double *partials, unsigned *ticket) {
+__global__ void __launch_bounds__(kUpdThreads) k_cg_update(size_t n, CgVecs v, KrylovScalars *S,
+                                                           double *partials, unsigned *ticket) {
   if (*(volatile int *)&S->done) return;
   using AT = XT;
   __shared__ double sh[32];
@@ -299,7 +312,35 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(size_t n, CgVecs v, Kryl
   const XT *__restrict__ KP = (const XT *)v.KP;
   const AT alpha = AT(S->alpha);
   AT acc = AT(0);
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+  size_t k0 = 0;
+  if constexpr (sizeof(XT) == 4) {
+    const size_t n4 = n / 4;
+    float4 *X4 = reinterpret_cast<float4 *>(X);
+    float4 *R4 = reinterpret_cast<float4 *>(R);
+    const float4 *P4 = reinterpret_cast<const float4 *>(P);
+    const float4 *K4 = reinterpret_cast<const float4 *>(KP);
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4;
+         k += (size_t)gridDim.x * blockDim.x) {
+      float4 x = X4[k], r = R4[k];
+      const float4 p = P4[k], q = K4[k];
+      x.x = fmaf(alpha, p.x, x.x);
+      x.y = fmaf(alpha, p.y, x.y);
+      x.z = fmaf(alpha, p.z, x.z);
+      x.w = fmaf(alpha, p.w, x.w);
+      r.x = fmaf(-alpha, q.x, r.x);
+      r.y = fmaf(-alpha, q.y, r.y);
+      r.z = fmaf(-alpha, q.z, r.z);
+      r.w = fmaf(-alpha, q.w, r.w);
+      X4[k] = x;
+      R4[k] = r;
+      acc = fmaf(r.x, r.x, acc);
+      acc = fmaf(r.y, r.y, acc);
+      acc = fmaf(r.z, r.z, acc);
+      acc = fmaf(r.w, r.w, acc);
+    }
+    k0 = n4 * 4;
+  }
+  for (size_t k = k0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (size_t)gridDim.x * blockDim.x) {
     X[k] = fma(alpha, P[k], X[k]);
     const AT r = fma(-alpha, KP[k], R[k]);
@@ -324,13 +365,17 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(size_t n, CgVecs v, Kryl
   }
 }
 
-// R_out = W * X
-template <class XT>
-__global__ void k_scale_out(size_t n, double *__restrict__ Rout, const XT *__restrict__ X,
+// R_out = W * X (X in node stride VD, R_out packed)
+template <int D, class XT>
+__global__ void k_scale_out(int nNo, double *__restrict__ Rout, const XT *__restrict__ X,
                             const double *__restrict__ W) {
+  constexpr int VD = VStride<D, XT>::v;
+  const size_t n = (size_t)nNo * D;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-       k += (size_t)gridDim.x * blockDim.x)
-    Rout[k] = W[k] * double(X[k]);
+       k += (size_t)gridDim.x * blockDim.x) {
+    const size_t a = k / D, c = k - a * D;
+    Rout[k] = W[k] * double(X[a * VD + c]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -442,9 +487,9 @@ static int wait_scalars(gsls_lhs *lhs) {
 // wave), capped by the lhs reduction grid; fixed per kernel and device, so
 // its reductions stay reproducible.
 template <class K>
-static int resident_grid(K kernel, int cap) {
+static int resident_grid(K kernel, int cap, int threads = kThreads) {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, 0);
   if (nb < 1) nb = 1;
   int g = nb * num_sms();
   return g < cap ? g : cap;
@@ -512,9 +557,9 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
   Workspace &ws = lhs->ws;
   const int nNo = lhs->nNo;
   static const int Gs = resident_grid(k_cg_spmv<D, VT, XT>, 1 << 30);
-  static const int Gu = resident_grid(k_cg_update<XT>, 1 << 30);
+  static const int Gu = resident_grid(k_cg_update<XT>, 1 << 30, kUpdThreads);
   const int G1 = Gs < lhs->grid ? Gs : lhs->grid, G2 = Gu < lhs->grid ? Gu : lhs->grid;
-  const size_t nv = (size_t)nNo * D;
+  const size_t nv = (size_t)nNo * VStride<D, XT>::v;
   KrylovScalars *S = ws.scal.as<KrylovScalars>();
   double *part = ws.partials.as<double>();
   unsigned *tk = ws.ticket.as<unsigned>();
@@ -528,7 +573,7 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
                                                     lhs->d_colPtr.as<int>(), Val, v, S, part, tk);
     GSLS_CHECK_LAUNCH();
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b + 1), st);
-    k_cg_update<XT><<<G2, kThreads, 0, st>>>(nv, v, S, part, tk);
+    k_cg_update<XT><<<G2, kUpdThreads, 0, st>>>(nv, v, S, part, tk);
     GSLS_CHECK_LAUNCH();
   }
   return GSLS_OK;
@@ -548,7 +593,8 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   unsigned *tk = ws.ticket.as<unsigned>();
   const int G = lhs->grid;
   auto t0 = std::chrono::steady_clock::now();
-  k_cg_init<XT><<<G, kThreads, 0, st>>>(nv, R, v, S, ls->absTol, ls->relTol, ls->mItr, part, tk);
+  k_cg_init<D, XT><<<G, kThreads, 0, st>>>(nNo, R, v, S, ls->absTol, ls->relTol, ls->mItr, part,
+                                            tk);
   GSLS_CHECK_LAUNCH();
   GSLS_TRY(wait_scalars(lhs));
   const bool prof = prof_on();
@@ -557,7 +603,12 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   // TMA-staged SpMV for FP32 values in a buffer with copy slack
   TmaTiles tt{};
   int tsmem = 0, tgrid = 0;
-  const bool use_tma = val_padded && sizeof(VT) == 4 && tma_setup<D, VT>(lhs, tt, tsmem, tgrid);
+  static const bool want_tma = [] {
+    const char *e = getenv("GSLS_SPMV");
+    return e && strcmp(e, "tma") == 0;
+  }();
+  const bool use_tma =
+      want_tma && val_padded && sizeof(VT) == 4 && tma_setup<D, VT>(lhs, tt, tsmem, tgrid);
   const TmaTiles *ttp = use_tma ? &tt : nullptr;
   if (use_tma) GSLS_CUDA(cudaMemsetAsync(ws.err.p, 0, sizeof(int), st));
   GraphKey key{D, (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma};
@@ -597,7 +648,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
       prof_add("cg_spmv", worked, ms);
     }
   }
-  k_scale_out<XT><<<G, kThreads, 0, st>>>(nv, R, (const XT *)v.X, Wc);
+  k_scale_out<D, XT><<<G, kThreads, 0, st>>>(nNo, R, (const XT *)v.X, Wc);
   GSLS_CHECK_LAUNCH();
   GSLS_CUDA(cudaStreamSynchronize(st));
   const KrylovScalars &h = *ws.h_scal;

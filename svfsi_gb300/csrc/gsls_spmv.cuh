@@ -47,24 +47,42 @@ __device__ __forceinline__ void load_row_seg<2, float, float>(const float *__res
   out[1] = v.y;
 }
 
+// Node stride of the Krylov work vectors: FP32 3-vectors are padded to 4
+// floats so that one 16-byte load gathers a node (the gather, not the matrix
+// stream, dominates the L1 sector lookups of the block SpMV).
+template <int D, class XT> struct VStride { static constexpr int v = D; };
+template <> struct VStride<3, float> { static constexpr int v = 4; };
+
+template <int D, int VD, class XT, class AT>
+__device__ __forceinline__ void load_node(const XT *__restrict__ p, AT out[D]) {
+  if constexpr (VD == 4 && D == 3 && sizeof(XT) == 4) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    out[0] = v.x;
+    out[1] = v.y;
+    out[2] = v.z;
+  } else {
+    load_row_seg<D, XT, AT>(p, out);
+  }
+}
+
 // Gathered vector access: either x itself, or x = R + beta*Pold computed on
 // the fly (CG direction update fused into the SpMV).
-template <int D, class XT, class AT>
+template <int D, class XT, class AT, int VD = D>
 struct GatherX {
   const XT *__restrict__ x;
   __device__ __forceinline__ void get(int col, AT out[D]) const {
-    load_row_seg<D, XT, AT>(x + (size_t)col * D, out);
+    load_node<D, VD, XT, AT>(x + (size_t)col * VD, out);
   }
 };
-template <int D, class XT, class AT>
+template <int D, class XT, class AT, int VD = D>
 struct GatherDir {
   const XT *__restrict__ R;
   const XT *__restrict__ Pold;
   AT beta;
   __device__ __forceinline__ void get(int col, AT out[D]) const {
     AT r[D], p[D];
-    load_row_seg<D, XT, AT>(R + (size_t)col * D, r);
-    load_row_seg<D, XT, AT>(Pold + (size_t)col * D, p);
+    load_node<D, VD, XT, AT>(R + (size_t)col * VD, r);
+    load_node<D, VD, XT, AT>(Pold + (size_t)col * VD, p);
 #pragma unroll
     for (int c = 0; c < D; c++) out[c] = r[c] + beta * p[c];
   }
