@@ -250,25 +250,33 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
       const VT *vrow = sv + ((long long)rs * DD - e0a) + r * D;
       const int *crow = sc + (rs - c0a);
       AT acc0 = AT(0), acc1 = AT(0);
-      int j = 0;
       const int nb = re - rs;
-      for (; j + 1 < nb; j += 2) {
-        const int cA = crow[j], cB = crow[j + 1];
-        AT xa[D], xb[D];
-        g.get(cA, xa);
-        g.get(cB, xb);
+      // all gathers of U blocks in flight before the first FMA (the L2
+      // gather latency is what bounds this kernel, not the staged stream)
+      constexpr int U = 8;
+      for (int j = 0; j < nb; j += U) {
+        AT xg[U][D];
 #pragma unroll
-        for (int c = 0; c < D; c++) {
-          acc0 = fma(AT(vrow[j * DD + c]), xa[c], acc0);
-          acc1 = fma(AT(vrow[(j + 1) * DD + c]), xb[c], acc1);
+        for (int u = 0; u < U; u++) {
+          if (j + u < nb) {
+            g.get(crow[j + u], xg[u]);
+          } else {
+#pragma unroll
+            for (int c = 0; c < D; c++) xg[u][c] = AT(0);
+          }
         }
-      }
-      if (j < nb) {
-        const int cA = crow[j];
-        AT xa[D];
-        g.get(cA, xa);
 #pragma unroll
-        for (int c = 0; c < D; c++) acc0 = fma(AT(vrow[j * DD + c]), xa[c], acc0);
+        for (int u = 0; u < U; u++) {
+          if (j + u < nb) {
+#pragma unroll
+            for (int c = 0; c < D; c++) {
+              if (u & 1)
+                acc1 = fma(AT(vrow[(j + u) * DD + c]), xg[u][c], acc1);
+              else
+                acc0 = fma(AT(vrow[(j + u) * DD + c]), xg[u][c], acc0);
+            }
+          }
+        }
       }
       const AT y = acc0 + acc1;
       const size_t kk = (size_t)i * VD + r;

@@ -97,27 +97,33 @@ __device__ __forceinline__ AT spmv_row_comp(int i, int r, const int *__restrict_
   const int rs = __ldg(rowPtr + i), re = __ldg(rowPtr + i + 1);
   const VT *__restrict__ v = Val + (size_t)rs * DD + r * D;
   AT acc0 = AT(0), acc1 = AT(0);
-  int j = rs;
-  for (; j + 1 < re; j += 2) {
-    const int c0 = __ldg(colPtr + j), c1 = __ldg(colPtr + j + 1);
-    AT a0[D], a1[D], x0[D], x1[D];
-    load_row_seg<D, VT, AT>(v + (size_t)(j - rs) * DD, a0);
-    load_row_seg<D, VT, AT>(v + (size_t)(j + 1 - rs) * DD, a1);
-    g.get(c0, x0);
-    g.get(c1, x1);
+  // U blocks per step: column loads, value loads and gathers of all U
+  // blocks are issued before the first FMA
+  constexpr int U = 4;
+  for (int j = rs; j < re; j += U) {
+    int cc[U];
 #pragma unroll
-    for (int c = 0; c < D; c++) {
-      acc0 = fma(a0[c], x0[c], acc0);
-      acc1 = fma(a1[c], x1[c], acc1);
+    for (int u = 0; u < U; u++) cc[u] = (j + u < re) ? __ldg(colPtr + j + u) : -1;
+    AT a[U][D], xg[U][D];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (cc[u] >= 0) {
+        load_row_seg<D, VT, AT>(v + (size_t)(j + u - rs) * DD, a[u]);
+        g.get(cc[u], xg[u]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < D; c++) a[u][c] = xg[u][c] = AT(0);
+      }
     }
-  }
-  if (j < re) {
-    const int c0 = __ldg(colPtr + j);
-    AT a0[D], x0[D];
-    load_row_seg<D, VT, AT>(v + (size_t)(j - rs) * DD, a0);
-    g.get(c0, x0);
 #pragma unroll
-    for (int c = 0; c < D; c++) acc0 = fma(a0[c], x0[c], acc0);
+    for (int u = 0; u < U; u++)
+#pragma unroll
+      for (int c = 0; c < D; c++) {
+        if (u & 1)
+          acc1 = fma(a[u][c], xg[u][c], acc1);
+        else
+          acc0 = fma(a[u][c], xg[u][c], acc0);
+      }
   }
   return acc0 + acc1;
 }
