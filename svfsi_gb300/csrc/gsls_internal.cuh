@@ -89,9 +89,10 @@ struct GraphKey {
   const void *x;
   int batch, nNo;
   bool tma;
+  bool fused;
   bool operator==(const GraphKey &o) const {
     return D == o.D && vsz == o.vsz && xsz == o.xsz && val == o.val && x == o.x &&
-           batch == o.batch && nNo == o.nNo && tma == o.tma;
+           batch == o.batch && nNo == o.nNo && tma == o.tma && fused == o.fused;
   }
 };
 

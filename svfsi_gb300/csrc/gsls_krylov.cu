@@ -29,7 +29,7 @@ struct CgVecs {
 
 // R_k = R; P0 = P1 = KP = 0; X = 0; iNorm = ||R||; eps; errO = err =
 // iNorm^2; beta = 0.  Work vectors use node stride VD (pads stay zero).
-template <int D, class XT>
+template <int D, class XT, bool FUSED>
 __global__ void __launch_bounds__(kThreads) k_cg_init(int nNo, const double *__restrict__ R,
                                                       CgVecs v, KrylovScalars *S, double absTol,
                                                       double relTol, int mItr, double *partials,
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_init(int nNo, const double *__r
     const double r = (c < D) ? R[a * D + c] : 0.0;
     acc += r * r;
     Rk[k] = XT(r);
-    P0[k] = XT(0);
+    P0[k] = FUSED ? XT(0) : XT(r);  // fused: P built from R in the first SpMV
     P1[k] = XT(0);
     KP[k] = XT(0);
     X[k] = XT(0);
@@ -77,7 +77,9 @@ __global__ void __launch_bounds__(kThreads) k_cg_init(int nNo, const double *__r
 
 // P_new = R + beta P_old (own rows), KP = K P_new with P_new gathered on the
 // fly, dot = P_new . KP, alpha = errO / dot.
-template <int D, class VT, class XT>
+// FUSED = false: the direction P (= P0) is updated by k_cg_pupdate and the
+// SpMV gathers P alone (half the gather traffic of the fused form).
+template <int D, class VT, class XT, bool FUSED>
 __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__restrict__ rowPtr,
                                                       const int *__restrict__ colPtr,
                                                       const VT *__restrict__ Val, CgVecs v,
@@ -95,7 +97,8 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
   const XT *__restrict__ R = (const XT *)v.R;
   XT *__restrict__ KP = (XT *)v.KP;
   const AT beta = AT(S->beta);
-  GatherDir<D, XT, AT, VD> g{R, Pold, beta};
+  GatherDir<D, XT, AT, VD> gd{R, Pold, beta};
+  GatherX<D, XT, AT, VD> gx{(const XT *)v.P0};
   const int lane = threadIdx.x & 31, grp = lane / D, r = lane - grp * D;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -103,10 +106,16 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
   for (int base = warp * RPW; base < nNo; base += nwarps * RPW) {
     const int i = base + grp;
     if (grp < RPW && i < nNo) {
-      const AT y = spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, g);
       const size_t k = (size_t)i * VD + r;
-      const AT pn = AT(R[k]) + beta * AT(Pold[k]);
-      Pnew[k] = XT(pn);
+      AT y, pn;
+      if constexpr (FUSED) {
+        y = spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, gd);
+        pn = AT(R[k]) + beta * AT(Pold[k]);
+        Pnew[k] = XT(pn);
+      } else {
+        y = spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, gx);
+        pn = AT(((const XT *)v.P0)[k]);
+      }
       KP[k] = XT(y);
       dot = fma(pn, y, dot);
     }
@@ -187,7 +196,7 @@ __device__ __forceinline__ void tma_issue_tile(int t, int nNo, const TmaTiles &t
   bulk_g2s(buf + tt.val_buf, colPtr + c0a, cb, bar);
 }
 
-template <int D, class VT, class XT, int NW>
+template <int D, class VT, class XT, int NW, bool FUSED>
 __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__restrict__ rowPtr,
                                                          const int *__restrict__ colPtr,
                                                          const VT *__restrict__ Val, CgVecs v,
@@ -209,7 +218,12 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
   const XT *__restrict__ R = (const XT *)v.R;
   XT *__restrict__ KP = (XT *)v.KP;
   const AT beta = AT(S->beta);
-  GatherDir<D, XT, AT, VD> g{R, Pold, beta};
+  using G = typename std::conditional<FUSED, GatherDir<D, XT, AT, VD>, GatherX<D, XT, AT, VD>>::type;
+  G g;
+  if constexpr (FUSED)
+    g = G{R, Pold, beta};
+  else
+    g = G{(const XT *)v.P0};
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, grp = lane / D, r = lane - grp * D;
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
@@ -280,8 +294,13 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
       }
       const AT y = acc0 + acc1;
       const size_t kk = (size_t)i * VD + r;
-      const AT pn = AT(R[kk]) + beta * AT(Pold[kk]);
-      Pnew[kk] = XT(pn);
+      AT pn;
+      if constexpr (FUSED) {
+        pn = AT(R[kk]) + beta * AT(Pold[kk]);
+        Pnew[kk] = XT(pn);
+      } else {
+        pn = AT(((const XT *)v.P0)[kk]);
+      }
       KP[kk] = XT(y);
       dot = fma(pn, y, dot);
     }
@@ -306,7 +325,7 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
 // Fat blocks (kUpdThreads) keep the grid -- and the last-block ticket chain
 // -- short; FP32 vectors are streamed as float4.
 constexpr int kUpdThreads = 1024;
-template <class XT>
+template <class XT, bool FUSED>
 __global__ void __launch_bounds__(kUpdThreads) k_cg_update(size_t n, CgVecs v, KrylovScalars *S,
                                                            double *partials, unsigned *ticket) {
   if (*(volatile int *)&S->done) return;
@@ -314,7 +333,7 @@ __global__ void __launch_bounds__(kUpdThreads) k_cg_update(size_t n, CgVecs v, K
   __shared__ double sh[32];
   __shared__ AT sha[32];
   const int par = S->itr & 1;
-  const XT *__restrict__ P = (const XT *)(par ? v.P0 : v.P1);
+  const XT *__restrict__ P = (const XT *)(FUSED ? (par ? v.P0 : v.P1) : v.P0);
   XT *__restrict__ X = (XT *)v.X;
   XT *__restrict__ R = (XT *)v.R;
   const XT *__restrict__ KP = (const XT *)v.KP;
@@ -371,6 +390,37 @@ __global__ void __launch_bounds__(kUpdThreads) k_cg_update(size_t n, CgVecs v, K
       S->suc = 1;
     }
   }
+}
+
+// P = R + beta P (the reference's OMPSUMS/OMPMULS pair, CGRAD.f:172-175),
+// non-fused mode; vectors are L2-resident between the CG kernels.
+template <class XT>
+__global__ void __launch_bounds__(kUpdThreads) k_cg_pupdate(size_t n, CgVecs v,
+                                                            const KrylovScalars *S) {
+  if (*(volatile const int *)&S->done) return;
+  const XT beta = XT(S->beta);
+  XT *__restrict__ P = (XT *)v.P0;
+  const XT *__restrict__ R = (const XT *)v.R;
+  size_t k0 = 0;
+  if constexpr (sizeof(XT) == 4) {
+    const size_t n4 = n / 4;
+    float4 *P4 = reinterpret_cast<float4 *>(P);
+    const float4 *R4 = reinterpret_cast<const float4 *>(R);
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4;
+         k += (size_t)gridDim.x * blockDim.x) {
+      float4 p = P4[k];
+      const float4 r = R4[k];
+      p.x = fmaf(beta, p.x, r.x);
+      p.y = fmaf(beta, p.y, r.y);
+      p.z = fmaf(beta, p.z, r.z);
+      p.w = fmaf(beta, p.w, r.w);
+      P4[k] = p;
+    }
+    k0 = n4 * 4;
+  }
+  for (size_t k = k0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    P[k] = fma(beta, P[k], R[k]);
 }
 
 // R_out = W * X (X in node stride VD, R_out packed)
@@ -541,8 +591,10 @@ static bool tma_setup(gsls_lhs *lhs, TmaTiles &tt, int &smem, int &grid) {
   bool ok = smem <= 200 * 1024;
   grid = 0;
   if (ok) {
-    auto kern = k_cg_spmv_tma<D, VT, VT, kTmaWarps>;
+    auto kern = k_cg_spmv_tma<D, VT, VT, kTmaWarps, true>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_cg_spmv_tma<D, VT, VT, kTmaWarps, false>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int nb = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kTmaWarps * 32, smem);
     if (nb < 1) ok = false;
@@ -557,16 +609,18 @@ static bool tma_setup(gsls_lhs *lhs, TmaTiles &tt, int &smem, int &grid) {
   return ok;
 }
 
-template <int D, class VT, class XT>
+template <int D, class VT, class XT, bool FUSED>
 static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter, bool prof,
                       int ev_base, const TmaTiles *tt = nullptr, int tma_smem = 0,
                       int tma_grid = 0) {
   cudaStream_t st = lhs->stream;
   Workspace &ws = lhs->ws;
   const int nNo = lhs->nNo;
-  static const int Gs = resident_grid(k_cg_spmv<D, VT, XT>, 1 << 30);
-  static const int Gu = resident_grid(k_cg_update<XT>, 1 << 30, kUpdThreads);
+  static const int Gs = resident_grid(k_cg_spmv<D, VT, XT, FUSED>, 1 << 30);
+  static const int Gu = resident_grid(k_cg_update<XT, FUSED>, 1 << 30, kUpdThreads);
+  static const int Gp = resident_grid(k_cg_pupdate<XT>, 1 << 30, kUpdThreads);
   const int G1 = Gs < lhs->grid ? Gs : lhs->grid, G2 = Gu < lhs->grid ? Gu : lhs->grid;
+  const int G3 = Gp < lhs->grid ? Gp : lhs->grid;
   const size_t nv = (size_t)nNo * VStride<D, XT>::v;
   KrylovScalars *S = ws.scal.as<KrylovScalars>();
   double *part = ws.partials.as<double>();
@@ -574,21 +628,25 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
   for (int b = 0; b < n_iter; b++) {
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b), st);
     if (tt)
-      k_cg_spmv_tma<D, VT, XT, kTmaWarps><<<tma_grid, kTmaWarps * 32, tma_smem, st>>>(
+      k_cg_spmv_tma<D, VT, XT, kTmaWarps, FUSED><<<tma_grid, kTmaWarps * 32, tma_smem, st>>>(
           nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, v, S, part, tk, *tt);
     else
-      k_cg_spmv<D, VT, XT><<<G1, kThreads, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
-                                                    lhs->d_colPtr.as<int>(), Val, v, S, part, tk);
+      k_cg_spmv<D, VT, XT, FUSED><<<G1, kThreads, 0, st>>>(
+          nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, v, S, part, tk);
     GSLS_CHECK_LAUNCH();
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b + 1), st);
-    k_cg_update<XT><<<G2, kUpdThreads, 0, st>>>(nv, v, S, part, tk);
+    k_cg_update<XT, FUSED><<<G2, kUpdThreads, 0, st>>>(nv, v, S, part, tk);
     GSLS_CHECK_LAUNCH();
+    if (!FUSED) {
+      k_cg_pupdate<XT><<<G3, kUpdThreads, 0, st>>>(nv, v, S);
+      GSLS_CHECK_LAUNCH();
+    }
   }
   return GSLS_OK;
 }
 
 // CG on the preconditioned system; R (double, device) in: rhs, out: W*X.
-template <int D, class VT, class XT>
+template <int D, class VT, class XT, bool FUSED>
 static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const double *Wc,
                 bool val_padded) {
   cudaStream_t st = lhs->stream;
@@ -601,8 +659,8 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   unsigned *tk = ws.ticket.as<unsigned>();
   const int G = lhs->grid;
   auto t0 = std::chrono::steady_clock::now();
-  k_cg_init<D, XT><<<G, kThreads, 0, st>>>(nNo, R, v, S, ls->absTol, ls->relTol, ls->mItr, part,
-                                            tk);
+  k_cg_init<D, XT, FUSED><<<G, kThreads, 0, st>>>(nNo, R, v, S, ls->absTol, ls->relTol, ls->mItr,
+                                                   part, tk);
   GSLS_CHECK_LAUNCH();
   GSLS_TRY(wait_scalars(lhs));
   const bool prof = prof_on();
@@ -619,7 +677,8 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
       want_tma && val_padded && sizeof(VT) == 4 && tma_setup<D, VT>(lhs, tt, tsmem, tgrid);
   const TmaTiles *ttp = use_tma ? &tt : nullptr;
   if (use_tma) GSLS_CUDA(cudaMemsetAsync(ws.err.p, 0, sizeof(int), st));
-  GraphKey key{D, (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma};
+  GraphKey key{D, (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma,
+               FUSED};
   if (!prof && !(ws.cg_graph && ws.cg_key == key)) {
     if (ws.cg_graph) {
       cudaGraphExecDestroy(ws.cg_graph);
@@ -627,7 +686,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
     }
     cudaGraph_t g;
     GSLS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int rc = cg_enqueue<D, VT, XT>(lhs, Val, v, B, false, 0, ttp, tsmem, tgrid);
+    int rc = cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, false, 0, ttp, tsmem, tgrid);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc != GSLS_OK) return rc;
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
@@ -638,10 +697,10 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   while (ws.h_scal->done == 0) {
     const int itr_before = ws.h_scal->itr;
     if (prof) {
-      GSLS_TRY(cg_enqueue<D, VT, XT>(lhs, Val, v, B, true, 0, ttp, tsmem, tgrid));
+      GSLS_TRY(cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, true, 0, ttp, tsmem, tgrid));
     } else {
       GSLS_CUDA(cudaGraphLaunch(ws.cg_graph, st));
-      count_launch_n(2 * B - 1);
+      count_launch_n((FUSED ? 2 : 3) * B - 1);
     }
     GSLS_TRY(wait_scalars(lhs));
     if (prof) {
@@ -696,7 +755,14 @@ static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, b
   }
   switch (ls->LS_type) {
     case GSLS_LS_TYPE_CG:
-      return cg_t<D, VT, XT>(lhs, &ls->RI, Val, dRi, W, padded);
+    {
+      static const bool fused = [] {
+        const char *e = getenv("GSLS_CG");
+        return e && strcmp(e, "fused") == 0;
+      }();
+      return fused ? cg_t<D, VT, XT, true>(lhs, &ls->RI, Val, dRi, W, padded)
+                   : cg_t<D, VT, XT, false>(lhs, &ls->RI, Val, dRi, W, padded);
+    }
     case GSLS_LS_TYPE_GMRES:
       return gmres_run(lhs, &ls->RI, D, sizeof(VT) == 4, Val, dRi, W);
     case GSLS_LS_TYPE_NS:
