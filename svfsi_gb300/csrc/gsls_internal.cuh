@@ -163,26 +163,57 @@ __device__ __forceinline__ double block_sum(double v, double *sh /*[32]*/) {
 // block (the last to arrive), whose thread 0 holds the totals in out[k].
 // The summation order depends only on gridDim.x, so results are bitwise
 // reproducible for a fixed grid.
+// Two levels (groups of kRedGroup blocks, then the group sums) keep the
+// chain of same-address atomics short; both levels sum in a fixed order.
+// ticket[0] counts groups, ticket[1 + g] counts blocks of group g (both are
+// reset by their last arrival).  partials holds NV*(grid + ngroups) values.
+constexpr int kRedGroup = 32;
 template <int NV>
 __device__ __forceinline__ bool grid_reduce_last(const double *vals, double *partials,
                                                  unsigned *ticket, double *out,
                                                  double *sh) {
-  __shared__ bool amLast;
+  __shared__ int stage;  // 0: not last, 1: last of its group, 2: last overall
+  const int G = gridDim.x, g = blockIdx.x / kRedGroup;
+  const int ngroups = (G + kRedGroup - 1) / kRedGroup;
+  const int gsz = min(kRedGroup, G - g * kRedGroup);
+  double *gpart = partials + (size_t)NV * G;
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; k++) partials[(size_t)k * gridDim.x + blockIdx.x] = vals[k];
+    for (int k = 0; k < NV; k++) partials[(size_t)k * G + blockIdx.x] = vals[k];
     __threadfence();
-    const unsigned t = atomicAdd(ticket, 1u);
-    amLast = (t == gridDim.x - 1);
+    const unsigned t = atomicAdd(ticket + 1 + g, 1u);
+    stage = (t == (unsigned)gsz - 1) ? 1 : 0;
   }
   __syncthreads();
-  if (!amLast) return false;
+  if (stage == 0) return false;
+  __threadfence();
+  // last block of group g: fixed-order sum of the group's partials
+  double gs[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < gsz; i += blockDim.x)
+      s += __ldcg(&partials[(size_t)k * G + g * kRedGroup + i]);
+    s = block_sum(s, sh);
+    gs[k] = s;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) gpart[(size_t)k * ngroups + g] = gs[k];
+    ticket[1 + g] = 0u;
+    __threadfence();
+    const unsigned t = atomicAdd(ticket, 1u);
+    stage = (t == (unsigned)ngroups - 1) ? 2 : 1;
+  }
+  __syncthreads();
+  if (stage != 2) return false;
   __threadfence();
 #pragma unroll
   for (int k = 0; k < NV; k++) {
     double s = 0.0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
-      s += __ldcg(&partials[(size_t)k * gridDim.x + i]);
+    for (int i = threadIdx.x; i < ngroups; i += blockDim.x)
+      s += __ldcg(&gpart[(size_t)k * ngroups + i]);
     s = block_sum(s, sh);
     if (threadIdx.x == 0) out[k] = s;
     __syncthreads();

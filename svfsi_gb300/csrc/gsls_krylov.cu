@@ -225,6 +225,7 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
   else
     g = G{(const XT *)v.P0};
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, grp = lane / D, r = lane - grp * D;
+  constexpr int SP = 2, RW = RPW / SP;  // lane groups per row, rows per warp
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
@@ -258,8 +259,13 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
     const int c0a = __ldg(rowPtr + r0) & ~3;
     const VT *__restrict__ sv = reinterpret_cast<const VT *>(buf);
     const int *__restrict__ sc = reinterpret_cast<const int *>(buf + tt.val_buf);
-    const int i = r0 + wid * RPW + grp;
-    if (grp < RPW && i < nNo && i < r0 + tt.tile_rows) {
+    // SP lane groups share a block row (blocks j = s, s+SP, ...) so that a
+    // tile keeps 2x the warps busy for the same shared-memory footprint
+    const int slot = grp / SP, s = grp - slot * SP;
+    const int i = r0 + wid * RW + slot;
+    const bool valid = grp < RPW && slot < RW && i < nNo && i < r0 + tt.tile_rows;
+    AT y = AT(0);
+    if (valid) {
       const int rs = __ldg(rowPtr + i), re = __ldg(rowPtr + i + 1);
       const VT *vrow = sv + ((long long)rs * DD - e0a) + r * D;
       const int *crow = sc + (rs - c0a);
@@ -268,12 +274,12 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
       // all gathers of U blocks in flight before the first FMA (the L2
       // gather latency is what bounds this kernel, not the staged stream)
       constexpr int U = 8;
-      for (int j = 0; j < nb; j += U) {
+      for (int j = s; j < nb; j += U * SP) {
         AT xg[U][D];
 #pragma unroll
         for (int u = 0; u < U; u++) {
-          if (j + u < nb) {
-            g.get(crow[j + u], xg[u]);
+          if (j + u * SP < nb) {
+            g.get(crow[j + u * SP], xg[u]);
           } else {
 #pragma unroll
             for (int c = 0; c < D; c++) xg[u][c] = AT(0);
@@ -281,18 +287,22 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
         }
 #pragma unroll
         for (int u = 0; u < U; u++) {
-          if (j + u < nb) {
+          if (j + u * SP < nb) {
 #pragma unroll
             for (int c = 0; c < D; c++) {
               if (u & 1)
-                acc1 = fma(AT(vrow[(j + u) * DD + c]), xg[u][c], acc1);
+                acc1 = fma(AT(vrow[(j + u * SP) * DD + c]), xg[u][c], acc1);
               else
-                acc0 = fma(AT(vrow[(j + u) * DD + c]), xg[u][c], acc0);
+                acc0 = fma(AT(vrow[(j + u * SP) * DD + c]), xg[u][c], acc0);
             }
           }
         }
       }
-      const AT y = acc0 + acc1;
+      y = acc0 + acc1;
+    }
+#pragma unroll
+    for (int o = 1; o < SP; o <<= 1) y += __shfl_down_sync(0xffffffffu, y, o * D);
+    if (valid && s == 0) {
       const size_t kk = (size_t)i * VD + r;
       AT pn;
       if constexpr (FUSED) {
@@ -324,9 +334,9 @@ __global__ void __launch_bounds__(NW * 32) k_cg_spmv_tma(int nNo, const int *__r
 // X += alpha P_new; R -= alpha KP; err = ||R||^2; beta; convergence test.
 // Fat blocks (kUpdThreads) keep the grid -- and the last-block ticket chain
 // -- short; FP32 vectors are streamed as float4.
-constexpr int kUpdThreads = 1024;
+constexpr int kUpdThreads = 512;
 template <class XT, bool FUSED>
-__global__ void __launch_bounds__(kUpdThreads) k_cg_update(size_t n, CgVecs v, KrylovScalars *S,
+__global__ void __launch_bounds__(kUpdThreads, 2) k_cg_update(size_t n, CgVecs v, KrylovScalars *S,
                                                            double *partials, unsigned *ticket) {
   if (*(volatile int *)&S->done) return;
   using AT = XT;
@@ -395,7 +405,7 @@ __global__ void __launch_bounds__(kUpdThreads) k_cg_update(size_t n, CgVecs v, K
 // P = R + beta P (the reference's OMPSUMS/OMPMULS pair, CGRAD.f:172-175),
 // non-fused mode; vectors are L2-resident between the CG kernels.
 template <class XT>
-__global__ void __launch_bounds__(kUpdThreads) k_cg_pupdate(size_t n, CgVecs v,
+__global__ void __launch_bounds__(kUpdThreads, 2) k_cg_pupdate(size_t n, CgVecs v,
                                                             const KrylovScalars *S) {
   if (*(volatile const int *)&S->done) return;
   const XT beta = XT(S->beta);
@@ -553,7 +563,7 @@ static int resident_grid(K kernel, int cap, int threads = kThreads) {
   return g < cap ? g : cap;
 }
 
-constexpr int kTmaWarps = 8;
+constexpr int kTmaWarps = 16;
 
 // Tile geometry of the staged SpMV for block size D and value type VT,
 // from the host copy of rowPtr; cached per lhs.  Returns false when the
@@ -569,7 +579,7 @@ static bool tma_setup(gsls_lhs *lhs, TmaTiles &tt, int &smem, int &grid) {
     return ws.tma_ok;
   }
   constexpr int DD = D * D, A = 16 / sizeof(VT);
-  const int rows = kTmaWarps * (32 / D);
+  const int rows = kTmaWarps * ((32 / D) / 2);  // SP = 2 lane groups per row
   const int nNo = lhs->nNo;
   const std::vector<int> &rp = lhs->h_rowPtr;
   long long vmax = 0, cmax = 0;

@@ -107,8 +107,9 @@ int lhs_prepare_ws(gsls_lhs *lhs, int dof) {
   const size_t nv = (size_t)lhs->nNo * dof;
   GSLS_TRY(ws.partials.alloc(sizeof(double) * (size_t)lhs->grid * 64));
   if (!ws.ticket.p) {
-    GSLS_TRY(ws.ticket.alloc(sizeof(unsigned) * 16));
-    GSLS_CUDA(cudaMemsetAsync(ws.ticket.p, 0, sizeof(unsigned) * 16, lhs->stream));
+    // one group counter per kRedGroup blocks of the largest grid + 1
+    GSLS_TRY(ws.ticket.alloc(sizeof(unsigned) * 256));
+    GSLS_CUDA(cudaMemsetAsync(ws.ticket.p, 0, sizeof(unsigned) * 256, lhs->stream));
   }
   GSLS_TRY(ws.scal.alloc(sizeof(KrylovScalars)));
   for (int k = 0; k < 6; k++) GSLS_TRY(ws.vec[k].alloc(sizeof(double) * nv));
