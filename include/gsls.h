@@ -134,6 +134,19 @@ int gsls_spmv_dev(gsls_lhs *lhs, int dof, const void *dVal, int val_prec,
    Code/Source/svFSILS/DOT.f:56-110, NORM.f:55-110); result on the host. */
 int gsls_dot_dev(gsls_lhs *lhs, int dof, const double *du, const double *dv,
                  double *result);
+
+/* No counterpart in the reference.  Dot product of two device vectors of
+   length n (result on the host), for callers that cannot call cudaMalloc:
+   it allocates no device memory.  Its reduction scratch is a fixed
+   ~139 KB array in the library's device image, held by every GPU that
+   loads the library until the process exits; n <= 67,108,864, larger n is
+   rejected with GSLS_ERR_ARG.  The first call on a device resolves the
+   array's address (cudaGetSymbolAddress) with that device current; make it
+   before any stream capture.  All calls share the array: calls that
+   overlap on the GPU (other streams, other host threads) race.  stream is
+   a cudaStream_t (NULL = the default stream). */
+int gsls_dot_noalloc(long long n, const double *du, const double *dv,
+                     double *result, void *stream);
 int gsls_norm_dev(gsls_lhs *lhs, int dof, const double *du, double *result);
 
 /* CUDA stream used by every call on this lhs (cudaStream_t as void*;

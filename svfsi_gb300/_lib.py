@@ -79,6 +79,8 @@ SIGNATURES = {
                                 C.c_void_p]),
     "gsls_dot_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, c_double_p]),
     "gsls_norm_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, c_double_p]),
+    "gsls_dot_noalloc": (C.c_int, [C.c_longlong, C.c_void_p, C.c_void_p, c_double_p,
+                                   C.c_void_p]),
     "gsls_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gsls_get_stream": (C.c_void_p, [C.c_void_p]),
     "gsls_mesh_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_int, C.c_int, c_int_p,

@@ -30,6 +30,7 @@ SOURCES = [
     "gsls_assemble.cu",
     "gsls_eq.cu",
     "gsls_gmres.cu",
+    "gsls_noalloc.cu",
 ]
 
 
