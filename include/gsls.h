@@ -250,6 +250,22 @@ typedef struct {
   double t_solve_ms;    /* device time in the linear solve */
 } gsls_step_info;
 
+/* Aliev-Panfilov cell model for a GSLS_PHYS_CEP equation: the reaction
+   step of CEPINTEG/CEPINTEGL (Code/Source/svFSI/CEPION.f:166-400,
+   CEPMOD_AP.f:125-184), run per node at the start of every step before
+   the diffusion solve.  The stimulus of amplitude A is applied on
+   [Ts + k CL, Ts + k CL + Td] to the listed nodes (1-based). */
+typedef struct {
+  int ode;          /* 0 forward Euler, 1 RK4 */
+  double dt_ode;    /* ODE substep (cep%dt); nt = round(dt/dt_ode) */
+  double A, Ts, Td, CL;
+  double V0, X20;   /* initial voltage and recovery variable */
+} gsls_cep_params;
+int gsls_eq_set_cep(gsls_eq *eq, const gsls_cep_params *c, int nStim,
+                    const int *stimNodes);
+/* Cell state Xion(2,nNo) (voltage, recovery) to the host. */
+int gsls_eq_get_cep_state(gsls_eq *eq, double *Xion);
+
 /* Advance one time step. */
 int gsls_eq_step(gsls_eq *eq, gsls_step_info *info);
 /* Per-element parameter update (host, original element order). */

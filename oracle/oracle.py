@@ -51,6 +51,11 @@ class TracBC(C.Structure):
     _fields_ = [("nFel", C.c_int), ("fIEN", c_int_p), ("h", C.c_double * 3)]
 
 
+class CepP(C.Structure):
+    _fields_ = [("ode", C.c_int), ("dt_ode", C.c_double), ("A", C.c_double), ("Ts", C.c_double),
+                ("Td", C.c_double), ("CL", C.c_double), ("Ksac", C.c_double)]
+
+
 class Eq(C.Structure):
     _fields_ = [("p", EqP), ("nNo", C.c_int), ("nEl", C.c_int), ("IEN", c_int_p),
                 ("x", c_double_p), ("rowPtr", c_int_p), ("colPtr", c_int_p), ("nnz", C.c_int),
@@ -63,7 +68,9 @@ class Eq(C.Structure):
                 ("eqAbsTol", C.c_double),
                 ("Ao", c_double_p), ("Yo", c_double_p), ("Do", c_double_p),
                 ("An", c_double_p), ("Yn", c_double_p), ("Dn", c_double_p),
-                ("eq_iNorm", C.c_double), ("eq_pNorm", C.c_double)]
+                ("eq_iNorm", C.c_double), ("eq_pNorm", C.c_double),
+                ("cep", CepP), ("stim", c_int_p), ("Xion", c_double_p), ("time", C.c_double),
+                ("cep_ipass_done", C.c_int)]
 
 
 class StepInfo(C.Structure):
@@ -279,6 +286,16 @@ class OracleEquation:
         self.An, self.Yn, self.Dn = (keep(np.zeros(shp)) for _ in range(3))
         eq.Ao, eq.Yo, eq.Do = dp(self.Ao), dp(self.Yo), dp(self.Do)
         eq.An, eq.Yn, eq.Dn = dp(self.An), dp(self.Yn), dp(self.Dn)
+        self.Xion = keep(np.zeros((p.nNo, 2)))
+        if getattr(p, "cep", None):
+            c = p.cep
+            eq.cep.ode, eq.cep.dt_ode = c["ode"], c["dt_ode"]
+            eq.cep.A, eq.cep.Ts, eq.cep.Td, eq.cep.CL = c["A"], c["Ts"], c["Td"], c["CL"]
+            eq.cep.Ksac = 0.0
+            eq.stim = ip(keep(i32(p.stim)))
+            self.Xion[:, 0] = c["V0"]
+            self.Xion[:, 1] = c["X20"]
+        eq.Xion = dp(self.Xion)
         self.eq = eq
 
     def set_state(self, Ao, Yo, Do):

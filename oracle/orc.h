@@ -135,6 +135,25 @@ void orc_pk2cc_nhk(double C10, double Kpen, const double F[9], double S[9],
 void orc_traction(int dof, int nFel, const int *fIEN, const double *x,
                   const double h[3], double *R);
 
+/* CEP3D with isotropic diffusivity, F/CEP.f:136-266 (no fibres) */
+void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12],
+                  const double *al, const double *yl, double lR[4], double lK[16]);
+
+/* Aliev-Panfilov cell model (F/CEPMOD_AP.f, F/PARAMS_AP.f:53-86) and the
+   per-node integration of CEPINTEGL (F/CEPION.f:319-400). */
+typedef struct {
+  int ode;          /* 0 forward Euler (AP_INTEGFE), 1 RK4 (AP_INTEGRK) */
+  double dt_ode;    /* cep%dt (substep), nt = NINT(dt/dt_ode) */
+  double A, Ts, Td, CL; /* stimulus amplitude, start, duration, cycle */
+  double Ksac;
+} orc_cep;
+void orc_ap_getf(const double X[2], double f[2], double fext);
+void orc_ap_step(double X[2], double t, double dt, double Istim, double Ksac,
+                 int rk4);
+/* integrate one node over [t1, t1+dt] (CEPINTEGL for cepModel_AP) */
+void orc_cep_integ_node(const orc_cep *c, double t1, double dt, int stim,
+                        double X[2]);
+
 /* gen-alpha coefficients, F/INITIALIZE.f:76-139 */
 void orc_genalpha(double roInf, int second_order, double *am, double *af,
                   double *beta, double *gam);
@@ -172,6 +191,13 @@ typedef struct {
   /* eq%iNorm (first Newton residual of the run) and eq%pNorm (first of the
      current step), F/MOD.f:700-706; start at 0 */
   double eq_iNorm, eq_pNorm;
+  /* CEP: cell model, stimulated-node flags (nNo, may be NULL), Xion(2,nNo),
+     simulation time and the first-pass flag of CEPINTEG */
+  orc_cep cep;
+  const int *stim;
+  double *Xion;
+  double time;
+  int cep_ipass_done;
 } orc_eq;
 
 typedef struct {

@@ -185,6 +185,97 @@ void orc_elem_heats(const orc_eqp *p, const double xl[12], const double *al,
   }
 }
 
+/* CEP3D, F/CEP.f:136-266, isotropic D = Diso I (no fibres, no
+   electromechanical coupling), one tet4 element. */
+void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12], const double *al,
+                  const double *yl, double lR[4], double lK[16]) {
+  double w4[4], N4[4][4], Nx[3][4], Jac;
+  tet4_gauss(w4, N4);
+  gnn3(xl, Nx, &Jac);
+  for (int a = 0; a < 4; a++) lR[a] = 0.0;
+  for (int k = 0; k < 16; k++) lK[k] = 0.0;
+  const double T1 = p->af * p->gam * p->dt;
+  const double amd = p->am / T1;
+  const int i = p->s, tD = p->tDof;
+  double D[3][3] = {{Diso, 0, 0}, {0, Diso, 0}, {0, 0, Diso}};
+  for (int g = 0; g < 4; g++) {
+    const double w = w4[g] * Jac, wl = w * T1;
+    const double *N = N4[g];
+    double Vd = 0.0, Vx[3] = {0, 0, 0}, DNx[3][4];
+    for (int a = 0; a < 4; a++) {
+      Vd = Vd + N[a] * al[a * tD + i];
+      for (int k = 0; k < 3; k++) Vx[k] = Vx[k] + Nx[k][a] * yl[a * tD + i];
+      for (int k = 0; k < 3; k++) DNx[k][a] = D[k][0] * Nx[0][a] + D[k][1] * Nx[1][a] + D[k][2] * Nx[2][a];
+    }
+    double DVx[3];
+    for (int k = 0; k < 3; k++) DVx[k] = D[k][0] * Vx[0] + D[k][1] * Vx[1] + D[k][2] * Vx[2];
+    for (int a = 0; a < 4; a++) {
+      lR[a] = lR[a] + w * (N[a] * Vd + Nx[0][a] * DVx[0] + Nx[1][a] * DVx[1] + Nx[2][a] * DVx[2]);
+      for (int b = 0; b < 4; b++)
+        lK[a * 4 + b] = lK[a * 4 + b] +
+                        wl * (N[a] * N[b] * amd + Nx[0][a] * DNx[0][b] + Nx[1][a] * DNx[1][b] +
+                              Nx[2][a] * DNx[2][b]);
+    }
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Aliev-Panfilov: parameters F/PARAMS_AP.f:53-86, AP_GETF
+   F/CEPMOD_AP.f:255-267, AP_INTEGFE/AP_INTEGRK F/CEPMOD_AP.f:125-184 */
+static const double AP_Vscale = 100.0, AP_Tscale = 12.9, AP_Voffset = -80.0;
+static const double AP_alpha = 1e-2, AP_a = 2e-3, AP_b = 0.15, AP_c = 8.0;
+static const double AP_mu1 = 0.2, AP_mu2 = 0.3, AP_Vrest = -80.0;
+
+void orc_ap_getf(const double X[2], double f[2], double fext) {
+  f[0] = X[0] * (AP_c * (X[0] - AP_alpha) * (1.0 - X[0]) - X[1]) + fext;
+  f[1] = (AP_a + AP_mu1 * X[1] / (AP_mu2 + X[0])) * (-X[1] - AP_c * X[0] * (X[0] - AP_b - 1.0));
+}
+
+void orc_ap_step(double X[2], double Ts, double Ti, double Istim, double Ksac, int rk4) {
+  const double dt = Ti / AP_Tscale;
+  const double Isac = Ksac * (AP_Vrest - X[0]);
+  const double fext = (Istim + Isac) * AP_Tscale / AP_Vscale;
+  (void)Ts;
+  X[0] = (X[0] - AP_Voffset) / AP_Vscale;
+  if (!rk4) {
+    double f[2];
+    orc_ap_getf(X, f, fext);
+    X[0] = X[0] + dt * f[0];
+    X[1] = X[1] + dt * f[1];
+  } else {
+    const double dt6 = dt / 6.0;
+    double Xr[2], f1[2], f2[2], f3[2], f4[2];
+    Xr[0] = X[0];
+    Xr[1] = X[1];
+    orc_ap_getf(Xr, f1, fext);
+    for (int k = 0; k < 2; k++) Xr[k] = X[k] + 0.5 * dt * f1[k];
+    orc_ap_getf(Xr, f2, fext);
+    for (int k = 0; k < 2; k++) Xr[k] = X[k] + 0.5 * dt * f2[k];
+    orc_ap_getf(Xr, f3, fext);
+    for (int k = 0; k < 2; k++) Xr[k] = X[k] + dt * f3[k];
+    orc_ap_getf(Xr, f4, fext);
+    for (int k = 0; k < 2; k++) X[k] = X[k] + dt6 * (f1[k] + 2.0 * (f2[k] + f3[k]) + f4[k]);
+  }
+  X[0] = X[0] * AP_Vscale + AP_Voffset;
+}
+
+/* CEPINTEGL for cepModel_AP, F/CEPION.f:319-370 (no stretch: I4f <= 1). */
+void orc_cep_integ_node(const orc_cep *c, double t1, double dt, int stim, double X[2]) {
+  const double eps = 2.220446049250313e-16;
+  const double Ksac = 0.0;
+  (void)c->Ksac;
+  const int nt = (int)lround(dt / c->dt_ode);
+  int icl = (int)floor(t1 / c->CL);
+  if (icl < 0) icl = 0;
+  const double Ts = c->Ts + (double)icl * c->CL;
+  const double Te = Ts + c->Td;
+  for (int i = 1; i <= nt; i++) {
+    const double t = t1 + (double)(i - 1) * c->dt_ode;
+    const double Istim = (stim && t >= Ts - eps && t <= Te + eps) ? c->A : 0.0;
+    orc_ap_step(X, t, c->dt_ode, Istim, Ksac, c->ode == 1);
+  }
+}
+
 /* ---------------------------------------------------------------------- */
 /* 3x3 helpers, F/MATFUN.f (MAT_DET:177, MAT_INV:238, TEN_*:419-478) */
 #define M3(A, i, j) A[(i)*3 + (j)]
@@ -404,6 +495,10 @@ int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
       const double C10e = p->eparam ? p->eparam[e] : 0.0;
       orc_elem_struct(p, C10e, xl, al, yl, dl, lR, lK);
       orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+    } else if (p->phys == 3) {
+      double lR[4], lK[16];
+      orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso, xl, al, yl, lR, lK);
+      orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
     } else {
       return -2;
     }
@@ -448,6 +543,10 @@ int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
         double lR[12], lK[144];
         orc_elem_struct(p, p->eparam ? p->eparam[e] : 0.0, xl, al, yl, dl, lR, lK);
         orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+      } else if (p->phys == 3) {
+        double lR[4], lK[16];
+        orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso, xl, al, yl, lR, lK);
+        orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
       }
     }
   }
@@ -524,6 +623,22 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
   const double dt = eq->p.dt, gam = eq->p.gam, beta = eq->p.beta;
   const int dFlag = (eq->p.phys == 2);
   memset(info, 0, sizeof(*info));
+  eq->time += dt;
+  /* CEP: reaction step (CEPINTEG, F/CEPION.f:166-314, called from PICP):
+     Xion(1) = Yo(v) (not on the first pass), integrate the cell model from
+     time-dt over dt, Yo(v) = Xion(1) */
+  if (eq->p.phys == 3) {
+    for (int a = 0; a < nNo; a++) {
+      double X[2];
+      X[0] = eq->cep_ipass_done ? eq->Yo[(size_t)a * tD + eq->p.s] : eq->Xion[(size_t)a * 2];
+      X[1] = eq->Xion[(size_t)a * 2 + 1];
+      orc_cep_integ_node(&eq->cep, eq->time - dt, dt, eq->stim ? eq->stim[a] : 0, X);
+      eq->Xion[(size_t)a * 2] = X[0];
+      eq->Xion[(size_t)a * 2 + 1] = X[1];
+      eq->Yo[(size_t)a * tD + eq->p.s] = X[0];
+    }
+    eq->cep_ipass_done = 1;
+  }
   /* PICP */
   const double coef = (gam - 1.0) / gam;
   for (size_t k = 0; k < nS; k++) eq->An[k] = eq->Ao[k] * coef;
@@ -622,6 +737,9 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
     info->r1_last = r1;
   }
   info->newton_itr = itr;
+  /* PICC for CEP: Xion(1) = Yn(s) (F/PIC.f:232-238) */
+  if (eq->p.phys == 3)
+    for (int a = 0; a < nNo; a++) eq->Xion[(size_t)a * 2] = eq->Yn[(size_t)a * tD + eq->p.s];
   memcpy(eq->Ao, eq->An, nS * sizeof(double));
   memcpy(eq->Yo, eq->Yn, nS * sizeof(double));
   if (dFlag) memcpy(eq->Do, eq->Dn, nS * sizeof(double));

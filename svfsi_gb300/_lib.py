@@ -53,6 +53,11 @@ class EqSolver(C.Structure):
                 ("tol", C.c_double), ("absTol", C.c_double), ("precision", C.c_int)]
 
 
+class CepParams(C.Structure):
+    _fields_ = [("ode", C.c_int), ("dt_ode", C.c_double), ("A", C.c_double), ("Ts", C.c_double),
+                ("Td", C.c_double), ("CL", C.c_double), ("V0", C.c_double), ("X20", C.c_double)]
+
+
 class StepInfo(C.Structure):
     _fields_ = [("newton_itr", C.c_int), ("ls_itr_total", C.c_int),
                 ("last_iNorm", C.c_double), ("r1_last", C.c_double), ("last_suc", C.c_int),
@@ -102,6 +107,8 @@ SIGNATURES = {
     "gsls_eq_state_dev": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                     C.POINTER(C.c_void_p)]),
     "gsls_eq_step": (C.c_int, [C.c_void_p, C.POINTER(StepInfo)]),
+    "gsls_eq_set_cep": (C.c_int, [C.c_void_p, C.POINTER(CepParams), C.c_int, c_int_p]),
+    "gsls_eq_get_cep_state": (C.c_int, [C.c_void_p, c_double_p]),
     "gsls_eq_set_eparam": (C.c_int, [C.c_void_p, c_double_p]),
     "gsls_launch_count": (C.c_longlong, []),
     "gsls_profile_enable": (C.c_int, [C.c_int]),

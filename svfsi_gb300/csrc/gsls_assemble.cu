@@ -213,6 +213,13 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   A.rho = p->rho;
   A.cond = p->cond;
   A.src = p->src;
+  if (p->phys == GSLS_PHYS_CEP) {
+    // isotropic CEP3D (Code/Source/svFSI/CEP.f:136-266) is HEATS3D with
+    // unit density, no source and conductivity Diso
+    A.rho = 1.0;
+    A.src = 0.0;
+    A.cond = p->Diso;
+  }
   A.C10 = p->C10;
   A.Kpen = p->Kpen;
   A.visc = p->visc;
@@ -234,7 +241,7 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
     A.nColorEl = m->color_off[c + 1] - m->color_off[c];
     if (A.nColorEl <= 0) continue;
     const int nb = (A.nColorEl + kAsmThreads - 1) / kAsmThreads;
-    if (p->phys == GSLS_PHYS_HEATS) {
+    if (p->phys == GSLS_PHYS_HEATS || p->phys == GSLS_PHYS_CEP) {
       if (dof != 1) return GSLS_ERR_ARG;
       if (mixed)
         k_asm_heats<float><<<nb, kAsmThreads, 0, st>>>(A);

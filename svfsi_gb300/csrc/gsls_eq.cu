@@ -40,6 +40,12 @@ struct gsls_eq {
   std::vector<Dir *> dirs;
   int nextFace = 0;
   double eq_iNorm = 0.0, eq_pNorm = 0.0;
+  // CEP cell model
+  bool has_cep = false, cep_first = true;
+  gsls_cep_params cep{};
+  gsls::DevBuf Xion;   // double 2 x nNo
+  gsls::DevBuf stim;   // int per node
+  double time = 0.0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   ~gsls_eq() {
     for (auto *d : dirs) delete d;
@@ -121,6 +127,67 @@ __global__ void k_picc(int nNo, int tDof, int s, int dof, double c1, double c2,
     Yn[k] = Yn[k] - r * c1;
     Dn[k] = Dn[k] - r * c2;
   }
+}
+
+// Aliev-Panfilov right-hand side (AP_GETF, Code/Source/svFSI/CEPMOD_AP.f:
+// 255-267) with the parameters of PARAMS_AP.f:53-86, in precision T.
+template <class T>
+__device__ __forceinline__ void ap_f(T x0, T x1, T fext, T &f0, T &f1) {
+  const T c = T(8.0), alpha = T(1e-2), a = T(2e-3), b = T(0.15), mu1 = T(0.2), mu2 = T(0.3);
+  f0 = x0 * (c * (x0 - alpha) * (T(1) - x0) - x1) + fext;
+  f1 = (a + mu1 * x1 / (mu2 + x0)) * (-x1 - c * x0 * (x0 - b - T(1)));
+}
+
+// Reaction step of CEPINTEG for every node: Xion(1) = Yo(v) (after the
+// first pass), nt substeps of AP_INTEGFE / AP_INTEGRK with the stimulus
+// window of CEPINTEGL, then Yo(v) = Xion(1).  T = float in mixed mode.
+template <class T>
+__global__ void k_cep_ionic(int nNo, int tDof, int s, double *__restrict__ Yo,
+                            double *__restrict__ Xion, const int *__restrict__ stim, int first,
+                            int ode, int nt, double dt_ode, double t1, double Ts, double Te,
+                            double A) {
+  const T Vscale = T(100.0), Tscale = T(12.9), Voffset = T(-80.0);
+  const double eps = 2.220446049250313e-16;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x) {
+    double V = first ? Xion[2 * (size_t)a] : Yo[(size_t)a * tDof + s];
+    T x1 = T(Xion[2 * (size_t)a + 1]);
+    const bool st = stim && stim[a];
+    const T dt = T(dt_ode) / Tscale;
+    T x0 = T(V);
+    for (int i = 1; i <= nt; i++) {
+      const double t = t1 + (double)(i - 1) * dt_ode;
+      const T Istim = (st && t >= Ts - eps && t <= Te + eps) ? T(A) : T(0);
+      const T fext = Istim * Tscale / Vscale;  // Isac = 0 (no stretch)
+      T X0 = (x0 - Voffset) / Vscale, X1 = x1;
+      if (ode == 0) {
+        T f0, f1;
+        ap_f<T>(X0, X1, fext, f0, f1);
+        X0 = X0 + dt * f0;
+        X1 = X1 + dt * f1;
+      } else {
+        T k0[4], k1[4];
+        ap_f<T>(X0, X1, fext, k0[0], k1[0]);
+        ap_f<T>(X0 + T(0.5) * dt * k0[0], X1 + T(0.5) * dt * k1[0], fext, k0[1], k1[1]);
+        ap_f<T>(X0 + T(0.5) * dt * k0[1], X1 + T(0.5) * dt * k1[1], fext, k0[2], k1[2]);
+        ap_f<T>(X0 + dt * k0[2], X1 + dt * k1[2], fext, k0[3], k1[3]);
+        const T dt6 = dt / T(6);
+        X0 = X0 + dt6 * (k0[0] + T(2) * (k0[1] + k0[2]) + k0[3]);
+        X1 = X1 + dt6 * (k1[0] + T(2) * (k1[1] + k1[2]) + k1[3]);
+      }
+      x0 = X0 * Vscale + Voffset;
+      x1 = X1;
+    }
+    Xion[2 * (size_t)a] = double(x0);
+    Xion[2 * (size_t)a + 1] = double(x1);
+    Yo[(size_t)a * tDof + s] = double(x0);
+  }
+}
+
+// Xion(1) = Yn(v) after the Newton loop (PICC for CEP, PIC.f:232-238)
+__global__ void k_cep_sync(int nNo, int tDof, int s, const double *__restrict__ Yn,
+                           double *__restrict__ Xion) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x)
+    Xion[2 * (size_t)a] = Yn[(size_t)a * tDof + s];
 }
 
 __global__ void k_axpy1(size_t n, double *__restrict__ y, const double *__restrict__ x) {
@@ -284,6 +351,45 @@ int gsls_eq_add_traction(gsls_eq *eq, int nFel, const int *fIEN, const double h[
   return GSLS_OK;
 }
 
+int gsls_eq_set_cep(gsls_eq *eq, const gsls_cep_params *c, int nStim, const int *stimNodes) {
+  if (!eq || !c || nStim < 0 || (nStim > 0 && !stimNodes)) return GSLS_ERR_ARG;
+  if (eq->p.phys != GSLS_PHYS_CEP || eq->p.dof != 1) {
+    set_error("gsls_eq_set_cep: the equation is not a CEP equation");
+    return GSLS_ERR_ARG;
+  }
+  if (!(c->dt_ode > 0.0) || (c->ode != 0 && c->ode != 1)) return GSLS_ERR_ARG;
+  const int nNo = eq->nNo;
+  std::vector<int> flag(nNo, 0);
+  for (int k = 0; k < nStim; k++) {
+    const int a = stimNodes[k] - 1;
+    if (a < 0 || a >= nNo) return GSLS_ERR_ARG;
+    flag[a] = 1;
+  }
+  std::vector<double> X((size_t)2 * nNo);
+  for (int a = 0; a < nNo; a++) {
+    X[2 * (size_t)a] = c->V0;
+    X[2 * (size_t)a + 1] = c->X20;
+  }
+  cudaStream_t st = eq->lhs->stream;
+  GSLS_TRY(eq->Xion.alloc(sizeof(double) * X.size()));
+  GSLS_TRY(eq->stim.alloc(sizeof(int) * nNo));
+  GSLS_CUDA(cudaMemcpyAsync(eq->Xion.p, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(eq->stim.p, flag.data(), sizeof(int) * nNo, cudaMemcpyHostToDevice, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  eq->cep = *c;
+  eq->has_cep = true;
+  eq->cep_first = true;
+  eq->time = 0.0;
+  return GSLS_OK;
+}
+
+int gsls_eq_get_cep_state(gsls_eq *eq, double *Xion) {
+  if (!eq || !Xion || !eq->has_cep) return GSLS_ERR_ARG;
+  GSLS_CUDA(cudaMemcpy(Xion, eq->Xion.p, sizeof(double) * 2 * (size_t)eq->nNo,
+                       cudaMemcpyDeviceToHost));
+  return GSLS_OK;
+}
+
 int gsls_eq_set_state(gsls_eq *eq, const double *Ao, const double *Yo, const double *Do) {
   if (!eq || !Ao || !Yo) return GSLS_ERR_ARG;
   const size_t nb = sizeof(double) * (size_t)eq->nNo * eq->p.tDof;
@@ -330,6 +436,30 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
   double *An = eq->st[3].as<double>(), *Yn = eq->st[4].as<double>(), *Dn = eq->st[5].as<double>();
   double *Ag = eq->st[6].as<double>(), *Yg = eq->st[7].as<double>(), *Dg = eq->st[8].as<double>();
   const int valp = eq->sv.precision;
+  eq->time += p.dt;
+  // CEP reaction step on Yo (CEPINTEG is called from PICP before Yn = Yo)
+  if (p.phys == GSLS_PHYS_CEP) {
+    if (!eq->has_cep) {
+      set_error("gsls_eq_step: CEP equation without gsls_eq_set_cep");
+      return GSLS_ERR_STATE;
+    }
+    const gsls_cep_params &c = eq->cep;
+    const double t1 = eq->time - p.dt;
+    const int nt = (int)llround(p.dt / c.dt_ode);
+    long long icl = (long long)floor(t1 / c.CL);
+    if (icl < 0) icl = 0;
+    const double Ts = c.Ts + (double)icl * c.CL, Te = Ts + c.Td;
+    if (valp == GSLS_PREC_MIXED)
+      k_cep_ionic<float><<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, Yo, eq->Xion.as<double>(),
+                                                   eq->stim.as<int>(), eq->cep_first ? 1 : 0,
+                                                   c.ode, nt, c.dt_ode, t1, Ts, Te, c.A);
+    else
+      k_cep_ionic<double><<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, Yo, eq->Xion.as<double>(),
+                                                    eq->stim.as<int>(), eq->cep_first ? 1 : 0,
+                                                    c.ode, nt, c.dt_ode, t1, Ts, Te, c.A);
+    GSLS_CHECK_LAUNCH();
+    eq->cep_first = false;
+  }
   // PICP: copy the whole state first so that unknowns of other equations
   // carry over, then predict this equation's block
   GSLS_CUDA(cudaMemcpyAsync(An, Ao, sizeof(double) * ns, cudaMemcpyDeviceToDevice, st));
@@ -395,6 +525,10 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     }
   }
   info->newton_itr = itr;
+  if (p.phys == GSLS_PHYS_CEP) {
+    k_cep_sync<<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, Yn, eq->Xion.as<double>());
+    GSLS_CHECK_LAUNCH();
+  }
   // Ao = An, Yo = Yn and, for equations with displacement, Do = Dn
   // (Code/Source/svFSI/MAIN.f:277-279): swap the buffers
   for (int k = 0; k < (eq->dFlag ? 3 : 2); k++) {

@@ -192,6 +192,19 @@ class Equation:
         check(_lib.load().gsls_eq_step(self.h, C.byref(info)), "gsls_eq_step")
         return info
 
+    def set_cep(self, cep: dict, stim_nodes0):
+        """Aliev-Panfilov reaction step (gsls_eq_set_cep); stim_nodes0 0-based."""
+        c = _lib.CepParams()
+        for k in ("ode", "dt_ode", "A", "Ts", "Td", "CL", "V0", "X20"):
+            setattr(c, k, cep[k])
+        s1 = _i32(np.asarray(stim_nodes0) + 1)
+        check(_lib.load().gsls_eq_set_cep(self.h, C.byref(c), s1.size, _ip(s1)), "gsls_eq_set_cep")
+
+    def get_cep_state(self):
+        X = np.zeros((self.nNo, 2))
+        check(_lib.load().gsls_eq_get_cep_state(self.h, _dp(X)), "gsls_eq_get_cep_state")
+        return X
+
     def set_eparam(self, ep):
         e = None if ep is None else _f64(ep)
         check(_lib.load().gsls_eq_set_eparam(self.h, _dp(e) if e is not None else None),

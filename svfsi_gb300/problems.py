@@ -16,7 +16,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import meshgen
-from ._lib import (LS_TYPE_CG, PHYS_HEATS, PHYS_STRUCT, PREC_FP64, PRECOND_FSILS, EqParams,
+from ._lib import (LS_TYPE_CG, PHYS_CEP, PHYS_HEATS, PHYS_STRUCT, PREC_FP64, PRECOND_FSILS, EqParams,
                    EqSolver)
 
 SEED = 20261203
@@ -70,6 +70,8 @@ class Problem:
     absTol: float = 1e-15
     nsteps: int = 10
     eparam: np.ndarray | None = None
+    cep: dict | None = None         # cell model and stimulus (CEP only)
+    stim: np.ndarray | None = None  # per-node stimulus flag (CEP only)
 
     @property
     def nNo(self):
@@ -107,7 +109,10 @@ class Problem:
 
     def initial_state(self):
         z = np.zeros((self.nNo, self.tDof))
-        return z.copy(), z.copy(), z.copy()
+        Y = z.copy()
+        if self.cep:
+            Y[:, 0] = self.cep["V0"]  # resting potential of the cell model
+        return z.copy(), Y, z.copy()
 
     def algorithmic_bytes(self, s_A: int, s_v: int):
         """Per-call algorithmic bytes of one CG iteration and one assembly
@@ -159,6 +164,26 @@ def struct_beam(nx: int = 176, ny: int = 44, nz: int = 44, nsteps: int = 10,
                    nsteps=nsteps, eparam=eparam)
 
 
+def cep_slab(nx: int = 135, ny: int = 135, nz: int = 27, nsteps: int = 5000,
+             A: float = -52.0, ode: int = 0, Diso: float = 0.1) -> Problem:
+    """Config: monodomain electrophysiology (Aliev-Panfilov) on a 10x10x2
+    slab (135x135x27 hexes -> 2,952,450 tets at full size), isotropic
+    diffusivity 0.1, stimulus amplitude A for 2 ms from t = 0 on the nodes
+    of the 1x1x2 corner block x <= 1, y <= 1, dt = 0.01, CG + diagonal
+    preconditioner.  The reference applies a stimulus per domain; here the
+    corner block is the explicit stimulated node set."""
+    x, ien = meshgen.kuhn_box(nx, ny, nz, 10.0, 10.0, 2.0)
+    rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
+    am, af, beta, gam = genalpha(0.2, second_order=False)
+    params = dict(am=am, af=af, beta=beta, gam=gam, dt=0.01, Diso=Diso)
+    stim = ((x[:, 0] <= 1.0 + 1e-12) & (x[:, 1] <= 1.0 + 1e-12)).astype(np.int32)
+    cep = dict(ode=ode, dt_ode=0.01, A=A, Ts=0.0, Td=2.0, CL=1e9, V0=-80.0, X20=1e-3)
+    return Problem(name=f"cep_slab_{nx}x{ny}x{nz}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
+                   phys=PHYS_CEP, dof=1, tDof=1, params=params, LS_type=LS_TYPE_CG,
+                   prec=PRECOND_FSILS, minItr=1, maxItr=5, tol=1e-6, nsteps=nsteps,
+                   cep=cep, stim=stim)
+
+
 def make_lhs_arrays(p: Problem):
     """1-based rowPtr/colPtr/gNodes for FSILS_LHS_CREATE."""
     return (np.arange(1, p.nNo + 1, dtype=np.int32), (p.rowPtr + 1).astype(np.int32),
@@ -179,6 +204,8 @@ def build_equation(p: Problem, precision=PREC_FP64):
         eq.add_dirichlet(d.nodes, d.g, d.gx, d.mask)
     for t in p.traction:
         eq.add_traction(t.faces, t.h)
+    if p.cep:
+        eq.set_cep(p.cep, np.nonzero(p.stim)[0])
     Ao, Yo, Do = p.initial_state()
     eq.set_state(Ao, Yo, Do)
     return lhs, mesh, eq

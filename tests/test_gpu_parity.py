@@ -255,3 +255,27 @@ def test_solve_dev_mixed_fp32_inner(gsls, orc, case, lstype):
     assert np.linalg.norm(r) < 1e-3 * np.linalg.norm(R0[free])
     if lstype == "cg":
         assert rel(x, Ro) < 1e-3
+
+
+@pytest.mark.parametrize("precision,ode,A", [("fp64", 0, -52.0), ("fp64", 1, 52.0),
+                                             ("mixed", 0, 52.0)])
+def test_cep_steps(gsls, orc, precision, ode, A):
+    """Monodomain Aliev-Panfilov slab: reaction step + diffusion solve per
+    step, against the oracle; the +52 amplitude fires an activation wave."""
+    p = problems.cep_slab(16, 16, 3, nsteps=60, A=A, ode=ode)
+    if precision == "mixed":
+        p.tol, p.maxItr = 1e-12, 8
+    prec = fsils.PREC_FP64 if precision == "fp64" else fsils.PREC_MIXED
+    lhs, mesh, eq = problems.build_equation(p, precision=prec)
+    oeq = orc.OracleEquation(p)
+    for s in range(p.nsteps):
+        eq.step()
+        oeq.step()
+    _, Y, _ = eq.get_state()
+    _, Yo, _ = oeq.state()
+    X = eq.get_cep_state()
+    tol = 1e-10 if precision == "fp64" else 1e-6
+    assert rel(Y, Yo) < tol
+    assert rel(X[:, 1], oeq.Xion[:, 1]) < (1e-9 if precision == "fp64" else 1e-5)
+    if A > 0:
+        assert Y.max() > 0.0  # the stimulated corner fired

@@ -247,3 +247,34 @@ def test_struct_tangent_is_residual_derivative(orc):
     fd = (R_at(h) - R_at(-h)).ravel() / (2 * h)
     pred = am * (Kc @ dA.ravel()) / am  # lK is scaled so that K dA = dR/dAn
     assert np.allclose(fd, pred, rtol=1e-5, atol=1e-6 * np.abs(pred).max())
+
+
+def _ap_run(orc, rk4, dt, T, stim_A=52.0):
+    import ctypes as C
+    X = (C.c_double * 2)(-80.0, 1e-3)
+    n = int(round(T / dt))
+    for i in range(n):
+        t = i * dt
+        orc.load().orc_ap_step(X, C.c_double(t), C.c_double(dt), C.c_double(stim_A if t < 2.0 else 0.0),
+                               C.c_double(0.0), rk4)
+    return np.array([X[0], X[1]])
+
+
+def test_aliev_panfilov_rest_and_convergence(orc):
+    import ctypes as C
+    L = orc.load()
+    L.orc_ap_getf.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double]
+    L.orc_ap_step.argtypes = [C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double,
+                              C.c_double, C.c_int]
+    X = (C.c_double * 2)(0.0, 0.0)
+    f = (C.c_double * 2)()
+    L.orc_ap_getf(X, f, 0.0)
+    assert f[0] == 0.0 and f[1] == 0.0  # the (scaled) rest state is a fixed point
+    # FE and RK4 trajectories converge to the same solution as dt -> 0:
+    # FE first order (error halves with dt), RK4 high order (>= 16x from
+    # dt 0.4 to 0.2, roundoff-level at the CEP step 0.01)
+    ref = _ap_run(orc, 1, 0.0025, 20.0)
+    e_fe = [np.abs(_ap_run(orc, 0, dt, 20.0) - ref).max() for dt in (0.02, 0.01)]
+    assert 1.8 < e_fe[0] / e_fe[1] < 2.2
+    e_rk = [np.abs(_ap_run(orc, 1, dt, 20.0) - ref).max() for dt in (0.4, 0.2, 0.01)]
+    assert e_rk[0] / e_rk[1] > 16 and e_rk[2] < 1e-10
