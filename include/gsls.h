@@ -224,9 +224,19 @@ int gsls_eq_free(gsls_eq *eq);
 /* Strong Dirichlet BC on a node list (1-based): component c of the
    equation is set to g*gx[a] (Yn) with An = 0 when bit c of mask is set
    (mask = 0: all components); the face also enters the linear solver as a
-   BC_TYPE_DIR face.  gx nullable (= 1). */
+   BC_TYPE_DIR face.  gx nullable (= 1).  For a dof = 4 (fluid) equation
+   only the three velocity components are constrained.  Replaces the
+   SETBCDIR/FSILSINI pair (Code/Source/svFSI/SETBC.f:39-228,
+   BAFINI.f:488-512). */
 int gsls_eq_add_dirichlet(gsls_eq *eq, int nNo, const int *gNodes,
                           const double *gx, double g, int mask);
+/* Same with unit normals nV (3 x nNo): component c is set to
+   g*gx[a]*nV[a][c], the vector form SETBCDIRL uses when the BC carries nsd
+   values (Code/Source/svFSI/SETBC.f:212-217), e.g. an inflow profile along
+   the inward normal.  nV nullable (= plain form). */
+int gsls_eq_add_dirichlet_nv(gsls_eq *eq, int nNo, const int *gNodes,
+                             const double *gx, const double *nV, double g,
+                             int mask);
 /* Constant traction h on tri3 faces (fIEN 1-based, 3 x nFel), integrated
    as SETBCTRACL does (Code/Source/svFSI/SETBC.f:319-416). */
 int gsls_eq_add_traction(gsls_eq *eq, int nFel, const int *fIEN,

@@ -38,13 +38,13 @@ class EqP(C.Structure):
                 ("rho", C.c_double), ("cond", C.c_double), ("src", C.c_double),
                 ("C10", C.c_double), ("Kpen", C.c_double), ("visc", C.c_double),
                 ("dmp", C.c_double), ("fb", C.c_double * 3), ("Diso", C.c_double),
-                ("mu_f", C.c_double), ("rho_f", C.c_double), ("ctM", C.c_double),
+                ("mu_f", C.c_double), ("ctM", C.c_double),
                 ("ctC", C.c_double), ("eparam", c_double_p)]
 
 
 class DirBC(C.Structure):
-    _fields_ = [("nNo", C.c_int), ("nodes", c_int_p), ("gx", c_double_p), ("g", C.c_double),
-                ("mask", C.c_int)]
+    _fields_ = [("nNo", C.c_int), ("nodes", c_int_p), ("gx", c_double_p), ("nV", c_double_p),
+                ("g", C.c_double), ("mask", C.c_int)]
 
 
 class TracBC(C.Structure):
@@ -113,6 +113,10 @@ def load():
                                      c_double_p, c_double_p]
         L.orc_elem_struct.argtypes = [C.POINTER(EqP), C.c_double, c_double_p, c_double_p,
                                       c_double_p, c_double_p, c_double_p, c_double_p]
+        L.orc_elem_fluid.argtypes = [C.POINTER(EqP), c_double_p, c_double_p, c_double_p,
+                                     c_double_p, c_double_p]
+        L.orc_ge.restype = C.c_int
+        L.orc_ge.argtypes = [C.c_int, C.c_int, c_double_p, c_double_p]
         L.orc_pk2cc_nhk.argtypes = [C.c_double, C.c_double, c_double_p, c_double_p, c_double_p]
         L.orc_genalpha.argtypes = [C.c_double, C.c_int, c_double_p, c_double_p, c_double_p,
                                    c_double_p]
@@ -262,6 +266,8 @@ class OracleEquation:
             dirs[k].nNo = d.nodes.size
             dirs[k].nodes = ip(keep(i32(d.nodes)))
             dirs[k].gx = dp(keep(f64(d.gx))) if d.gx is not None else None
+            nV = getattr(d, "nV", None)
+            dirs[k].nV = dp(keep(f64(nV))) if nV is not None else None
             dirs[k].g = d.g
             dirs[k].mask = d.mask
         keep(dirs)

@@ -90,6 +90,9 @@ void orc_gmres_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val,
                  double *R);
 void orc_gmres_ns(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val,
                   const double *R, double *X);
+void orc_cgrad_schur(orc_lhs *lhs, orc_subls *ls, int dof, const double *D,
+                     const double *G, const double *L, double *R);
+int orc_ge(int nV, int N, const double *A, double *B);
 void orc_nssolver(orc_lhs *lhs, orc_ls *ls, int dof, const double *Val, double *Ri);
 int orc_solve(orc_lhs *lhs, orc_ls *ls, int dof, double *Ri, double *Val,
               int prec, const int *incL, const double *res);
@@ -111,7 +114,7 @@ typedef struct {
   double C10, Kpen, visc, dmp; /* STRUCT nHK + ST91, solid_viscosity, damping */
   double fb[3];                /* body force */
   double Diso;                 /* CEP isotropic diffusivity */
-  double mu_f, rho_f;          /* FLUID viscosity, density */
+  double mu_f;                 /* FLUID viscosity (density: rho) */
   double ctM, ctC;             /* FLUID stabilisation constants */
   const double *eparam;        /* optional per-element parameter (mu or Diso) */
 } orc_eqp;
@@ -125,6 +128,8 @@ int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
                          const double *Dg, const int *rowPtr, const int *colPtr,
                          double *R, double *Val, int ncolor, const int *color_off,
                          const int *order);
+void orc_elem_fluid(const orc_eqp *p, const double xl[12], const double *al,
+                    const double *yl, double lR[16], double lK[256]);
 void orc_elem_heats(const orc_eqp *p, const double xl[12], const double *al,
                     const double *yl, double lR[4], double lK[16]);
 void orc_elem_struct(const orc_eqp *p, double mu_e, const double xl[12],
@@ -164,6 +169,7 @@ typedef struct {
   int nNo;
   const int *nodes;   /* 0-based */
   const double *gx;   /* spatial profile, length nNo (NULL = 1) */
+  const double *nV;   /* unit normals 3 x nNo for a vector BC (NULL = none) */
   double g;           /* value (dirY); dirA = 0 */
   int mask;           /* bit i set = component i constrained; 0 = all */
 } orc_dirbc;

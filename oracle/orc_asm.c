@@ -149,6 +149,184 @@ static void gnn3(const double xl[12], double Nx[3][4], double *Jac) {
   *Jac = J;
 }
 
+/* GNN (insd = 3) with the metric ks = xiX^T xiX, F/NN.f:1527-1545 */
+static void gnn3k(const double xl[12], double Nx[3][4], double *Jac, double ks[3][3]) {
+  double xXi[3][3] = {{0}}, xiX[3][3];
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++)
+      for (int k = 0; k < 3; k++) xXi[i][k] += xl[a * 3 + i] * TET4_NXI[k][a];
+  const double J = xXi[0][0] * xXi[1][1] * xXi[2][2] + xXi[0][1] * xXi[1][2] * xXi[2][0] +
+                   xXi[0][2] * xXi[1][0] * xXi[2][1] - xXi[0][0] * xXi[1][2] * xXi[2][1] -
+                   xXi[0][1] * xXi[1][0] * xXi[2][2] - xXi[0][2] * xXi[1][1] * xXi[2][0];
+  xiX[0][0] = (xXi[1][1] * xXi[2][2] - xXi[1][2] * xXi[2][1]) / J;
+  xiX[0][1] = (xXi[2][1] * xXi[0][2] - xXi[2][2] * xXi[0][1]) / J;
+  xiX[0][2] = (xXi[0][1] * xXi[1][2] - xXi[0][2] * xXi[1][1]) / J;
+  xiX[1][0] = (xXi[1][2] * xXi[2][0] - xXi[1][0] * xXi[2][2]) / J;
+  xiX[1][1] = (xXi[2][2] * xXi[0][0] - xXi[2][0] * xXi[0][2]) / J;
+  xiX[1][2] = (xXi[0][2] * xXi[1][0] - xXi[0][0] * xXi[1][2]) / J;
+  xiX[2][0] = (xXi[1][0] * xXi[2][1] - xXi[1][1] * xXi[2][0]) / J;
+  xiX[2][1] = (xXi[2][0] * xXi[0][1] - xXi[2][1] * xXi[0][0]) / J;
+  xiX[2][2] = (xXi[0][0] * xXi[1][1] - xXi[0][1] * xXi[1][0]) / J;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      ks[i][j] = xiX[0][i] * xiX[0][j] + xiX[1][i] * xiX[1][j] + xiX[2][i] * xiX[2][j];
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++)
+      Nx[i][a] = 0.0 + TET4_NXI[0][a] * xiX[0][i] + TET4_NXI[1][a] * xiX[1][i] +
+                 TET4_NXI[2][a] * xiX[2][i];
+  *Jac = J;
+}
+
+/* ISZERO, F/MATFUN.f:763-780: |a| / max(|a|, eps) < eps */
+static int iszero(double v) {
+  const double e = 2.220446049250313e-16;
+  const double a = fabs(v);
+  return a / fmax(a, e) < e;
+}
+
+/* CONSTRUCT_FLUID with FLUID3D_M and FLUID3D_C, F/FLUID.f:40-190,
+   :192-560, :813-1084, for one P1-P1 tet4 element with VMS stabilisation
+   (GETTHOODFS gives both passes the element's own basis and 4-point rule,
+   F/FS.f:270-286) and constant viscosity (GETVISCOSITY, F/FLUID.f:1705-1708:
+   mu_g = 0).  For tet4 the second derivatives Nwxx vanish (affine map), so
+   uxx, d2u2, es_x, mu_x and rS are identically zero and are left out; no
+   mesh motion.  al, yl: tDof x 4 (u, v, w, p first); lR[a*4+i]; lK[(a*4+b)*16
+   + r*4 + c] with the reference's lK(k,a,b), k = r*4 + c + 1. */
+void orc_elem_fluid(const orc_eqp *p, const double xl[12], const double *al,
+                    const double *yl, double lR[16], double lK[256]) {
+  double w4[4], N4[4][4], Nx[3][4], Jac, Kxi[3][3];
+  tet4_gauss(w4, N4);
+  gnn3k(xl, Nx, &Jac, Kxi);
+  for (int k = 0; k < 16; k++) lR[k] = 0.0;
+  for (int k = 0; k < 256; k++) lK[k] = 0.0;
+  const int tD = p->tDof;
+  const double ctM = p->ctM, ctC = p->ctC;
+  const double rho = p->rho, mu = p->mu_f;
+  const double f[3] = {p->fb[0], p->fb[1], p->fb[2]};
+  const double T1c = p->af * p->gam * p->dt;
+  const double amd = p->am / T1c;
+  const double eps = 2.220446049250313e-16;
+#define LK(k, a, b) lK[((a) * 4 + (b)) * 16 + (k) - 1]
+  /* pass 1: momentum (FLUID3D_M); pass 2: continuity (FLUID3D_C) -- both over
+     the same four Gauss points; they write disjoint lR/lK entries. */
+  for (int pass = 0; pass < 2; pass++)
+    for (int g = 0; g < 4; g++) {
+      const double w = w4[g] * Jac;
+      const double *N = N4[g];
+      const double wl = w * T1c, wr = w * rho;
+      double ud[3] = {-f[0], -f[1], -f[2]}, u[3] = {0, 0, 0}, ux[3][3] = {{0}};
+      for (int a = 0; a < 4; a++) {
+        for (int i = 0; i < 3; i++) {
+          ud[i] = ud[i] + N[a] * (al[a * tD + i] - 0.0);
+          u[i] = u[i] + N[a] * yl[a * tD + i];
+        }
+        for (int j = 0; j < 3; j++)
+          for (int i = 0; i < 3; i++) ux[i][j] = ux[i][j] + Nx[i][a] * yl[a * tD + j];
+      }
+      const double divU = ux[0][0] + ux[1][1] + ux[2][2];
+      double pr = 0.0, px[3] = {0, 0, 0};
+      for (int a = 0; a < 4; a++) {
+        pr = pr + N[a] * yl[a * tD + 3];
+        for (int i = 0; i < 3; i++) px[i] = px[i] + Nx[i][a] * yl[a * tD + 3];
+      }
+      double es[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) es[i][j] = ux[i][j] + ux[j][i];
+      double esNx[3][4];
+      for (int a = 0; a < 4; a++)
+        for (int i = 0; i < 3; i++)
+          esNx[i][a] = es[0][i] * Nx[0][a] + es[1][i] * Nx[1][a] + es[2][i] * Nx[2][a];
+      const double mu_g = 0.0;
+      const double kT = 4.0 * pow(ctM / p->dt, 2.0);
+      double kU = 0.0, kS = 0.0;
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) {
+          kU = kU + u[i] * u[j] * Kxi[i][j];
+          kS = kS + Kxi[i][j] * Kxi[i][j];
+        }
+      kS = ctC * kS * pow(mu / rho, 2.0);
+      const double tauM = 1.0 / (rho * sqrt(kT + kU + kS));
+      double rV[3], up[3];
+      for (int j = 0; j < 3; j++) rV[j] = ud[j] + u[0] * ux[0][j] + u[1] * ux[1][j] + u[2] * ux[2][j];
+      for (int j = 0; j < 3; j++) up[j] = -tauM * (rho * rV[j] + px[j] - 0.0);
+      if (pass == 0) {
+        const double tauC = 1.0 / (tauM * (Kxi[0][0] + Kxi[1][1] + Kxi[2][2]));
+        double tauB = 0.0;
+        for (int j = 0; j < 3; j++)
+          for (int i = 0; i < 3; i++) tauB = tauB + up[i] * up[j] * Kxi[i][j];
+        if (iszero(tauB)) tauB = eps;
+        tauB = rho / sqrt(tauB);
+        double ua[3];
+        for (int i = 0; i < 3; i++) ua[i] = u[i] + up[i];
+        const double pa = pr - tauC * divU;
+        double rM[3][3];
+        for (int j = 0; j < 3; j++)
+          rV[j] = tauB * (up[0] * ux[0][j] + up[1] * ux[1][j] + up[2] * ux[2][j]);
+        for (int j = 0; j < 3; j++)
+          for (int i = 0; i < 3; i++)
+            rM[i][j] = mu * es[i][j] - rho * up[j] * ua[i] + rV[j] * up[i] - (i == j ? pa : 0.0);
+        for (int j = 0; j < 3; j++)
+          rV[j] = ud[j] + ua[0] * ux[0][j] + ua[1] * ux[1][j] + ua[2] * ux[2][j];
+        double uNx[4], upNx[4], uaNx[4];
+        for (int a = 0; a < 4; a++) {
+          for (int j = 0; j < 3; j++)
+            lR[a * 4 + j] = lR[a * 4 + j] + wr * N[a] * rV[j] +
+                            w * (Nx[0][a] * rM[0][j] + Nx[1][a] * rM[1][j] + Nx[2][a] * rM[2][j]);
+          uNx[a] = u[0] * Nx[0][a] + u[1] * Nx[1][a] + u[2] * Nx[2][a];
+          upNx[a] = up[0] * Nx[0][a] + up[1] * Nx[1][a] + up[2] * Nx[2][a];
+          uaNx[a] = uNx[a] + upNx[a];
+        }
+        /* updu(i,j,b) = delta_ij (-rho uNx(b)) when Nwxx = mu_x = 0 */
+        for (int b = 0; b < 4; b++)
+          for (int a = 0; a < 4; a++) {
+            double NN[3][3];
+            for (int i = 0; i < 3; i++)
+              for (int j = 0; j < 3; j++) NN[i][j] = Nx[i][a] * Nx[j][b];
+            const double NxNx = Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b];
+            const double T1 = mu * NxNx + rho * amd * N[b] * (N[a] + rho * tauM * uaNx[a]) +
+                              rho * N[a] * (uNx[b] + upNx[b]) + tauB * upNx[a] * upNx[b];
+            const double upd = -rho * uNx[b];
+            /* row i (momentum component), column j (velocity component) */
+            for (int i = 0; i < 3; i++)
+              for (int j = 0; j < 3; j++) {
+                double T2 = (i == j ? (mu + tauC) * NN[i][i] : mu * NN[j][i] + tauC * NN[i][j]) +
+                            esNx[i][a] * mu_g * esNx[j][b] -
+                            rho * tauM * uaNx[a] * (i == j ? upd : 0.0);
+                LK(i * 4 + j + 1, a, b) += wl * (i == j ? T2 + T1 : T2);
+              }
+          }
+        for (int b = 0; b < 4; b++)
+          for (int a = 0; a < 4; a++) {
+            const double T1 = rho * tauM * uaNx[a];
+            for (int i = 0; i < 3; i++)
+              LK(i * 4 + 4, a, b) -= wl * (Nx[i][a] * N[b] - Nx[i][b] * T1);
+          }
+      } else {
+        for (int a = 0; a < 4; a++) {
+          const double upNx = up[0] * Nx[0][a] + up[1] * Nx[1][a] + up[2] * Nx[2][a];
+          lR[a * 4 + 3] = lR[a * 4 + 3] + w * (N[a] * divU - upNx);
+        }
+        for (int b = 0; b < 4; b++) {
+          const double T1 = rho * amd * N[b];
+          const double uNxb = u[0] * Nx[0][b] + u[1] * Nx[1][b] + u[2] * Nx[2][b];
+          const double upd = -rho * uNxb; /* updu(j,j,b) */
+          for (int a = 0; a < 4; a++)
+            for (int j = 0; j < 3; j++) {
+              /* T2 = sum_i Nqx(i,a) updu(j,i,b) - Nqx(j,a) T1 */
+              const double T2 = Nx[j][a] * (upd - T1);
+              LK(13 + j, a, b) += wl * (N[a] * Nx[j][b] - tauM * T2);
+            }
+        }
+        for (int b = 0; b < 4; b++)
+          for (int a = 0; a < 4; a++) {
+            const double NxNx = Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b];
+            LK(16, a, b) += wl * tauM * NxNx;
+          }
+      }
+    }
+#undef LK
+}
+
 /* ---------------------------------------------------------------------- */
 /* CONSTRUCT_HEATS / HEATS3D, F/HEATS.f:39-159 for one tet4 element.
    al, yl: tDof x 4 local copies; uses component p->s. */
@@ -499,6 +677,10 @@ int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
       double lR[4], lK[16];
       orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso, xl, al, yl, lR, lK);
       orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+    } else if (p->phys == 4) {
+      double lR[16], lK[256];
+      orc_elem_fluid(p, xl, al, yl, lR, lK);
+      orc_doassem(4, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
     } else {
       return -2;
     }
@@ -605,13 +787,18 @@ static void apply_dir(orc_eq *eq, double *lA, double *lY) {
   const int tD = eq->p.tDof, s = eq->p.s, dof = eq->p.dof;
   for (int ib = 0; ib < eq->nDir; ib++) {
     const orc_dirbc *bc = &eq->dir[ib];
+    /* the pressure of a dof = nsd+1 equation is never constrained
+       (F/SETBC.f:77); with lDof = nsd the value is g*gx*nV (SETBCDIRL,
+       F/SETBC.f:212-217), else g*gx */
+    const int ncomp = (dof == 4) ? 3 : dof;
     for (int a = 0; a < bc->nNo; a++) {
       const int Ac = bc->nodes[a];
       const double gx = bc->gx ? bc->gx[a] : 1.0;
-      for (int c = 0; c < dof; c++) {
+      for (int c = 0; c < ncomp; c++) {
         if (bc->mask && !((bc->mask >> c) & 1)) continue;
-        lA[(size_t)Ac * tD + s + c] = 0.0 * gx;
-        lY[(size_t)Ac * tD + s + c] = bc->g * gx;
+        const double nv = (bc->nV && ncomp == 3) ? bc->nV[(size_t)a * 3 + c] : 1.0;
+        lA[(size_t)Ac * tD + s + c] = 0.0 * gx * nv;
+        lY[(size_t)Ac * tD + s + c] = bc->g * gx * nv;
       }
     }
   }

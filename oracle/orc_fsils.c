@@ -164,10 +164,8 @@ void orc_spar_vs(const orc_lhs *lhs, int dof, const double *K, const double *U,
     double acc = 0.0;
     for (int j = lhs->rowS[i]; j <= lhs->rowE[i]; j++) {
       const int col = lhs->colPtr[j];
-      double s = 0.0;
-      for (int m = 0; m < dof; m++)
-        s += K[(size_t)j * dof + m] * U[(size_t)col * dof + m];
-      acc += s;
+      for (int m = 0; m < dof; m++)  /* ((KU + K1 U1) + K2 U2) + ... */
+        acc += K[(size_t)j * dof + m] * U[(size_t)col * dof + m];
     }
     KU[i] = acc;
   }

@@ -31,6 +31,7 @@ SOURCES = [
     "gsls_eq.cu",
     "gsls_gmres.cu",
     "gsls_noalloc.cu",
+    "gsls_ns.cu",
 ]
 
 

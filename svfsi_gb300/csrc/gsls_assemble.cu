@@ -1,5 +1,6 @@
-// Element assembly for tet4 meshes: HEATS (Code/Source/svFSI/HEATS.f:39-159)
-// and STRUCT with the neo-Hookean + ST91 material
+// Element assembly for tet4 meshes: HEATS (Code/Source/svFSI/HEATS.f:39-159),
+// isotropic CEP (CEP.f:136-266), FLUID with VMS stabilisation
+// (FLUID.f:40-1084) and STRUCT with the neo-Hookean + ST91 material
 // (Code/Source/svFSI/STRUCT.f:39-496, MATMODELS.f:41-150,539-564,1588-1647),
 // scattered into block CSR as DOASSEM does (Code/Source/svFSI/LHSA.f:266-298).
 //
@@ -107,6 +108,7 @@ struct AsmArgs {
   double rho, cond, src;
   double C10, Kpen, visc, dmp;
   double fb[3];
+  double mu_f, ctM, ctC;
   const int4 *ien;
   const int4 *map;  // 4 int4 per element: map[e*4 + a] = (b0..b3)
   const double *x;
@@ -188,6 +190,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
 }  // namespace gsls
 
 #include "gsls_asm_struct.cuh"
+#include "gsls_asm_fluid.cuh"
 
 namespace gsls {
 
@@ -225,6 +228,9 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   A.visc = p->visc;
   A.dmp = p->dmp;
   for (int i = 0; i < 3; i++) A.fb[i] = p->fb[i];
+  A.mu_f = p->mu_f;
+  A.ctM = p->ctM;
+  A.ctC = p->ctC;
   A.ien = m->d_ien.as<int4>();
   A.map = m->d_map.as<int4>();
   A.x = m->d_x.as<double>();
@@ -253,6 +259,12 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
         k_asm_struct<float><<<nb, kAsmThreads, 0, st>>>(A);
       else
         k_asm_struct<double><<<nb, kAsmThreads, 0, st>>>(A);
+    } else if (p->phys == GSLS_PHYS_FLUID) {
+      if (dof != 4 || p->s + 4 > p->tDof || !(p->rho > 0.0) || !(p->dt > 0.0)) return GSLS_ERR_ARG;
+      if (mixed)
+        k_asm_fluid<float><<<nb, kAsmThreads, 0, st>>>(A);
+      else
+        k_asm_fluid<double><<<nb, kAsmThreads, 0, st>>>(A);
     } else {
       set_error("assembly: physics not built in this version of the library");
       return GSLS_ERR_UNSUPPORTED;

@@ -32,7 +32,7 @@ struct gsls_eq {
   gsls::DevBuf R, Val, Ftrac;
   bool has_trac = false;
   struct Dir {
-    gsls::DevBuf nodes, gx;
+    gsls::DevBuf nodes, gx, nV;
     int n = 0;
     double g = 0.0;
     int mask = 0;
@@ -84,16 +84,21 @@ __global__ void k_picp(int nNo, int tDof, int s, int dof, double coef, int dFlag
 }
 
 // SETBCDIR with dirA = 0, dirY = g*gx on the masked components
+// SETBCDIR/SETBCDIRL (Code/Source/svFSI/SETBC.f:39-228): the pressure of a
+// dof = nsd+1 equation is never constrained (SETBC.f:77); with nsd values
+// per node the value is g*gx*nV (SETBC.f:212-217), else g*gx.
 __global__ void k_setbcdir(int n, const int *__restrict__ nodes, const double *__restrict__ gx,
-                           double g, int mask, int tDof, int s, int dof, double *__restrict__ An,
-                           double *__restrict__ Yn) {
+                           const double *__restrict__ nV, double g, int mask, int tDof, int s,
+                           int dof, double *__restrict__ An, double *__restrict__ Yn) {
+  const int ncomp = (dof == 4) ? 3 : dof;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
     const size_t Ac = nodes[a];
     const double v = gx ? gx[a] : 1.0;
-    for (int c = 0; c < dof; c++) {
+    for (int c = 0; c < ncomp; c++) {
       if (mask && !((mask >> c) & 1)) continue;
-      An[Ac * tDof + s + c] = 0.0 * v;
-      Yn[Ac * tDof + s + c] = g * v;
+      const double nv = (nV && ncomp == 3) ? nV[(size_t)a * 3 + c] : 1.0;
+      An[Ac * tDof + s + c] = 0.0 * v * nv;
+      Yn[Ac * tDof + s + c] = g * v * nv;
     }
   }
 }
@@ -267,6 +272,11 @@ int gsls_eq_set_eparam(gsls_eq *eq, const double *eparam) {
 
 int gsls_eq_add_dirichlet(gsls_eq *eq, int nNo, const int *gNodes, const double *gx, double g,
                           int mask) {
+  return gsls_eq_add_dirichlet_nv(eq, nNo, gNodes, gx, nullptr, g, mask);
+}
+
+int gsls_eq_add_dirichlet_nv(gsls_eq *eq, int nNo, const int *gNodes, const double *gx,
+                             const double *nV, double g, int mask) {
   if (!eq || nNo < 0 || (nNo > 0 && !gNodes)) return GSLS_ERR_ARG;
   gsls_lhs *lhs = eq->lhs;
   if (eq->nextFace >= lhs->nFaces) {
@@ -295,6 +305,11 @@ int gsls_eq_add_dirichlet(gsls_eq *eq, int nNo, const int *gNodes, const double 
   if (gx) {
     GSLS_TRY(d->gx.alloc(sizeof(double) * (nNo > 0 ? nNo : 1)));
     GSLS_CUDA(cudaMemcpyAsync(d->gx.p, gx, sizeof(double) * nNo, cudaMemcpyHostToDevice,
+                              lhs->stream));
+  }
+  if (nV) {
+    GSLS_TRY(d->nV.alloc(sizeof(double) * 3 * (nNo > 0 ? nNo : 1)));
+    GSLS_CUDA(cudaMemcpyAsync(d->nV.p, nV, sizeof(double) * 3 * nNo, cudaMemcpyHostToDevice,
                               lhs->stream));
   }
   GSLS_CUDA(cudaStreamSynchronize(lhs->stream));
@@ -472,8 +487,9 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
   GSLS_CHECK_LAUNCH();
   for (auto *d : eq->dirs) {
     if (d->n == 0) continue;
-    k_setbcdir<<<nblk(d->n), kT, 0, st>>>(d->n, d->nodes.as<int>(), d->gx.as<double>(), d->g,
-                                          d->mask, tD, p.s, dof, An, Yn);
+    k_setbcdir<<<nblk(d->n), kT, 0, st>>>(d->n, d->nodes.as<int>(), d->gx.as<double>(),
+                                          d->nV.as<double>(), d->g, d->mask, tD, p.s, dof, An,
+                                          Yn);
     GSLS_CHECK_LAUNCH();
   }
   GSLS_TRY(lhs_update_faces(lhs, nullptr, nullptr));

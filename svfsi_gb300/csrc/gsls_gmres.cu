@@ -1,4 +1,5 @@
-// Restarted GMRES (GMRESS/GMRESV, Code/Source/svFSILS/GMRES.f:171-431):
+// Restarted GMRES (GMRESS/GMRESV, Code/Source/svFSILS/GMRES.f:171-431, and
+// the GMRES of the NS solver, GMRES.f:51-169):
 // classical Gram-Schmidt with one batched multi-dot per Arnoldi step and the
 // Pythagorean norm (GMRES.f:116-126), Givens rotations (GMRES.f:130-141),
 // back-substitution (GMRES.f:149-155).  Basis vectors in the Krylov vector
@@ -231,8 +232,15 @@ __global__ void k_vmul(size_t n, double *__restrict__ R, const double *__restric
     R[k] *= W[k];
 }
 
+// Restart loop shared by GMRESV (GMRES.f:273-431) and the GMRES that the NS
+// solver calls (GMRES.f:51-169) on device vectors: Rk (right-hand side, not
+// modified) and X (solution, zeroed here).  ns selects the latter's
+// bookkeeping: no iteration counted for the first restart, eps and iNorm set
+// from the first residual, and an initial residual at or below absTol
+// returns X = 0 (*early = true).  Otherwise eps is the caller's.
 template <int D, class VT, class XT>
-static int gmres_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const double *Wc) {
+static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *Rk, XT *X,
+                      bool ns, double eps, bool *early) {
   cudaStream_t st = lhs->stream;
   Workspace &ws = lhs->ws;
   const int nNo = lhs->nNo, sD = ls->sD;
@@ -257,44 +265,13 @@ static int gmres_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, con
   double *y = err + (sD + 2);
   GmresCtl *ctl = reinterpret_cast<GmresCtl *>(y + (sD + 2));
   XT *basis = ws.basis.as<XT>();
-  XT *X = ws.vec[0].as<XT>(), *Rk = ws.vec[3].as<XT>();
   double *part = ws.partials.as<double>();
   unsigned *tk = ws.ticket.as<unsigned>();
-  double *dnorm = ws.scal.as<double>();
-
-  auto t0 = std::chrono::steady_clock::now();
-  ls->suc = 0;
-  k_norm2<<<G, kT, 0, st>>>(nv, R, dnorm, part, tk);
-  GSLS_CHECK_LAUNCH();
-  double n2;
-  GSLS_CUDA(cudaMemcpyAsync(&n2, dnorm, sizeof(double), cudaMemcpyDeviceToHost, st));
-  GSLS_CUDA(cudaStreamSynchronize(st));
-  double eps = sqrt(n2);
-  ls->iNorm = eps;
-  ls->fNorm = eps;
-  eps = fmax(ls->absTol, ls->relTol * eps);
-  ls->itr = 0;
-  if (!std::isfinite(n2)) {
-    set_error("GMRES: NaN/Inf in the right-hand side");
-    return GSLS_ERR_NAN;
-  }
-  if (ls->iNorm <= ls->absTol) {
-    // the reference returns with R untouched (GMRES.f:310-314); SOLVE then
-    // applies R = Wc*R
-    ls->callD = 2.220446049250313e-16;
-    ls->dB = 0.0;
-    k_vmul<<<G, kT, 0, st>>>(nv, R, Wc);
-    GSLS_CHECK_LAUNCH();
-    GSLS_CUDA(cudaStreamSynchronize(st));
-    return GSLS_OK;
-  }
-  k_to_xt<XT><<<G, kT, 0, st>>>(nv, R, Rk);
-  GSLS_CHECK_LAUNCH();
+  *early = false;
   GSLS_CUDA(cudaMemsetAsync(X, 0, sizeof(XT) * nv, st));
   GmresCtl hc;
   for (int l = 1; l <= ls->mItr; l++) {
-    ls->dB = ls->fNorm;
-    ls->itr++;
+    if (!ns || l > 1) ls->itr++;
     XT *u1 = basis;
     memset(&hc, 0, sizeof(hc));
     hc.eps = eps;
@@ -307,6 +284,27 @@ static int gmres_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, con
     }
     k_gm_residual<XT><<<G, kT, 0, st>>>(nv, Rk, u1, l > 1 ? 1 : 0, part, tk, err);
     GSLS_CHECK_LAUNCH();
+    if (ns && l == 1) {
+      double e0;
+      GSLS_CUDA(cudaMemcpyAsync(&e0, err, sizeof(double), cudaMemcpyDeviceToHost, st));
+      GSLS_CUDA(cudaStreamSynchronize(st));
+      if (!std::isfinite(e0)) {
+        set_error("GMRES: NaN/Inf in the right-hand side");
+        return GSLS_ERR_NAN;
+      }
+      if (e0 <= ls->absTol) {
+        ls->callD = 2.220446049250313e-16;
+        ls->dB = 0.0;
+        *early = true;
+        return GSLS_OK;
+      }
+      ls->iNorm = e0;
+      ls->fNorm = e0;
+      eps = fmax(ls->absTol, ls->relTol * e0);
+      hc.eps = eps;
+      GSLS_CUDA(cudaMemcpyAsync(ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+    }
+    ls->dB = ls->fNorm;
     k_gm_scale<XT><<<G, kT, 0, st>>>(nv, u1, err);
     GSLS_CHECK_LAUNCH();
     int i_next = 1, batch = 4;
@@ -350,6 +348,52 @@ static int gmres_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, con
       break;
     }
   }
+  return GSLS_OK;
+}
+
+template <int D, class VT, class XT>
+static int gmres_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const double *Wc) {
+  cudaStream_t st = lhs->stream;
+  Workspace &ws = lhs->ws;
+  const int nNo = lhs->nNo;
+  const size_t nv = (size_t)nNo * D;
+  const int G = lhs->grid;
+  GSLS_TRY(ws.partials.alloc(sizeof(double) * (size_t)G * 4 + 64));
+  XT *X = ws.vec[0].as<XT>(), *Rk = ws.vec[3].as<XT>();
+  double *part = ws.partials.as<double>();
+  unsigned *tk = ws.ticket.as<unsigned>();
+  double *dnorm = ws.scal.as<double>();
+
+  auto t0 = std::chrono::steady_clock::now();
+  ls->suc = 0;
+  k_norm2<<<G, kT, 0, st>>>(nv, R, dnorm, part, tk);
+  GSLS_CHECK_LAUNCH();
+  double n2;
+  GSLS_CUDA(cudaMemcpyAsync(&n2, dnorm, sizeof(double), cudaMemcpyDeviceToHost, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  double eps = sqrt(n2);
+  ls->iNorm = eps;
+  ls->fNorm = eps;
+  eps = fmax(ls->absTol, ls->relTol * eps);
+  ls->itr = 0;
+  if (!std::isfinite(n2)) {
+    set_error("GMRES: NaN/Inf in the right-hand side");
+    return GSLS_ERR_NAN;
+  }
+  if (ls->iNorm <= ls->absTol) {
+    // the reference returns with R untouched (GMRES.f:310-314); SOLVE then
+    // applies R = Wc*R
+    ls->callD = 2.220446049250313e-16;
+    ls->dB = 0.0;
+    k_vmul<<<G, kT, 0, st>>>(nv, R, Wc);
+    GSLS_CHECK_LAUNCH();
+    GSLS_CUDA(cudaStreamSynchronize(st));
+    return GSLS_OK;
+  }
+  k_to_xt<XT><<<G, kT, 0, st>>>(nv, R, Rk);
+  GSLS_CHECK_LAUNCH();
+  bool early = false;
+  GSLS_TRY((gmres_loop<D, VT, XT>(lhs, ls, Val, Rk, X, false, eps, &early)));
   k_scale_out_g<XT><<<G, kT, 0, st>>>(nv, R, X, Wc);
   GSLS_CHECK_LAUNCH();
   GSLS_CUDA(cudaStreamSynchronize(st));
@@ -357,6 +401,24 @@ static int gmres_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, con
   ls->callD = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return GSLS_OK;
 }
+
+// GMRES of the NS solver (GMRES.f:51-169) on the K block: X = K^-1 Rk
+// approximately; itr and callD accumulate in ls.
+template <int D, class VT, class XT>
+int gmres_ns(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *Rk, XT *X) {
+  auto t0 = std::chrono::steady_clock::now();
+  ls->suc = 0;
+  bool early = false;
+  GSLS_TRY((gmres_loop<D, VT, XT>(lhs, ls, Val, Rk, X, true, 0.0, &early)));
+  if (early) return GSLS_OK;
+  ls->callD += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  ls->dB = 10.0 * log(ls->fNorm / ls->dB);
+  return GSLS_OK;
+}
+template int gmres_ns<3, float, float>(gsls_lhs *, gsls_sub_ls *, const float *, const float *,
+                                       float *);
+template int gmres_ns<3, double, double>(gsls_lhs *, gsls_sub_ls *, const double *,
+                                         const double *, double *);
 
 int gmres_run(gsls_lhs *lhs, gsls_sub_ls *ls, int D, bool mixed, const void *Val, double *R,
               const double *Wc) {

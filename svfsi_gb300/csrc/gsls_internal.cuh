@@ -90,9 +90,11 @@ struct GraphKey {
   int batch, nNo;
   bool tma;
   bool fused;
+  const void *part, *scal, *w;  // workspace buffers baked into the graph
   bool operator==(const GraphKey &o) const {
     return D == o.D && vsz == o.vsz && xsz == o.xsz && val == o.val && x == o.x &&
-           batch == o.batch && nNo == o.nNo && tma == o.tma && fused == o.fused;
+           batch == o.batch && nNo == o.nNo && tma == o.tma && fused == o.fused &&
+           part == o.part && scal == o.scal && w == o.w;
   }
 };
 
@@ -116,6 +118,9 @@ struct Workspace {
   DevBuf hcol;        // GMRES Hessenberg column (double)
   DevBuf io;          // host<->device staging for gsls_solve
   DevBuf io2;
+  DevBuf ns_vec;      // NS solver vectors (Rm, Rc, U, P, MU, MP, Schur CG)
+  DevBuf ns_mat;      // NS solver blocks (mK, mG, mD, mL, Gt)
+  DevBuf rcs;         // RCS scaling state (W1, Wr, Wc, control words)
   KrylovScalars *h_scal = nullptr;  // pinned host mirror
   int mask_dof = -1;
   std::vector<int> mask_key;
@@ -127,6 +132,8 @@ struct gsls_lhs {
   int gnNo = 0, nNo = 0, nnz = 0, nFaces = 0, mynNo = 0;
   std::vector<int> h_rowPtr, h_colPtr, h_diagPtr;  // 0-based
   gsls::DevBuf d_rowPtr, d_colPtr, d_diagPtr, d_rowOf;
+  gsls::DevBuf d_tpos;   // CSR position of the transposed block (built on first use)
+  bool tpos_ok = false;
   std::vector<gsls::Face> faces;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -239,4 +246,11 @@ int spmv_launch(gsls_lhs *lhs, int dof, const void *dVal, int val_prec,
 // restarted GMRES on the preconditioned system (gsls_gmres.cu)
 int gmres_run(gsls_lhs *lhs, gsls_sub_ls *ls, int D, bool mixed, const void *Val,
               double *R, const double *Wc);
+// GMRES of the NS solver on device vectors (gsls_gmres.cu)
+template <int D, class VT, class XT>
+int gmres_ns(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *Rk, XT *X);
+// RCS preconditioner and NS block solver (gsls_ns.cu)
+int precond_rcs_run(gsls_lhs *lhs, int D, bool mixed, void *Val, double *R, double *W);
+int ns_run(gsls_lhs *lhs, gsls_ls *ls, int D, bool mixed, const void *Val, double *R,
+           const double *W);
 }  // namespace gsls

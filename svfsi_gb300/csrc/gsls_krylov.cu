@@ -687,8 +687,8 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
       want_tma && val_padded && sizeof(VT) == 4 && tma_setup<D, VT>(lhs, tt, tsmem, tgrid);
   const TmaTiles *ttp = use_tma ? &tt : nullptr;
   if (use_tma) GSLS_CUDA(cudaMemsetAsync(ws.err.p, 0, sizeof(int), st));
-  GraphKey key{D, (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma,
-               FUSED};
+  GraphKey key{D,  (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma,
+               FUSED, ws.partials.p, ws.scal.p, ws.Wf.p};
   if (!prof && !(ws.cg_graph && ws.cg_key == key)) {
     if (ws.cg_graph) {
       cudaGraphExecDestroy(ws.cg_graph);
@@ -757,8 +757,7 @@ static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, b
   if (prec == GSLS_PRECOND_FSILS) {
     GSLS_TRY(precond_diag_t<D, VT>(lhs, Val, dRi, W));
   } else if (prec == GSLS_PRECOND_RCS) {
-    set_error("PRECOND_RCS is not built in this version of the library");
-    return GSLS_ERR_UNSUPPORTED;
+    GSLS_TRY(precond_rcs_run(lhs, D, sizeof(VT) == 4, Val, dRi, W));
   } else {
     set_error("This linear solver and preconditioner combination is not supported.");
     return GSLS_ERR_ARG;
@@ -776,8 +775,7 @@ static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, b
     case GSLS_LS_TYPE_GMRES:
       return gmres_run(lhs, &ls->RI, D, sizeof(VT) == 4, Val, dRi, W);
     case GSLS_LS_TYPE_NS:
-      set_error("LS_TYPE_NS is not built in this version of the library");
-      return GSLS_ERR_UNSUPPORTED;
+      return ns_run(lhs, ls, D, sizeof(VT) == 4, Val, dRi, W);
     default:
       set_error("LS_type not defined");
       return GSLS_ERR_ARG;

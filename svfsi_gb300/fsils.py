@@ -160,12 +160,15 @@ class Equation:
         self.nNo = mesh.lhs.nNo
         self.tDof = params.tDof
 
-    def add_dirichlet(self, nodes0, g, gx=None, mask=0):
+    def add_dirichlet(self, nodes0, g, gx=None, mask=0, nV=None):
         n1 = _i32(np.asarray(nodes0) + 1)
         gxa = None if gx is None else _f64(gx)
-        check(_lib.load().gsls_eq_add_dirichlet(self.h, n1.size, _ip(n1),
-                                                _dp(gxa) if gxa is not None else None,
-                                                float(g), int(mask)), "gsls_eq_add_dirichlet")
+        nva = None if nV is None else _f64(nV)
+        check(_lib.load().gsls_eq_add_dirichlet_nv(self.h, n1.size, _ip(n1),
+                                                   _dp(gxa) if gxa is not None else None,
+                                                   _dp(nva) if nva is not None else None,
+                                                   float(g), int(mask)),
+              "gsls_eq_add_dirichlet_nv")
 
     def add_traction(self, faces0, h):
         f1 = _i32(np.asarray(faces0) + 1)

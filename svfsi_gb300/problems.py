@@ -8,6 +8,9 @@ conventions.  The workloads follow the five benchmark configurations:
                       (20^3 hexes -> 48,000 tets, 9,261 nodes at full size).
 * ``struct_beam``  -- neo-Hookean + ST91 elastodynamics of a 4x1x1 beam
                       (176x44x44 hexes -> 2,044,416 tets, 358,425 nodes).
+* ``fluid_cylinder`` -- VMS incompressible Navier-Stokes in a cylinder
+                      (R 0.5, L 5; ~1.2M tets, ~0.2M nodes at full size).
+* ``cep_slab``     -- Aliev-Panfilov monodomain on a 10x10x2 slab.
 """
 from __future__ import annotations
 
@@ -16,8 +19,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import meshgen
-from ._lib import (LS_TYPE_CG, PHYS_CEP, PHYS_HEATS, PHYS_STRUCT, PREC_FP64, PRECOND_FSILS, EqParams,
-                   EqSolver)
+from ._lib import (LS_TYPE_CG, LS_TYPE_NS, PHYS_CEP, PHYS_FLUID, PHYS_HEATS, PHYS_STRUCT, PREC_FP64,
+                   PRECOND_FSILS, PRECOND_RCS, EqParams, EqSolver)
 
 SEED = 20261203
 
@@ -37,6 +40,7 @@ class DirBC:
     g: float
     gx: np.ndarray | None = None
     mask: int = 0       # 0 = all components
+    nV: np.ndarray | None = None  # (n, 3) unit normals: value g*gx*nV
 
 
 @dataclass
@@ -184,6 +188,30 @@ def cep_slab(nx: int = 135, ny: int = 135, nz: int = 27, nsteps: int = 5000,
                    cep=cep, stim=stim)
 
 
+def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float = 5.0,
+                   u_max: float = 30.0, rho: float = 1.06, mu: float = 0.04,
+                   dt: float = 1e-3) -> Problem:
+    """Config: cylinder R=0.5, L=5 (seeded Delaunay cross-section), rho 1.06,
+    mu 0.04, parabolic inlet with peak u_max at z=0 (value -u_max along the
+    outward normal -z, profile of BCINI), no-slip wall, traction-free outlet
+    (p = 0 Neumann: no term), dt 1e-3, NS solver with RCS preconditioning and
+    Krylov dimension 100.  Fluid starts at rest."""
+    x, ien, info = meshgen.cylinder(R, L, h)
+    rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
+    am, af, beta, gam = genalpha(0.2, second_order=False)
+    params = dict(am=am, af=af, beta=beta, gam=gam, dt=dt, rho=rho, mu_f=mu, ctM=1.0, ctC=36.0,
+                  fb=(0.0, 0.0, 0.0))
+    inlet, wall = info["inlet"], info["wall"]
+    perim = np.intersect1d(inlet, wall)
+    gx = meshgen.parabolic_profile(x, info["inlet_faces"], inlet, perim)
+    nV = np.tile(np.array([0.0, 0.0, -1.0]), (inlet.size, 1))
+    return Problem(name=f"fluid_cylinder_h{h:g}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
+                   phys=PHYS_FLUID, dof=4, tDof=4, params=params,
+                   dirichlet=[DirBC(inlet, -u_max, gx=gx, nV=nV), DirBC(wall, 0.0)],
+                   LS_type=LS_TYPE_NS, prec=PRECOND_RCS, ls_sD=100, minItr=1, maxItr=5,
+                   tol=1e-6, nsteps=nsteps)
+
+
 def make_lhs_arrays(p: Problem):
     """1-based rowPtr/colPtr/gNodes for FSILS_LHS_CREATE."""
     return (np.arange(1, p.nNo + 1, dtype=np.int32), (p.rowPtr + 1).astype(np.int32),
@@ -201,7 +229,7 @@ def build_equation(p: Problem, precision=PREC_FP64):
     if p.eparam is not None:
         eq.set_eparam(p.eparam)
     for d in p.dirichlet:
-        eq.add_dirichlet(d.nodes, d.g, d.gx, d.mask)
+        eq.add_dirichlet(d.nodes, d.g, d.gx, d.mask, d.nV)
     for t in p.traction:
         eq.add_traction(t.faces, t.h)
     if p.cep:

@@ -1,0 +1,164 @@
+"""GPU parity of the fluid path against the oracle: VMS assembly (FLUID3D_M/C),
+row-column scaling (PRECONDRCS), the NS block solver (NSSOLVER with its
+GMRES and Schur CG) and full time steps on a seeded cylinder.
+
+Tolerances: FP64 assembly 1e-12 relative; FP32 tangent 1e-5 relative with
+the FP64 residual at 1e-12; one NS solve 1e-8 relative L2 with identical
+outer-iteration counts; FP64 time steps 1e-8 relative L2 on the state.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from svfsi_gb300 import _lib, fsils, problems
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float).ravel(), np.asarray(b, float).ravel()
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _cyl(h=0.1, nsteps=3):
+    return problems.fluid_cylinder(h=h, nsteps=nsteps)
+
+
+def _state(p, seed=0):
+    rng = np.random.default_rng(seed)
+    Y = np.zeros((p.nNo, 4))
+    r2 = p.x[:, 0] ** 2 + p.x[:, 1] ** 2
+    Y[:, 2] = 30.0 * (1.0 - r2 / 0.25) + rng.standard_normal(p.nNo)
+    Y[:, :2] = rng.standard_normal((p.nNo, 2))
+    Y[:, 3] = 100.0 * rng.standard_normal(p.nNo)
+    A = 1e3 * rng.standard_normal((p.nNo, 4))
+    return A, Y
+
+
+def _lhs(p, nFaces):
+    g, rp1, cp1 = problems.make_lhs_arrays(p)
+    return fsils.FSILS_LHS_CREATE(p.nNo, p.nNo, p.nnz, g, rp1, cp1, nFaces)
+
+
+def test_fluid_assembly_fp64(gsls, orc):
+    p = _cyl()
+    A, Y = _state(p)
+    R0, V0 = orc.assemble(p, A, Y)
+    lhs = _lhs(p, 1)
+    mesh = fsils.Mesh(lhs, p.ien, p.x)
+    R, Val = mesh.assemble(p.eq_params(), A, Y, np.zeros_like(Y), p.dof)
+    assert rel(R, R0) < 1e-12
+    assert rel(Val, V0) < 1e-12
+
+
+def test_fluid_assembly_fp32_tangent(gsls, orc):
+    torch = pytest.importorskip("torch")
+    p = _cyl()
+    A, Y = _state(p, seed=1)
+    R0, V0 = orc.assemble(p, A, Y)
+    lhs = _lhs(p, 1)
+    mesh = fsils.Mesh(lhs, p.ien, p.x)
+    dA = torch.tensor(A, device="cuda")
+    dY = torch.tensor(Y, device="cuda")
+    dD = torch.zeros_like(dY)
+    dR = torch.zeros((p.nNo, 4), dtype=torch.float64, device="cuda")
+    dV = torch.zeros((p.nnz, 16), dtype=torch.float32, device="cuda")
+    prm = p.eq_params()
+    _lib.check(gsls.gsls_assemble_dev(mesh.h, C.byref(prm), C.c_void_p(dA.data_ptr()),
+                                      C.c_void_p(dY.data_ptr()), C.c_void_p(dD.data_ptr()),
+                                      C.c_void_p(dR.data_ptr()), C.c_void_p(dV.data_ptr()),
+                                      fsils.PREC_MIXED))
+    torch.cuda.synchronize()
+    assert rel(dR.cpu().numpy(), R0) < 1e-12
+    assert rel(dV.cpu().numpy().astype(np.float64), V0) < 1e-5
+
+
+def test_rcs_cg_matches_oracle(gsls, orc):
+    """PRECOND_RCS with CG on the heat equation (dof 1)."""
+    p = problems.heats_cube(6)
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((p.nNo, 1))
+    Y = rng.standard_normal((p.nNo, 1))
+    R0, V0 = orc.assemble(p, A, Y)
+    dirn = p.dirichlet[0].nodes
+    lhs = _lhs(p, 1)
+    fsils.FSILS_BC_CREATE(lhs, 1, dirn.size, 3, fsils.BC_TYPE_DIR, dirn + 1, np.zeros((dirn.size, 3)))
+    ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_CG, relTol=1e-10, maxItr=2000)
+    R, Val = R0.copy(), V0.copy()
+    fsils.FSILS_SOLVE(lhs, ls, 1, R, Val, fsils.PRECOND_RCS)
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
+    s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
+    ols = orc.ls_create(orc.LS_TYPE_CG, relTol=1e-10, mItr=2000)
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, 1, Ro, Vo, orc.PRECOND_RCS)
+    assert rel(Val, Vo) < 1e-13
+    assert ls.RI.suc == ols.RI.suc == 1
+    assert abs(ls.RI.itr - ols.RI.itr) <= 1
+    assert rel(R, Ro) < 1e-8
+
+
+def _fluid_faces(p):
+    return [d.nodes for d in p.dirichlet]
+
+
+@pytest.mark.parametrize("tight", [False, True])
+def test_ns_solve_matches_oracle(gsls, orc, tight):
+    p = _cyl()
+    A, Y = _state(p, seed=3)
+    R0, V0 = orc.assemble(p, A, Y)
+    faces = _fluid_faces(p)
+    lhs = _lhs(p, len(faces))
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, len(faces))
+    for k, nodes in enumerate(faces):
+        fsils.FSILS_BC_CREATE(lhs, k + 1, nodes.size, 3, fsils.BC_TYPE_DIR, nodes + 1,
+                              np.zeros((nodes.size, 3)))
+        s.bc_create(k + 1, nodes, 3, 0, np.zeros((nodes.size, 3)))
+    kw = dict(dimKry=100)
+    if tight:
+        kw["relTol"] = 1e-4
+    ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_NS, **kw)
+    ols = orc.ls_create(orc.LS_TYPE_NS, sD=100, relTol=kw.get("relTol"))
+    assert (ls.RI.mItr, ls.GM.mItr, ls.CG.mItr) == (ols.RI.mItr, ols.GM.mItr, ols.CG.mItr)
+    R, Val = R0.copy(), V0.copy()
+    fsils.FSILS_SOLVE(lhs, ls, 4, R, Val, fsils.PRECOND_RCS)
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, 4, Ro, Vo, orc.PRECOND_RCS)
+    assert rel(Val, Vo) < 1e-13
+    assert abs(ls.RI.iNorm - ols.RI.iNorm) <= 1e-12 * ols.RI.iNorm
+    assert ls.RI.itr == ols.RI.itr
+    assert ls.RI.suc == ols.RI.suc
+    assert abs(ls.GM.itr - ols.GM.itr) <= 2 * ls.RI.itr
+    assert rel(R, Ro) < 1e-8
+
+
+def test_fluid_steps_fp64(gsls, orc):
+    p = _cyl(nsteps=3)
+    lhs, mesh, eq = problems.build_equation(p)
+    oeq = orc.OracleEquation(p)
+    for s in range(p.nsteps):
+        gi = eq.step()
+        oi = oeq.step()
+        assert gi.newton_itr == oi.newton_itr
+    A, Y, D = eq.get_state()
+    Ao, Yo, Do = oeq.state()
+    assert rel(Y[:, :3], Yo[:, :3]) < 1e-8
+    assert rel(Y[:, 3], Yo[:, 3]) < 1e-8
+    # inlet profile imposed: peak 30 along +z at the centre node
+    c = np.argmin(np.hypot(p.x[:, 0], p.x[:, 1]) + 10 * p.x[:, 2])
+    assert abs(Y[c, 2] - 30.0) < 1e-12
+
+
+def test_fluid_mixed_tracks_fp64(gsls, orc):
+    """Mixed precision (FP32 tangent and Krylov, FP64 residual) follows the
+    FP64 trajectory when Newton converges tightly."""
+    p = _cyl(nsteps=2)
+    p.tol, p.maxItr = 1e-9, 12
+    lhs, mesh, eq = problems.build_equation(p, precision=fsils.PREC_MIXED)
+    oeq = orc.OracleEquation(p)
+    for s in range(p.nsteps):
+        eq.step()
+        oeq.step()
+    _, Y, _ = eq.get_state()
+    _, Yo, _ = oeq.state()
+    assert rel(Y, Yo) < 1e-7

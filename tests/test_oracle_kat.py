@@ -278,3 +278,135 @@ def test_aliev_panfilov_rest_and_convergence(orc):
     assert 1.8 < e_fe[0] / e_fe[1] < 2.2
     e_rk = [np.abs(_ap_run(orc, 1, dt, 20.0) - ref).max() for dt in (0.4, 0.2, 0.01)]
     assert e_rk[0] / e_rk[1] > 16 and e_rk[2] < 1e-10
+
+
+# ---------------------------------------------------------------- fluid / NS
+def _fluid_box(n=3):
+    """Small fluid problem on a Kuhn box (interior nodes exist for n >= 3)."""
+    x, ien = meshgen.kuhn_box(n, n, n)
+    rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
+    am, af, beta, gam = problems.genalpha(0.2, False)
+    params = dict(am=am, af=af, beta=beta, gam=gam, dt=1e-3, rho=1.06, mu_f=0.04, ctM=1.0,
+                  ctC=36.0, fb=(0.0, 0.0, 0.0))
+    return problems.Problem(name="fluid_box", x=x, ien=ien, rowPtr=rp, colPtr=cp,
+                            phys=problems.PHYS_FLUID, dof=4, tDof=4, params=params)
+
+
+def _interior(x):
+    return np.all((x > 1e-12) & (x < 1 - 1e-12), axis=1)
+
+
+@pytest.mark.parametrize("flow", ["uniform", "couette"])
+def test_fluid_exact_solutions_have_zero_interior_residual(orc, flow):
+    """Uniform flow and plane Couette flow (u_x = y) with constant pressure
+    are exact steady Navier-Stokes solutions represented by P1: the VMS
+    residual vanishes at interior nodes (momentum and continuity)."""
+    p = _fluid_box(3)
+    Y = np.zeros((p.nNo, 4))
+    if flow == "uniform":
+        Y[:, :3] = (0.3, -0.2, 0.5)
+    else:
+        Y[:, 0] = p.x[:, 1]
+    Y[:, 3] = 7.0
+    R, Val = orc.assemble(p, np.zeros_like(Y), Y)
+    inner = _interior(p.x)
+    assert inner.sum() > 0
+    scale = np.abs(R).max()
+    assert scale > 0
+    assert np.abs(R[inner]).max() < 1e-12 * max(scale, 1.0)
+
+
+def test_fluid_element_blocks_match_reference_structure(orc):
+    """At rest (u = a = p = 0) FLUID3D_M/C reduce to the Stokes blocks:
+    K_uu = wl (mu Nx_b Nx_a^T + mu Nx.Nx I + tauC Nx_a Nx_b^T + rho amd M I),
+    K_pp = wl tauM Nx.Nx, K_up = -wl Nx_a Ns_b, K_pu = wl (Ns_a Nx_b + rho amd tauM Nx_a)."""
+    p = _fluid_box(1)
+    eqp = orc.eqp_from(p)
+    xl = orc.f64(_unit_tet().ravel())
+    z = np.zeros(16)
+    lR = np.zeros(16)
+    lK = np.zeros(256)
+    orc.load().orc_elem_fluid(C.byref(eqp), orc.dp(xl), orc.dp(z), orc.dp(z), orc.dp(lR), orc.dp(lK))
+    assert np.abs(lR).max() == 0.0
+    prm = p.params
+    rho, mu, dt = prm["rho"], prm["mu_f"], prm["dt"]
+    T1 = prm["af"] * prm["gam"] * dt
+    amd = prm["am"] / T1
+    w = 1.0 / 24.0
+    wl = w * T1
+    Nx = np.array([[1, 0, 0, -1], [0, 1, 0, -1], [0, 0, 1, -1]], float)  # unit tet: xiX = I
+    K = np.eye(3)
+    kT = 4.0 / dt ** 2
+    kS = 36.0 * 3.0 * (mu / rho) ** 2
+    tauM = 1.0 / (rho * np.sqrt(kT + kS))
+    tauC = 1.0 / (tauM * 3.0)
+    s, t = (5 + 3 * np.sqrt(5)) / 20, (5 - np.sqrt(5)) / 20
+    N = np.full((4, 4), t) + np.eye(4) * (s - t)
+    M = N.T @ N
+    for a in range(4):
+        for b in range(4):
+            blk = lK[(a * 4 + b) * 16:(a * 4 + b + 1) * 16].reshape(4, 4)
+            NN = Nx[:, a] @ Nx[:, b]
+            Kuu = 4 * wl * (mu * np.outer(Nx[:, b], Nx[:, a]) + mu * NN * np.eye(3)
+                            + tauC * np.outer(Nx[:, a], Nx[:, b])) + wl * rho * amd * M[a, b] * np.eye(3)
+            assert np.allclose(blk[:3, :3], Kuu, rtol=1e-12, atol=1e-14)
+            assert np.allclose(blk[3, 3], 4 * wl * tauM * NN, rtol=1e-12)
+            assert np.allclose(blk[:3, 3], -wl * Nx[:, a] * 1.0, rtol=1e-12)
+            assert np.allclose(blk[3, :3], wl * (Nx[:, b] + 4 * rho * amd * tauM * 0.25 * Nx[:, a]),
+                               rtol=1e-12)
+
+
+def test_ge_matches_dense_solve(orc):
+    rng = np.random.default_rng(11)
+    for n in (1, 2, 5, 12):
+        Q = rng.standard_normal((n, n))
+        A = Q @ Q.T + n * np.eye(n)
+        nV = 20
+        Af = np.zeros((nV, nV))
+        Af[:n, :n] = A
+        Acol = np.asfortranarray(Af).ravel(order="F").copy()
+        b = rng.standard_normal(nV)
+        x = b.copy()
+        ok = orc.load().orc_ge(nV, n, orc.dp(Acol), orc.dp(x))
+        assert ok == 1
+        assert np.allclose(x[:n], np.linalg.solve(A, b[:n]), rtol=1e-10)
+
+
+def test_ns_solver_with_tight_tolerances_solves_the_system(orc):
+    """RCS + NSSOLVER with tight inner/outer tolerances returns the solution
+    of the Dirichlet-masked block system (checked by a dense solve); the
+    x = 1 face is left traction-free so that the pressure is determined."""
+    p = _fluid_box(3)
+    rng = np.random.default_rng(4)
+    Y = np.zeros((p.nNo, 4))
+    Y[:, :3] = 0.5 * rng.standard_normal((p.nNo, 3))
+    Y[:, 3] = rng.standard_normal(p.nNo)
+    A = rng.standard_normal((p.nNo, 4))
+    R, Val = orc.assemble(p, A, Y)
+    walls = np.nonzero(~_interior(p.x) & (p.x[:, 0] < 1 - 1e-12))[0].astype(np.int32)
+    n = p.nNo
+    Kd = np.zeros((4 * n, 4 * n))
+    for i in range(n):
+        for j in range(p.rowPtr[i], p.rowPtr[i + 1]):
+            c = p.colPtr[j]
+            Kd[4 * i:4 * i + 4, 4 * c:4 * c + 4] = Val[j].reshape(4, 4)
+    mask = np.ones(4 * n)
+    for a in walls:
+        mask[4 * a:4 * a + 3] = 0.0
+    Km = Kd * mask[:, None] * mask[None, :]
+    Km[mask == 0, mask == 0] = 1.0
+    x = np.linalg.solve(Km, R.ravel() * mask)
+    s = orc.OracleSolver(n, p.rowPtr, p.colPtr, 1)
+    s.bc_create(1, walls, 3, 0, np.zeros((walls.size, 3)))
+    # the outer residual is iNorm^2 - xB.B (NSSOLVER.f:167), so relative
+    # tolerances below ~1e-8 cannot be met; the inner solves are tight
+    ls = orc.ls_create(orc.LS_TYPE_NS, relTol=1e-6, absTol=1e-30, mItr=10, sD=200)
+    ls.GM.relTol = ls.CG.relTol = 1e-13
+    ls.GM.absTol = ls.CG.absTol = 1e-30
+    ls.CG.mItr = 2000
+    Rs, Vs = R.copy(), Val.copy()
+    s.solve(ls, 4, Rs, Vs, orc.PRECOND_RCS)
+    assert ls.RI.suc == 1
+    # CGRAD_SCHUR takes S = L - Gt G (K^-1 ~ I after scaling), so the outer
+    # least-squares loop converges linearly; relTol 1e-6 at cond ~1e8
+    assert np.abs(Rs.ravel() - x).max() < 1e-4 * np.abs(x).max()
