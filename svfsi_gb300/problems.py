@@ -195,7 +195,9 @@ def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float 
     mu 0.04, parabolic inlet with peak u_max at z=0 (value -u_max along the
     outward normal -z, profile of BCINI), no-slip wall, traction-free outlet
     (p = 0 Neumann: no term), dt 1e-3, NS solver with RCS preconditioning and
-    Krylov dimension 100.  Fluid starts at rest."""
+    Krylov dimension 100 (outer tolerance 1e-2, inner GMRES 1e-2 and Schur CG
+    0.2 as LS_CREATE sets them), Newton to 1e-9 (a converged implicit step:
+    ~8 iterations).  Fluid starts at rest."""
     x, ien, info = meshgen.cylinder(R, L, h)
     rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
     am, af, beta, gam = genalpha(0.2, second_order=False)
@@ -208,8 +210,8 @@ def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float 
     return Problem(name=f"fluid_cylinder_h{h:g}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
                    phys=PHYS_FLUID, dof=4, tDof=4, params=params,
                    dirichlet=[DirBC(inlet, -u_max, gx=gx, nV=nV), DirBC(wall, 0.0)],
-                   LS_type=LS_TYPE_NS, prec=PRECOND_RCS, ls_sD=100, minItr=1, maxItr=5,
-                   tol=1e-6, nsteps=nsteps)
+                   LS_type=LS_TYPE_NS, prec=PRECOND_RCS, ls_relTol=1e-2, ls_sD=100, minItr=1,
+                   maxItr=12, tol=1e-9, nsteps=nsteps)
 
 
 def make_lhs_arrays(p: Problem):
