@@ -6,6 +6,11 @@ mixed precision (FP32 tangent + FP32 inner CG, FP64 residual/Newton) beside
 the plain FP64 GPU path, with the relative L2 distance between the two.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gsls|reference]
+                  [--workload struct|fluid]
+
+--workload fluid times the VMS Navier-Stokes workload instead (cylinder
+R 0.5, L 5, ~1.06M tet4, 4x4 blocks; RCS + NS block solver), the same line
+format with its own roofline kernel (the GMRES block SpMV on the K block).
 
 --impl reference times the CPU restatement of the reference's algorithm
 (oracle/, OpenMP over all host cores) on the same workload.  N > 1 runs
@@ -43,6 +48,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--only", choices=["all", "mixed", "fp64"], default="all",
                     help="time one precision only (profiling runs)")
+    ap.add_argument("--workload", choices=["struct", "fluid"], default="struct")
+    ap.add_argument("--fluid-h", type=float, default=0.027,
+                    help="cylinder mesh spacing (profiling captures use a coarser mesh)")
     return ap.parse_args()
 
 
@@ -53,12 +61,23 @@ def dist_env():
 
 def workload(args):
     from svfsi_gb300 import problems
+    if args.workload == "fluid":
+        return problems.fluid_cylinder(h=0.08 if args.small else args.fluid_h, nsteps=args.steps)
     if args.small:
         return problems.struct_beam(24, 6, 6, nsteps=args.steps)
     return problems.struct_beam(**WORKLOAD, nsteps=args.steps)
 
 
+def is_fluid(p):
+    return p.dof == 4
+
+
 def workload_desc(p):
+    if is_fluid(p):
+        return (f"{p.name}: VMS incompressible Navier-Stokes (rho 1.06, mu 0.04, parabolic "
+                f"inlet peak 30, impulsive start), {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
+                f"{p.nnz:,} 4x4 blocks, RCS + NS solver (sD 100, relTol 1e-2), dt 1e-3, Newton "
+                f"tol 1e-10")
     return (f"{p.name}: neo-Hookean+ST91 elastodynamics, {p.nEl:,} tet4, {p.nNo:,} nodes, "
             f"nnz {p.nnz:,} 3x3 blocks, CG+diag, dt 1e-3, Newton tol 1e-8")
 
@@ -185,7 +204,8 @@ def run_gsls(args):
         if profile:
             L.gsls_profile_enable(0)
             cnt, tot = C.c_longlong(), C.c_double()
-            L.gsls_profile_read(b"cg_spmv", C.byref(cnt), C.byref(tot))
+            L.gsls_profile_read(b"gm_spmv_d3" if is_fluid(p) else b"cg_spmv", C.byref(cnt),
+                                C.byref(tot))
             acnt, atot = C.c_longlong(), C.c_double()
             L.gsls_profile_read(b"assembly", C.byref(acnt), C.byref(atot))
             prof = {"cg_spmv": (cnt.value, tot.value), "assembly": (acnt.value, atot.value)}
@@ -224,7 +244,8 @@ def run_gsls(args):
     profd = timed_run(fsils.PREC_MIXED, profile=True, nsteps=2, nwarm=1)
     ms_mixed = max_over_ranks(mixed["ms"]) / K
     ms_fp64 = max_over_ranks(fp64["ms"]) / K
-    D_m, D_f = mixed["state"][2], fp64["state"][2]
+    sidx = 1 if is_fluid(p) else 2  # compare Y (fluid) or D (struct)
+    D_m, D_f = mixed["state"][sidx], fp64["state"][sidx]
     rel_l2 = float(np.linalg.norm(D_m - D_f) / np.linalg.norm(D_f))
 
     # e2e through the public API with host buffers (pinned), H2D + D2H per step
@@ -251,27 +272,37 @@ def run_gsls(args):
     lhs.free()
     state_bytes = 3 * p.nNo * p.tDof * 8
 
-    # roofline of the dominant kernel (CG SpMV + fused dot, FP32 values)
+    # roofline of the dominant kernel: the CG SpMV + fused dot (struct) or
+    # the GMRES SpMV on the 3x3 K block (fluid), FP32 values
     cnt, tot_ms = profd["prof"]["cg_spmv"]
     peak, peak_kind = peaks()
-    B = p.algorithmic_bytes(4, 4)["spmv"]
+    if is_fluid(p):
+        B = p.nnz * (9 * 4 + 4) + 8 * p.nNo + 2 * p.nNo * 3 * 4
+        kname = "k_gm_spmv<3,float,float> (block-CSR SpMV on the K block of the NS solver)"
+        tkey = "gm_spmv_d3_f32_fluid_cylinder"
+    else:
+        B = p.algorithmic_bytes(4, 4)["spmv"]
+        kname = "k_cg_spmv<3,float,float> (block-CSR SpMV + fused P.KP)"
+        tkey = "cg_spmv_d3_f32_struct_beam_176x44x44"
     avg_s = (tot_ms / max(cnt, 1)) / 1e3
     achieved = B / avg_s / 1e9 if cnt else None
-    roof = {"kernel": "k_cg_spmv<3,float,float> (block-CSR SpMV + fused P.KP)",
+    roof = {"kernel": kname,
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None,
             "peak_source": f"{peak_kind} hbm_gbs", "bytes_per_launch": B,
             "avg_launch_us": avg_s * 1e6, "launches": cnt,
-            "traffic": traffic_from_profiles("cg_spmv_d3_f32_struct_beam_176x44x44")}
+            "traffic": traffic_from_profiles(tkey)}
 
     out = {
         "metric": METRIC, "value": ms_mixed / 1e3 / world, "unit": "s/step",
         "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": ms_mixed,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 tangent+inner CG / f64 residual,Newton,reductions",
-        "data": "synthetic: seeded Kuhn-split beam mesh, no external data",
+        "data": ("synthetic: seeded Delaunay cylinder mesh, no external data" if is_fluid(p)
+                 else "synthetic: seeded Kuhn-split beam mesh, no external data"),
         "config": {"workload": workload_desc(p), "precision": "mixed",
-                   "l2": "inputs larger than L2 (FP32 Val 188 MB, FP64 Val 377 MB)",
+                   "l2": (f"inputs larger than L2 (FP32 Val {p.nnz * p.dof ** 2 * 4 / 1e6:.0f} MB, "
+                          f"FP64 Val {p.nnz * p.dof ** 2 * 8 / 1e6:.0f} MB)"),
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "fp64": {"value": ms_fp64 / 1e3 / world, "ms_per_step": ms_fp64,
                  "newton_itr_per_step": fp64["newton"], "cg_itr_per_step": fp64["cg"],
@@ -279,6 +310,7 @@ def run_gsls(args):
         "mixed": {"newton_itr_per_step": mixed["newton"], "cg_itr_per_step": mixed["cg"],
                   "assembly_ms_per_newton": mixed["asm_ms"] / max(mixed["newton"], 1),
                   "all_solves_converged": bool(mixed["suc"])},
+        "ls_itr_note": ("NS outer iterations per step" if is_fluid(p) else "CG iterations per step"),
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "rel_l2_mixed_vs_fp64": rel_l2,
         "roofline": roof,
@@ -288,7 +320,8 @@ def run_gsls(args):
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(p, fp64["newton"], fp64["cg"])
+        out["cpu_baseline"] = (cpu_baseline_fluid(p, fp64["newton"]) if is_fluid(p)
+                               else cpu_baseline(p, fp64["newton"], fp64["cg"]))
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -361,6 +394,42 @@ def cpu_baseline(p, newton, cg):
                        f"+ {cg:.1f} CG iters, the counts of the FP64 GPU run of the same algorithm")}
 
 
+def cpu_sample_fluid(p, threads):
+    """Time, on the host cores with the oracle: one fluid assembly (one
+    thread, element loop) and one RCS + NS solve of that system with the
+    workload's solver settings (OpenMP SpMV)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    O.set_threads(threads)
+    rng = np.random.default_rng(0)
+    Y = np.zeros((p.nNo, 4))
+    Y[:, 2] = 30.0 * np.clip(1.0 - (p.x[:, 0] ** 2 + p.x[:, 1] ** 2) / 0.25, 0.0, None)
+    Y[:, 3] = rng.standard_normal(p.nNo)
+    A = 1e3 * rng.standard_normal((p.nNo, 4))
+    t0 = time.perf_counter()
+    R, Val = O.assemble(p, A, Y)
+    t_asm = time.perf_counter() - t0
+    s = O.OracleSolver(p.nNo, p.rowPtr, p.colPtr, len(p.dirichlet))
+    for k, d in enumerate(p.dirichlet):
+        s.bc_create(k + 1, d.nodes, 3, 0, np.zeros((d.nodes.size, 3)))
+    ls = O.ls_create(O.LS_TYPE_NS, relTol=p.ls_relTol, sD=p.ls_sD)
+    t0 = time.perf_counter()
+    s.solve(ls, 4, R, Val, O.PRECOND_RCS)
+    t_solve = time.perf_counter() - t0
+    return t_asm, t_solve
+
+
+def cpu_baseline_fluid(p, newton):
+    threads = os.cpu_count() or 1
+    t_asm, t_solve = cpu_sample_fluid(p, threads)
+    return {"value": newton * (t_asm + t_solve), "unit": "s/step", "cores": threads,
+            "kind": "port",
+            "sample": (f"oracle (C restatement, FP64) on the full mesh: 1 assembly {t_asm:.2f}s "
+                       f"(1 thread), 1 RCS + NS solve {t_solve:.2f}s (OpenMP {threads} threads "
+                       f"in the SpMVs); per step = {newton:.2f} Newton x (asm + solve), the "
+                       f"count of the FP64 GPU run")}
+
+
 def run_reference(args):
     rank, local, world = dist_env()
     if rank != 0:
@@ -370,6 +439,25 @@ def run_reference(args):
     import oracle as O
     threads = os.cpu_count() or 1
     O.set_threads(threads)
+    if is_fluid(p):
+        vals = []
+        for k in range(args.warmup + args.steps):
+            t_asm, t_solve = cpu_sample_fluid(p, threads)
+            if k >= args.warmup:
+                vals.append(REF_NEWTON_FLUID * (t_asm + t_solve))
+        v = statistics.median(vals)
+        print(json.dumps({
+            "metric": METRIC, "value": v, "unit": "s/step", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic: seeded Delaunay cylinder mesh, no external data",
+            "config": {"workload": workload_desc(p), "precision": "fp64 (reference CPU)"},
+            "cpu_baseline": {"value": v, "unit": "s/step", "cores": threads, "kind": "port",
+                             "sample": (f"per step: {REF_NEWTON_FLUID} Newton x (1 assembly + 1 "
+                                        f"RCS + NS solve) on the full mesh")},
+            "e2e": {"value": v, "unit": "s/step", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}))
+        return
     # Newton / CG counts of this workload's first step, by the CPU oracle itself
     if args.small:
         eq = O.OracleEquation(p)
@@ -401,7 +489,9 @@ def run_reference(args):
 
 # Newton iterations and total CG iterations per step of the full-size beam
 # (FP64 path), used to scale the CPU sample in the reference arm.
-REF_COUNTS = (5.0, 500.0)
+REF_COUNTS = (5.0, 1911.4)
+# Newton iterations per step of the full-size cylinder (FP64 path)
+REF_NEWTON_FLUID = 7.0
 
 
 def main():

@@ -307,15 +307,20 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
     ls->dB = ls->fNorm;
     k_gm_scale<XT><<<G, kT, 0, st>>>(nv, u1, err);
     GSLS_CHECK_LAUNCH();
-    int i_next = 1, batch = 4;
+    // profiling runs time every Arnoldi SpMV with events and poll after
+    // each step, so that no skipped launch is counted
+    const bool prof = prof_on();
+    int i_next = 1, batch = prof ? 1 : 4;
     bool inner_done = false;
     while (!inner_done) {
       for (int b = 0; b < batch && i_next <= sD; b++, i_next++) {
         const int i = i_next;
         XT *ui = basis + ld * (i - 1), *ui1 = basis + ld * i;
+        if (prof) cudaEventRecord(prof_event(0), st);
         k_gm_spmv<D, VT, XT><<<G, kT, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
                                                lhs->d_colPtr.as<int>(), Val, ui, ui1, ctl);
         GSLS_CHECK_LAUNCH();
+        if (prof) cudaEventRecord(prof_event(1), st);
         k_gm_multidot<XT><<<Gd, kT, 0, st>>>(nv, basis, ld, i + 1, ui1, part, ctl);
         GSLS_CHECK_LAUNCH();
         k_gm_colsum<<<i + 1, kT, 0, st>>>(Gd, part, hcol, ctl);
@@ -327,8 +332,13 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
       }
       GSLS_CUDA(cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, st));
       GSLS_CUDA(cudaStreamSynchronize(st));
+      if (prof) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, prof_event(0), prof_event(1));
+        prof_add(D == 3 ? "gm_spmv_d3" : "gm_spmv", 1, t);
+      }
       if (hc.done || i_next > sD) inner_done = true;
-      if (batch < 16) batch *= 2;
+      if (!prof && batch < 16) batch *= 2;
     }
     if (hc.nan) {
       set_error("GMRES: NaN/Inf in the Arnoldi process");

@@ -695,10 +695,310 @@ static bool ge_solve(int nV, int N, const std::vector<double> &A, std::vector<do
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Persistent Schur CG: every iteration of CGRAD_SCHUR in one cooperative
+// launch.  Phases are separated by a grid barrier (generation counter; each
+// wait is bounded and sets an error word when it gives up, after which
+// every block returns).  Data written by other blocks is read through L2
+// (__ldcg); the matrix blocks are read-only.  Reductions: one FP64 partial
+// per block, summed in block order by every block (identical result in all
+// blocks, reproducible for a fixed grid).
+struct GridBar {
+  unsigned count;  // arrivals, monotonic within one launch (zeroed before it)
+  unsigned pad;
+  int err, pad2;
+};
+constexpr unsigned kBarSpin = 1u << 24;  // x ~20 ns sleep: well under a second
+
+// Barrier number `epoch` (1, 2, ...) of the launch: every block adds one
+// arrival and waits until all nblk * epoch arrivals are in; no reset, so
+// the last arriver has nothing more to publish.
+__device__ __forceinline__ bool grid_bar(GridBar *b, unsigned nblk, unsigned &epoch) {
+  __shared__ int s_ok;
+  __syncthreads();
+  epoch += 1;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned target = epoch * nblk;
+    __threadfence();
+    atomicAdd(&b->count, 1u);
+    unsigned it = 0;
+    while (*(volatile unsigned *)&b->count < target) {
+      if (*(volatile int *)&b->err) {
+        ok = 0;
+        break;
+      }
+      if (++it > kBarSpin) {
+        atomicExch(&b->err, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(20);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// sum of nblk block partials in block order, broadcast to the block
+__device__ __forceinline__ double sum_partials(const double *part, unsigned nblk, double *sh) {
+  double v = 0.0;
+  for (unsigned k = threadIdx.x; k < nblk; k += blockDim.x) v += __ldcg(part + k);
+  v = block_sum(v, sh);
+  __shared__ double s_tot;
+  if (threadIdx.x == 0) s_tot = v;
+  __syncthreads();
+  const double r = s_tot;
+  __syncthreads();
+  return r;
+}
+
+template <class VT, class XT>
+struct SchurArgs {
+  int nNo;
+  const int *rowPtr, *colPtr;
+  const VT *mG, *Gt, *mL;
+  XT *X, *Pa, *Pb, *R, *SP, *GP;  // Pa holds the initial direction
+  double *part;                   // 2 * gridDim.x
+  GridBar *bar;
+  SchurScal *sc;
+  int K;                          // rows per 4-lane group (row slots)
+};
+
+constexpr int kPT = 1024;
+constexpr int kPQ = kPT / kRL;  // 4-lane groups per block
+
+// Row slots of a block: slot (k, g) is row blockIdx.x*kPQ + g + k*gridDim.x*kPQ.
+// The K segments of a block are contiguous in the CSR; their column
+// indices and row ranges are staged in shared memory once per launch:
+//   srp[k*kPQ + g] = (first, end) of the row in scol, sdel[k] = global - local
+__device__ __forceinline__ void schur_stage(const int *__restrict__ rowPtr,
+                                            const int *__restrict__ colPtr, int nNo, int K,
+                                            int2 *srp, int *sdel, int *scol) {
+  const int nq = gridDim.x * kPQ;
+  int off = 0;
+  for (int k = 0; k < K; k++) {
+    const int base = blockIdx.x * kPQ + k * nq;
+    if (base >= nNo) {
+      if (threadIdx.x < kPQ) srp[k * kPQ + threadIdx.x] = make_int2(0, 0);
+      if (threadIdx.x == 0) sdel[k] = 0;
+      continue;
+    }
+    const int hi = min(base + kPQ, nNo);
+    const int s0 = __ldg(rowPtr + base), s1 = __ldg(rowPtr + hi);
+    for (int j = threadIdx.x; j < s1 - s0; j += blockDim.x) scol[off + j] = __ldg(colPtr + s0 + j);
+    if (threadIdx.x < kPQ) {
+      const int i = base + threadIdx.x;
+      srp[k * kPQ + threadIdx.x] =
+          (i < nNo) ? make_int2(__ldg(rowPtr + i) - s0 + off, __ldg(rowPtr + i + 1) - s0 + off)
+                    : make_int2(0, 0);
+    }
+    if (threadIdx.x == 0) sdel[k] = s0 - off;
+    off += s1 - s0;
+  }
+  __syncthreads();
+}
+
+// Iteration k of CGRAD_SCHUR (CGRAD.f:86-110), three phases:
+//  1. P_k = (err/errO) (P_{k-1} + (errO/err) R) formed on the fly from the
+//     previous direction (the reference's two OMPSUMS/OMPMULS steps; P_1 = R
+//     exactly with errO/err = 0, err/errO = 1) and GP = mG P_k; the owner of
+//     row i stores P_k(i) in the other buffer;
+//  2. SP = mL P_k - Gt GP and the block partials of P_k.SP;
+//  3. alpha = errO/dot, X += alpha P_k, R -= alpha SP and the partials of |R|^2.
+template <class VT, class XT>
+__global__ void __launch_bounds__(kPT, 1) k_schur_persistent(SchurArgs<VT, XT> A) {
+  using AT = typename AccOf<VT>::T;
+  constexpr int kPU = sizeof(AT) == 4 ? 4 : 2;  // blocks per lane issued together
+  extern __shared__ int4 smem_raw[];
+  int2 *srp = reinterpret_cast<int2 *>(smem_raw);
+  int *sdel = reinterpret_cast<int *>(srp + A.K * kPQ);
+  int *scol = sdel + ((A.K + 3) & ~3);
+  __shared__ double sh[32];
+  const unsigned nblk = gridDim.x;
+  const int nNo = A.nNo, K = A.K;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  const int q = t & (kRL - 1), g = threadIdx.x / kRL;
+  const int nq = gridDim.x * kPQ;
+  double err = A.sc->err;
+  const double eps = A.sc->eps;
+  const int mItr = A.sc->mItr;
+  int done = A.sc->done, suc = A.sc->suc, itr = 0;
+  double errO = A.sc->errO;
+  XT c1 = XT(0), c2 = XT(1);
+  XT *Pold = A.Pa, *Pnew = A.Pb;
+  bool ok = true;
+  unsigned epoch = 0;
+  schur_stage(A.rowPtr, A.colPtr, nNo, K, srp, sdel, scol);
+  while (!done) {
+    // phase 1: P_k on the fly, GP = mG P_k
+    for (int k = 0; k < K; k++) {
+      const int i = blockIdx.x * kPQ + g + k * nq;
+      if ((i & ~7) >= nNo) break;  // warp-uniform: a warp covers 8 consecutive rows
+      const int2 rr = srp[k * kPQ + g];
+      const int dl = sdel[k];
+      AT a0 = AT(0), a1 = AT(0), a2 = AT(0);
+      for (int j0 = rr.x + q; j0 < rr.y; j0 += kPU * kRL) {
+        AT pv[kPU], gv[kPU][3];
+#pragma unroll
+        for (int u = 0; u < kPU; u++) {
+          const int jl = j0 + u * kRL;
+          if (jl < rr.y) {
+            const int col = scol[jl];
+            const size_t j = (size_t)(jl + dl);
+            pv[u] = AT(c2 * (__ldcg(Pold + col) + c1 * __ldcg(A.R + col)));
+#pragma unroll
+            for (int m = 0; m < 3; m++) gv[u][m] = AT(__ldg(A.mG + j * 3 + m));
+          } else {
+            pv[u] = AT(0);
+#pragma unroll
+            for (int m = 0; m < 3; m++) gv[u][m] = AT(0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kPU; u++) {
+          a0 = fma(gv[u][0], pv[u], a0);
+          a1 = fma(gv[u][1], pv[u], a1);
+          a2 = fma(gv[u][2], pv[u], a2);
+        }
+      }
+      a0 = quad_sum(a0);
+      a1 = quad_sum(a1);
+      a2 = quad_sum(a2);
+      if (q == 0 && i < nNo) {
+        __stcg(A.GP + (size_t)i * 3 + 0, XT(a0));
+        __stcg(A.GP + (size_t)i * 3 + 1, XT(a1));
+        __stcg(A.GP + (size_t)i * 3 + 2, XT(a2));
+        __stcg(Pnew + i, XT(c2 * (__ldcg(Pold + i) + c1 * __ldcg(A.R + i))));
+      }
+    }
+    if (!(ok = grid_bar(A.bar, nblk, epoch))) break;
+    // phase 2: SP = mL P - Gt GP; dot = P.SP
+    AT dloc = AT(0);
+    for (int k = 0; k < K; k++) {
+      const int i = blockIdx.x * kPQ + g + k * nq;
+      if ((i & ~7) >= nNo) break;
+      const int2 rr = srp[k * kPQ + g];
+      const int dl = sdel[k];
+      AT sl = AT(0), sd = AT(0);
+      for (int j0 = rr.x + q; j0 < rr.y; j0 += kPU * kRL) {
+        AT lv[kPU], pv[kPU], gt[kPU][3], gp[kPU][3];
+#pragma unroll
+        for (int u = 0; u < kPU; u++) {
+          const int jl = j0 + u * kRL;
+          if (jl < rr.y) {
+            const int col = scol[jl];
+            const size_t j = (size_t)(jl + dl);
+            lv[u] = AT(__ldg(A.mL + j));
+            pv[u] = AT(__ldcg(Pnew + col));
+#pragma unroll
+            for (int m = 0; m < 3; m++) {
+              gt[u][m] = AT(__ldg(A.Gt + j * 3 + m));
+              gp[u][m] = AT(__ldcg(A.GP + (size_t)col * 3 + m));
+            }
+          } else {
+            lv[u] = pv[u] = AT(0);
+#pragma unroll
+            for (int m = 0; m < 3; m++) gt[u][m] = gp[u][m] = AT(0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kPU; u++) {
+          sl = fma(lv[u], pv[u], sl);
+#pragma unroll
+          for (int m = 0; m < 3; m++) sd = fma(gt[u][m], gp[u][m], sd);
+        }
+      }
+      sl = quad_sum(sl);
+      sd = quad_sum(sd);
+      if (q == 0 && i < nNo) {
+        const XT v = XT(sl + AT(-1) * sd);
+        __stcg(A.SP + i, v);
+        dloc = fma(AT(__ldcg(Pnew + i)), AT(v), dloc);
+      }
+    }
+    {
+      const double bs = block_sum(double(dloc), sh);
+      if (threadIdx.x == 0) __stcg(A.part + blockIdx.x, bs);
+    }
+    if (!(ok = grid_bar(A.bar, nblk, epoch))) break;
+    // phase 3: X, R and |R|^2
+    const double dot = sum_partials(A.part, nblk, sh);
+    errO = err;
+    const double alpha = errO / dot;
+    const XT al = XT(alpha), mal = XT(-alpha);
+    double eloc = 0.0;
+    for (int k = t; k < nNo; k += nthr) {
+      __stcg(A.X + k, XT(__ldcg(A.X + k) + al * __ldcg(Pnew + k)));
+      const XT r = XT(__ldcg(A.R + k) + mal * __ldcg(A.SP + k));
+      __stcg(A.R + k, r);
+      eloc += double(r) * double(r);
+    }
+    {
+      const double bs = block_sum(eloc, sh);
+      if (threadIdx.x == 0) __stcg(A.part + nblk + blockIdx.x, bs);
+    }
+    if (!(ok = grid_bar(A.bar, nblk, epoch))) break;
+    double e = sqrt(sum_partials(A.part + nblk, nblk, sh));
+    e = e * e;
+    err = e;
+    itr++;
+    c1 = XT(errO / err);
+    c2 = XT(err / errO);
+    XT *tmp = Pold;
+    Pold = Pnew;
+    Pnew = tmp;
+    if (!isfinite(err)) {
+      done = 3;
+    } else if (itr >= mItr) {
+      done = 2;  // no stop test after the last iteration
+    } else if (err < eps) {
+      suc = 1;
+      done = 1;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    SchurScal *sc = A.sc;
+    sc->err = err;
+    sc->errO = errO;
+    sc->itr = itr;
+    sc->suc = suc;
+    sc->done = ok ? done : 4;
+  }
+}
+
+// Launch geometry of the persistent Schur CG: one block per SM, K row slots
+// per 4-lane group, shared memory for the staged rows of the largest block
+// (0 when it does not fit: the caller then uses the per-kernel path).
+static size_t schur_geometry(const gsls_lhs *lhs, int nblk, int *K_out) {
+  const int nNo = lhs->nNo, nq = nblk * kPQ;
+  const int K = (nNo + nq - 1) / nq;
+  const std::vector<int> &rp = lhs->h_rowPtr;
+  long long mx = 0;
+  for (int b = 0; b < nblk; b++) {
+    long long tot = 0;
+    for (int k = 0; k < K; k++) {
+      const int base = b * kPQ + k * nq;
+      if (base >= nNo) break;
+      const int hi = std::min(base + kPQ, nNo);
+      tot += rp[hi] - rp[base];
+    }
+    mx = std::max(mx, tot);
+  }
+  *K_out = K;
+  const size_t bytes = (size_t)K * kPQ * sizeof(int2) + (size_t)((K + 3) & ~3) * sizeof(int) +
+                       (size_t)mx * sizeof(int);
+  return bytes <= 200 * 1024 ? bytes : 0;
+}
+
 // CGRAD_SCHUR on P (in: right-hand side, out: solution)
 template <class VT, class XT>
 static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, const VT *mL,
-                    XT *P, XT *Rs, XT *Ps, XT *SP, XT *GP, SchurScal *sc, SchurScal *h_sc) {
+                    XT *P, XT *Rs, XT *Ps, XT *Pb, XT *SP, XT *GP, SchurScal *sc,
+                    SchurScal *h_sc, GridBar *db) {
   cudaStream_t st = lhs->stream;
   const int nNo = lhs->nNo, G = lhs->grid;
   double *part = lhs->ws.partials.as<double>();
@@ -708,8 +1008,44 @@ static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, 
   ls->suc = 0;
   k_schur_init<XT><<<G, kNT, 0, st>>>(nNo, P, Rs, Ps, part, tk, sc, ls->absTol, ls->relTol, ls->mItr);
   GSLS_CHECK_LAUNCH();
+  static const bool kernels = [] {
+    const char *e = getenv("GSLS_SCHUR");
+    return e && strcmp(e, "kernels") == 0;
+  }();
+  bool use_kernels = kernels;
+  if (!use_kernels) {
+    // persistent cooperative kernel: one block per SM
+    const int nblk = num_sms();
+    int K = 0;
+    const size_t smem = schur_geometry(lhs, nblk, &K);
+    int nb = 0;
+    if (smem) {
+      GSLS_CUDA(cudaFuncSetAttribute(k_schur_persistent<VT, XT>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      GSLS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_schur_persistent<VT, XT>, kPT,
+                                                              smem));
+    }
+    if (nb < 1) {
+      use_kernels = true;  // rows of a block do not fit in shared memory
+    } else {
+      GSLS_TRY(lhs->ws.partials.alloc(sizeof(double) * ((size_t)2 * nblk + 64) + 64));
+      GSLS_CUDA(cudaMemsetAsync(db, 0, sizeof(GridBar), st));
+      SchurArgs<VT, XT> a{nNo, rp, cp, mG, Gt, mL, P, Ps, Pb, Rs, SP, GP,
+                          lhs->ws.partials.as<double>(), db, sc, K};
+      void *args[] = {&a};
+      GSLS_CUDA(cudaLaunchCooperativeKernel((const void *)k_schur_persistent<VT, XT>, dim3(nblk),
+                                            dim3(kPT), args, smem, st));
+      GSLS_CHECK_LAUNCH();
+      GSLS_CUDA(cudaMemcpyAsync(h_sc, sc, sizeof(SchurScal), cudaMemcpyDeviceToHost, st));
+      GSLS_CUDA(cudaStreamSynchronize(st));
+      if (h_sc->done == 4) {
+        set_error("NS: grid barrier of the Schur-complement CG timed out");
+        return GSLS_ERR_CUDA;
+      }
+    }
+  }
   const int batch = 8;
-  for (;;) {
+  for (; use_kernels;) {
     GSLS_CUDA(cudaMemcpyAsync(h_sc, sc, sizeof(SchurScal), cudaMemcpyDeviceToHost, st));
     GSLS_CUDA(cudaStreamSynchronize(st));
     if (h_sc->done) break;
@@ -750,18 +1086,19 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
   }
   const int nB = 2 * mI;
   auto t0 = std::chrono::steady_clock::now();
-  // vectors: Rmi Rm MU(nB) U(mI) GPs (3-vectors); Rci Rc MP(nB) P(mI) Rs Ps SP (scalars)
+  // vectors: Rmi Rm GP MU(nB) U(mI) (3-vectors); Rci Rc Rs Ps SP Pb MP(nB) P(mI) (scalars)
   const size_t l3 = ((size_t)nNo * 3 + 63) & ~(size_t)63, l1 = ((size_t)nNo + 63) & ~(size_t)63;
-  const size_t nvec3 = 3 + (size_t)nB + mI, nvec1 = 5 + (size_t)nB + mI;
-  GSLS_TRY(ws.ns_vec.alloc(sizeof(XT) * (nvec3 * l3 + nvec1 * l1) + 1024 + 2 * sizeof(SchurScal)));
+  const size_t nvec3 = 3 + (size_t)nB + mI, nvec1 = 6 + (size_t)nB + mI;
+  GSLS_TRY(ws.ns_vec.alloc(sizeof(XT) * (nvec3 * l3 + nvec1 * l1) + 2048 + 2 * sizeof(SchurScal)));
   XT *v3 = ws.ns_vec.as<XT>();
   XT *Rmi = v3, *Rm = v3 + l3, *GP = v3 + 2 * l3, *MU = v3 + 3 * l3, *U = MU + (size_t)nB * l3;
   XT *v1 = v3 + nvec3 * l3;
   XT *Rci = v1, *Rc = v1 + l1, *Rs = v1 + 2 * l1, *Ps = v1 + 3 * l1, *SP = v1 + 4 * l1;
-  XT *MP = v1 + 5 * l1, *P = MP + (size_t)nB * l1;
+  XT *Pb = v1 + 5 * l1, *MP = v1 + 6 * l1, *P = MP + (size_t)nB * l1;
   SchurScal *sc = reinterpret_cast<SchurScal *>(
       (reinterpret_cast<uintptr_t>(v1 + nvec1 * l1) + 127) & ~(uintptr_t)127);
   double *dsc = reinterpret_cast<double *>(sc + 2);  // 96 doubles: norms and dots
+  GridBar *bar = reinterpret_cast<GridBar *>(dsc + 96);
   const size_t m9 = (size_t)nnz * 9, m3 = (size_t)nnz * 3;
   GSLS_TRY(ws.ns_mat.alloc(sizeof(VT) * (m9 + 4 * m3 + nnz) + 64));
   VT *mK = ws.ns_mat.as<VT>(), *mG = mK + m9, *mD = mG + m3, *Gt = mD + m3, *mL = Gt + m3;
@@ -812,7 +1149,7 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
     part = ws.partials.as<double>();
     k_ns_vs<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mD, Ui, Rc, Pi, nullptr);
     GSLS_CHECK_LAUNCH();
-    GSLS_TRY((schur_cg<VT, XT>(lhs, &ls->CG, mG, Gt, mL, Pi, Rs, Ps, SP, GP, sc, &h_sc)));
+    GSLS_TRY((schur_cg<VT, XT>(lhs, &ls->CG, mG, Gt, mL, Pi, Rs, Ps, Pb, SP, GP, sc, &h_sc, bar)));
     k_ns_sv<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mG, Pi, MUiB, Rm, MUiBB, nullptr);
     GSLS_CHECK_LAUNCH();
     GSLS_TRY((gmres_ns<3, VT, XT>(lhs, &ls->GM, mK, MUiBB, Ui)));

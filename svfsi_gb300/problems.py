@@ -196,7 +196,7 @@ def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float 
     outward normal -z, profile of BCINI), no-slip wall, traction-free outlet
     (p = 0 Neumann: no term), dt 1e-3, NS solver with RCS preconditioning and
     Krylov dimension 100 (outer tolerance 1e-2, inner GMRES 1e-2 and Schur CG
-    0.2 as LS_CREATE sets them), Newton to 1e-9 (a converged implicit step:
+    0.2 as LS_CREATE sets them), Newton to 1e-10 (a converged implicit step:
     ~8 iterations).  Fluid starts at rest."""
     x, ien, info = meshgen.cylinder(R, L, h)
     rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
@@ -211,7 +211,7 @@ def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float 
                    phys=PHYS_FLUID, dof=4, tDof=4, params=params,
                    dirichlet=[DirBC(inlet, -u_max, gx=gx, nV=nV), DirBC(wall, 0.0)],
                    LS_type=LS_TYPE_NS, prec=PRECOND_RCS, ls_relTol=1e-2, ls_sD=100, minItr=1,
-                   maxItr=12, tol=1e-9, nsteps=nsteps)
+                   maxItr=12, tol=1e-10, nsteps=nsteps)
 
 
 def make_lhs_arrays(p: Problem):

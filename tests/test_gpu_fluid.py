@@ -139,7 +139,7 @@ def test_ns_solve_matches_oracle(gsls, orc, tight):
 
 
 def test_fluid_steps_fp64(gsls, orc):
-    """Converged implicit steps (Newton to 1e-9) land on the oracle's state."""
+    """Converged implicit steps (Newton to 1e-10) land on the oracle's state."""
     p = _cyl(nsteps=3)
     lhs, mesh, eq = problems.build_equation(p)
     oeq = orc.OracleEquation(p)
