@@ -294,6 +294,33 @@ int gsls_profile_enable(int on);
 int gsls_profile_reset(void);
 int gsls_profile_read(const char *name, long long *count, double *total_ms);
 
+/* ---- discrete adjoint (forward/backward pair) --------------------------
+   Gradient of an objective of the final state with respect to the
+   per-element parameter of the equation (gsls_eq_set_eparam: STRUCT C10 =
+   mu/2, HEATS conductivity), through every implicit step: transpose solve
+   on the assembled tangent, element kernel for dR/dp, checkpoint every
+   `every` steps and recompute of each segment on the way back.  New
+   capability (the reference has no adjoint); FP64 throughout. */
+typedef struct gsls_tape gsls_tape;
+/* Take nsteps steps of eq (as gsls_eq_step), storing checkpoints. */
+int gsls_adjoint_forward(gsls_eq *eq, int nsteps, int every, gsls_tape **tape);
+/* Given dJ/dA_N, dJ/dY_N, dJ/dD_N (host, tDof x nNo, each nullable = 0),
+   write dJ/dp (host, nEl, original element order).  eq is left at step N. */
+int gsls_adjoint_backward(gsls_tape *tape, const double *Abar, const double *Ybar,
+                          const double *Dbar, double *grad);
+int gsls_tape_free(gsls_tape *tape);
+
+/* Linearisation point of one step: old and new state (device, tDof x nNo). */
+typedef struct {
+  const double *Ao, *Yo, *Do, *An, *Yn, *Dn;
+} gsls_adj_point;
+/* lambda = K^-T rhs with K = dR/dA_n assembled at pt (Dirichlet rows
+   masked as in the forward solve); rhs, lambda: device, dof x nNo. */
+int gsls_adjoint_solve(gsls_eq *eq, const gsls_adj_point *pt, const double *rhs,
+                       double *lambda);
+/* out[e] = (d R / d p_e)^T lambda at pt (device, nEl, original element order). */
+int gsls_dRdp(gsls_eq *eq, const gsls_adj_point *pt, const double *lambda, double *out);
+
 #ifdef __cplusplus
 }
 #endif

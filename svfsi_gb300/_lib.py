@@ -58,6 +58,10 @@ class CepParams(C.Structure):
                 ("Td", C.c_double), ("CL", C.c_double), ("V0", C.c_double), ("X20", C.c_double)]
 
 
+class AdjPoint(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("Ao", "Yo", "Do", "An", "Yn", "Dn")]
+
+
 class StepInfo(C.Structure):
     _fields_ = [("newton_itr", C.c_int), ("ls_itr_total", C.c_int),
                 ("last_iNorm", C.c_double), ("r1_last", C.c_double), ("last_suc", C.c_int),
@@ -112,6 +116,12 @@ SIGNATURES = {
     "gsls_eq_set_cep": (C.c_int, [C.c_void_p, C.POINTER(CepParams), C.c_int, c_int_p]),
     "gsls_eq_get_cep_state": (C.c_int, [C.c_void_p, c_double_p]),
     "gsls_eq_set_eparam": (C.c_int, [C.c_void_p, c_double_p]),
+    "gsls_adjoint_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "gsls_adjoint_backward": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p,
+                                        c_double_p]),
+    "gsls_tape_free": (C.c_int, [C.c_void_p]),
+    "gsls_adjoint_solve": (C.c_int, [C.c_void_p, C.POINTER(AdjPoint), C.c_void_p, C.c_void_p]),
+    "gsls_dRdp": (C.c_int, [C.c_void_p, C.POINTER(AdjPoint), C.c_void_p, C.c_void_p]),
     "gsls_launch_count": (C.c_longlong, []),
     "gsls_profile_enable": (C.c_int, [C.c_int]),
     "gsls_profile_reset": (C.c_int, []),

@@ -274,6 +274,173 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   return GSLS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Parameter sensitivity of the element residual (adjoint dR/dp), one element
+// per thread, no scatter: out[e] += scale * lambda_e . d(lR_e)/d(p_e) with
+// p_e the per-element parameter of the physics (STRUCT: C10 = mu/2;
+// HEATS/CEP: conductivity/diffusivity), evaluated at (Ag, Yg, Dg).
+//   STRUCT: S_iso = J^-2/3 (2 C10 I - (2 C10 trC / 3) C^-1) is linear in C10,
+//           so d lR(a,c)/d C10 = W Nx_a . (F S_iso / C10)(c,:)
+//           (STRUCT.f:276-296, MATMODELS.f:136-150; W = sum_g w).
+//   HEATS:  d lR(a)/d nu = W Nx_a . grad T (HEATS.f:146-154).
+__global__ void __launch_bounds__(kAsmThreads) k_dRdp_struct(AsmArgs A, int nEl,
+                                                             const double *__restrict__ lam,
+                                                             double *out, double scale) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nEl) return;
+  const int4 nd = A.ien[e];
+  const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
+  double xl[4][3];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) xl[a][i] = A.x[(size_t)n4[a] * 3 + i];
+  double xXi[3][3], adj[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) xXi[i][k] = xl[k][i] - xl[3][i];
+  const double Jac = adj_det3(xXi, adj);
+  const double iJ = 1.0 / Jac;
+  double Nx[3][4];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    Nx[i][0] = adj[0][i] * iJ;
+    Nx[i][1] = adj[1][i] * iJ;
+    Nx[i][2] = adj[2][i] * iJ;
+    Nx[i][3] = -(Nx[i][0] + Nx[i][1] + Nx[i][2]);
+  }
+  const double W = 4.0 * c_rule.w * Jac;
+  double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const double d = A.Dg[(size_t)n4[a] * A.tDof + A.s + c];
+#pragma unroll
+      for (int m = 0; m < 3; m++) F[c][m] += Nx[m][a] * d;
+    }
+  double Fi[3][3];
+  const double J = adj_det3(F, Fi);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) Fi[i][j] /= J;
+  double Ci[3][3], trC = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      Ci[i][j] = Fi[i][0] * Fi[j][0] + Fi[i][1] * Fi[j][1] + Fi[i][2] * Fi[j][2];
+      trC += F[i][j] * F[i][j];
+    }
+  const double J2d = jm23(J);
+  double St[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) St[i][j] = 2.0 * J2d * ((i == j ? 1.0 : 0.0) - trC / 3.0 * Ci[i][j]);
+  double acc = 0.0;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    double Pt[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) Pt[k] = F[c][0] * St[0][k] + F[c][1] * St[1][k] + F[c][2] * St[2][k];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+      acc += lam[(size_t)n4[a] * 3 + c] * W * (Nx[0][a] * Pt[0] + Nx[1][a] * Pt[1] + Nx[2][a] * Pt[2]);
+  }
+  out[e] += scale * acc;
+}
+
+__global__ void __launch_bounds__(kAsmThreads) k_dRdp_heats(AsmArgs A, int nEl,
+                                                            const double *__restrict__ lam,
+                                                            double *out, double scale) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nEl) return;
+  const int4 nd = A.ien[e];
+  const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
+  double xl[4][3], yl[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) xl[a][i] = A.x[(size_t)n4[a] * 3 + i];
+    yl[a] = A.Yg[(size_t)n4[a] * A.tDof + A.s];
+  }
+  double Nx[3][4], Jac;
+  gnn_tet4(xl, Nx, Jac);
+  double Tx[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) Tx[i] = Nx[i][0] * yl[0] + Nx[i][1] * yl[1] + Nx[i][2] * yl[2] + Nx[i][3] * yl[3];
+  const double W = 4.0 * c_rule.w * Jac;
+  double acc = 0.0;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+    acc += lam[n4[a]] * W * (Nx[0][a] * Tx[0] + Nx[1][a] * Tx[1] + Nx[2][a] * Tx[2]);
+  out[e] += scale * acc;
+}
+
+// out (colour order, nEl) += scale * (dR/dp)^T lambda
+int mesh_dRdp(gsls_mesh *m, const gsls_eq_params *p, const double *Yg, const double *Dg,
+              const double *lam, double *out, double scale) {
+  AsmArgs A;
+  memset(&A, 0, sizeof(A));
+  A.tDof = p->tDof;
+  A.s = p->s;
+  A.ien = m->d_ien.as<int4>();
+  A.x = m->d_x.as<double>();
+  A.Yg = Yg;
+  A.Dg = Dg;
+  cudaStream_t st = m->lhs->stream;
+  const int nb = (m->nEl + kAsmThreads - 1) / kAsmThreads;
+  if (p->phys == GSLS_PHYS_STRUCT) {
+    if (p->dof != 3 || !Dg) return GSLS_ERR_ARG;
+    k_dRdp_struct<<<nb, kAsmThreads, 0, st>>>(A, m->nEl, lam, out, scale);
+  } else if (p->phys == GSLS_PHYS_HEATS || p->phys == GSLS_PHYS_CEP) {
+    k_dRdp_heats<<<nb, kAsmThreads, 0, st>>>(A, m->nEl, lam, out, scale);
+  } else {
+    set_error("dR/dp: physics without a per-element parameter sensitivity");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  GSLS_CHECK_LAUNCH();
+  return GSLS_OK;
+}
+
+// Consistent mass matrix M_ab = sum_g w N_a N_b as a scalar CSR (the HEATS
+// element with unit density, no conduction and unit gen-alpha factors).
+int mesh_mass(gsls_mesh *m, const double *zeros, double *R, double *Val) {
+  gsls_lhs *lhs = m->lhs;
+  cudaStream_t st = lhs->stream;
+  GSLS_CUDA(cudaMemsetAsync(R, 0, sizeof(double) * (size_t)lhs->nNo, st));
+  GSLS_CUDA(cudaMemsetAsync(Val, 0, sizeof(double) * (size_t)lhs->nnz, st));
+  AsmArgs A;
+  memset(&A, 0, sizeof(A));
+  A.tDof = 1;
+  A.am = A.af = A.gam = A.dt = 1.0;
+  A.rho = 1.0;
+  A.ien = m->d_ien.as<int4>();
+  A.map = m->d_map.as<int4>();
+  A.x = m->d_x.as<double>();
+  A.Ag = A.Yg = A.Dg = zeros;
+  A.R = R;
+  A.Val = Val;
+  A.err = m->d_err.as<int>();
+  for (int c = 0; c < m->ncolors; c++) {
+    A.el0 = m->color_off[c];
+    A.nColorEl = m->color_off[c + 1] - m->color_off[c];
+    if (A.nColorEl <= 0) continue;
+    k_asm_heats<double><<<(A.nColorEl + kAsmThreads - 1) / kAsmThreads, kAsmThreads, 0, st>>>(A);
+    GSLS_CHECK_LAUNCH();
+  }
+  return GSLS_OK;
+}
+
+// colour-order index -> original element index
+const int *mesh_perm(gsls_mesh *m, int *nEl) {
+  *nEl = m->nEl;
+  return m->perm.data();
+}
+
 int mesh_set_eparam(gsls_mesh *m, const double *eparam) {
   if (!eparam) {
     m->has_eparam = false;

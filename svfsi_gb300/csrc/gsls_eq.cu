@@ -4,6 +4,7 @@
 // assembly -> SETBCNEU traction (SETBC.f:319-416) -> FSILS_SOLVE -> PICC
 // (PIC.f:169-297).  State arrays stay in HBM between steps; the host reads
 // one scalar (RI%iNorm) per Newton iteration for the stopping test.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -14,6 +15,10 @@
 namespace gsls {
 int assemble_dev(gsls_mesh *m, const gsls_eq_params *p, const double *Ag, const double *Yg,
                  const double *Dg, double *R, void *Val, int val_prec);
+int mesh_dRdp(gsls_mesh *m, const gsls_eq_params *p, const double *Yg, const double *Dg,
+              const double *lam, double *out, double scale);
+int mesh_mass(gsls_mesh *m, const double *zeros, double *R, double *Val);
+const int *mesh_perm(gsls_mesh *m, int *nEl);
 int mesh_set_eparam(gsls_mesh *m, const double *eparam);
 int mesh_check_error(gsls_mesh *m);
 gsls_lhs *mesh_lhs(gsls_mesh *m);
@@ -552,6 +557,355 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     std::swap(eq->st[k].bytes, eq->st[k + 3].bytes);
   }
   GSLS_CUDA(cudaStreamSynchronize(st));
+  return GSLS_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Discrete adjoint of the implicit time stepping (checkpoint-and-recompute).
+//
+// A converged step n satisfies R(A_n; s_{n-1}, p) = 0 with the Newmark
+// relations Y_n = Y_{n-1} + dt((1-gam) A_{n-1} + gam A_n) and
+// D_n = D_{n-1} + dt Y_{n-1} + dt^2((1/2-beta) A_{n-1} + beta A_n), which the
+// predictor (PICP, PIC.f:80-130) and corrector (PICC, PIC.f:169-213) keep
+// exactly.  R depends on the state through Ag = (1-am) A_{n-1} + am A_n,
+// Yg, Dg (PICI, PIC.f:133-166) with partials R_a = rho M, R_y (= dmp M for
+// STRUCT) and R_d, and the assembled tangent is
+// K = dR/dA_n = am R_a + af gam dt R_y + af beta dt^2 R_d.  Given the
+// cotangent (Abar, Ybar, Dbar) of s_n, one reverse step is
+//   g = Abar + gam dt Ybar + beta dt^2 Dbar;   K^T lambda = g (K symmetric,
+//   Dirichlet rows masked as in the forward solve)
+//   Abar' = dt(1-gam) Ybar + dt^2(1/2-beta) Dbar - [(1-am) R_a + af dt(1-gam) R_y
+//           + af dt^2 (1/2-beta) R_d]^T lambda
+//   Ybar' = Ybar + dt Dbar - [R_y + af dt R_d]^T lambda,  Dbar' = Dbar - R_d^T lambda
+//   dJ/dp -= (dR/dp)^T lambda.
+// R_d lambda is formed from K lambda and the mass matrix:
+// R_d = (K - (am rho + af gam dt dmp) M) / (af beta dt^2); for HEATS
+// (no displacement) R_y = (K - am rho M) / (af gam dt).
+// ===========================================================================
+struct gsls_tape {
+  gsls_eq *eq = nullptr;
+  int nsteps = 0, every = 1, nseg = 0;
+  struct Ck {
+    gsls::DevBuf st;  // Ao, Yo, Do (3 x ns doubles)
+    double iN = 0.0, pN = 0.0, time = 0.0;
+  };
+  std::vector<Ck *> ck;
+  gsls::DevBuf seg;     // states of one recomputed segment ((every+1) x 3 x ns)
+  gsls::DevBuf last;    // final state, restored after the backward pass
+  gsls::DevBuf M, Mz;   // mass CSR values; zeros / scratch (nNo)
+  gsls::DevBuf ValK, Val0, Rk;
+  gsls::DevBuf cot, lam, tmp;  // cotangents (3 x nr), lambda, M lambda / K lambda
+  gsls::DevBuf grad;    // per-element gradient (colour order)
+  ~gsls_tape() {
+    for (auto *c : ck) delete c;
+  }
+};
+
+namespace gsls {
+
+static int save_state(gsls_eq *eq, double *dst) {
+  const size_t ns = (size_t)eq->nNo * eq->p.tDof;
+  for (int k = 0; k < 3; k++)
+    GSLS_CUDA(cudaMemcpyAsync(dst + k * ns, eq->st[k].p, sizeof(double) * ns,
+                              cudaMemcpyDeviceToDevice, eq->lhs->stream));
+  return GSLS_OK;
+}
+static int load_state(gsls_eq *eq, const double *src) {
+  const size_t ns = (size_t)eq->nNo * eq->p.tDof;
+  for (int k = 0; k < 3; k++)
+    GSLS_CUDA(cudaMemcpyAsync(eq->st[k].p, src + k * ns, sizeof(double) * ns,
+                              cudaMemcpyDeviceToDevice, eq->lhs->stream));
+  return GSLS_OK;
+}
+
+// g = Abar + gam dt Ybar (+ beta dt^2 Dbar)
+__global__ void k_adj_rhs(size_t n, const double *Ab, const double *Yb, const double *Db, double c1,
+                          double c2, int dflag, double *g) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    g[k] = Ab[k] + c1 * Yb[k] + (dflag ? c2 * Db[k] : 0.0);
+}
+
+// y(i,c) = sum_j M_j x(col_j, c) for a scalar CSR M and dof-vectors x
+__global__ void k_spmv_scalar_vec(int nNo, int dof, const int *__restrict__ rowPtr,
+                                  const int *__restrict__ colPtr, const double *__restrict__ M,
+                                  const double *__restrict__ x, double *y) {
+  const size_t n = (size_t)nNo * dof;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / dof), c = (int)(t - (size_t)i * dof);
+    double acc = 0.0;
+    for (int j = rowPtr[i]; j < rowPtr[i + 1]; j++) acc += M[j] * x[(size_t)colPtr[j] * dof + c];
+    y[t] = acc;
+  }
+}
+
+struct AdjCoef {
+  double dt, gam, beta, am, af, rho, dmp;
+  int dflag;
+};
+// cotangent update of one reverse step (see the header comment); Ml = M lambda,
+// Kl = K lambda; masked entries (Dirichlet) are zeroed
+__global__ void k_adj_update(size_t n, AdjCoef c, const double *Ml, const double *Kl,
+                             const double *mask, double *Ab, double *Yb, double *Db) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const double m = (mask[k] > 0.5) ? 1.0 : 0.0;
+    const double ml = Ml[k], kl = Kl[k];
+    const double yb = Yb[k];
+    if (c.dflag) {
+      const double db = Db[k];
+      const double rd = (kl - (c.am * c.rho + c.af * c.gam * c.dt * c.dmp) * ml) /
+                        (c.af * c.beta * c.dt * c.dt);
+      const double ry = c.dmp * ml;
+      const double a = c.dt * (1.0 - c.gam) * yb + c.dt * c.dt * (0.5 - c.beta) * db -
+                       ((1.0 - c.am) * c.rho * ml + c.af * c.dt * (1.0 - c.gam) * ry +
+                        c.af * c.dt * c.dt * (0.5 - c.beta) * rd);
+      const double y = yb + c.dt * db - (ry + c.af * c.dt * rd);
+      Ab[k] = m * a;
+      Yb[k] = m * y;
+      Db[k] = m * (db - rd);
+    } else {
+      const double ry = (kl - c.am * c.rho * ml) / (c.af * c.gam * c.dt);
+      Ab[k] = m * (c.dt * (1.0 - c.gam) * yb - ((1.0 - c.am) * c.rho * ml + c.af * c.dt * (1.0 - c.gam) * ry));
+      Yb[k] = m * (yb - ry);
+    }
+  }
+}
+
+static int tape_alloc(gsls_tape *t) {
+  gsls_eq *eq = t->eq;
+  gsls_lhs *lhs = eq->lhs;
+  const size_t ns = (size_t)eq->nNo * eq->p.tDof, nr = (size_t)eq->nNo * eq->p.dof;
+  const size_t vk = (size_t)eq->nnz * eq->p.dof * eq->p.dof;
+  int nEl = 0;
+  mesh_perm(eq->mesh, &nEl);
+  GSLS_TRY(t->seg.alloc(sizeof(double) * 3 * ns * (size_t)(t->every + 1)));
+  GSLS_TRY(t->last.alloc(sizeof(double) * 3 * ns));
+  GSLS_TRY(t->M.alloc(sizeof(double) * (size_t)eq->nnz));
+  GSLS_TRY(t->Mz.alloc(sizeof(double) * 2 * (size_t)eq->nNo));
+  GSLS_TRY(t->ValK.alloc(sizeof(double) * vk + 64));
+  GSLS_TRY(t->Val0.alloc(sizeof(double) * vk + 64));
+  GSLS_TRY(t->Rk.alloc(sizeof(double) * nr));
+  GSLS_TRY(t->cot.alloc(sizeof(double) * 3 * nr));
+  GSLS_TRY(t->lam.alloc(sizeof(double) * nr));
+  GSLS_TRY(t->tmp.alloc(sizeof(double) * 2 * nr));
+  GSLS_TRY(t->grad.alloc(sizeof(double) * (size_t)(nEl > 0 ? nEl : 1)));
+  double *z = t->Mz.as<double>();
+  GSLS_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * (size_t)eq->nNo, lhs->stream));
+  GSLS_TRY(mesh_mass(eq->mesh, z, z + eq->nNo, t->M.as<double>()));
+  return GSLS_OK;
+}
+
+// lambda = K^-T g at the linearisation point (Ao, Yo, Do) -> (An, Yn, Dn);
+// assembles K (FP64) into t->ValK, keeps an unscaled copy in t->Val0 and
+// leaves Ag/Yg/Dg in eq->st[6..8]
+static int adj_solve_at(gsls_tape *t, const double *Ao, const double *Yo, const double *Do,
+                        const double *An, const double *Yn, const double *Dn, const double *g,
+                        double *lam) {
+  gsls_eq *eq = t->eq;
+  gsls_lhs *lhs = eq->lhs;
+  cudaStream_t st = lhs->stream;
+  const gsls_eq_params &p = eq->p;
+  const size_t ns = (size_t)eq->nNo * p.tDof, nr = (size_t)eq->nNo * p.dof;
+  const size_t vk = (size_t)eq->nnz * p.dof * p.dof;
+  double *Ag = eq->st[6].as<double>(), *Yg = eq->st[7].as<double>(), *Dg = eq->st[8].as<double>();
+  k_pici<<<nblk(ns), kT, 0, st>>>(ns, p.am, p.af, Ao, An, Yo, Yn, Do, Dn, Ag, Yg, Dg);
+  GSLS_CHECK_LAUNCH();
+  GSLS_TRY(assemble_dev(eq->mesh, &p, Ag, Yg, Dg, t->Rk.as<double>(), t->ValK.p, GSLS_PREC_FP64));
+  GSLS_TRY(mesh_check_error(eq->mesh));
+  GSLS_CUDA(cudaMemcpyAsync(t->Val0.p, t->ValK.p, sizeof(double) * vk, cudaMemcpyDeviceToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(lam, g, sizeof(double) * nr, cudaMemcpyDeviceToDevice, st));
+  gsls_ls ls = eq->ls;  // the forward solver, converged tightly
+  ls.RI.relTol = 1e-12;
+  ls.RI.absTol = 1e-300;
+  if (ls.RI.mItr < 20000 && ls.LS_type == GSLS_LS_TYPE_CG) ls.RI.mItr = 20000;
+  GSLS_TRY(lhs_update_faces(lhs, nullptr, nullptr));
+  GSLS_TRY(solve_dev(lhs, &ls, p.dof, lam, t->ValK.p, GSLS_PREC_FP64, eq->sv.prec, true));
+  if (!ls.RI.suc) {
+    set_error("adjoint: transpose solve did not converge");
+    return GSLS_ERR_NAN;
+  }
+  return GSLS_OK;
+}
+
+static int adj_reverse_step(gsls_tape *t, const double *so, const double *sn) {
+  gsls_eq *eq = t->eq;
+  cudaStream_t st = eq->lhs->stream;
+  const gsls_eq_params &p = eq->p;
+  const size_t ns = (size_t)eq->nNo * p.tDof, nr = (size_t)eq->nNo * p.dof;
+  double *Ab = t->cot.as<double>(), *Yb = Ab + nr, *Db = Yb + nr;
+  double *g = t->tmp.as<double>(), *Kl = g + nr;
+  double *lam = t->lam.as<double>();
+  k_adj_rhs<<<nblk(nr), kT, 0, st>>>(nr, Ab, Yb, Db, p.gam * p.dt, p.beta * p.dt * p.dt,
+                                     eq->dFlag ? 1 : 0, g);
+  GSLS_CHECK_LAUNCH();
+  GSLS_TRY(adj_solve_at(t, so, so + ns, so + 2 * ns, sn, sn + ns, sn + 2 * ns, g, lam));
+  // g <- M lambda, Kl <- K lambda (unscaled tangent)
+  gsls_lhs *lhs = eq->lhs;
+  k_spmv_scalar_vec<<<nblk(nr), kT, 0, st>>>(eq->nNo, p.dof, lhs->d_rowPtr.as<int>(),
+                                             lhs->d_colPtr.as<int>(), t->M.as<double>(), lam, g);
+  GSLS_CHECK_LAUNCH();
+  GSLS_TRY(spmv_launch(lhs, p.dof, t->Val0.p, GSLS_PREC_FP64, lam, Kl, GSLS_PREC_FP64));
+  // dJ/dp -= (dR/dp)^T lambda at (Yg, Dg)
+  GSLS_TRY(mesh_dRdp(eq->mesh, &p, eq->st[7].as<double>(), eq->st[8].as<double>(), lam,
+                     t->grad.as<double>(), -1.0));
+  AdjCoef c{p.dt, p.gam, p.beta, p.am, p.af, p.rho, p.dmp, eq->dFlag ? 1 : 0};
+  k_adj_update<<<nblk(nr), kT, 0, st>>>(nr, c, g, Kl, lhs->ws.mask.as<double>(), Ab, Yb, Db);
+  GSLS_CHECK_LAUNCH();
+  return GSLS_OK;
+}
+
+static int adj_check(gsls_eq *eq) {
+  const gsls_eq_params &p = eq->p;
+  if (p.phys != GSLS_PHYS_STRUCT && p.phys != GSLS_PHYS_HEATS) {
+    set_error("adjoint: built for STRUCT and HEATS equations");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  if (p.s != 0 || p.tDof != p.dof) {
+    set_error("adjoint: single-equation problems only (s = 0, tDof = dof)");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  if (p.phys == GSLS_PHYS_STRUCT && p.visc != 0.0) {
+    set_error("adjoint: solid viscosity is not differentiated");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  return GSLS_OK;
+}
+
+}  // namespace gsls
+
+extern "C" {
+
+int gsls_adjoint_forward(gsls_eq *eq, int nsteps, int every, gsls_tape **out) {
+  if (!eq || !out || nsteps < 1 || every < 1) return GSLS_ERR_ARG;
+  GSLS_TRY(adj_check(eq));
+  gsls_tape *t = new gsls_tape();
+  t->eq = eq;
+  t->nsteps = nsteps;
+  t->every = every;
+  t->nseg = (nsteps + every - 1) / every;
+  int rc = tape_alloc(t);
+  const size_t ns = (size_t)eq->nNo * eq->p.tDof;
+  for (int n = 0; rc == GSLS_OK && n < nsteps; n++) {
+    if (n % every == 0) {
+      auto *c = new gsls_tape::Ck();
+      t->ck.push_back(c);
+      if ((rc = c->st.alloc(sizeof(double) * 3 * ns)) != GSLS_OK) break;
+      if ((rc = save_state(eq, c->st.as<double>())) != GSLS_OK) break;
+      c->iN = eq->eq_iNorm;
+      c->pN = eq->eq_pNorm;
+      c->time = eq->time;
+    }
+    gsls_step_info info;
+    rc = gsls_eq_step(eq, &info);
+  }
+  if (rc == GSLS_OK) rc = save_state(eq, t->last.as<double>());
+  if (rc == GSLS_OK) {
+    cudaError_t e = cudaStreamSynchronize(eq->lhs->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "adjoint forward", __FILE__, __LINE__);
+  }
+  if (rc != GSLS_OK) {
+    delete t;
+    return rc;
+  }
+  *out = t;
+  return GSLS_OK;
+}
+
+int gsls_adjoint_backward(gsls_tape *t, const double *Abar, const double *Ybar,
+                          const double *Dbar, double *grad) {
+  if (!t || !grad) return GSLS_ERR_ARG;
+  gsls_eq *eq = t->eq;
+  cudaStream_t st = eq->lhs->stream;
+  const size_t ns = (size_t)eq->nNo * eq->p.tDof, nr = (size_t)eq->nNo * eq->p.dof;
+  int nEl = 0;
+  const int *perm = mesh_perm(eq->mesh, &nEl);
+  double *cot = t->cot.as<double>();
+  const double *in[3] = {Abar, Ybar, Dbar};
+  for (int k = 0; k < 3; k++) {
+    if (in[k])
+      GSLS_CUDA(cudaMemcpyAsync(cot + k * nr, in[k], sizeof(double) * nr, cudaMemcpyHostToDevice, st));
+    else
+      GSLS_CUDA(cudaMemsetAsync(cot + k * nr, 0, sizeof(double) * nr, st));
+  }
+  GSLS_CUDA(cudaMemsetAsync(t->grad.p, 0, sizeof(double) * (size_t)nEl, st));
+  const double iN_end = eq->eq_iNorm, pN_end = eq->eq_pNorm, time_end = eq->time;
+  double *seg = t->seg.as<double>();
+  for (int sgi = t->nseg - 1; sgi >= 0; sgi--) {
+    const int n0 = sgi * t->every, n1 = std::min(n0 + t->every, t->nsteps);
+    gsls_tape::Ck *c = t->ck[sgi];
+    GSLS_TRY(load_state(eq, c->st.as<double>()));
+    eq->eq_iNorm = c->iN;
+    eq->eq_pNorm = c->pN;
+    eq->time = c->time;
+    GSLS_TRY(save_state(eq, seg));
+    for (int k = 1; k <= n1 - n0; k++) {
+      gsls_step_info info;
+      GSLS_TRY(gsls_eq_step(eq, &info));
+      GSLS_TRY(save_state(eq, seg + (size_t)k * 3 * ns));
+    }
+    for (int k = n1 - n0; k >= 1; k--)
+      GSLS_TRY(adj_reverse_step(t, seg + (size_t)(k - 1) * 3 * ns, seg + (size_t)k * 3 * ns));
+  }
+  // leave the equation at its final state
+  GSLS_TRY(load_state(eq, t->last.as<double>()));
+  eq->eq_iNorm = iN_end;
+  eq->eq_pNorm = pN_end;
+  eq->time = time_end;
+  std::vector<double> g((size_t)nEl);
+  GSLS_CUDA(cudaMemcpyAsync(g.data(), t->grad.p, sizeof(double) * (size_t)nEl,
+                            cudaMemcpyDeviceToHost, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  for (int k = 0; k < nEl; k++) grad[perm[k]] = g[k];
+  return GSLS_OK;
+}
+
+int gsls_tape_free(gsls_tape *t) {
+  if (!t) return GSLS_ERR_ARG;
+  cudaStreamSynchronize(t->eq->lhs->stream);
+  delete t;
+  return GSLS_OK;
+}
+
+int gsls_adjoint_solve(gsls_eq *eq, const gsls_adj_point *pt, const double *dRhs,
+                       double *dLambda) {
+  if (!eq || !pt || !dRhs || !dLambda || !pt->Ao || !pt->Yo || !pt->Do || !pt->An ||
+      !pt->Yn || !pt->Dn)
+    return GSLS_ERR_ARG;
+  GSLS_TRY(adj_check(eq));
+  gsls_tape t;
+  t.eq = eq;
+  t.every = 1;
+  GSLS_TRY(tape_alloc(&t));
+  GSLS_TRY(adj_solve_at(&t, pt->Ao, pt->Yo, pt->Do, pt->An, pt->Yn, pt->Dn, dRhs, dLambda));
+  GSLS_CUDA(cudaStreamSynchronize(eq->lhs->stream));
+  return GSLS_OK;
+}
+
+int gsls_dRdp(gsls_eq *eq, const gsls_adj_point *pt, const double *dLambda, double *dOut) {
+  if (!eq || !pt || !dLambda || !dOut) return GSLS_ERR_ARG;
+  GSLS_TRY(adj_check(eq));
+  cudaStream_t st = eq->lhs->stream;
+  const gsls_eq_params &p = eq->p;
+  const size_t ns = (size_t)eq->nNo * p.tDof;
+  int nEl = 0;
+  const int *perm = mesh_perm(eq->mesh, &nEl);
+  double *Ag = eq->st[6].as<double>(), *Yg = eq->st[7].as<double>(), *Dg = eq->st[8].as<double>();
+  k_pici<<<nblk(ns), kT, 0, st>>>(ns, p.am, p.af, pt->Ao, pt->An, pt->Yo, pt->Yn, pt->Do, pt->Dn,
+                                  Ag, Yg, Dg);
+  GSLS_CHECK_LAUNCH();
+  DevBuf tmp, pm;
+  GSLS_TRY(tmp.alloc(sizeof(double) * (size_t)nEl));
+  GSLS_CUDA(cudaMemsetAsync(tmp.p, 0, sizeof(double) * (size_t)nEl, st));
+  GSLS_TRY(mesh_dRdp(eq->mesh, &p, Yg, Dg, dLambda, tmp.as<double>(), 1.0));
+  std::vector<double> h((size_t)nEl), o((size_t)nEl);
+  GSLS_CUDA(cudaMemcpyAsync(h.data(), tmp.p, sizeof(double) * (size_t)nEl, cudaMemcpyDeviceToHost, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  for (int k = 0; k < nEl; k++) o[perm[k]] = h[k];
+  GSLS_CUDA(cudaMemcpy(dOut, o.data(), sizeof(double) * (size_t)nEl, cudaMemcpyHostToDevice));
   return GSLS_OK;
 }
 

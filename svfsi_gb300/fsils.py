@@ -208,6 +208,14 @@ class Equation:
         check(_lib.load().gsls_eq_get_cep_state(self.h, _dp(X)), "gsls_eq_get_cep_state")
         return X
 
+    def adjoint_forward(self, nsteps, every=5):
+        """Take nsteps steps with checkpoints every `every` steps; returns a
+        Tape whose backward() gives dJ/dp for the per-element parameter."""
+        h = C.c_void_p()
+        check(_lib.load().gsls_adjoint_forward(self.h, int(nsteps), int(every), C.byref(h)),
+              "gsls_adjoint_forward")
+        return Tape(h, self)
+
     def set_eparam(self, ep):
         e = None if ep is None else _f64(ep)
         check(_lib.load().gsls_eq_set_eparam(self.h, _dp(e) if e is not None else None),
@@ -217,3 +225,32 @@ class Equation:
         if self.h:
             _lib.load().gsls_eq_free(self.h)
             self.h = None
+
+
+class Tape:
+    """Checkpoints of an adjoint forward run (gsls_tape)."""
+
+    def __init__(self, h, eq: Equation):
+        self.h = h
+        self.eq = eq
+
+    def backward(self, Abar=None, Ybar=None, Dbar=None):
+        """dJ/dp (nEl) from the cotangents of the final state (nNo x tDof each)."""
+        nEl = self.eq.mesh.nEl
+        g = np.zeros(nEl)
+        arrs = [None if a is None else _f64(a) for a in (Abar, Ybar, Dbar)]
+        ptrs = [None if a is None else _dp(a) for a in arrs]
+        check(_lib.load().gsls_adjoint_backward(self.h, ptrs[0], ptrs[1], ptrs[2], _dp(g)),
+              "gsls_adjoint_backward")
+        return g
+
+    def free(self):
+        if self.h:
+            _lib.load().gsls_tape_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

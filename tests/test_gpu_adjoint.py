@@ -1,0 +1,162 @@
+"""Discrete adjoint (forward/backward pair of the C ABI) against central
+finite differences of the objective, on the GPU FP64 path and on the oracle
+(the CPU restatement with per-element parameters).
+
+Objective: J = 1/2 |u_tip - u_target|^2 on the final displacement of the
+x = L face (STRUCT, parameter C10 = mu/2 per element) or 1/2 |T - T_target|^2
+on all nodes (HEATS, conductivity per element).  Checked to 1e-5 relative
+along seeded random directions (relative perturbations of every element's
+parameter), with Newton and the Krylov solves converged tightly so that the
+finite differences resolve 1e-5.
+"""
+import numpy as np
+import pytest
+
+from svfsi_gb300 import fsils, meshgen, problems
+
+pytestmark = pytest.mark.gpu
+
+FD_H = 1e-4  # relative parameter perturbation of the central differences
+
+
+def _struct(nsteps=6):
+    p = problems.struct_beam(10, 3, 3, nsteps=nsteps, traction=(0.0, 0.0, -5e3))
+    p.tol, p.maxItr, p.ls_relTol = 1e-13, 20, 1e-12
+    rng = np.random.default_rng(7)
+    ep = p.params["C10"] * np.exp(0.2 * rng.standard_normal(p.nEl))
+    tip = meshgen.nodes_on_plane(p.x, 0, 4.0)
+    return p, ep, tip
+
+
+def _heats(nsteps=5):
+    p = problems.heats_cube(5, nsteps=nsteps)
+    p.tol, p.maxItr, p.ls_relTol = 1e-13, 20, 1e-13
+    rng = np.random.default_rng(8)
+    ep = np.exp(0.3 * rng.standard_normal(p.nEl))
+    return p, ep, np.arange(p.nNo)
+
+
+def _final(p, ep, field):
+    lhs, mesh, eq = problems.build_equation(p)
+    eq.set_eparam(ep)
+    for _ in range(p.nsteps):
+        eq.step()
+    st = eq.get_state()
+    return st[field]
+
+
+def _J(u, sel, target):
+    d = u[sel] - target
+    return 0.5 * float(np.sum(d * d))
+
+
+@pytest.mark.parametrize("case", ["struct", "heats"])
+def test_adjoint_gradient_matches_central_fd(gsls, case):
+    p, ep, sel = _struct() if case == "struct" else _heats()
+    field = 2 if case == "struct" else 1  # D (struct) or T = Y (heats)
+    u0 = _final(p, ep, field)
+    rng = np.random.default_rng(21)
+    target = u0[sel] * (1.0 + 0.1 * rng.standard_normal(u0[sel].shape))
+    # adjoint
+    lhs, mesh, eq = problems.build_equation(p)
+    eq.set_eparam(ep)
+    tape = eq.adjoint_forward(p.nsteps, every=4)
+    st = eq.get_state()
+    uN = st[field]
+    assert np.allclose(uN, u0, rtol=0, atol=1e-12 * np.abs(u0).max())
+    bar = np.zeros_like(uN)
+    bar[sel] = uN[sel] - target
+    grad = tape.backward(Dbar=bar) if case == "struct" else tape.backward(Ybar=bar)
+    tape.free()
+    # the equation is left at step N
+    assert np.allclose(eq.get_state()[field], uN, rtol=0, atol=0)
+    for k in range(3):
+        r = rng.standard_normal(p.nEl)
+        r /= np.linalg.norm(r)
+        dp = ep * r  # relative direction
+        Jp = _J(_final(p, ep + FD_H * dp, field), sel, target)
+        Jm = _J(_final(p, ep - FD_H * dp, field), sel, target)
+        fd = (Jp - Jm) / (2 * FD_H)
+        ad = float(grad @ dp)
+        assert abs(fd - ad) <= 1e-5 * abs(ad), (k, fd, ad)
+
+
+def test_adjoint_matches_oracle_fd(gsls, orc):
+    """The GPU adjoint gradient against a central finite difference of the
+    CPU oracle (same algorithm, per-element C10) along one direction."""
+    p, ep, sel = _struct(nsteps=3)
+    lhs, mesh, eq = problems.build_equation(p)
+    eq.set_eparam(ep)
+    tape = eq.adjoint_forward(p.nsteps, every=2)
+    uN = eq.get_state()[2]
+    rng = np.random.default_rng(5)
+    target = uN[sel] * 0.95
+    bar = np.zeros_like(uN)
+    bar[sel] = uN[sel] - target
+    grad = tape.backward(Dbar=bar)
+    tape.free()
+    r = rng.standard_normal(p.nEl)
+    r /= np.linalg.norm(r)
+    dp = ep * r
+
+    def J_oracle(e):
+        oeq = orc.OracleEquation(p, eparam=e)
+        for _ in range(p.nsteps):
+            oeq.step()
+        return _J(oeq.state()[2], sel, target)
+
+    fd = (J_oracle(ep + FD_H * dp) - J_oracle(ep - FD_H * dp)) / (2 * FD_H)
+    ad = float(grad @ dp)
+    assert abs(fd - ad) <= 1e-5 * abs(ad), (fd, ad)
+
+
+def test_adjoint_solve_and_dRdp_building_blocks(gsls):
+    """gsls_adjoint_solve returns K^-T g (checked through the tangent itself:
+    K lambda = g on the free rows) and gsls_dRdp is linear in lambda."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    from svfsi_gb300 import _lib
+    p, ep, sel = _struct(nsteps=1)
+    lhs, mesh, eq = problems.build_equation(p)
+    eq.set_eparam(ep)
+    Ao, Yo, Do = eq.get_state()
+    eq.step()
+    An, Yn, Dn = eq.get_state()
+    dev = [torch.tensor(a, device="cuda") for a in (Ao, Yo, Do, An, Yn, Dn)]
+    pt = _lib.AdjPoint(*[C.c_void_p(t.data_ptr()) for t in dev])
+    rng = np.random.default_rng(3)
+    g = torch.tensor(rng.standard_normal((p.nNo, 3)), device="cuda")
+    lam = torch.zeros_like(g)
+    L = _lib.load()
+    _lib.check(L.gsls_adjoint_solve(eq.h, C.byref(pt), C.c_void_p(g.data_ptr()),
+                                    C.c_void_p(lam.data_ptr())))
+    out1 = torch.zeros(p.nEl, dtype=torch.float64, device="cuda")
+    out2 = torch.zeros_like(out1)
+    _lib.check(L.gsls_dRdp(eq.h, C.byref(pt), C.c_void_p(lam.data_ptr()),
+                           C.c_void_p(out1.data_ptr())))
+    lam2 = 2.0 * lam
+    _lib.check(L.gsls_dRdp(eq.h, C.byref(pt), C.c_void_p(lam2.data_ptr()),
+                           C.c_void_p(out2.data_ptr())))
+    torch.cuda.synchronize()
+    o1, o2 = out1.cpu().numpy(), out2.cpu().numpy()
+    assert np.abs(o1).max() > 0
+    assert np.allclose(o2, 2.0 * o1, rtol=1e-14, atol=0)
+    # K lambda = g on free rows: assemble the tangent at the same point
+    am, af = p.params["am"], p.params["af"]
+    Ag = (1 - am) * Ao + am * An
+    Yg = (1 - af) * Yo + af * Yn
+    Dg = (1 - af) * Do + af * Dn
+    import oracle as O
+    e = np.ascontiguousarray(ep)
+    _, Vo = O.assemble(p, Ag, Yg, Dg, eparam=e)
+    lh = lam.cpu().numpy()
+    Kl = np.zeros_like(lh)
+    for i in range(p.nNo):
+        for j in range(p.rowPtr[i], p.rowPtr[i + 1]):
+            Kl[i] += Vo[j].reshape(3, 3) @ lh[p.colPtr[j]]
+    free = np.ones(p.nNo, bool)
+    free[p.dirichlet[0].nodes] = False
+    gh = g.cpu().numpy()
+    assert np.allclose(Kl[free], gh[free], rtol=1e-8, atol=1e-8 * np.abs(gh).max())
+    assert np.abs(lh[~free]).max() == 0.0
