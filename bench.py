@@ -48,7 +48,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--only", choices=["all", "mixed", "fp64"], default="all",
                     help="time one precision only (profiling runs)")
-    ap.add_argument("--workload", choices=["struct", "fluid"], default="struct")
+    ap.add_argument("--workload", choices=["struct", "fluid", "adjoint"], default="struct")
+    ap.add_argument("--fd-dirs", type=int, default=4,
+                    help="adjoint workload: random directions of the central-FD check")
+    ap.add_argument("--fd-h", type=float, default=1e-3,
+                    help="adjoint workload: relative step of the central differences")
     ap.add_argument("--fluid-h", type=float, default=0.027,
                     help="cylinder mesh spacing (profiling captures use a coarser mesh)")
     return ap.parse_args()
@@ -494,8 +498,91 @@ REF_COUNTS = (5.0, 1911.4)
 REF_NEWTON_FLUID = 7.0
 
 
+def run_adjoint(args):
+    """Adjoint of the elastodynamics workload: per-element shear modulus
+    mu_e = 3.45e5 exp(0.2 N(0,1)) (seeded), J = 1/2 |u_tip - u_target|^2 with
+    u_target from a seeded perturbed-mu run, checkpoints every 5 steps; times
+    the forward (with checkpoints) + backward pass and checks the gradient
+    against central finite differences along seeded directions."""
+    import torch
+    from svfsi_gb300 import _lib, build, fsils, meshgen, problems
+    rank, local, world = dist_env()
+    torch.cuda.set_device(local)
+    build.build()
+    L = _lib.load()
+    _lib.check(L.gsls_init(local), "gsls_init")
+    nsteps = args.steps if args.steps else 10
+    if args.small:
+        p = problems.struct_beam(24, 6, 6, nsteps=nsteps)
+    else:
+        p = problems.struct_beam(**WORKLOAD, nsteps=nsteps)
+    p.tol, p.maxItr, p.ls_relTol = 1e-12, 25, 1e-8
+    rng = np.random.default_rng(20261203)
+    mu = 3.45e5 * np.exp(0.2 * rng.standard_normal(p.nEl))
+    c10 = 0.5 * mu
+    tip = meshgen.nodes_on_plane(p.x, 0, 4.0)
+
+    def forward(e):
+        lhs, mesh, eq = problems.build_equation(p)
+        eq.set_eparam(e)
+        for _ in range(nsteps):
+            eq.step()
+        D = eq.get_state()[2]
+        eq.free(); mesh.free(); lhs.free()
+        return D
+
+    t_pert = c10 * np.exp(0.05 * rng.standard_normal(p.nEl))
+    target = forward(t_pert)[tip]
+
+    def J(D):
+        d = D[tip] - target
+        return 0.5 * float(np.sum(d * d))
+
+    lhs, mesh, eq = problems.build_equation(p)
+    eq.set_eparam(c10)
+    stream = torch.cuda.ExternalStream(L.gsls_get_stream(lhs.h))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tape = eq.adjoint_forward(nsteps, every=5)
+    t1 = time.perf_counter()
+    DN = eq.get_state()[2]
+    bar = np.zeros_like(DN)
+    bar[tip] = DN[tip] - target
+    g_c10 = tape.backward(Dbar=bar)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    tape.free()
+    grad_mu = 0.5 * g_c10
+    h = args.fd_h
+    errs, pairs = [], []
+    for k in range(args.fd_dirs):
+        r = rng.standard_normal(p.nEl)
+        r /= np.linalg.norm(r)
+        dmu = mu * r
+        fd = (J(forward(0.5 * (mu + h * dmu))) - J(forward(0.5 * (mu - h * dmu)))) / (2 * h)
+        ad = float(grad_mu @ dmu)
+        errs.append(abs(fd - ad) / abs(ad))
+        pairs.append([fd, ad])
+    out = {"metric": "adjoint s/step (forward with checkpoints + backward), FP64", "impl": "gsls",
+           "value": (t2 - t0) / nsteps, "unit": "s/step", "n_gpus": 1, "steps": nsteps,
+           "higher_is_better": False, "dtype": "f64", "data": "synthetic: seeded Kuhn-split beam",
+           "config": {"workload": workload_desc(p) + "; per-element mu log-normal sigma 0.2, "
+                      "checkpoint every 5, Newton tol 1e-12", "params": p.nEl},
+           "forward_s": t1 - t0, "backward_s": t2 - t1, "J": J(DN),
+           "fd_check": {"directions": args.fd_dirs, "h_rel": h, "rel_errs": errs, "fd_ad": pairs,
+                        "max_rel_err": max(errs) if errs else None,
+                        # FD noise is absolute: normalise by the RMS directional derivative
+                        "max_err_over_rms": (max(abs(a - b) for a, b in pairs) /
+                                             float(np.sqrt(np.mean([b * b for _, b in pairs]))))
+                        if pairs else None}}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    if args.workload == "adjoint":
+        run_adjoint(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
