@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--only", choices=["all", "mixed", "fp64"], default="all",
                     help="time one precision only (profiling runs)")
-    ap.add_argument("--workload", choices=["struct", "fluid", "adjoint"], default="struct")
+    ap.add_argument("--workload", choices=["struct", "fluid", "cep", "adjoint"], default="struct")
     ap.add_argument("--fd-dirs", type=int, default=4,
                     help="adjoint workload: random directions of the central-FD check")
     ap.add_argument("--fd-h", type=float, default=1e-3,
@@ -67,6 +67,12 @@ def workload(args):
     from svfsi_gb300 import problems
     if args.workload == "fluid":
         return problems.fluid_cylinder(h=0.08 if args.small else args.fluid_h, nsteps=args.steps)
+    if args.workload == "cep":
+        # the stimulus amplitude of the configuration is -52 (AP sign: no upstroke);
+        # +52 is timed so that the front propagates and the CG works at full range
+        if args.small:
+            return problems.cep_slab(27, 27, 6, nsteps=args.steps, A=52.0)
+        return problems.cep_slab(nsteps=args.steps, A=52.0)
     if args.small:
         return problems.struct_beam(24, 6, 6, nsteps=args.steps)
     return problems.struct_beam(**WORKLOAD, nsteps=args.steps)
@@ -76,7 +82,15 @@ def is_fluid(p):
     return p.dof == 4
 
 
+def is_cep(p):
+    return bool(getattr(p, "cep", None))
+
+
 def workload_desc(p):
+    if is_cep(p):
+        return (f"{p.name}: monodomain Aliev-Panfilov (FE reaction step), Diso 0.1, stimulus "
+                f"+52 for 2 ms on the 1x1x2 corner block, {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
+                f"{p.nnz:,}, CG+diag, dt 0.01, Newton tol 1e-6")
     if is_fluid(p):
         return (f"{p.name}: VMS incompressible Navier-Stokes (rho 1.06, mu 0.04, parabolic "
                 f"inlet peak 30, impulsive start), {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
@@ -248,7 +262,7 @@ def run_gsls(args):
     profd = timed_run(fsils.PREC_MIXED, profile=True, nsteps=2, nwarm=1)
     ms_mixed = max_over_ranks(mixed["ms"]) / K
     ms_fp64 = max_over_ranks(fp64["ms"]) / K
-    sidx = 1 if is_fluid(p) else 2  # compare Y (fluid) or D (struct)
+    sidx = 1 if (is_fluid(p) or is_cep(p)) else 2  # compare Y (fluid, CEP) or D (struct)
     D_m, D_f = mixed["state"][sidx], fp64["state"][sidx]
     rel_l2 = float(np.linalg.norm(D_m - D_f) / np.linalg.norm(D_f))
 
@@ -257,6 +271,8 @@ def run_gsls(args):
     shp = (p.nNo, p.tDof)
     host = [torch.zeros(shp, dtype=torch.float64).pin_memory() for _ in range(3)]
     hv = [h.numpy() for h in host]
+    for h_, s_ in zip(hv, p.initial_state()):
+        h_[:] = s_
     for _ in range(W):
         eq.set_state(*hv)
         eq.step()
@@ -284,6 +300,10 @@ def run_gsls(args):
         B = p.nnz * (9 * 4 + 4) + 8 * p.nNo + 2 * p.nNo * 3 * 4
         kname = "k_gm_spmv<3,float,float> (block-CSR SpMV on the K block of the NS solver)"
         tkey = "gm_spmv_d3_f32_fluid_cylinder"
+    elif is_cep(p):
+        B = p.algorithmic_bytes(4, 4)["spmv"]
+        kname = "k_cg_spmv<1,float,float> (CSR SpMV + fused P.KP)"
+        tkey = "cg_spmv_d1_f32_cep_slab"
     else:
         B = p.algorithmic_bytes(4, 4)["spmv"]
         kname = "k_cg_spmv<3,float,float> (block-CSR SpMV + fused P.KP)"
@@ -303,6 +323,7 @@ def run_gsls(args):
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 tangent+inner CG / f64 residual,Newton,reductions",
         "data": ("synthetic: seeded Delaunay cylinder mesh, no external data" if is_fluid(p)
+                 else "synthetic: Kuhn-split slab mesh, no external data" if is_cep(p)
                  else "synthetic: seeded Kuhn-split beam mesh, no external data"),
         "config": {"workload": workload_desc(p), "precision": "mixed",
                    "l2": (f"inputs larger than L2 (FP32 Val {p.nnz * p.dof ** 2 * 4 / 1e6:.0f} MB, "
@@ -323,7 +344,7 @@ def run_gsls(args):
         "gpu_launches": int(mixed["launches"]),
         "clocks": clk,
     }
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and not is_cep(p):
         out["cpu_baseline"] = (cpu_baseline_fluid(p, fp64["newton"]) if is_fluid(p)
                                else cpu_baseline(p, fp64["newton"], fp64["cg"]))
     if rank == 0:
