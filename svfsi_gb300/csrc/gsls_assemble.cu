@@ -119,8 +119,20 @@ struct AsmArgs {
   int *err;
 };
 
+}  // namespace gsls
+
+#include "gsls_asm_struct.cuh"
+
+namespace gsls {
+
 // ---------------------------------------------------------------------------
-// HEATS3D (one tet per thread)
+// HEATS3D (Code/Source/svFSI/HEATS.f:116-159) and isotropic CEP3D, one tet per
+// thread.  tet4 gradients are constant, so the Gauss-point sums reduce to
+// the rule's tables: with W = sum_g w and M_ab = sum_g N_a N_b,
+//   lR(a)   = w rho (sum_b M_ab al_b - s Ns_a) + W nu Nx_a . grad T
+//   lK(a,b) = wl (amd M_ab + 4 nu Nx_a . Nx_b)
+// (the reference's per-point sums, reordered).  Geometry by the adjugate
+// with one division; residual FP64, tangent in VT.
 template <class VT>
 __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -128,68 +140,62 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
   const int e = A.el0 + t;
   const int4 nd = A.ien[e];
   const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
-  double xl[4][3], al[4], yl[4];
+  double xXi[3][3], x3[3], al[4], yl[4];
+#pragma unroll
+  for (int i = 0; i < 3; i++) x3[i] = __ldg(A.x + (size_t)n4[3] * 3 + i);
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) xXi[i][k] = __ldg(A.x + (size_t)n4[k] * 3 + i) - x3[i];
 #pragma unroll
   for (int a = 0; a < 4; a++) {
-#pragma unroll
-    for (int i = 0; i < 3; i++) xl[a][i] = A.x[(size_t)n4[a] * 3 + i];
-    al[a] = A.Ag[(size_t)n4[a] * A.tDof + A.s];
-    yl[a] = A.Yg[(size_t)n4[a] * A.tDof + A.s];
+    al[a] = __ldg(A.Ag + (size_t)n4[a] * A.tDof + A.s);
+    yl[a] = __ldg(A.Yg + (size_t)n4[a] * A.tDof + A.s);
   }
-  double Nx[3][4], Jac;
-  gnn_tet4(xl, Nx, Jac);
+  double adj[3][3];
+  const double Jac = adj_det3(xXi, adj);
   if (!(Jac != 0.0) || !isfinite(Jac)) atomicOr(A.err, 1);
+  const double iJ = 1.0 / Jac;
+  double Nx[3][4];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    Nx[i][0] = adj[0][i] * iJ;
+    Nx[i][1] = adj[1][i] * iJ;
+    Nx[i][2] = adj[2][i] * iJ;
+    Nx[i][3] = -(Nx[i][0] + Nx[i][1] + Nx[i][2]);
+  }
   const double nu = A.eparam ? A.eparam[e] : A.cond;
+  const double w = c_rule.w * Jac, W = 4.0 * w;
   const double T1 = A.af * A.gam * A.dt;
   const double amd = A.am * A.rho / T1;
-  using AT = VT;
-  double lR[4] = {0, 0, 0, 0};
-  AT lK[16];
+  double Tx[3];
 #pragma unroll
-  for (int k = 0; k < 16; k++) lK[k] = AT(0);
-  const AT NxNx_scale = AT(nu);
-#pragma unroll
-  for (int g = 0; g < 4; g++) {
-    const double w = c_rule.w * Jac;
-    const double wl = w * T1;
-    double Td = -A.src, Tx0 = 0, Tx1 = 0, Tx2 = 0;
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-      const double N = c_rule.N[g][a];
-      Td = Td + N * al[a];
-      Tx0 = Tx0 + Nx[0][a] * yl[a];
-      Tx1 = Tx1 + Nx[1][a] * yl[a];
-      Tx2 = Tx2 + Nx[2][a] * yl[a];
-    }
-    Td = Td * A.rho;
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-      const double Na = c_rule.N[g][a];
-      lR[a] = lR[a] + w * (Na * Td + (Nx[0][a] * Tx0 + Nx[1][a] * Tx1 + Nx[2][a] * Tx2) * nu);
-#pragma unroll
-      for (int b = 0; b < 4; b++) {
-        const AT Nb = AT(c_rule.N[g][b]);
-        const AT dd = AT(Nx[0][a]) * AT(Nx[0][b]) + AT(Nx[1][a]) * AT(Nx[1][b]) +
-                      AT(Nx[2][a]) * AT(Nx[2][b]);
-        lK[a * 4 + b] = lK[a * 4 + b] + AT(wl) * (AT(Na) * Nb * AT(amd) + NxNx_scale * dd);
-      }
-    }
-  }
+  for (int i = 0; i < 3; i++) Tx[i] = Nx[i][0] * yl[0] + Nx[i][1] * yl[1] + Nx[i][2] * yl[2] + Nx[i][3] * yl[3];
   VT *Val = reinterpret_cast<VT *>(A.Val);
+  const VT wl = VT(w * T1), kM = VT(amd), kS = VT(4.0 * nu);
+  VT Nxa[3][4];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int a = 0; a < 4; a++) Nxa[i][a] = VT(Nx[i][a]);
 #pragma unroll
   for (int a = 0; a < 4; a++) {
-    A.R[n4[a]] += lR[a];
-    const int4 m = A.map[(size_t)e * 4 + a];
-    Val[m.x] += VT(lK[a * 4 + 0]);
-    Val[m.y] += VT(lK[a * 4 + 1]);
-    Val[m.z] += VT(lK[a * 4 + 2]);
-    Val[m.w] += VT(lK[a * 4 + 3]);
+    double m = -A.src * c_rule.Ns[a];
+#pragma unroll
+    for (int b = 0; b < 4; b++) m += c_rule.M[a][b] * al[b];
+    A.R[n4[a]] += w * A.rho * m + W * nu * (Nx[0][a] * Tx[0] + Nx[1][a] * Tx[1] + Nx[2][a] * Tx[2]);
+    const int4 mp = A.map[(size_t)e * 4 + a];
+    const int pos[4] = {mp.x, mp.y, mp.z, mp.w};
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const VT dd = Nxa[0][a] * Nxa[0][b] + Nxa[1][a] * Nxa[1][b] + Nxa[2][a] * Nxa[2][b];
+      Val[pos[b]] += wl * (kM * VT(c_rule.M[a][b]) + kS * dd);
+    }
   }
 }
 
 }  // namespace gsls
 
-#include "gsls_asm_struct.cuh"
 #include "gsls_asm_fluid.cuh"
 
 namespace gsls {
