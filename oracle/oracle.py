@@ -205,10 +205,12 @@ class OracleSolver:
                                   dp(v) if v is not None else None)
         assert rc == 0
 
-    def solve(self, ls: Ls, dof, R, Val, prec, incL=None):
+    def solve(self, ls: Ls, dof, R, Val, prec, incL=None, res=None):
         il = None if incL is None else i32(incL)
+        rs = None if res is None else f64(res)
         rc = load().orc_solve(self.h, C.byref(ls), dof, dp(R), dp(Val), prec,
-                              ip(il) if il is not None else None, None)
+                              ip(il) if il is not None else None,
+                              dp(rs) if rs is not None else None)
         assert rc == 0, rc
 
     def spmv(self, dof, Val, U):

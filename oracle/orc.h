@@ -90,6 +90,13 @@ void orc_gmres_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val,
                  double *R);
 void orc_gmres_ns(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val,
                   const double *R, double *X);
+/* ADDBCMUL, L/ADDBCMUL.f:53-114 (serial faces): op 0 = BCOP_TYPE_ADD
+   (coef = res), 1 = BCOP_TYPE_PRE (coef = -res/(1 + res nS)); Y += coef
+   valM (valM . X) for every coupled face */
+void orc_addbcmul(orc_lhs *lhs, int op, int dof, const double *X, double *Y);
+/* BCPRE, L/NSSOLVER.f:307-343: nS = |valM(1:nsd,:)|^2 of each coupled face */
+void orc_bcpre(orc_lhs *lhs, int nsd);
+int orc_any_coupled(const orc_lhs *lhs);
 void orc_cgrad_schur(orc_lhs *lhs, orc_subls *ls, int dof, const double *D,
                      const double *G, const double *L, double *R);
 int orc_ge(int nV, int N, const double *A, double *B);

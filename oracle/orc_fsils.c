@@ -345,6 +345,45 @@ void orc_precond_rcs(orc_lhs *lhs, int dof, double *Val, double *R, double *W1,
   free(Wc);
 }
 
+/* ADDBCMUL, L/ADDBCMUL.f:53-114 (non-shared faces) */
+void orc_addbcmul(orc_lhs *lhs, int op, int dof, const double *X, double *Y) {
+  for (int f = 0; f < lhs->nFaces; f++) {
+    orc_face *fa = &lhs->face[f];
+    if (!fa->coupledFlag) continue;
+    const double coef = (op == 0) ? fa->res : -fa->res / (1.0 + fa->res * fa->nS);
+    const int nsd = fa->dof < dof ? fa->dof : dof;
+    double S = 0.0;
+    for (int a = 0; a < fa->nNo; a++) {
+      const int Ac = fa->glob[a];
+      for (int i = 0; i < nsd; i++) S = S + fa->valM[(size_t)a * fa->dof + i] * X[(size_t)Ac * dof + i];
+    }
+    S = coef * S;
+    for (int a = 0; a < fa->nNo; a++) {
+      const int Ac = fa->glob[a];
+      for (int i = 0; i < nsd; i++)
+        Y[(size_t)Ac * dof + i] = Y[(size_t)Ac * dof + i] + fa->valM[(size_t)a * fa->dof + i] * S;
+    }
+  }
+}
+
+/* BCPRE, L/NSSOLVER.f:307-343 and L/GMRES.f:395-431 (non-shared faces) */
+void orc_bcpre(orc_lhs *lhs, int nsd) {
+  for (int f = 0; f < lhs->nFaces; f++) {
+    orc_face *fa = &lhs->face[f];
+    if (!fa->coupledFlag) continue;
+    fa->nS = 0.0;
+    for (int a = 0; a < fa->nNo; a++)
+      for (int i = 0; i < nsd; i++)
+        fa->nS = fa->nS + pow(fa->valM[(size_t)a * fa->dof + i], 2.0);
+  }
+}
+
+int orc_any_coupled(const orc_lhs *lhs) {
+  for (int f = 0; f < lhs->nFaces; f++)
+    if (lhs->face[f].coupledFlag) return 1;
+  return 0;
+}
+
 /* CGRADS / CGRADV, L/CGRAD.f:125-242 */
 void orc_cgrad_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *K, double *R) {
   const int nNo = lhs->nNo, mynNo = lhs->mynNo;
@@ -412,6 +451,7 @@ void orc_gmres_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val, double
     ls->dB = ls->fNorm;
     ls->itr++;
     orc_spar_vv(lhs, dof, Val, X, u);
+    orc_addbcmul(lhs, 0, dof, X, u);
     for (size_t k = 0; k < n; k++) u[k] = R[k] - u[k];
     err[0] = orc_normv(dof, mynNo, u);
     for (size_t k = 0; k < n; k++) u[k] /= err[0];
@@ -420,6 +460,7 @@ void orc_gmres_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val, double
       ls->itr++;
       double *ui = u + n * (size_t)(i - 1), *ui1 = u + n * (size_t)i;
       orc_spar_vv(lhs, dof, Val, ui, ui1);
+      orc_addbcmul(lhs, 0, dof, ui, ui1);
       for (int j = 1; j <= i + 1; j++) H(j - 1, i - 1) = orc_dotv(dof, mynNo, u + n * (size_t)(j - 1), ui1);
       for (int j = 1; j <= i; j++) {
         const double hj = H(j - 1, i - 1);

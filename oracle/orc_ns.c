@@ -1,8 +1,8 @@
 /*
  * Oracle (test infrastructure only): restatement of the svFSILS NS block
  * solver (L/NSSOLVER.f:52-382, L/GE.f:51-151, L/CGRAD.f:51-123,
- * L/GMRES.f:51-169).  Serial branch: no MPI reductions, no coupled-Neumann
- * faces (ADDBCMUL is the identity when no face has coupledFlag set).
+ * L/GMRES.f:51-169), with the coupled-Neumann terms of ADDBCMUL where the
+ * reference applies them.  Serial branch: no MPI reductions.
  */
 #include "orc.h"
 
@@ -52,6 +52,7 @@ void orc_gmres_ns(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val, const
   double *c = (double *)xcalloc(sD + 1, sizeof(double));
   double *s = (double *)xcalloc(sD + 1, sizeof(double));
   double *err = (double *)xcalloc(sD + 2, sizeof(double));
+  double *unc = (double *)xcalloc(n, sizeof(double));
   ls->suc = 0;
   double eps = 0.0;
   memset(X, 0, n * sizeof(double));
@@ -61,7 +62,12 @@ void orc_gmres_ns(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val, const
     } else {
       ls->itr++;
       orc_spar_vv(lhs, dof, Val, X, u);
+      orc_addbcmul(lhs, 0, dof, X, u);
       for (size_t k = 0; k < n; k++) u[k] = R[k] - u[k];
+    }
+    if (orc_any_coupled(lhs)) {
+      memcpy(unc, u, n * sizeof(double));
+      orc_addbcmul(lhs, 1, dof, unc, u);
     }
     err[0] = orc_normv(dof, mynNo, u);
     if (l == 1) {
@@ -82,6 +88,11 @@ void orc_gmres_ns(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val, const
       ls->itr++;
       double *ui = u + n * (size_t)(i - 1), *ui1 = u + n * (size_t)i;
       orc_spar_vv(lhs, dof, Val, ui, ui1);
+      orc_addbcmul(lhs, 0, dof, ui, ui1);
+      if (orc_any_coupled(lhs)) {
+        memcpy(unc, ui1, n * sizeof(double));
+        orc_addbcmul(lhs, 1, dof, unc, ui1);
+      }
       for (int j = 1; j <= i + 1; j++)
         H(j - 1, i - 1) = ncdotv(dof, mynNo, u + n * (size_t)(j - 1), ui1);
       for (int j = 1; j <= i; j++) {
@@ -132,6 +143,7 @@ done:
   free(c);
   free(s);
   free(err);
+  free(unc);
 }
 
 /* CGRAD_SCHUR, L/CGRAD.f:51-123: CG on S = L - D G for the pressure block;
@@ -144,6 +156,7 @@ void orc_cgrad_schur(orc_lhs *lhs, orc_subls *ls, int dof, const double *D, cons
   double *SP = (double *)xcalloc(nNo, sizeof(double));
   double *DGP = (double *)xcalloc(nNo, sizeof(double));
   double *GP = (double *)xcalloc((size_t)dof * nNo, sizeof(double));
+  double *unc = (double *)xcalloc((size_t)dof * nNo, sizeof(double));
   ls->suc = 0;
   ls->iNorm = sqrt(ncdots(mynNo, R, R));
   double eps = fmax(ls->absTol, ls->relTol * ls->iNorm);
@@ -158,6 +171,10 @@ void orc_cgrad_schur(orc_lhs *lhs, orc_subls *ls, int dof, const double *D, cons
     }
     errO = err;
     orc_spar_sv(lhs, dof, G, P, GP);
+    if (orc_any_coupled(lhs)) {
+      memcpy(unc, GP, sizeof(double) * (size_t)dof * nNo);
+      orc_addbcmul(lhs, 1, dof, unc, GP);
+    }
     orc_spar_vs(lhs, dof, D, GP, DGP);
     orc_spar_ss(lhs, L, P, SP);
     for (int k = 0; k < nNo; k++) SP[k] = SP[k] + (-1.0) * DGP[k];
@@ -178,6 +195,7 @@ void orc_cgrad_schur(orc_lhs *lhs, orc_subls *ls, int dof, const double *D, cons
   free(SP);
   free(DGP);
   free(GP);
+  free(unc);
 }
 
 /* GE, L/GE.f:51-151: symmetric diagonal scaling, then Gaussian elimination
@@ -343,6 +361,7 @@ void orc_nssolver(orc_lhs *lhs, orc_ls *ls, int dof, const double *Val, double *
   eps = fmax(ls->RI.absTol, ls->RI.relTol * eps);
 
   depart3(lhs, Val, mK, mG, mD, mL, Gt);
+  orc_bcpre(lhs, nsd);
 
   int i, iB = 0, iBB = 0;
   for (i = 1; i <= ls->RI.mItr; i++) {
@@ -358,6 +377,7 @@ void orc_nssolver(orc_lhs *lhs, orc_ls *ls, int dof, const double *Val, double *
     for (size_t k = 0; k < nv; k++) MUI(iBB)[k] = Rm[k] - MUI(iB)[k];
     orc_gmres_ns(lhs, &ls->GM, nsd, mK, MUI(iBB), UI(i));
     orc_spar_vv(lhs, nsd, mK, UI(i), MUI(iBB));
+    orc_addbcmul(lhs, 0, nsd, UI(i), MUI(iBB));
     orc_spar_ss(lhs, mL, PI(i), MPI_(iB));
     orc_spar_vs(lhs, nsd, mD, UI(i), MPI_(iBB));
 

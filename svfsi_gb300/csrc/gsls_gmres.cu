@@ -48,6 +48,22 @@ __global__ void __launch_bounds__(kT) k_gm_residual(size_t n, const XT *__restri
     *outNorm = sqrt(tot);
 }
 
+// err = |u| (after the coupled-face PRE term)
+template <class XT>
+__global__ void __launch_bounds__(kT) k_gm_norm(size_t n, const XT *__restrict__ u,
+                                                double *partials, unsigned *ticket,
+                                                double *outNorm) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    acc += double(u[k]) * double(u[k]);
+  double bs = block_sum(acc, sh);
+  double tot;
+  if (grid_reduce_last<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0)
+    *outNorm = sqrt(tot);
+}
+
 template <class XT>
 __global__ void k_gm_scale(size_t n, XT *__restrict__ u, const double *normp) {
   const XT inv = XT(1.0 / *normp);
@@ -281,9 +297,16 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
       k_gm_spmv<D, VT, XT><<<G, kT, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
                                              lhs->d_colPtr.as<int>(), Val, X, u1, ctl);
       GSLS_CHECK_LAUNCH();
+      launch_addbcmul<XT>(lhs, 0, D, X, u1, &ctl->done);
     }
     k_gm_residual<XT><<<G, kT, 0, st>>>(nv, Rk, u1, l > 1 ? 1 : 0, part, tk, err);
     GSLS_CHECK_LAUNCH();
+    if (ns && ws.cpl_on) {
+      // u1 = PRE(u1), then its norm (GMRES.f:88-91)
+      launch_addbcmul<XT>(lhs, 1, D, u1, u1, &ctl->done);
+      k_gm_norm<XT><<<G, kT, 0, st>>>(nv, u1, part, tk, err);
+      GSLS_CHECK_LAUNCH();
+    }
     if (ns && l == 1) {
       double e0;
       GSLS_CUDA(cudaMemcpyAsync(&e0, err, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -321,6 +344,10 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
                                                lhs->d_colPtr.as<int>(), Val, ui, ui1, ctl);
         GSLS_CHECK_LAUNCH();
         if (prof) cudaEventRecord(prof_event(1), st);
+        if (ws.cpl_on) {
+          launch_addbcmul<XT>(lhs, 0, D, ui, ui1, &ctl->done);
+          if (ns) launch_addbcmul<XT>(lhs, 1, D, ui1, ui1, &ctl->done);
+        }
         k_gm_multidot<XT><<<Gd, kT, 0, st>>>(nv, basis, ld, i + 1, ui1, part, ctl);
         GSLS_CHECK_LAUNCH();
         k_gm_colsum<<<i + 1, kT, 0, st>>>(Gd, part, hcol, ctl);

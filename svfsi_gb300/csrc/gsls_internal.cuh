@@ -82,6 +82,19 @@ struct Face {
   double nS = 0.0, res = 0.0;
 };
 
+// Coupled-Neumann (resistance) faces of one solve, ADDBCMUL
+// (Code/Source/svFSILS/ADDBCMUL.f:53-114): face f holds entries
+// off[f]..off[f+1] of the concatenated node list and valM (fdof values per
+// node); cadd = res, cpre = -res/(1 + res nS).
+constexpr int kMaxCpl = 8;
+struct CplFaces {
+  int nf;
+  int off[kMaxCpl + 1];
+  int fdof[kMaxCpl];
+  int voff[kMaxCpl];  // offset of face f in valM
+  double cadd[kMaxCpl], cpre[kMaxCpl];
+};
+
 // Identity of a captured CG batch graph (kernel arguments baked in).
 struct GraphKey {
   int D, vsz, xsz;
@@ -121,6 +134,9 @@ struct Workspace {
   DevBuf ns_vec;      // NS solver vectors (Rm, Rc, U, P, MU, MP, Schur CG)
   DevBuf ns_mat;      // NS solver blocks (mK, mG, mD, mL, Gt)
   DevBuf rcs;         // RCS scaling state (W1, Wr, Wc, control words)
+  DevBuf cpl_glob, cpl_valM;  // coupled faces of the current solve
+  CplFaces cpl{};
+  bool cpl_on = false;
   KrylovScalars *h_scal = nullptr;  // pinned host mirror
   int mask_dof = -1;
   std::vector<int> mask_key;
@@ -249,6 +265,12 @@ int gmres_run(gsls_lhs *lhs, gsls_sub_ls *ls, int D, bool mixed, const void *Val
 // GMRES of the NS solver on device vectors (gsls_gmres.cu)
 template <int D, class VT, class XT>
 int gmres_ns(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *Rk, XT *X);
+// coupled faces: valM, nS from the diagonal scaling W (gsls_lhs.cu)
+int cpl_prepare(gsls_lhs *lhs, int dof, const double *dW, int prec);
+// Y += coef_f valM_f (valM_f . X) over the coupled faces; op 0 ADD, 1 PRE;
+// vectors with vdof values per node; skipped when *done is set
+template <class XT>
+void launch_addbcmul(gsls_lhs *lhs, int op, int vdof, const XT *X, XT *Y, const int *done);
 // RCS preconditioner and NS block solver (gsls_ns.cu)
 int precond_rcs_run(gsls_lhs *lhs, int D, bool mixed, void *Val, double *R, double *W);
 int ns_run(gsls_lhs *lhs, gsls_ls *ls, int D, bool mixed, const void *Val, double *R,

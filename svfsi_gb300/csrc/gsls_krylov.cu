@@ -762,6 +762,8 @@ static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, b
     set_error("This linear solver and preconditioner combination is not supported.");
     return GSLS_ERR_ARG;
   }
+  // coupled faces: ADDBCMUL enters GMRES and NS (CGRADS/V do not call it)
+  GSLS_TRY(cpl_prepare(lhs, D, W, prec));
   switch (ls->LS_type) {
     case GSLS_LS_TYPE_CG:
     {

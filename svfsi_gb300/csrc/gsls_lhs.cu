@@ -1,6 +1,7 @@
 // svFSILS-shaped object management: LHS (CSR + faces), BC faces, LS
 // defaults, device workspace, error state, stream.
 #include <atomic>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -151,13 +152,115 @@ int lhs_update_faces(gsls_lhs *lhs, const int *incL, const double *res) {
       fa.coupledFlag = true;
     }
   }
-  for (auto &fa : lhs->faces)
-    if (fa.coupledFlag) {
-      set_error("coupled Neumann (resistance) faces are not supported");
-      return GSLS_ERR_UNSUPPORTED;
-    }
   return GSLS_OK;
 }
+
+// valM = val W on the coupled faces (PRECONDDIAG, Code/Source/svFSILS/
+// PRECOND.f:133-143) and nS = |valM(1:dof-1,:)|^2 (BCPRE, NSSOLVER.f:307-343).
+// The reference sets valM in PRECONDDIAG only (its RCS counterpart is
+// commented out), so coupled faces require PRECOND_FSILS.
+int cpl_prepare(gsls_lhs *lhs, int dof, const double *dW, int prec) {
+  Workspace &ws = lhs->ws;
+  ws.cpl_on = false;
+  int nf = 0;
+  for (auto &fa : lhs->faces)
+    if (fa.foC && fa.coupledFlag) nf++;
+  if (nf == 0) return GSLS_OK;
+  if (prec != GSLS_PRECOND_FSILS) {
+    set_error("coupled Neumann faces need PRECOND_FSILS (valM is set by PRECONDDIAG)");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  if (nf > kMaxCpl) {
+    set_error("at most 8 coupled Neumann faces per solve");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  std::vector<double> W((size_t)lhs->nNo * dof);
+  GSLS_CUDA(cudaMemcpyAsync(W.data(), dW, sizeof(double) * W.size(), cudaMemcpyDeviceToHost,
+                            lhs->stream));
+  GSLS_CUDA(cudaStreamSynchronize(lhs->stream));
+  CplFaces &F = ws.cpl;
+  memset(&F, 0, sizeof(F));
+  std::vector<int> glob;
+  std::vector<double> valM;
+  for (auto &fa : lhs->faces) {
+    if (!(fa.foC && fa.coupledFlag)) continue;
+    const int f = F.nf++;
+    F.off[f] = (int)glob.size();
+    F.fdof[f] = fa.dof;
+    F.voff[f] = (int)valM.size();
+    const int m = fa.dof < dof ? fa.dof : dof;
+    double nS = 0.0;
+    for (int a = 0; a < fa.nNo; a++) {
+      const int Ac = fa.glob[a];
+      glob.push_back(Ac);
+      for (int i = 0; i < fa.dof; i++) {
+        const double v = (i < m) ? fa.val[(size_t)a * fa.dof + i] * W[(size_t)Ac * dof + i] : 0.0;
+        valM.push_back(v);
+        if (i < dof - 1) nS = nS + pow(v, 2.0);
+      }
+    }
+    fa.nS = nS;
+    F.cadd[f] = fa.res;
+    F.cpre[f] = -fa.res / (1.0 + fa.res * nS);
+  }
+  F.off[F.nf] = (int)glob.size();
+  GSLS_TRY(ws.cpl_glob.alloc(sizeof(int) * (glob.size() + 1)));
+  GSLS_TRY(ws.cpl_valM.alloc(sizeof(double) * (valM.size() + 1)));
+  GSLS_CUDA(cudaMemcpyAsync(ws.cpl_glob.p, glob.data(), sizeof(int) * glob.size(),
+                            cudaMemcpyHostToDevice, lhs->stream));
+  GSLS_CUDA(cudaMemcpyAsync(ws.cpl_valM.p, valM.data(), sizeof(double) * valM.size(),
+                            cudaMemcpyHostToDevice, lhs->stream));
+  ws.cpl_on = true;
+  return GSLS_OK;
+}
+
+// One block: all face products first (from X), then the updates face by
+// face, so that Y may alias X (the PRE form) as in the reference.
+template <class XT>
+__global__ void __launch_bounds__(1024) k_addbcmul(CplFaces F, const int *__restrict__ glob,
+                                                   const double *__restrict__ valM, int op,
+                                                   int vdof, const XT *X, XT *Y, const int *done) {
+  if (done && *(volatile const int *)done) return;
+  __shared__ double sh[32];
+  __shared__ double sS[kMaxCpl];
+  for (int f = 0; f < F.nf; f++) {
+    const int fd = F.fdof[f], m = fd < vdof ? fd : vdof;
+    double s = 0.0;
+    for (int a = F.off[f] + threadIdx.x; a < F.off[f + 1]; a += blockDim.x) {
+      const int Ac = glob[a];
+      const double *v = valM + F.voff[f] + (size_t)(a - F.off[f]) * fd;
+      for (int i = 0; i < m; i++) s += v[i] * double(X[(size_t)Ac * vdof + i]);
+    }
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) sS[f] = (op == 0 ? F.cadd[f] : F.cpre[f]) * s;
+    __syncthreads();
+  }
+  for (int f = 0; f < F.nf; f++) {
+    const int fd = F.fdof[f], m = fd < vdof ? fd : vdof;
+    const double S = sS[f];
+    for (int a = F.off[f] + threadIdx.x; a < F.off[f + 1]; a += blockDim.x) {
+      const int Ac = glob[a];
+      const double *v = valM + F.voff[f] + (size_t)(a - F.off[f]) * fd;
+      for (int i = 0; i < m; i++) {
+        XT *y = Y + (size_t)Ac * vdof + i;
+        *y = XT(double(*y) + v[i] * S);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <class XT>
+void launch_addbcmul(gsls_lhs *lhs, int op, int vdof, const XT *X, XT *Y, const int *done) {
+  Workspace &ws = lhs->ws;
+  if (!ws.cpl_on) return;
+  k_addbcmul<XT><<<1, 1024, 0, lhs->stream>>>(ws.cpl, ws.cpl_glob.as<int>(),
+                                              ws.cpl_valM.as<double>(), op, vdof, X, Y, done);
+  count_launch();
+}
+template void launch_addbcmul<float>(gsls_lhs *, int, int, const float *, float *, const int *);
+template void launch_addbcmul<double>(gsls_lhs *, int, int, const double *, double *,
+                                      const int *);
 
 // Dirichlet mask = product over included Dir faces of val(1:min(dof,fdof)),
 // the factor PRECONDDIAG applies to W (Code/Source/svFSILS/PRECOND.f:107-117).

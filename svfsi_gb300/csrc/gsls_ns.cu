@@ -1012,7 +1012,9 @@ static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, 
     const char *e = getenv("GSLS_SCHUR");
     return e && strcmp(e, "kernels") == 0;
   }();
-  bool use_kernels = kernels;
+  // the coupled-face PRE term needs a global dot between the two Schur
+  // products: the per-kernel path carries it
+  bool use_kernels = kernels || lhs->ws.cpl_on;
   if (!use_kernels) {
     // persistent cooperative kernel: one block per SM
     const int nblk = num_sms();
@@ -1052,6 +1054,7 @@ static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, 
     for (int b = 0; b < batch; b++) {
       k_ns_sv<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mG, Ps, GP, nullptr, nullptr, &sc->done);
       GSLS_CHECK_LAUNCH();
+      launch_addbcmul<XT>(lhs, 1, 3, GP, GP, &sc->done);
       k_schur_sp<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mL, Gt, Ps, GP, SP, part, tk, sc);
       GSLS_CHECK_LAUNCH();
       k_schur_update<XT><<<G, kNT, 0, st>>>(nNo, P, Ps, Rs, SP, part, tk, sc);
@@ -1156,6 +1159,7 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
     part = ws.partials.as<double>();
     k_spmv<3, VT, XT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mK, Ui, MUiBB);
     GSLS_CHECK_LAUNCH();
+    launch_addbcmul<XT>(lhs, 0, 3, Ui, MUiBB, nullptr);
     k_ns_ss_vs<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mL, Pi, mD, Ui, MPiB, MPiBB);
     GSLS_CHECK_LAUNCH();
     // least-squares dots for columns iB and iBB (NSSOLVER.f:131-143)

@@ -11,7 +11,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from svfsi_gb300 import _lib, fsils, problems
+from svfsi_gb300 import _lib, fsils, meshgen, problems
 
 pytestmark = pytest.mark.gpu
 
@@ -170,3 +170,34 @@ def test_fluid_mixed_tracks_fp64(gsls, orc):
     _, Y, _ = eq.get_state()
     _, Yo, _ = oeq.state()
     assert rel(Y, Yo) < 1e-8
+
+
+def test_ns_solve_coupled_outlet_matches_oracle(gsls, orc):
+    """NS solver with a coupled (resistance) outlet face: ADDBCMUL in the
+    K-block GMRES (ADD and PRE), in NSSOLVER's MU product and the PRE term of
+    the Schur CG (diagonal preconditioner: the reference sets valM there)."""
+    p = _cyl()
+    A, Y = _state(p, seed=5)
+    R0, V0 = orc.assemble(p, A, Y)
+    faces = _fluid_faces(p)
+    outlet = meshgen.nodes_on_plane(p.x, 2, 5.0)
+    outlet = outlet[~np.isin(outlet, p.dirichlet[1].nodes)].astype(np.int32)
+    val = np.tile(np.array([0.0, 0.0, 1.0]), (outlet.size, 1)) * 0.01
+    res = np.array([0.0, 0.0, 2.0])
+    lhs = _lhs(p, 3)
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 3)
+    for k, nodes in enumerate(faces):
+        fsils.FSILS_BC_CREATE(lhs, k + 1, nodes.size, 3, fsils.BC_TYPE_DIR, nodes + 1,
+                              np.zeros((nodes.size, 3)))
+        s.bc_create(k + 1, nodes, 3, 0, np.zeros((nodes.size, 3)))
+    fsils.FSILS_BC_CREATE(lhs, 3, outlet.size, 3, fsils.BC_TYPE_NEU, outlet + 1, val)
+    s.bc_create(3, outlet, 3, 1, val)
+    ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_NS, dimKry=100)
+    ols = orc.ls_create(orc.LS_TYPE_NS, sD=100)
+    R, Val = R0.copy(), V0.copy()
+    fsils.FSILS_SOLVE(lhs, ls, 4, R, Val, fsils.PRECOND_FSILS, res=res)
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, 4, Ro, Vo, orc.PRECOND_FSILS, res=res)
+    assert ls.RI.suc == ols.RI.suc
+    assert ls.RI.itr == ols.RI.itr
+    assert rel(R, Ro) < 1e-8

@@ -279,3 +279,36 @@ def test_cep_steps(gsls, orc, precision, ode, A):
     assert rel(X[:, 1], oeq.Xion[:, 1]) < (1e-9 if precision == "fp64" else 1e-5)
     if A > 0:
         assert Y.max() > -60.0  # the stimulated corner depolarised well above rest (-80 mV)
+
+
+def test_gmres_coupled_neumann_face_matches_oracle(gsls, orc):
+    """GMRES with a coupled Neumann (resistance) face: ADDBCMUL's rank-one
+    term after every SpMV, as in GMRESV."""
+    p = problems.struct_beam(8, 3, 3)
+    _, _, _, R0, V0 = _assembled_system(p, seed=4)
+    dirn = p.dirichlet[0].nodes
+    from svfsi_gb300 import meshgen
+    face = meshgen.nodes_on_plane(p.x, 0, 4.0).astype(np.int32)
+    rng = np.random.default_rng(6)
+    val = rng.random((face.size, 3)) + 0.5
+    res = np.array([0.0, 50.0])
+    lhs = _lhs_for(p, nFaces=2)
+    fsils.FSILS_BC_CREATE(lhs, 1, dirn.size, 3, fsils.BC_TYPE_DIR, dirn + 1, np.zeros((dirn.size, 3)))
+    fsils.FSILS_BC_CREATE(lhs, 2, face.size, 3, fsils.BC_TYPE_NEU, face + 1, val)
+    ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_GMRES, relTol=1e-5, maxItr=10, dimKry=40)
+    R, Val = R0.copy(), V0.copy()
+    fsils.FSILS_SOLVE(lhs, ls, 3, R, Val, fsils.PRECOND_FSILS, res=res)
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 2)
+    s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
+    s.bc_create(2, face, 3, 1, val)
+    ols = orc.ls_create(orc.LS_TYPE_GMRES, relTol=1e-5, mItr=10, sD=40)
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, 3, Ro, Vo, orc.PRECOND_FSILS, res=res)
+    assert ls.RI.suc == ols.RI.suc == 1
+    assert abs(ls.RI.itr - ols.RI.itr) <= 1
+    assert rel(R, Ro) < 1e-6
+    # without the coupling the answer differs
+    R2, V2 = R0.copy(), V0.copy()
+    ls2 = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_GMRES, relTol=1e-5, maxItr=10, dimKry=40)
+    fsils.FSILS_SOLVE(lhs, ls2, 3, R2, V2, fsils.PRECOND_FSILS, res=np.array([0.0, 0.0]))
+    assert rel(R2, Ro) > 1e-4

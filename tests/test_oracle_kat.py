@@ -410,3 +410,43 @@ def test_ns_solver_with_tight_tolerances_solves_the_system(orc):
     # CGRAD_SCHUR takes S = L - Gt G (K^-1 ~ I after scaling), so the outer
     # least-squares loop converges linearly; relTol 1e-6 at cond ~1e8
     assert np.abs(Rs.ravel() - x).max() < 1e-4 * np.abs(x).max()
+
+
+def test_coupled_neumann_face_adds_rank_one_term(orc):
+    """GMRES with a coupled Neumann face (ADDBCMUL) solves (K + res v v^T) x = b
+    on the free rows, v the face's val vector (checked by a dense solve)."""
+    p = problems.heats_cube(4)
+    rng = np.random.default_rng(9)
+    A = rng.standard_normal((p.nNo, 1))
+    Y = rng.standard_normal((p.nNo, 1))
+    R, Val = orc.assemble(p, A, Y)
+    n = p.nNo
+    K = np.zeros((n, n))
+    for i in range(n):
+        K[i, p.colPtr[p.rowPtr[i]:p.rowPtr[i + 1]]] = Val[p.rowPtr[i]:p.rowPtr[i + 1], 0]
+    dirn = p.dirichlet[0].nodes
+    face = meshgen.nodes_on_plane(p.x, 1, 1.0)
+    face = face[~np.isin(face, dirn)].astype(np.int32)
+    v = 0.5 + rng.random(face.size)
+    res = 3.0
+    s = orc.OracleSolver(n, p.rowPtr, p.colPtr, 2)
+    s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
+    s.bc_create(2, face, 1, 1, v.reshape(-1, 1))
+    ls = orc.ls_create(orc.LS_TYPE_GMRES, relTol=1e-12, mItr=10, sD=120)
+    Rs, Vs = R.copy(), Val.copy()
+    s.solve(ls, 1, Rs, Vs, orc.PRECOND_FSILS, res=np.array([0.0, res]))
+    free = np.ones(n, bool)
+    free[dirn] = False
+    vv = np.zeros(n)
+    vv[face] = v
+    Kc = K + res * np.outer(vv, vv)
+    x = np.zeros(n)
+    x[free] = np.linalg.solve(Kc[np.ix_(free, free)], R[free, 0])
+    assert ls.RI.suc == 1
+    # GMRES stops on its Givens estimate, which classical Gram-Schmidt lets
+    # drift from the true residual at tight tolerances (cond here ~5e4)
+    assert np.abs(Rs[:, 0] - x).max() < 1e-4 * np.abs(x).max()
+    # the coupled term matters: without it the solution is far away
+    x0 = np.zeros(n)
+    x0[free] = np.linalg.solve(K[np.ix_(free, free)], R[free, 0])
+    assert np.abs(x0 - x).max() > 1e-2 * np.abs(x).max()
