@@ -17,7 +17,7 @@ LIB = HERE / "build" / "liboracle.so"
 c_int_p = C.POINTER(C.c_int)
 c_double_p = C.POINTER(C.c_double)
 
-LS_TYPE_CG, LS_TYPE_GMRES, LS_TYPE_NS = 798, 797, 796
+LS_TYPE_CG, LS_TYPE_GMRES, LS_TYPE_NS, LS_TYPE_BICGS = 798, 797, 796, 795
 PRECOND_FSILS, PRECOND_RCS = 701, 709
 
 

@@ -86,6 +86,7 @@ void orc_precond_diag(orc_lhs *lhs, int dof, double *Val, double *R, double *W);
 void orc_precond_rcs(orc_lhs *lhs, int dof, double *Val, double *R, double *W1,
                      double *W2);
 void orc_cgrad_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *K, double *R);
+void orc_bicgs_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *K, double *R);
 void orc_gmres_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val,
                  double *R);
 void orc_gmres_ns(orc_lhs *lhs, orc_subls *ls, int dof, const double *Val,

@@ -384,6 +384,58 @@ int orc_any_coupled(const orc_lhs *lhs) {
   return 0;
 }
 
+/* BICGSS / BICGSV, L/BICGS.f:51-230 */
+void orc_bicgs_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *K, double *R) {
+  const int nNo = lhs->nNo, mynNo = lhs->mynNo;
+  const size_t n = (size_t)nNo * dof;
+  double *P = (double *)xcalloc(n, sizeof(double));
+  double *Rh = (double *)xcalloc(n, sizeof(double));
+  double *X = (double *)xcalloc(n, sizeof(double));
+  double *V = (double *)xcalloc(n, sizeof(double));
+  double *S = (double *)xcalloc(n, sizeof(double));
+  double *T = (double *)xcalloc(n, sizeof(double));
+  ls->suc = 0;
+  double err = orc_normv(dof, mynNo, R);
+  ls->iNorm = err;
+  double errO = err;
+  const double eps = fmax(ls->absTol, ls->relTol * err);
+  double rho = err * err, rhoO, beta = rho, alpha, omega;
+  (void)beta;
+  memcpy(P, R, n * sizeof(double));
+  memcpy(Rh, R, n * sizeof(double));
+  int i;
+  for (i = 1; i <= ls->mItr; i++) {
+    if (err < eps) {
+      ls->suc = 1;
+      break;
+    }
+    orc_spar_vv(lhs, dof, K, P, V);
+    alpha = rho / orc_dotv(dof, mynNo, Rh, V);
+    for (size_t k = 0; k < n; k++) S[k] = R[k] - alpha * V[k];
+    orc_spar_vv(lhs, dof, K, S, T);
+    omega = orc_normv(dof, mynNo, T);
+    omega = orc_dotv(dof, mynNo, T, S) / (omega * omega);
+    for (size_t k = 0; k < n; k++) X[k] = X[k] + alpha * P[k] + omega * S[k];
+    for (size_t k = 0; k < n; k++) R[k] = S[k] - omega * T[k];
+    errO = err;
+    err = orc_normv(dof, mynNo, R);
+    rhoO = rho;
+    rho = orc_dotv(dof, mynNo, R, Rh);
+    beta = rho * alpha / (rhoO * omega);
+    for (size_t k = 0; k < n; k++) P[k] = R[k] + beta * (P[k] - omega * V[k]);
+  }
+  memcpy(R, X, n * sizeof(double));
+  ls->itr = i - 1;
+  ls->fNorm = err;
+  ls->dB = (errO < 2.220446049250313e-16) ? 0.0 : 10.0 * log(err / errO);
+  free(P);
+  free(Rh);
+  free(X);
+  free(V);
+  free(S);
+  free(T);
+}
+
 /* CGRADS / CGRADV, L/CGRAD.f:125-242 */
 void orc_cgrad_v(orc_lhs *lhs, orc_subls *ls, int dof, const double *K, double *R) {
   const int nNo = lhs->nNo, mynNo = lhs->mynNo;
@@ -556,6 +608,9 @@ int orc_solve(orc_lhs *lhs, orc_ls *ls, int dof, double *Ri, double *Val,
     break;
   case ORC_LS_TYPE_CG:
     orc_cgrad_v(lhs, &ls->RI, dof, Val, R);
+    break;
+  case ORC_LS_TYPE_BICGS:
+    orc_bicgs_v(lhs, &ls->RI, dof, Val, R);
     break;
   default:
     rc = -4;

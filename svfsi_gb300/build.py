@@ -32,6 +32,7 @@ SOURCES = [
     "gsls_gmres.cu",
     "gsls_noalloc.cu",
     "gsls_ns.cu",
+    "gsls_bicgs.cu",
 ]
 
 

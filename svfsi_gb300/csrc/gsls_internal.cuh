@@ -271,6 +271,9 @@ int cpl_prepare(gsls_lhs *lhs, int dof, const double *dW, int prec);
 // vectors with vdof values per node; skipped when *done is set
 template <class XT>
 void launch_addbcmul(gsls_lhs *lhs, int op, int vdof, const XT *X, XT *Y, const int *done);
+// BiCGStab on the preconditioned system (gsls_bicgs.cu)
+int bicgs_run(gsls_lhs *lhs, gsls_sub_ls *ls, int D, bool mixed, const void *Val, double *R,
+              const double *W);
 // RCS preconditioner and NS block solver (gsls_ns.cu)
 int precond_rcs_run(gsls_lhs *lhs, int D, bool mixed, void *Val, double *R, double *W);
 int ns_run(gsls_lhs *lhs, gsls_ls *ls, int D, bool mixed, const void *Val, double *R,

@@ -778,6 +778,8 @@ static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, b
       return gmres_run(lhs, &ls->RI, D, sizeof(VT) == 4, Val, dRi, W);
     case GSLS_LS_TYPE_NS:
       return ns_run(lhs, ls, D, sizeof(VT) == 4, Val, dRi, W);
+    case GSLS_LS_TYPE_BICGS:
+      return bicgs_run(lhs, &ls->RI, D, sizeof(VT) == 4, Val, dRi, W);
     default:
       set_error("LS_type not defined");
       return GSLS_ERR_ARG;

@@ -312,3 +312,38 @@ def test_gmres_coupled_neumann_face_matches_oracle(gsls, orc):
     ls2 = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_GMRES, relTol=1e-5, maxItr=10, dimKry=40)
     fsils.FSILS_SOLVE(lhs, ls2, 3, R2, V2, fsils.PRECOND_FSILS, res=np.array([0.0, 0.0]))
     assert rel(R2, Ro) > 1e-4
+
+
+@pytest.mark.parametrize("case", ["heats", "struct"])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_bicgstab_matches_oracle(gsls, orc, case, mixed):
+    """LS_TYPE_BICGS (BICGSS/BICGSV) through FSILS_SOLVE against the oracle;
+    mixed precision runs FP32 vectors and values on the device."""
+    torch = pytest.importorskip("torch")
+    p = problems.heats_cube(6) if case == "heats" else problems.struct_beam(8, 3, 3)
+    _, _, _, R0, V0 = _assembled_system(p, seed=8)
+    d = p.dof
+    dirn = p.dirichlet[0].nodes
+    lhs = _lhs_for(p, nFaces=1)
+    fsils.FSILS_BC_CREATE(lhs, 1, dirn.size, 3, fsils.BC_TYPE_DIR, dirn + 1, np.zeros((dirn.size, 3)))
+    ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_BICGS, relTol=1e-8, maxItr=2000)
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
+    s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
+    ols = orc.ls_create(orc.LS_TYPE_BICGS, relTol=1e-8, mItr=2000)
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, d, Ro, Vo, orc.PRECOND_FSILS)
+    if not mixed:
+        R, Val = R0.copy(), V0.copy()
+        fsils.FSILS_SOLVE(lhs, ls, d, R, Val, fsils.PRECOND_FSILS)
+        assert ls.RI.suc == ols.RI.suc == 1
+        assert abs(ls.RI.itr - ols.RI.itr) <= 1
+        assert rel(R, Ro) < 1e-6
+    else:
+        dR = torch.tensor(R0, device="cuda")
+        dV = torch.tensor(V0, device="cuda").to(torch.float32)
+        _lib.check(gsls.gsls_solve_dev(lhs.h, C.byref(ls), d, C.c_void_p(dR.data_ptr()),
+                                       C.c_void_p(dV.data_ptr()), fsils.PREC_MIXED,
+                                       fsils.PRECOND_FSILS, None, None))
+        torch.cuda.synchronize()
+        assert ls.RI.suc == 1
+        assert rel(dR.cpu().numpy(), Ro) < 1e-3

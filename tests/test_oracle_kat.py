@@ -174,6 +174,35 @@ def test_krylov_1d_laplacian_exact(orc, lstype):
         assert ls.RI.itr <= n
 
 
+def test_bicgstab_solves_the_system(orc):
+    """BICGSV on an assembled beam tangent against a dense solve."""
+    p = problems.struct_beam(4, 2, 2)
+    rng = np.random.default_rng(12)
+    A = 1e-3 * rng.standard_normal((p.nNo, 3))
+    Y = 1e-3 * rng.standard_normal((p.nNo, 3))
+    D = 1e-2 * rng.standard_normal((p.nNo, 3))
+    R, Val = orc.assemble(p, A, Y, D)
+    n = p.nNo
+    K = np.zeros((3 * n, 3 * n))
+    for i in range(n):
+        for j in range(p.rowPtr[i], p.rowPtr[i + 1]):
+            c = p.colPtr[j]
+            K[3 * i:3 * i + 3, 3 * c:3 * c + 3] = Val[j].reshape(3, 3)
+    dirn = p.dirichlet[0].nodes
+    free = np.ones(3 * n, bool)
+    for a in dirn:
+        free[3 * a:3 * a + 3] = False
+    x = np.zeros(3 * n)
+    x[free] = np.linalg.solve(K[np.ix_(free, free)], R.ravel()[free])
+    s = orc.OracleSolver(n, p.rowPtr, p.colPtr, 1)
+    s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
+    ls = orc.ls_create(orc.LS_TYPE_BICGS, relTol=1e-12, mItr=2000)
+    Rs, Vs = R.copy(), Val.copy()
+    s.solve(ls, 3, Rs, Vs, orc.PRECOND_FSILS)
+    assert ls.RI.suc == 1
+    assert np.abs(Rs.ravel() - x).max() < 1e-8 * np.abs(x).max()
+
+
 @pytest.mark.parametrize("roInf", [0.0, 0.2, 0.5, 1.0])
 def test_genalpha_closed_form(orc, roInf):
     out = [C.c_double() for _ in range(4)]
