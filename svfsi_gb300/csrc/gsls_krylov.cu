@@ -85,6 +85,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
                                                       const VT *__restrict__ Val, CgVecs v,
                                                       KrylovScalars *S, double *partials,
                                                       unsigned *ticket) {
+  cudaGridDependencySynchronize();  // launched with programmatic serialization
   if (*(volatile int *)&S->done) return;
   using AT = typename AccOf<VT>::T;
   constexpr int VD = VStride<D, XT>::v;
@@ -338,6 +339,7 @@ constexpr int kUpdThreads = 512;
 template <class XT, bool FUSED>
 __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_update(size_t n, CgVecs v, KrylovScalars *S,
                                                            double *partials, unsigned *ticket) {
+  cudaGridDependencySynchronize();
   if (*(volatile int *)&S->done) return;
   using AT = XT;
   __shared__ double sh[32];
@@ -407,6 +409,7 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_update(size_t n, CgVecs v
 template <class XT>
 __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_pupdate(size_t n, CgVecs v,
                                                             const KrylovScalars *S) {
+  cudaGridDependencySynchronize();
   if (*(volatile const int *)&S->done) return;
   const XT beta = XT(S->beta);
   XT *__restrict__ P = (XT *)v.P0;
@@ -619,6 +622,16 @@ static bool tma_setup(gsls_lhs *lhs, TmaTiles &tt, int &smem, int &grid) {
   return ok;
 }
 
+// Programmatic dependent launch of the CG batch (default on; GSLS_PDL=0
+// serialises the launches plainly).
+static bool use_pdl() {
+  static const bool on = [] {
+    const char *e = getenv("GSLS_PDL");
+    return !(e && strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
 template <int D, class VT, class XT, bool FUSED>
 static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter, bool prof,
                       int ev_base, const TmaTiles *tt = nullptr, int tma_smem = 0,
@@ -637,18 +650,35 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
   unsigned *tk = ws.ticket.as<unsigned>();
   for (int b = 0; b < n_iter; b++) {
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b), st);
-    if (tt)
+    // programmatic dependent launch: each kernel's blocks may be scheduled
+    // while its predecessor drains; they wait (cudaGridDependencySynchronize)
+    // for its completion before reading anything it wrote
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = (prof || !use_pdl()) ? 0 : 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.stream = st;
+    cfg.attrs = pdl;
+    cfg.numAttrs = 1;
+    if (tt) {
       k_cg_spmv_tma<D, VT, XT, kTmaWarps, FUSED><<<tma_grid, kTmaWarps * 32, tma_smem, st>>>(
           nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, v, S, part, tk, *tt);
-    else
-      k_cg_spmv<D, VT, XT, FUSED><<<G1, kThreads, 0, st>>>(
-          nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, v, S, part, tk);
+    } else {
+      cfg.gridDim = dim3(G1);
+      cfg.blockDim = dim3(kThreads);
+      GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_spmv<D, VT, XT, FUSED>, nNo,
+                                   (const int *)lhs->d_rowPtr.as<int>(),
+                                   (const int *)lhs->d_colPtr.as<int>(), Val, v, S, part, tk));
+    }
     GSLS_CHECK_LAUNCH();
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b + 1), st);
-    k_cg_update<XT, FUSED><<<G2, kUpdThreads, 0, st>>>(nv, v, S, part, tk);
+    cfg.gridDim = dim3(G2);
+    cfg.blockDim = dim3(kUpdThreads);
+    GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_update<XT, FUSED>, nv, v, S, part, tk));
     GSLS_CHECK_LAUNCH();
     if (!FUSED) {
-      k_cg_pupdate<XT><<<G3, kUpdThreads, 0, st>>>(nv, v, S);
+      cfg.gridDim = dim3(G3);
+      GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_pupdate<XT>, nv, v, (const KrylovScalars *)S));
       GSLS_CHECK_LAUNCH();
     }
   }
