@@ -302,10 +302,11 @@ __global__ void __launch_bounds__(kNT) k_ns_split(int nNo, const double *__restr
   }
 }
 
-// DEPART (NSSOLVER.f:237-305) for nsd = 3
+// DEPART (NSSOLVER.f:237-305) for nsd = 3.  Also writes the Schur operands
+// packed four to a block for the persistent CG: A1 = (mG, 0), A2 = (Gt, mL).
 template <class VT>
 __global__ void k_depart(int nnz, const VT *__restrict__ Val, const int *__restrict__ tpos, VT *mK,
-                         VT *mG, VT *mD, VT *mL, VT *Gt) {
+                         VT *mG, VT *mD, VT *mL, VT *Gt, VT *A1, VT *A2) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nnz; j += gridDim.x * blockDim.x) {
     const VT *t = Val + (size_t)j * 16;
     VT *k = mK + (size_t)j * 9;
@@ -320,10 +321,46 @@ __global__ void k_depart(int nnz, const VT *__restrict__ Val, const int *__restr
       mG[(size_t)j * 3 + m] = g;
       mD[(size_t)j * 3 + m] = t[12 + m];
       Gt[(size_t)l * 3 + m] = -g;
+      A1[(size_t)j * 4 + m] = g;
+      A2[(size_t)l * 4 + m] = -g;
     }
+    A1[(size_t)j * 4 + 3] = VT(0);
     mL[j] = t[15];
+    A2[(size_t)j * 4 + 3] = t[15];
   }
 }
+
+// 16-byte (FP32) / 2 x 16-byte (FP64) vector access to 4 packed values
+template <class T> struct V4;
+template <> struct V4<float> {
+  static __device__ __forceinline__ void ldg(const float *p, float o[4]) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+  static __device__ __forceinline__ void ldcg(const float *p, float o[4]) {
+    const float4 v = __ldcg(reinterpret_cast<const float4 *>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+  static __device__ __forceinline__ void stcg(float *p, float a, float b, float c, float d) {
+    __stcg(reinterpret_cast<float4 *>(p), make_float4(a, b, c, d));
+  }
+};
+template <> struct V4<double> {
+  static __device__ __forceinline__ void ldg(const double *p, double o[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+  }
+  static __device__ __forceinline__ void ldcg(const double *p, double o[4]) {
+    const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldcg(reinterpret_cast<const double2 *>(p) + 1);
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+  }
+  static __device__ __forceinline__ void stcg(double *p, double a, double b, double c, double d) {
+    __stcg(reinterpret_cast<double2 *>(p), make_double2(a, b));
+    __stcg(reinterpret_cast<double2 *>(p) + 1, make_double2(c, d));
+  }
+};
 
 // 4 lanes per block row, 8 rows per warp; lane q takes blocks rs+q, rs+q+4, ...
 constexpr int kRL = 4;
@@ -759,8 +796,8 @@ template <class VT, class XT>
 struct SchurArgs {
   int nNo;
   const int *rowPtr, *colPtr;
-  const VT *mG, *Gt, *mL;
-  XT *X, *Pa, *Pb, *R, *SP, *GP;  // Pa holds the initial direction
+  const VT *A1, *A2;              // (mG, 0) and (Gt, mL) per CSR block
+  XT *X, *Pa, *Pb, *R, *SP, *GP;  // Pa holds the initial direction; GP 4 per node
   double *part;                   // 2 * gridDim.x
   GridBar *bar;
   SchurScal *sc;
@@ -850,8 +887,10 @@ __global__ void __launch_bounds__(kPT, 1) k_schur_persistent(SchurArgs<VT, XT> A
             const int col = scol[jl];
             const size_t j = (size_t)(jl + dl);
             pv[u] = AT(c2 * (__ldcg(Pold + col) + c1 * __ldcg(A.R + col)));
+            VT a4[4];
+            V4<VT>::ldg(A.A1 + j * 4, a4);
 #pragma unroll
-            for (int m = 0; m < 3; m++) gv[u][m] = AT(__ldg(A.mG + j * 3 + m));
+            for (int m = 0; m < 3; m++) gv[u][m] = AT(a4[m]);
           } else {
             pv[u] = AT(0);
 #pragma unroll
@@ -869,9 +908,7 @@ __global__ void __launch_bounds__(kPT, 1) k_schur_persistent(SchurArgs<VT, XT> A
       a1 = quad_sum(a1);
       a2 = quad_sum(a2);
       if (q == 0 && i < nNo) {
-        __stcg(A.GP + (size_t)i * 3 + 0, XT(a0));
-        __stcg(A.GP + (size_t)i * 3 + 1, XT(a1));
-        __stcg(A.GP + (size_t)i * 3 + 2, XT(a2));
+        V4<XT>::stcg(A.GP + (size_t)i * 4, XT(a0), XT(a1), XT(a2), XT(0));
         __stcg(Pnew + i, XT(c2 * (__ldcg(Pold + i) + c1 * __ldcg(A.R + i))));
       }
     }
@@ -892,12 +929,16 @@ __global__ void __launch_bounds__(kPT, 1) k_schur_persistent(SchurArgs<VT, XT> A
           if (jl < rr.y) {
             const int col = scol[jl];
             const size_t j = (size_t)(jl + dl);
-            lv[u] = AT(__ldg(A.mL + j));
+            VT a4[4];
+            V4<VT>::ldg(A.A2 + j * 4, a4);
+            XT g4[4];
+            V4<XT>::ldcg(A.GP + (size_t)col * 4, g4);
+            lv[u] = AT(a4[3]);
             pv[u] = AT(__ldcg(Pnew + col));
 #pragma unroll
             for (int m = 0; m < 3; m++) {
-              gt[u][m] = AT(__ldg(A.Gt + j * 3 + m));
-              gp[u][m] = AT(__ldcg(A.GP + (size_t)col * 3 + m));
+              gt[u][m] = AT(a4[m]);
+              gp[u][m] = AT(g4[m]);
             }
           } else {
             lv[u] = pv[u] = AT(0);
@@ -997,8 +1038,8 @@ static size_t schur_geometry(const gsls_lhs *lhs, int nblk, int *K_out) {
 // CGRAD_SCHUR on P (in: right-hand side, out: solution)
 template <class VT, class XT>
 static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, const VT *mL,
-                    XT *P, XT *Rs, XT *Ps, XT *Pb, XT *SP, XT *GP, SchurScal *sc,
-                    SchurScal *h_sc, GridBar *db) {
+                    const VT *A1, const VT *A2, XT *P, XT *Rs, XT *Ps, XT *Pb, XT *SP, XT *GP,
+                    XT *GP4, SchurScal *sc, SchurScal *h_sc, GridBar *db) {
   cudaStream_t st = lhs->stream;
   const int nNo = lhs->nNo, G = lhs->grid;
   double *part = lhs->ws.partials.as<double>();
@@ -1032,7 +1073,7 @@ static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, 
     } else {
       GSLS_TRY(lhs->ws.partials.alloc(sizeof(double) * ((size_t)2 * nblk + 64) + 64));
       GSLS_CUDA(cudaMemsetAsync(db, 0, sizeof(GridBar), st));
-      SchurArgs<VT, XT> a{nNo, rp, cp, mG, Gt, mL, P, Ps, Pb, Rs, SP, GP,
+      SchurArgs<VT, XT> a{nNo, rp, cp, A1, A2, P, Ps, Pb, Rs, SP, GP4,
                           lhs->ws.partials.as<double>(), db, sc, K};
       void *args[] = {&a};
       GSLS_CUDA(cudaLaunchCooperativeKernel((const void *)k_schur_persistent<VT, XT>, dim3(nblk),
@@ -1091,10 +1132,11 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
   auto t0 = std::chrono::steady_clock::now();
   // vectors: Rmi Rm GP MU(nB) U(mI) (3-vectors); Rci Rc Rs Ps SP Pb MP(nB) P(mI) (scalars)
   const size_t l3 = ((size_t)nNo * 3 + 63) & ~(size_t)63, l1 = ((size_t)nNo + 63) & ~(size_t)63;
-  const size_t nvec3 = 3 + (size_t)nB + mI, nvec1 = 6 + (size_t)nB + mI;
+  const size_t nvec3 = 5 + (size_t)nB + mI, nvec1 = 6 + (size_t)nB + mI;
   GSLS_TRY(ws.ns_vec.alloc(sizeof(XT) * (nvec3 * l3 + nvec1 * l1) + 2048 + 2 * sizeof(SchurScal)));
   XT *v3 = ws.ns_vec.as<XT>();
-  XT *Rmi = v3, *Rm = v3 + l3, *GP = v3 + 2 * l3, *MU = v3 + 3 * l3, *U = MU + (size_t)nB * l3;
+  XT *Rmi = v3, *Rm = v3 + l3, *GP = v3 + 2 * l3, *GP4 = v3 + 3 * l3;  // GP4: 4 per node
+  XT *MU = v3 + 5 * l3, *U = MU + (size_t)nB * l3;
   XT *v1 = v3 + nvec3 * l3;
   XT *Rci = v1, *Rc = v1 + l1, *Rs = v1 + 2 * l1, *Ps = v1 + 3 * l1, *SP = v1 + 4 * l1;
   XT *Pb = v1 + 5 * l1, *MP = v1 + 6 * l1, *P = MP + (size_t)nB * l1;
@@ -1103,8 +1145,11 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
   double *dsc = reinterpret_cast<double *>(sc + 2);  // 96 doubles: norms and dots
   GridBar *bar = reinterpret_cast<GridBar *>(dsc + 96);
   const size_t m9 = (size_t)nnz * 9, m3 = (size_t)nnz * 3;
-  GSLS_TRY(ws.ns_mat.alloc(sizeof(VT) * (m9 + 4 * m3 + nnz) + 64));
+  const size_t m1 = ((size_t)nnz + 15) & ~(size_t)15;
+  GSLS_TRY(ws.ns_mat.alloc(sizeof(VT) * (m9 + 4 * m3 + m1 + 8 * (size_t)nnz) + 256));
   VT *mK = ws.ns_mat.as<VT>(), *mG = mK + m9, *mD = mG + m3, *Gt = mD + m3, *mL = Gt + m3;
+  VT *A1 = reinterpret_cast<VT *>((reinterpret_cast<uintptr_t>(mL + m1) + 63) & ~(uintptr_t)63);
+  VT *A2 = A1 + 4 * (size_t)nnz;
   // the GMRES workspace may grow ws.partials: size it for both up front
   const int Gd = num_sms() * 2;
   const int sD = ls->GM.sD > 0 ? ls->GM.sD : 1;
@@ -1118,7 +1163,7 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
   k_ns_split<XT><<<G, kNT, 0, st>>>(nNo, R, Rmi, Rci, Rm, Rc, part, tk, dsc);
   GSLS_CHECK_LAUNCH();
   k_depart<VT><<<grid_for(nnz, G * 4), kNT, 0, st>>>(nnz, Val, lhs->d_tpos.as<int>(), mK, mG, mD, mL,
-                                                      Gt);
+                                                      Gt, A1, A2);
   GSLS_CHECK_LAUNCH();
   double n2[2];
   GSLS_CUDA(cudaMemcpyAsync(n2, dsc, sizeof(n2), cudaMemcpyDeviceToHost, st));
@@ -1152,7 +1197,8 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
     part = ws.partials.as<double>();
     k_ns_vs<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mD, Ui, Rc, Pi, nullptr);
     GSLS_CHECK_LAUNCH();
-    GSLS_TRY((schur_cg<VT, XT>(lhs, &ls->CG, mG, Gt, mL, Pi, Rs, Ps, Pb, SP, GP, sc, &h_sc, bar)));
+    GSLS_TRY((schur_cg<VT, XT>(lhs, &ls->CG, mG, Gt, mL, A1, A2, Pi, Rs, Ps, Pb, SP, GP, GP4, sc,
+                               &h_sc, bar)));
     k_ns_sv<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mG, Pi, MUiB, Rm, MUiBB, nullptr);
     GSLS_CHECK_LAUNCH();
     GSLS_TRY((gmres_ns<3, VT, XT>(lhs, &ls->GM, mK, MUiBB, Ui)));
