@@ -46,8 +46,10 @@ __device__ __forceinline__ double jm23(double J) {
   return z * z;
 }
 
+// FP32 tangent: 3 blocks per SM fit in 168 registers (28 bytes of spill);
+// the FP64 variant stays at its natural register count
 template <class VT>
-__global__ void __launch_bounds__(kAsmThreads) k_asm_struct(AsmArgs A) {
+__global__ void __launch_bounds__(kAsmThreads, sizeof(VT) == 4 ? 3 : 1) k_asm_struct(AsmArgs A) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.nColorEl) return;
   using AT = VT;
