@@ -33,41 +33,14 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_fluid(AsmArgs A) {
   const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
   const int tD = A.tDof, s0 = A.s;
 
-  // ---- geometry (GNN with ks, FP64)
-  double Nx[3][4], w, K[3][3];
-  {
-    double xl[4][3];
+  // ---- geometry (GNN with ks, FP64, precomputed per mesh): xiX(a,i) = Nx(i,a)
+  double Nx[3][4], K[3][3];
+  const double w = c_rule.w * load_geo(A, e, Nx);
 #pragma unroll
-    for (int a = 0; a < 4; a++)
+  for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int i = 0; i < 3; i++) xl[a][i] = __ldg(A.x + (size_t)n4[a] * 3 + i);
-    double xXi[3][3], adj[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int k = 0; k < 3; k++) xXi[i][k] = xl[k][i] - xl[3][i];
-    const double Jac = adj_det3(xXi, adj);
-    if (!(Jac != 0.0) || !isfinite(Jac)) atomicOr(A.err, 1);
-    const double iJ = 1.0 / Jac;
-    double xiX[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) xiX[i][j] = adj[i][j] * iJ;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      Nx[i][0] = xiX[0][i];
-      Nx[i][1] = xiX[1][i];
-      Nx[i][2] = xiX[2][i];
-      Nx[i][3] = -(xiX[0][i] + xiX[1][i] + xiX[2][i]);
-    }
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++)
-        K[i][j] = xiX[0][i] * xiX[0][j] + xiX[1][i] * xiX[1][j] + xiX[2][i] * xiX[2][j];
-    w = c_rule.w * Jac;
-  }
+    for (int j = 0; j < 3; j++)
+      K[i][j] = Nx[i][0] * Nx[j][0] + Nx[i][1] * Nx[j][1] + Nx[i][2] * Nx[j][2];
 
   // ---- nodal values and element-constant gradients (FP64)
   double yl[4][4], al[4][3];

@@ -58,31 +58,9 @@ __global__ void __launch_bounds__(kAsmThreads, sizeof(VT) == 4 ? 3 : 1) k_asm_st
   const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
   const int tD = A.tDof, s0 = A.s;
 
-  // ---- geometry (GNN, FP64): xXi(:,k) = x_k - x_4, Nx = xiX rows
-  double Nx[3][4], w;
-  {
-    double xl[4][3];
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int i = 0; i < 3; i++) xl[a][i] = __ldg(A.x + (size_t)n4[a] * 3 + i);
-    double xXi[3][3], adj[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int k = 0; k < 3; k++) xXi[i][k] = xl[k][i] - xl[3][i];
-    const double Jac = adj_det3(xXi, adj);
-    if (!(Jac != 0.0) || !isfinite(Jac)) atomicOr(A.err, 1);
-    const double iJ = 1.0 / Jac;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      Nx[i][0] = adj[0][i] * iJ;
-      Nx[i][1] = adj[1][i] * iJ;
-      Nx[i][2] = adj[2][i] * iJ;
-      Nx[i][3] = -(Nx[i][0] + Nx[i][1] + Nx[i][2]);
-    }
-    w = c_rule.w * Jac;
-  }
+  // ---- geometry (GNN, FP64, precomputed per mesh)
+  double Nx[3][4];
+  const double w = c_rule.w * load_geo(A, e, Nx);
 
   // ---- kinematics (FP64)
   double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};

@@ -29,6 +29,8 @@ struct gsls_mesh {
   gsls::DevBuf d_x;               // double nNo*3
   gsls::DevBuf d_eparam;          // double per element (colour order)
   gsls::DevBuf d_err;             // int error word
+  gsls::DevBuf d_geo;             // per-element Nx (12) and Jacobian, SoA: geo[k * nEl + e]
+  bool bad_jac = false;           // a zero or non-finite element Jacobian
   const double *eparam_src = nullptr;
   bool has_eparam = false;
 };
@@ -70,37 +72,6 @@ static Tet4Rule make_rule() {
   return r;
 }
 
-// GNN for tet4 (Code/Source/svFSI/NN.f:1469-1565, insd = 3):
-// Nxi = [[1,0,0,-1],[0,1,0,-1],[0,0,1,-1]], so xXi(:,k) = x_k - x_4.
-__device__ __forceinline__ void gnn_tet4(const double xl[4][3], double Nx[3][4], double &Jac) {
-  double xXi[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int k = 0; k < 3; k++) xXi[i][k] = xl[k][i] - xl[3][i];
-  const double J = xXi[0][0] * xXi[1][1] * xXi[2][2] + xXi[0][1] * xXi[1][2] * xXi[2][0] +
-                   xXi[0][2] * xXi[1][0] * xXi[2][1] - xXi[0][0] * xXi[1][2] * xXi[2][1] -
-                   xXi[0][1] * xXi[1][0] * xXi[2][2] - xXi[0][2] * xXi[1][1] * xXi[2][0];
-  double xiX[3][3];
-  xiX[0][0] = (xXi[1][1] * xXi[2][2] - xXi[1][2] * xXi[2][1]) / J;
-  xiX[0][1] = (xXi[2][1] * xXi[0][2] - xXi[2][2] * xXi[0][1]) / J;
-  xiX[0][2] = (xXi[0][1] * xXi[1][2] - xXi[0][2] * xXi[1][1]) / J;
-  xiX[1][0] = (xXi[1][2] * xXi[2][0] - xXi[1][0] * xXi[2][2]) / J;
-  xiX[1][1] = (xXi[2][2] * xXi[0][0] - xXi[2][0] * xXi[0][2]) / J;
-  xiX[1][2] = (xXi[0][2] * xXi[1][0] - xXi[0][0] * xXi[1][2]) / J;
-  xiX[2][0] = (xXi[1][0] * xXi[2][1] - xXi[1][1] * xXi[2][0]) / J;
-  xiX[2][1] = (xXi[2][0] * xXi[0][1] - xXi[2][1] * xXi[0][0]) / J;
-  xiX[2][2] = (xXi[0][0] * xXi[1][1] - xXi[0][1] * xXi[1][0]) / J;
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    Nx[i][0] = xiX[0][i];
-    Nx[i][1] = xiX[1][i];
-    Nx[i][2] = xiX[2][i];
-    Nx[i][3] = -xiX[0][i] - xiX[1][i] - xiX[2][i];
-  }
-  Jac = J;
-}
-
 struct AsmArgs {
   int nColorEl, el0;
   int tDof, s;
@@ -113,11 +84,27 @@ struct AsmArgs {
   const int4 *map;  // 4 int4 per element: map[e*4 + a] = (b0..b3)
   const double *x;
   const double *Ag, *Yg, *Dg;
+  const double *geo;     // kGeo x nEl (structure of arrays, colour order)
+  int nElAll;            // leading dimension of geo
   const double *eparam;
   double *R;
   void *Val;
   int *err;
 };
+
+// ---------------------------------------------------------------------------
+// Static tet4 geometry (GNN, Code/Source/svFSI/NN.f:1469-1565): the shape-
+// function gradients Nx(3,4) and the Jacobian depend on the mesh only, so
+// they are computed once per mesh (adjugate, one division) and read by every
+// assembly as 13 coalesced streams instead of 12 gathered coordinates.
+constexpr int kGeo = 13;  // Nx[i][a] at k = i*4 + a, Jac at k = 12
+__device__ __forceinline__ double load_geo(const AsmArgs &A, int e, double Nx[3][4]) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int a = 0; a < 4; a++) Nx[i][a] = __ldg(A.geo + (size_t)(i * 4 + a) * A.nElAll + e);
+  return __ldg(A.geo + (size_t)12 * A.nElAll + e);
+}
 
 }  // namespace gsls
 
@@ -125,14 +112,42 @@ struct AsmArgs {
 
 namespace gsls {
 
+__global__ void k_geo_tet4(int nEl, const int4 *__restrict__ ien, const double *__restrict__ x,
+                           double *geo, int *err) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nEl) return;
+  const int4 nd = ien[e];
+  const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
+  double xXi[3][3], x3[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) x3[i] = x[(size_t)n4[3] * 3 + i];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) xXi[i][k] = x[(size_t)n4[k] * 3 + i] - x3[i];
+  double adj[3][3];
+  const double Jac = adj_det3(xXi, adj);
+  if (!(Jac != 0.0) || !isfinite(Jac)) atomicOr(err, 1);
+  const double iJ = 1.0 / Jac;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const double n0 = adj[0][i] * iJ, n1 = adj[1][i] * iJ, n2 = adj[2][i] * iJ;
+    geo[(size_t)(i * 4 + 0) * nEl + e] = n0;
+    geo[(size_t)(i * 4 + 1) * nEl + e] = n1;
+    geo[(size_t)(i * 4 + 2) * nEl + e] = n2;
+    geo[(size_t)(i * 4 + 3) * nEl + e] = -(n0 + n1 + n2);
+  }
+  geo[(size_t)12 * nEl + e] = Jac;
+}
+
 // ---------------------------------------------------------------------------
 // HEATS3D (Code/Source/svFSI/HEATS.f:116-159) and isotropic CEP3D, one tet per
 // thread.  tet4 gradients are constant, so the Gauss-point sums reduce to
 // the rule's tables: with W = sum_g w and M_ab = sum_g N_a N_b,
 //   lR(a)   = w rho (sum_b M_ab al_b - s Ns_a) + W nu Nx_a . grad T
 //   lK(a,b) = wl (amd M_ab + 4 nu Nx_a . Nx_b)
-// (the reference's per-point sums, reordered).  Geometry by the adjugate
-// with one division; residual FP64, tangent in VT.
+// (the reference's per-point sums, reordered).  Geometry from the per-mesh
+// table; residual FP64, tangent in VT.
 template <class VT>
 __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -140,30 +155,14 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
   const int e = A.el0 + t;
   const int4 nd = A.ien[e];
   const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
-  double xXi[3][3], x3[3], al[4], yl[4];
-#pragma unroll
-  for (int i = 0; i < 3; i++) x3[i] = __ldg(A.x + (size_t)n4[3] * 3 + i);
-#pragma unroll
-  for (int k = 0; k < 3; k++)
-#pragma unroll
-    for (int i = 0; i < 3; i++) xXi[i][k] = __ldg(A.x + (size_t)n4[k] * 3 + i) - x3[i];
+  double al[4], yl[4];
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     al[a] = __ldg(A.Ag + (size_t)n4[a] * A.tDof + A.s);
     yl[a] = __ldg(A.Yg + (size_t)n4[a] * A.tDof + A.s);
   }
-  double adj[3][3];
-  const double Jac = adj_det3(xXi, adj);
-  if (!(Jac != 0.0) || !isfinite(Jac)) atomicOr(A.err, 1);
-  const double iJ = 1.0 / Jac;
   double Nx[3][4];
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    Nx[i][0] = adj[0][i] * iJ;
-    Nx[i][1] = adj[1][i] * iJ;
-    Nx[i][2] = adj[2][i] * iJ;
-    Nx[i][3] = -(Nx[i][0] + Nx[i][1] + Nx[i][2]);
-  }
+  const double Jac = load_geo(A, e, Nx);
   const double nu = A.eparam ? A.eparam[e] : A.cond;
   const double w = c_rule.w * Jac, W = 4.0 * w;
   const double T1 = A.af * A.gam * A.dt;
@@ -240,6 +239,8 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   A.ien = m->d_ien.as<int4>();
   A.map = m->d_map.as<int4>();
   A.x = m->d_x.as<double>();
+  A.geo = m->d_geo.as<double>();
+  A.nElAll = m->nEl;
   A.Ag = Ag;
   A.Yg = Yg;
   A.Dg = Dg;
@@ -296,27 +297,8 @@ __global__ void __launch_bounds__(kAsmThreads) k_dRdp_struct(AsmArgs A, int nEl,
   if (e >= nEl) return;
   const int4 nd = A.ien[e];
   const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
-  double xl[4][3];
-#pragma unroll
-  for (int a = 0; a < 4; a++)
-#pragma unroll
-    for (int i = 0; i < 3; i++) xl[a][i] = A.x[(size_t)n4[a] * 3 + i];
-  double xXi[3][3], adj[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int k = 0; k < 3; k++) xXi[i][k] = xl[k][i] - xl[3][i];
-  const double Jac = adj_det3(xXi, adj);
-  const double iJ = 1.0 / Jac;
   double Nx[3][4];
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    Nx[i][0] = adj[0][i] * iJ;
-    Nx[i][1] = adj[1][i] * iJ;
-    Nx[i][2] = adj[2][i] * iJ;
-    Nx[i][3] = -(Nx[i][0] + Nx[i][1] + Nx[i][2]);
-  }
-  const double W = 4.0 * c_rule.w * Jac;
+  const double W = 4.0 * c_rule.w * load_geo(A, e, Nx);
   double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
 #pragma unroll
   for (int a = 0; a < 4; a++)
@@ -366,15 +348,11 @@ __global__ void __launch_bounds__(kAsmThreads) k_dRdp_heats(AsmArgs A, int nEl,
   if (e >= nEl) return;
   const int4 nd = A.ien[e];
   const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
-  double xl[4][3], yl[4];
+  double yl[4];
 #pragma unroll
-  for (int a = 0; a < 4; a++) {
-#pragma unroll
-    for (int i = 0; i < 3; i++) xl[a][i] = A.x[(size_t)n4[a] * 3 + i];
-    yl[a] = A.Yg[(size_t)n4[a] * A.tDof + A.s];
-  }
-  double Nx[3][4], Jac;
-  gnn_tet4(xl, Nx, Jac);
+  for (int a = 0; a < 4; a++) yl[a] = A.Yg[(size_t)n4[a] * A.tDof + A.s];
+  double Nx[3][4];
+  const double Jac = load_geo(A, e, Nx);
   double Tx[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) Tx[i] = Nx[i][0] * yl[0] + Nx[i][1] * yl[1] + Nx[i][2] * yl[2] + Nx[i][3] * yl[3];
@@ -395,6 +373,8 @@ int mesh_dRdp(gsls_mesh *m, const gsls_eq_params *p, const double *Yg, const dou
   A.s = p->s;
   A.ien = m->d_ien.as<int4>();
   A.x = m->d_x.as<double>();
+  A.geo = m->d_geo.as<double>();
+  A.nElAll = m->nEl;
   A.Yg = Yg;
   A.Dg = Dg;
   cudaStream_t st = m->lhs->stream;
@@ -427,6 +407,8 @@ int mesh_mass(gsls_mesh *m, const double *zeros, double *R, double *Val) {
   A.ien = m->d_ien.as<int4>();
   A.map = m->d_map.as<int4>();
   A.x = m->d_x.as<double>();
+  A.geo = m->d_geo.as<double>();
+  A.nElAll = m->nEl;
   A.Ag = A.Yg = A.Dg = zeros;
   A.R = R;
   A.Val = Val;
@@ -475,6 +457,10 @@ int mesh_coords_host(gsls_mesh *m, double *x) {
 }
 
 int mesh_check_error(gsls_mesh *m) {
+  if (m->bad_jac) {
+    set_error("assembly: zero or non-finite element Jacobian");
+    return GSLS_ERR_JAC;
+  }
   int h = 0;
   GSLS_CUDA(cudaMemcpyAsync(&h, m->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, m->lhs->stream));
   GSLS_CUDA(cudaStreamSynchronize(m->lhs->stream));
@@ -593,11 +579,22 @@ int gsls_mesh_create(gsls_mesh **out, gsls_lhs *lhs, int nEl, int eNoN, const in
   cudaMemcpyAsync(m->d_map.p, map.data(), sizeof(int) * 16 * (size_t)nEl, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(m->d_x.p, x, sizeof(double) * 3 * (size_t)nNo, cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(m->d_err.p, 0, 16, st);
+  if ((rc = m->d_geo.alloc(sizeof(double) * kGeo * (size_t)nEl))) {
+    delete m;
+    return rc;
+  }
+  k_geo_tet4<<<(nEl + 127) / 128, 128, 0, st>>>(nEl, m->d_ien.as<int4>(), m->d_x.as<double>(),
+                                                m->d_geo.as<double>(), m->d_err.as<int>());
+  count_launch();
+  int herr = 0;
+  cudaMemcpyAsync(&herr, m->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaError_t ce = cudaStreamSynchronize(st);
   if (ce != cudaSuccess) {
     delete m;
     return cuda_fail(ce, "mesh upload", __FILE__, __LINE__);
   }
+  m->bad_jac = herr != 0;
+  cudaMemsetAsync(m->d_err.p, 0, 16, st);
   *out = m;
   return GSLS_OK;
 }
