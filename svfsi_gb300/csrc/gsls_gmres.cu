@@ -72,13 +72,14 @@ __global__ void k_gm_scale(size_t n, XT *__restrict__ u, const double *normp) {
     u[k] = u[k] * inv;
 }
 
-// SpMV that is skipped once the Arnoldi loop is done
+// SpMV that is skipped once the Arnoldi loop is done; rev: rows walked from
+// the end (zig-zag order across Arnoldi steps, zigzag_on)
 template <int D, class VT, class XT>
 __global__ void __launch_bounds__(kT) k_gm_spmv(int nNo, const int *__restrict__ rowPtr,
                                                 const int *__restrict__ colPtr,
                                                 const VT *__restrict__ Val,
                                                 const XT *__restrict__ x, XT *__restrict__ y,
-                                                const GmresCtl *ctl) {
+                                                const GmresCtl *ctl, int rev) {
   if (*(volatile const int *)&ctl->done) return;
   using AT = typename AccOf<VT>::T;
   constexpr int RPW = 32 / D;
@@ -87,8 +88,8 @@ __global__ void __launch_bounds__(kT) k_gm_spmv(int nNo, const int *__restrict__
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   GatherX<D, XT, AT> g{x};
   for (int base = warp * RPW; base < nNo; base += nwarps * RPW) {
-    const int i = base + grp;
-    if (grp < RPW && i < nNo)
+    const int i = rev ? nNo - 1 - (base + grp) : base + grp;
+    if (grp < RPW && i >= 0 && i < nNo)
       y[(size_t)i * D + r] = XT(spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, g));
   }
 }
@@ -295,7 +296,7 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
     GSLS_CUDA(cudaMemcpyAsync(ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice, st));
     if (l > 1) {
       k_gm_spmv<D, VT, XT><<<G, kT, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
-                                             lhs->d_colPtr.as<int>(), Val, X, u1, ctl);
+                                             lhs->d_colPtr.as<int>(), Val, X, u1, ctl, 0);
       GSLS_CHECK_LAUNCH();
       launch_addbcmul<XT>(lhs, 0, D, X, u1, &ctl->done);
     }
@@ -341,7 +342,8 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
         XT *ui = basis + ld * (i - 1), *ui1 = basis + ld * i;
         if (prof) cudaEventRecord(prof_event(0), st);
         k_gm_spmv<D, VT, XT><<<G, kT, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
-                                               lhs->d_colPtr.as<int>(), Val, ui, ui1, ctl);
+                                               lhs->d_colPtr.as<int>(), Val, ui, ui1, ctl,
+                                               zigzag_on() & i);
         GSLS_CHECK_LAUNCH();
         if (prof) cudaEventRecord(prof_event(1), st);
         if (ws.cpl_on) {

@@ -38,6 +38,12 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 void count_launch();
 void count_launch_n(int n);
 int num_sms();
+// Zig-zag traversal of the Krylov SpMVs: a matrix larger than L2 streamed in
+// the same order every iteration leaves L2 holding its tail, which the next
+// forward pass evicts before reaching it; reversing the row order every
+// other iteration starts each pass on what the previous one left in L2.
+// Default on; GSLS_ZIGZAG=0 keeps the forward order.
+int zigzag_on();
 
 // kernel timing registry (gsls_profile_*)
 bool prof_on();
@@ -104,10 +110,11 @@ struct GraphKey {
   bool tma;
   bool fused;
   const void *part, *scal, *w;  // workspace buffers baked into the graph
+  const void *sval;             // sliced copy of the matrix (null: CSR SpMV)
   bool operator==(const GraphKey &o) const {
     return D == o.D && vsz == o.vsz && xsz == o.xsz && val == o.val && x == o.x &&
            batch == o.batch && nNo == o.nNo && tma == o.tma && fused == o.fused &&
-           part == o.part && scal == o.scal && w == o.w;
+           part == o.part && scal == o.scal && w == o.w && sval == o.sval;
   }
 };
 
@@ -118,8 +125,15 @@ struct Workspace {
   int tma_key = -1, tma_smem = 0, tma_grid = 0;
   bool tma_ok = false;
   long long tma_info[3] = {0, 0, 0};  // TmaTiles of the cached geometry
-  cudaGraphExec_t cg_graph = nullptr;
+  cudaGraphExec_t cg_graph = nullptr;      // CG batch on the CSR matrix
   GraphKey cg_key{};
+  cudaGraphExec_t cg_graph_s = nullptr;    // CG batch on the sliced copy
+  GraphKey cg_key_s{};
+  // sliced block-ELL layout of the CG SpMV (structure per block size D,
+  // values per solve): slice offsets, slot rows, columns, CSR block -> slot
+  int sell_D = 0, sell_nS = 0, sell_vkey = 0;
+  long long sell_steps = 0;
+  DevBuf sell_off, sell_row, sell_col, sell_pos, sell_val;
   DevBuf partials;    // double[grid * 64]
   DevBuf ticket;      // unsigned[8]
   DevBuf scal;        // KrylovScalars

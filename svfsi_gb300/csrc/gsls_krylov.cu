@@ -8,6 +8,7 @@
 // fused into the next SpMV (double-buffered P), so one CG iteration is two
 // kernels: SpMV+dot and update+norm.  Reductions use a fixed grid and a
 // last-block pass: every sum is bitwise reproducible.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -79,12 +80,13 @@ __global__ void __launch_bounds__(kThreads) k_cg_init(int nNo, const double *__r
 // fly, dot = P_new . KP, alpha = errO / dot.
 // FUSED = false: the direction P (= P0) is updated by k_cg_pupdate and the
 // SpMV gathers P alone (half the gather traffic of the fused form).
+// zz: odd iterations walk the rows from the end (see zigzag_rev).
 template <int D, class VT, class XT, bool FUSED>
 __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__restrict__ rowPtr,
                                                       const int *__restrict__ colPtr,
                                                       const VT *__restrict__ Val, CgVecs v,
                                                       KrylovScalars *S, double *partials,
-                                                      unsigned *ticket) {
+                                                      unsigned *ticket, int zz) {
   cudaGridDependencySynchronize();  // launched with programmatic serialization
   if (*(volatile int *)&S->done) return;
   using AT = typename AccOf<VT>::T;
@@ -104,9 +106,10 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   AT dot = AT(0);
+  const bool rev = zz && (S->itr & 1);
   for (int base = warp * RPW; base < nNo; base += nwarps * RPW) {
-    const int i = base + grp;
-    if (grp < RPW && i < nNo) {
+    const int i = rev ? nNo - 1 - (base + grp) : base + grp;
+    if (grp < RPW && i >= 0 && i < nNo) {
       const size_t k = (size_t)i * VD + r;
       AT y, pn;
       if constexpr (FUSED) {
@@ -131,6 +134,12 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
     if (!isfinite(S->alpha)) S->done = 3;
   }
 }
+
+}  // namespace gsls
+
+#include "gsls_sell.cuh"
+
+namespace gsls {
 
 // ---------------------------------------------------------------------------
 // TMA-staged variant of k_cg_spmv.  A tile is NW*(32/D) consecutive block
@@ -632,14 +641,115 @@ static bool use_pdl() {
   return on;
 }
 
+// Sliced copy of the matrix (structure per lhs and block size, built on the
+// host once): rows sorted by decreasing length within windows of 32 slices.
+template <int D>
+static int sell_setup(gsls_lhs *lhs) {
+  Workspace &ws = lhs->ws;
+  if (ws.sell_D == D) return GSLS_OK;
+  constexpr int RPW = 32 / D, WIN = 32 * RPW;
+  const int nNo = lhs->nNo;
+  const std::vector<int> &rp = lhs->h_rowPtr, &cp = lhs->h_colPtr;
+  const int nS = (nNo + RPW - 1) / RPW;
+  std::vector<int> slotRow((size_t)nS * RPW, -1), idx;
+  for (int w0 = 0; w0 < nNo; w0 += WIN) {
+    const int w1 = std::min(nNo, w0 + WIN);
+    idx.resize(w1 - w0);
+    for (int i = w0; i < w1; i++) idx[i - w0] = i;
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int a, int b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
+    for (int k = 0; k < w1 - w0; k++) slotRow[(size_t)w0 + k] = idx[k];
+  }
+  std::vector<int> off((size_t)nS + 1, 0);
+  for (int s = 0; s < nS; s++) {
+    int m = 0;
+    for (int g = 0; g < RPW; g++) {
+      const int i = slotRow[(size_t)s * RPW + g];
+      if (i >= 0) m = std::max(m, rp[i + 1] - rp[i]);
+    }
+    if ((long long)off[s] + m > (1LL << 31) / RPW - 1) {
+      set_error("sliced matrix copy: too many blocks");
+      return GSLS_ERR_UNSUPPORTED;
+    }
+    off[s + 1] = off[s] + m;
+  }
+  const long long steps = off[nS];
+  std::vector<int> scol((size_t)steps * RPW, 0), pos((size_t)lhs->nnz, 0);
+  for (int s = 0; s < nS; s++)
+    for (int g = 0; g < RPW; g++) {
+      const int i = slotRow[(size_t)s * RPW + g];
+      if (i < 0) continue;
+      const int len = rp[i + 1] - rp[i];
+      for (int t = 0; t < off[s + 1] - off[s]; t++) {
+        const int P = (off[s] + t) * RPW + g;
+        if (t < len) {
+          scol[P] = cp[rp[i] + t];
+          pos[rp[i] + t] = P;
+        } else {
+          scol[P] = i;  // zero block on the row's own column
+        }
+      }
+    }
+  GSLS_TRY(ws.sell_off.alloc(sizeof(int) * off.size()));
+  GSLS_TRY(ws.sell_row.alloc(sizeof(int) * slotRow.size()));
+  GSLS_TRY(ws.sell_col.alloc(sizeof(int) * scol.size()));
+  GSLS_TRY(ws.sell_pos.alloc(sizeof(int) * pos.size()));
+  cudaStream_t st = lhs->stream;
+  GSLS_CUDA(cudaMemcpyAsync(ws.sell_off.p, off.data(), sizeof(int) * off.size(),
+                            cudaMemcpyHostToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(ws.sell_row.p, slotRow.data(), sizeof(int) * slotRow.size(),
+                            cudaMemcpyHostToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(ws.sell_col.p, scol.data(), sizeof(int) * scol.size(),
+                            cudaMemcpyHostToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(ws.sell_pos.p, pos.data(), sizeof(int) * pos.size(),
+                            cudaMemcpyHostToDevice, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));  // host vectors go out of scope
+  ws.sell_D = D;
+  ws.sell_nS = nS;
+  ws.sell_steps = steps;
+  ws.sell_vkey = 0;
+  return GSLS_OK;
+}
+
+// Copy the (preconditioned) values into the sliced layout; padding blocks
+// are zeroed when the buffer is (re)laid out and never written after.
+template <int D, class VT>
+static int sell_pack(gsls_lhs *lhs, const VT *Val, SellArgs &sa) {
+  Workspace &ws = lhs->ws;
+  GSLS_TRY(sell_setup<D>(lhs));
+  constexpr int RPW = 32 / D, DD = D * D;
+  const size_t vbytes = sizeof(VT) * (size_t)ws.sell_steps * RPW * DD;
+  const int vkey = D * 16 + (int)sizeof(VT);
+  cudaStream_t st = lhs->stream;
+  if (ws.sell_vkey != vkey) {
+    GSLS_TRY(ws.sell_val.alloc(vbytes));
+    GSLS_CUDA(cudaMemsetAsync(ws.sell_val.p, 0, vbytes, st));
+    ws.sell_vkey = vkey;
+  }
+  const size_t n = (size_t)lhs->nnz * DD;
+  k_sell_pack<D, VT><<<lhs->grid, kThreads, 0, st>>>(n, ws.sell_pos.as<int>(), Val,
+                                                     ws.sell_val.as<VT>());
+  GSLS_CHECK_LAUNCH();
+  sa.nS = ws.sell_nS;
+  sa.off = ws.sell_off.as<int>();
+  sa.slotRow = ws.sell_row.as<int>();
+  sa.scol = ws.sell_col.as<int>();
+  sa.sval = ws.sell_val.p;
+  return GSLS_OK;
+}
+
 template <int D, class VT, class XT, bool FUSED>
 static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter, bool prof,
                       int ev_base, const TmaTiles *tt = nullptr, int tma_smem = 0,
-                      int tma_grid = 0) {
+                      int tma_grid = 0, const SellArgs *sa = nullptr) {
   cudaStream_t st = lhs->stream;
   Workspace &ws = lhs->ws;
   const int nNo = lhs->nNo;
   static const int Gs = resident_grid(k_cg_spmv<D, VT, XT, FUSED>, 1 << 30);
+  // sliced SpMV: 8 steps per group in FP32 (64 registers, 4 blocks per SM),
+  // 4 in FP64
+  constexpr int SU = sizeof(VT) == 4 ? 8 : 4;
+  static const int Gsl = resident_grid(k_cg_spmv_sell<D, VT, XT, SU>, 1 << 30);
   static const int Gu = resident_grid(k_cg_update<XT, FUSED>, 1 << 30, kUpdThreads);
   static const int Gp = resident_grid(k_cg_pupdate<XT>, 1 << 30, kUpdThreads);
   const int G1 = Gs < lhs->grid ? Gs : lhs->grid, G2 = Gu < lhs->grid ? Gu : lhs->grid;
@@ -648,6 +758,7 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
   KrylovScalars *S = ws.scal.as<KrylovScalars>();
   double *part = ws.partials.as<double>();
   unsigned *tk = ws.ticket.as<unsigned>();
+  const int zz = zigzag_on();
   for (int b = 0; b < n_iter; b++) {
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b), st);
     // programmatic dependent launch: each kernel's blocks may be scheduled
@@ -663,12 +774,18 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
     if (tt) {
       k_cg_spmv_tma<D, VT, XT, kTmaWarps, FUSED><<<tma_grid, kTmaWarps * 32, tma_smem, st>>>(
           nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, v, S, part, tk, *tt);
+    } else if (sa && !FUSED) {
+      cfg.gridDim = dim3(Gsl < lhs->grid ? Gsl : lhs->grid);
+      cfg.blockDim = dim3(kThreads);
+      GSLS_CUDA(
+          cudaLaunchKernelEx(&cfg, k_cg_spmv_sell<D, VT, XT, SU>, *sa, v, S, part, tk, zz));
     } else {
       cfg.gridDim = dim3(G1);
       cfg.blockDim = dim3(kThreads);
       GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_spmv<D, VT, XT, FUSED>, nNo,
                                    (const int *)lhs->d_rowPtr.as<int>(),
-                                   (const int *)lhs->d_colPtr.as<int>(), Val, v, S, part, tk));
+                                   (const int *)lhs->d_colPtr.as<int>(), Val, v, S, part, tk,
+                                   zz));
     }
     GSLS_CHECK_LAUNCH();
     if (prof) cudaEventRecord(prof_event(ev_base + 2 * b + 1), st);
@@ -705,7 +822,6 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   GSLS_TRY(wait_scalars(lhs));
   const bool prof = prof_on();
   const int B = nv < (1u << 20) ? 8 : 16;
-  // CUDA graph of B iterations, cached per (D, types, Val, workspace)
   // TMA-staged SpMV for FP32 values in a buffer with copy slack
   TmaTiles tt{};
   int tsmem = 0, tgrid = 0;
@@ -717,29 +833,58 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
       want_tma && val_padded && sizeof(VT) == 4 && tma_setup<D, VT>(lhs, tt, tsmem, tgrid);
   const TmaTiles *ttp = use_tma ? &tt : nullptr;
   if (use_tma) GSLS_CUDA(cudaMemsetAsync(ws.err.p, 0, sizeof(int), st));
-  GraphKey key{D,  (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma,
-               FUSED, ws.partials.p, ws.scal.p, ws.Wf.p};
-  if (!prof && !(ws.cg_graph && ws.cg_key == key)) {
-    if (ws.cg_graph) {
-      cudaGraphExecDestroy(ws.cg_graph);
-      ws.cg_graph = nullptr;
+  // Sliced SpMV: a solve that is still running after its first batch packs
+  // the matrix into the sliced layout (one pass over Val) and continues on
+  // it; short solves (a few iterations) never pay for the copy.
+  // GSLS_SPMV=csr keeps the CSR kernel throughout.
+  static const bool want_sell = [] {
+    const char *e = getenv("GSLS_SPMV");
+    return !(e && (strcmp(e, "csr") == 0 || strcmp(e, "tma") == 0));
+  }();
+  const bool sell_ok = want_sell && !FUSED && !use_tma;
+  SellArgs sa{};
+  bool sell_on = false;
+  // CUDA graph of B iterations, cached per (D, types, Val, workspace,
+  // layout); one slot for the CSR batch and one for the sliced batch
+  auto graph_for = [&](bool sl, cudaGraphExec_t *&ge) -> int {
+    cudaGraphExec_t &gx = sl ? ws.cg_graph_s : ws.cg_graph;
+    GraphKey &gk = sl ? ws.cg_key_s : ws.cg_key;
+    GraphKey key{D,  (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma,
+                 FUSED, ws.partials.p, ws.scal.p, ws.Wf.p, sl ? sa.sval : nullptr};
+    ge = &gx;
+    if (gx && gk == key) return GSLS_OK;
+    if (gx) {
+      cudaGraphExecDestroy(gx);
+      gx = nullptr;
     }
     cudaGraph_t g;
     GSLS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int rc = cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, false, 0, ttp, tsmem, tgrid);
+    int rc = cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, false, 0, ttp, tsmem, tgrid,
+                                          sl ? &sa : nullptr);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc != GSLS_OK) return rc;
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
-    GSLS_CUDA(cudaGraphInstantiate(&ws.cg_graph, g, 0));
+    GSLS_CUDA(cudaGraphInstantiate(&gx, g, 0));
     cudaGraphDestroy(g);
-    ws.cg_key = key;
-  }
+    gk = key;
+    return GSLS_OK;
+  };
+  int nbatch = 0;
   while (ws.h_scal->done == 0) {
     const int itr_before = ws.h_scal->itr;
+    if (sell_ok && !sell_on && nbatch >= 1) {
+      GSLS_TRY(sell_pack<D, VT>(lhs, Val, sa));
+      count_launch();
+      sell_on = true;
+    }
+    nbatch++;
     if (prof) {
-      GSLS_TRY(cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, true, 0, ttp, tsmem, tgrid));
+      GSLS_TRY(cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, true, 0, ttp, tsmem, tgrid,
+                                            sell_on ? &sa : nullptr));
     } else {
-      GSLS_CUDA(cudaGraphLaunch(ws.cg_graph, st));
+      cudaGraphExec_t *ge = nullptr;
+      GSLS_TRY(graph_for(sell_on, ge));
+      GSLS_CUDA(cudaGraphLaunch(*ge, st));
       count_launch_n((FUSED ? 2 : 3) * B - 1);
     }
     GSLS_TRY(wait_scalars(lhs));

@@ -3,6 +3,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -36,6 +37,14 @@ static std::vector<std::pair<std::string, ProfEntry>> g_prof_tab;
 static std::vector<cudaEvent_t> g_events;
 
 bool prof_on() { return g_prof; }
+
+int zigzag_on() {
+  static const int on = [] {
+    const char *e = getenv("GSLS_ZIGZAG");
+    return (e && strcmp(e, "0") == 0) ? 0 : 1;
+  }();
+  return on;
+}
 
 void prof_add(const char *name, long long count, double ms) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -424,6 +433,7 @@ int gsls_lhs_free(gsls_lhs *lhs) {
   if (lhs->stream) cudaStreamSynchronize(lhs->stream);
   if (lhs->ws.h_scal) cudaFreeHost(lhs->ws.h_scal);
   if (lhs->ws.cg_graph) cudaGraphExecDestroy(lhs->ws.cg_graph);
+  if (lhs->ws.cg_graph_s) cudaGraphExecDestroy(lhs->ws.cg_graph_s);
   if (lhs->ev0) cudaEventDestroy(lhs->ev0);
   if (lhs->ev1) cudaEventDestroy(lhs->ev1);
   cudaStream_t s = lhs->own_stream ? lhs->stream : nullptr;

@@ -347,3 +347,77 @@ def test_bicgstab_matches_oracle(gsls, orc, case, mixed):
         torch.cuda.synchronize()
         assert ls.RI.suc == 1
         assert rel(dR.cpu().numpy(), Ro) < 1e-3
+
+
+def _spd_block_system(p, dof, seed):
+    """Symmetric positive definite block matrix on the mesh graph: random
+    blocks with K_ji = K_ij^T, the diagonal shifted so that the spectrum
+    spans [0.02, 1] x its width (condition number ~50)."""
+    rng = np.random.default_rng(seed)
+    rp, cp = np.asarray(p.rowPtr), np.asarray(p.colPtr)
+    pos = {}
+    for i in range(p.nNo):
+        for j in range(rp[i], rp[i + 1]):
+            pos[(i, int(cp[j]))] = j
+    Val = np.zeros((p.nnz, dof, dof))
+    for i in range(p.nNo):
+        for j in range(rp[i], rp[i + 1]):
+            c = int(cp[j])
+            if c > i:
+                b = rng.standard_normal((dof, dof))
+                Val[j] = b
+                Val[pos[(c, i)]] = b.T
+            elif c == i:
+                s = rng.standard_normal((dof, dof))
+                Val[j] = 0.5 * (s + s.T)
+    n = p.nNo * dof
+    Kd = np.zeros((n, n))
+    for i in range(p.nNo):
+        for j in range(rp[i], rp[i + 1]):
+            c = int(cp[j])
+            Kd[i * dof:(i + 1) * dof, c * dof:(c + 1) * dof] = Val[j]
+    ev = np.linalg.eigvalsh(Kd)
+    shift = -ev[0] + 0.02 * (ev[-1] - ev[0])
+    for i in range(p.nNo):
+        Val[pos[(i, i)]] += shift * np.eye(dof)
+    R = rng.standard_normal((p.nNo, dof))
+    return R, Val.reshape(p.nnz, dof * dof)
+
+
+@pytest.mark.parametrize("dof", [1, 2, 3, 4])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_cg_block_sizes_matches_oracle(gsls, orc, dof, mixed):
+    """CG (diagonal preconditioner) on SPD block systems of every block size;
+    solves run past the first batch of iterations, so they switch to the
+    sliced copy of the matrix."""
+    torch = torch_dev()
+    p = problems.heats_cube(6)
+    R0, V0 = _spd_block_system(p, dof, seed=10 + dof)
+    dirn = p.dirichlet[0].nodes
+    lhs = _lhs_for(p)
+    fsils.FSILS_BC_CREATE(lhs, 1, dirn.size, 3, fsils.BC_TYPE_DIR, dirn + 1, np.zeros((dirn.size, 3)))
+    ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_CG, relTol=1e-8, maxItr=2000)
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
+    s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
+    ols = orc.ls_create(orc.LS_TYPE_CG, relTol=1e-8, mItr=2000)
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, dof, Ro, Vo, orc.PRECOND_FSILS)
+    assert ols.RI.itr > 16  # past the first batch on the device
+    if mixed:
+        ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_CG, relTol=1e-5, maxItr=2000)
+        dR = torch.tensor(R0, dtype=torch.float64, device="cuda")
+        dV = torch.tensor(V0, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        _lib.check(gsls.gsls_solve_dev(lhs.h, C.byref(ls), dof, C.c_void_p(dR.data_ptr()),
+                                       C.c_void_p(dV.data_ptr()), _lib.PREC_MIXED,
+                                       fsils.PRECOND_FSILS, None, None))
+        R = dR.cpu().numpy()
+        assert ls.RI.itr > 8
+        assert rel(R, Ro) < 1e-4
+    else:
+        R, Val = R0.copy(), V0.copy()
+        fsils.FSILS_SOLVE(lhs, ls, dof, R, Val, fsils.PRECOND_FSILS)
+        assert rel(Val, Vo) < 1e-15
+        assert abs(ls.RI.itr - ols.RI.itr) <= 1
+        assert rel(R, Ro) < 1e-7
+    assert ls.RI.suc == 1
