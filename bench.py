@@ -319,8 +319,9 @@ def run_gsls(args):
         tkey = "cg_spmv_d1_f32_cep_slab"
     else:
         B = p.algorithmic_bytes(4, 4)["spmv"]
-        kname = "k_cg_spmv<3,float,float> (block-CSR SpMV + fused P.KP)"
-        tkey = "cg_spmv_d3_f32_struct_beam_176x44x44"
+        kname = ("k_cg_spmv_sell<3,float,float,8> (sliced block-ELL SpMV + fused P.KP, "
+                 "zig-zag order; the first batch of each solve runs k_cg_spmv on the CSR)")
+        tkey = "cg_spmv_sell_d3_f32_struct_beam_176x44x44"
     avg_s = (tot_ms / max(cnt, 1)) / 1e3
     achieved = B / avg_s / 1e9 if cnt else None
     roof = {"kernel": kname,
