@@ -6,11 +6,13 @@ mixed precision (FP32 tangent + FP32 inner CG, FP64 residual/Newton) beside
 the plain FP64 GPU path, with the relative L2 distance between the two.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gsls|reference]
-                  [--workload struct|fluid]
+                  [--workload struct|fluid|cep|lelas|adjoint]
 
 --workload fluid times the VMS Navier-Stokes workload instead (cylinder
-R 0.5, L 5, ~1.06M tet4, 4x4 blocks; RCS + NS block solver), the same line
-format with its own roofline kernel (the GMRES block SpMV on the K block).
+R 0.5, L 5, ~1.2M tet4, 4x4 blocks; RCS + NS block solver), the same line
+format with its own roofline kernel (the GMRES block SpMV on the K block);
+cep the monodomain slab, lelas linear elastodynamics on the beam mesh,
+adjoint the discrete adjoint of the beam with a finite-difference check.
 
 --impl reference times the CPU restatement of the reference's algorithm
 (oracle/, OpenMP over all host cores) on the same workload.  N > 1 runs
@@ -48,7 +50,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--only", choices=["all", "mixed", "fp64"], default="all",
                     help="time one precision only (profiling runs)")
-    ap.add_argument("--workload", choices=["struct", "fluid", "cep", "adjoint"], default="struct")
+    ap.add_argument("--workload", choices=["struct", "fluid", "cep", "lelas", "adjoint"],
+                    default="struct")
     ap.add_argument("--fd-dirs", type=int, default=4,
                     help="adjoint workload: random directions of the central-FD check")
     ap.add_argument("--fd-h", type=float, default=1e-3,
@@ -91,6 +94,10 @@ def workload(args):
         if args.small:
             return problems.cep_slab(27, 27, 6, nsteps=args.steps, A=52.0)
         return problems.cep_slab(nsteps=args.steps, A=52.0)
+    if args.workload == "lelas":
+        if args.small:
+            return problems.lelas_beam(24, 6, 6, nsteps=args.steps)
+        return problems.lelas_beam(**WORKLOAD, nsteps=args.steps)
     if args.small:
         return problems.struct_beam(24, 6, 6, nsteps=args.steps)
     return problems.struct_beam(**WORKLOAD, nsteps=args.steps)
@@ -114,8 +121,16 @@ def workload_desc(p):
                 f"inlet peak 30, impulsive start), {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
                 f"{p.nnz:,} 4x4 blocks, RCS + NS solver (sD 100, relTol 1e-2), dt 1e-3, Newton "
                 f"tol 1e-10")
+    if p.phys == problems_phys_lelas():
+        return (f"{p.name}: linear elastodynamics (LELAS3D, E 1e6, nu 0.45), {p.nEl:,} tet4, "
+                f"{p.nNo:,} nodes, nnz {p.nnz:,} 3x3 blocks, CG+diag, dt 1e-3, Newton tol 1e-8")
     return (f"{p.name}: neo-Hookean+ST91 elastodynamics, {p.nEl:,} tet4, {p.nNo:,} nodes, "
             f"nnz {p.nnz:,} 3x3 blocks, CG+diag, dt 1e-3, Newton tol 1e-8")
+
+
+def problems_phys_lelas():
+    from svfsi_gb300 import problems
+    return problems.PHYS_LELAS
 
 
 # ---------------------------------------------------------------------------
@@ -321,7 +336,7 @@ def run_gsls(args):
         B = p.algorithmic_bytes(4, 4)["spmv"]
         kname = ("k_cg_spmv_sell<3,float,float,8> (sliced block-ELL SpMV + fused P.KP, "
                  "zig-zag order; the first batch of each solve runs k_cg_spmv on the CSR)")
-        tkey = "cg_spmv_sell_d3_f32_struct_beam_176x44x44"
+        tkey = f"cg_spmv_sell_d3_f32_{p.name}"
     avg_s = (tot_ms / max(cnt, 1)) / 1e3
     achieved = B / avg_s / 1e9 if cnt else None
     roof = {"kernel": kname,

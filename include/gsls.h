@@ -58,6 +58,7 @@ extern "C" {
 #define GSLS_PHYS_STRUCT 2
 #define GSLS_PHYS_CEP 3
 #define GSLS_PHYS_FLUID 4
+#define GSLS_PHYS_LELAS 5  /* linear elasticity, Code/Source/svFSI/LELAS.f */
 
 /* Mirrors FSILS_subLsType, Code/Source/svFSILS/FSILS_STRUCT.h:162-191
    (Fortran LOGICAL stored as int32). */
@@ -188,6 +189,8 @@ typedef struct {
   double ctM, ctC;  /* FLUID stabilisation constants */
   const double *eparam; /* host, per element (original order) or NULL:
                            STRUCT C10, CEP Diso, HEATS conductivity */
+  double elM, nu;   /* LELAS elasticity modulus and Poisson ratio (body
+                       force f_x, f_y, f_z in fb) */
 } gsls_eq_params;
 
 /* Assemble R(dof,nNo) (double) and Val(dof*dof,nnz) (double or float per

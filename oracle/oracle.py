@@ -39,7 +39,8 @@ class EqP(C.Structure):
                 ("C10", C.c_double), ("Kpen", C.c_double), ("visc", C.c_double),
                 ("dmp", C.c_double), ("fb", C.c_double * 3), ("Diso", C.c_double),
                 ("mu_f", C.c_double), ("ctM", C.c_double),
-                ("ctC", C.c_double), ("eparam", c_double_p)]
+                ("ctC", C.c_double), ("eparam", c_double_p), ("elM", C.c_double),
+                ("nu", C.c_double)]
 
 
 class DirBC(C.Structure):

@@ -115,7 +115,7 @@ void orc_doassem(int dof, int eNoN, const int *ptr, const double *lK,
 
 /* Equation parameters for one assembly call (one domain, constant props). */
 typedef struct {
-  int phys;      /* 1 HEATS, 2 STRUCT, 3 CEP, 4 FLUID */
+  int phys;      /* 1 HEATS, 2 STRUCT, 3 CEP, 4 FLUID, 5 LELAS */
   int dof, tDof, s; /* eq dof, total dof, 0-based start of this eq in tDof */
   double am, af, beta, gam, dt;
   double rho, cond, src;       /* HEATS: solid_density, conductivity, source */
@@ -125,6 +125,7 @@ typedef struct {
   double mu_f;                 /* FLUID viscosity (density: rho) */
   double ctM, ctC;             /* FLUID stabilisation constants */
   const double *eparam;        /* optional per-element parameter (mu or Diso) */
+  double elM, nu;              /* LELAS elasticity modulus, Poisson ratio (f in fb) */
 } orc_eqp;
 
 int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
@@ -140,6 +141,10 @@ void orc_elem_fluid(const orc_eqp *p, const double xl[12], const double *al,
                     const double *yl, double lR[16], double lK[256]);
 void orc_elem_heats(const orc_eqp *p, const double xl[12], const double *al,
                     const double *yl, double lR[4], double lK[16]);
+/* LELAS3D, F/LELAS.f:130-238 (no prestress, no nodal body force Bf), one
+   tet4 element: lR(3,4), lK(9,4,4) */
+void orc_elem_lelas(const orc_eqp *p, const double xl[12], const double *al,
+                    const double *dl, double lR[12], double lK[144]);
 void orc_elem_struct(const orc_eqp *p, double mu_e, const double xl[12],
                      const double *al, const double *yl, const double *dl,
                      double lR[12], double lK[144]);

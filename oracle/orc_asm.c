@@ -363,6 +363,72 @@ void orc_elem_heats(const orc_eqp *p, const double xl[12], const double *al,
   }
 }
 
+/* LELAS3D, F/LELAS.f:130-238, one tet4 element, per Gauss point as the
+   reference: lambda = E nu/(1+nu)/(1-2nu), mu = E/2/(1+nu), lDm = lambda/mu,
+   T1 = af beta dt^2, amd = am/T1 rho, wl = w T1 mu; ud = -f + sum N al,
+   ed = symmetric gradient of dl (Voigt, engineering shear), S = lambda tr I
+   + 2 mu eps (pS0 = 0, Bf = 0); lR(:,a) += w (rho N_a ud + Nx_a . S);
+   lK(rc,a,b) += wl (d_rc (amd N_a N_b / mu + Nx_a.Nx_b) + lDm Nx(r,a) Nx(c,b)
+   + Nx(c,a) Nx(r,b)). */
+void orc_elem_lelas(const orc_eqp *p, const double xl[12], const double *al,
+                    const double *dl, double lR[12], double lK[144]) {
+  double w4[4], N4[4][4], Nx[3][4], Jac;
+  tet4_gauss(w4, N4);
+  gnn3(xl, Nx, &Jac);
+  for (int k = 0; k < 12; k++) lR[k] = 0.0;
+  for (int k = 0; k < 144; k++) lK[k] = 0.0;
+  const int dof = 3, tD = p->tDof;
+  const int i = p->s, j = i + 1, k = j + 1;
+  const double rho = p->rho, elM = p->elM, nu = p->nu;
+  const double lambda = elM * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+  const double mu = elM * 0.5 / (1.0 + nu);
+  const double lDm = lambda / mu;
+  const double T1 = p->af * p->beta * p->dt * p->dt;
+  const double amd = p->am / T1 * rho;
+  for (int g = 0; g < 4; g++) {
+    const double w = w4[g] * Jac;
+    const double *N = N4[g];
+    const double wl = w * T1 * mu;
+    double ed[6] = {0, 0, 0, 0, 0, 0};
+    double ud[3] = {-p->fb[0], -p->fb[1], -p->fb[2]};
+    for (int a = 0; a < 4; a++) {
+      ud[0] = ud[0] + N[a] * al[a * tD + i];
+      ud[1] = ud[1] + N[a] * al[a * tD + j];
+      ud[2] = ud[2] + N[a] * al[a * tD + k];
+      ed[0] = ed[0] + Nx[0][a] * dl[a * tD + i];
+      ed[1] = ed[1] + Nx[1][a] * dl[a * tD + j];
+      ed[2] = ed[2] + Nx[2][a] * dl[a * tD + k];
+      ed[3] = ed[3] + Nx[1][a] * dl[a * tD + i] + Nx[0][a] * dl[a * tD + j];
+      ed[4] = ed[4] + Nx[2][a] * dl[a * tD + j] + Nx[1][a] * dl[a * tD + k];
+      ed[5] = ed[5] + Nx[0][a] * dl[a * tD + k] + Nx[2][a] * dl[a * tD + i];
+    }
+    const double divD = lambda * (ed[0] + ed[1] + ed[2]);
+    double S[6];
+    S[0] = divD + 2.0 * mu * ed[0];
+    S[1] = divD + 2.0 * mu * ed[1];
+    S[2] = divD + 2.0 * mu * ed[2];
+    S[3] = mu * ed[3];
+    S[4] = mu * ed[4];
+    S[5] = mu * ed[5];
+    for (int a = 0; a < 4; a++) {
+      lR[a * dof + 0] += w * (rho * N[a] * ud[0] + Nx[0][a] * S[0] + Nx[1][a] * S[3] + Nx[2][a] * S[5]);
+      lR[a * dof + 1] += w * (rho * N[a] * ud[1] + Nx[0][a] * S[3] + Nx[1][a] * S[1] + Nx[2][a] * S[4]);
+      lR[a * dof + 2] += w * (rho * N[a] * ud[2] + Nx[0][a] * S[5] + Nx[1][a] * S[4] + Nx[2][a] * S[2]);
+      for (int b = 0; b < 4; b++) {
+        const double NxdNx = Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b];
+        const double T = amd * N[a] * N[b] / mu + NxdNx;
+        double *K = lK + (size_t)(a * 4 + b) * 9;
+        for (int r = 0; r < 3; r++)
+          for (int c = 0; c < 3; c++) {
+            double v = lDm * Nx[r][a] * Nx[c][b] + Nx[c][a] * Nx[r][b];
+            if (r == c) v = T + (1.0 + lDm) * Nx[r][a] * Nx[r][b];
+            K[r * 3 + c] += wl * v;
+          }
+      }
+    }
+  }
+}
+
 /* CEP3D, F/CEP.f:136-266, isotropic D = Diso I (no fibres, no
    electromechanical coupling), one tet4 element. */
 void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12], const double *al,
@@ -681,6 +747,10 @@ int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
       double lR[16], lK[256];
       orc_elem_fluid(p, xl, al, yl, lR, lK);
       orc_doassem(4, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+    } else if (p->phys == 5) {
+      double lR[12], lK[144];
+      orc_elem_lelas(p, xl, al, dl, lR, lK);
+      orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
     } else {
       return -2;
     }
@@ -729,6 +799,10 @@ int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
         double lR[4], lK[16];
         orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso, xl, al, yl, lR, lK);
         orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+      } else if (p->phys == 5) {
+        double lR[12], lK[144];
+        orc_elem_lelas(p, xl, al, dl, lR, lK);
+        orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
       }
     }
   }
@@ -808,7 +882,7 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
   const int nNo = eq->nNo, tD = eq->p.tDof, dof = eq->p.dof;
   const size_t nS = (size_t)nNo * tD;
   const double dt = eq->p.dt, gam = eq->p.gam, beta = eq->p.beta;
-  const int dFlag = (eq->p.phys == 2);
+  const int dFlag = (eq->p.phys == 2 || eq->p.phys == 5);
   memset(info, 0, sizeof(*info));
   eq->time += dt;
   /* CEP: reaction step (CEPINTEG, F/CEPION.f:166-314, called from PICP):

@@ -18,7 +18,7 @@ LS_TYPE_CG, LS_TYPE_GMRES, LS_TYPE_NS, LS_TYPE_BICGS = 798, 797, 796, 795
 PRECOND_FSILS, PRECOND_RCS = 701, 709
 BC_TYPE_DIR, BC_TYPE_NEU = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-PHYS_HEATS, PHYS_STRUCT, PHYS_CEP, PHYS_FLUID = 1, 2, 3, 4
+PHYS_HEATS, PHYS_STRUCT, PHYS_CEP, PHYS_FLUID, PHYS_LELAS = 1, 2, 3, 4, 5
 
 
 class SubLs(C.Structure):
@@ -41,7 +41,7 @@ class EqParams(C.Structure):
                 ("C10", C.c_double), ("Kpen", C.c_double), ("visc", C.c_double),
                 ("dmp", C.c_double), ("fb", C.c_double * 3), ("Diso", C.c_double),
                 ("mu_f", C.c_double), ("ctM", C.c_double), ("ctC", C.c_double),
-                ("eparam", c_double_p)]
+                ("eparam", c_double_p), ("elM", C.c_double), ("nu", C.c_double)]
 
 
 class EqSolver(C.Structure):

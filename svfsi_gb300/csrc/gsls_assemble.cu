@@ -80,6 +80,7 @@ struct AsmArgs {
   double C10, Kpen, visc, dmp;
   double fb[3];
   double mu_f, ctM, ctC;
+  double lam_le, mu_le;  // LELAS Lame parameters
   const int4 *ien;
   const int4 *map;  // 4 int4 per element: map[e*4 + a] = (b0..b3)
   const double *x;
@@ -196,6 +197,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
 }  // namespace gsls
 
 #include "gsls_asm_fluid.cuh"
+#include "gsls_asm_lelas.cuh"
 
 namespace gsls {
 
@@ -236,6 +238,11 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   A.mu_f = p->mu_f;
   A.ctM = p->ctM;
   A.ctC = p->ctC;
+  if (p->phys == GSLS_PHYS_LELAS) {
+    // F/LELAS.f:166-167
+    A.lam_le = p->elM * p->nu / (1.0 + p->nu) / (1.0 - 2.0 * p->nu);
+    A.mu_le = p->elM * 0.5 / (1.0 + p->nu);
+  }
   A.ien = m->d_ien.as<int4>();
   A.map = m->d_map.as<int4>();
   A.x = m->d_x.as<double>();
@@ -272,6 +279,14 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
         k_asm_fluid<float><<<nb, kAsmThreads, 0, st>>>(A);
       else
         k_asm_fluid<double><<<nb, kAsmThreads, 0, st>>>(A);
+    } else if (p->phys == GSLS_PHYS_LELAS) {
+      if (dof != 3 || p->s + 3 > p->tDof || !Dg || !(p->elM > 0.0) || !(p->nu > -1.0) ||
+          !(p->nu < 0.5) || !(p->dt > 0.0))
+        return GSLS_ERR_ARG;
+      if (mixed)
+        k_asm_lelas<float><<<nb, kAsmThreads, 0, st>>>(A);
+      else
+        k_asm_lelas<double><<<nb, kAsmThreads, 0, st>>>(A);
     } else {
       set_error("assembly: physics not built in this version of the library");
       return GSLS_ERR_UNSUPPORTED;

@@ -225,7 +225,7 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
   eq->sv = *sv;
   if (eq->sv.maxItr <= 0) eq->sv.maxItr = 5;
   if (eq->sv.minItr <= 0) eq->sv.minItr = 1;
-  eq->dFlag = (p->phys == GSLS_PHYS_STRUCT);
+  eq->dFlag = (p->phys == GSLS_PHYS_STRUCT || p->phys == GSLS_PHYS_LELAS);
   eq->nNo = eq->lhs->nNo;
   eq->nnz = eq->lhs->nnz;
   int rc = gsls_ls_create(&eq->ls, sv->LS_type, sv->ls_relTol > 0 ? &sv->ls_relTol : nullptr,

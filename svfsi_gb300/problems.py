@@ -11,6 +11,9 @@ conventions.  The workloads follow the five benchmark configurations:
 * ``fluid_cylinder`` -- VMS incompressible Navier-Stokes in a cylinder
                       (R 0.5, L 5; ~1.2M tets, ~0.2M nodes at full size).
 * ``cep_slab``     -- Aliev-Panfilov monodomain on a 10x10x2 slab.
+
+and, on the same boundary, ``lelas_beam`` -- linear elastodynamics of the
+struct beam.
 """
 from __future__ import annotations
 
@@ -19,7 +22,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import meshgen
-from ._lib import (LS_TYPE_CG, LS_TYPE_NS, PHYS_CEP, PHYS_FLUID, PHYS_HEATS, PHYS_STRUCT, PREC_FP64,
+from ._lib import (LS_TYPE_CG, LS_TYPE_NS, PHYS_CEP, PHYS_FLUID, PHYS_HEATS, PHYS_LELAS, PHYS_STRUCT, PREC_FP64,
                    PRECOND_FSILS, PRECOND_RCS, EqParams, EqSolver)
 
 SEED = 20261203
@@ -124,7 +127,7 @@ class Problem:
         nnz, nNo, d = self.nnz, self.nNo, self.dof
         B_spmv = nnz * (d * d * s_A + 4) + 8 * nNo + 2 * nNo * d * s_v
         B_cg = nnz * (d * d * s_A + 4) + 8 * nNo + 11 * nNo * d * s_v
-        fields = 3 if self.phys == PHYS_STRUCT else 2
+        fields = 3 if self.phys in (PHYS_STRUCT, PHYS_LELAS) else 2
         B_asm = 16 * self.nEl + 24 * nNo + fields * nNo * self.tDof * 8 + nnz * d * d * s_A + 8 * nNo * d
         return {"spmv": B_spmv, "cg_iter": B_cg, "assembly": B_asm}
 
@@ -166,6 +169,27 @@ def struct_beam(nx: int = 176, ny: int = 44, nz: int = 44, nsteps: int = 10,
                    dirichlet=[DirBC(clamp, 0.0)], traction=[TracBC(tface, tuple(traction))],
                    LS_type=LS_TYPE_CG, prec=PRECOND_FSILS, minItr=1, maxItr=10, tol=1e-8,
                    nsteps=nsteps, eparam=eparam)
+
+
+def lelas_beam(nx: int = 176, ny: int = 44, nz: int = 44, nsteps: int = 10,
+               E: float = 1e6, nu: float = 0.45, traction=(0.0, 0.0, -1e3),
+               f=(0.0, 0.0, 0.0)) -> Problem:
+    """Linear elasticity (LELAS3D) on the struct beam: E=1e6, nu=0.45,
+    rho=1, domain force f, x=0 clamped, constant traction on x=4 (BLELAS),
+    dt=1e-3, second-order generalized-alpha with rho_inf 0.2, CG + diagonal
+    preconditioner (the reference's default for lElas)."""
+    x, ien = meshgen.kuhn_box(nx, ny, nz, 4.0, 1.0, 1.0)
+    rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
+    am, af, beta, gam = genalpha(0.2, second_order=True)
+    params = dict(am=am, af=af, beta=beta, gam=gam, dt=1e-3, rho=1.0, elM=E, nu=nu,
+                  fb=tuple(f))
+    clamp = meshgen.nodes_on_plane(x, 0, 0.0)
+    tface = meshgen.faces_on_plane(x, ien, 0, 4.0)
+    return Problem(name=f"lelas_beam_{nx}x{ny}x{nz}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
+                   phys=PHYS_LELAS, dof=3, tDof=3, params=params,
+                   dirichlet=[DirBC(clamp, 0.0)], traction=[TracBC(tface, tuple(traction))],
+                   LS_type=LS_TYPE_CG, prec=PRECOND_FSILS, minItr=1, maxItr=10, tol=1e-8,
+                   nsteps=nsteps)
 
 
 def cep_slab(nx: int = 135, ny: int = 135, nz: int = 27, nsteps: int = 5000,

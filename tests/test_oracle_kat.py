@@ -479,3 +479,61 @@ def test_coupled_neumann_face_adds_rank_one_term(orc):
     x0 = np.zeros(n)
     x0[free] = np.linalg.solve(K[np.ix_(free, free)], R[free, 0])
     assert np.abs(x0 - x).max() > 1e-2 * np.abs(x).max()
+
+
+def _lelas_K(p, Val):
+    n = p.nNo
+    K = np.zeros((3 * n, 3 * n))
+    for i in range(n):
+        for j in range(p.rowPtr[i], p.rowPtr[i + 1]):
+            c = p.colPtr[j]
+            K[3 * i:3 * i + 3, 3 * c:3 * c + 3] = Val[j].reshape(3, 3)
+    return K
+
+
+def test_lelas_patch_test_and_uniaxial_stress(orc):
+    """LELAS3D: an affine displacement (constant strain) at rest leaves no
+    residual at interior nodes, and on a boundary face the residual is the
+    traction of the Hooke stress sigma = lambda tr(eps) I + 2 mu eps."""
+    p = problems.lelas_beam(4, 2, 2)
+    E, nu = p.params["elM"], p.params["nu"]
+    lam = E * nu / (1 + nu) / (1 - 2 * nu)
+    mu = E / (2 * (1 + nu))
+    G = np.array([[1e-3, 2e-4, 0.0], [0.0, -3e-4, 5e-4], [1e-4, 0.0, 2e-4]])
+    D = p.x @ G.T
+    A = np.zeros_like(D)
+    R, Val = orc.assemble(p, A, np.zeros_like(D), D)
+    lo, hi = p.x.min(0), p.x.max(0)
+    interior = np.all((p.x > lo + 1e-12) & (p.x < hi - 1e-12), axis=1)
+    scale = np.abs(R).max()
+    assert scale > 0
+    assert np.abs(R[interior]).max() < 1e-12 * scale
+    # total force on the x = 4 face nodes = (sigma . n) * area (n = +x, area 1)
+    eps = 0.5 * (G + G.T)
+    sig = lam * np.trace(eps) * np.eye(3) + 2 * mu * eps
+    right = np.isclose(p.x[:, 0], hi[0])
+    assert np.allclose(R[right].sum(0), sig[:, 0] * 1.0, rtol=1e-12, atol=1e-12 * scale)
+    # the tangent is symmetric
+    K = _lelas_K(p, Val)
+    assert np.allclose(K, K.T, rtol=0, atol=1e-12 * np.abs(K).max())
+
+
+def test_lelas_tangent_is_residual_derivative(orc):
+    """The LELAS tangent is dR/dA through the gen-alpha chain; the problem is
+    linear, so one difference is exact up to rounding."""
+    p = problems.lelas_beam(3, 1, 1, f=(0.5, -1.0, 2.0))
+    rng = np.random.default_rng(6)
+    A0 = rng.standard_normal((p.nNo, 3))
+    D0 = 1e-3 * rng.standard_normal((p.nNo, 3))
+    prm = p.params
+    am, af, beta, dt = prm["am"], prm["af"], prm["beta"], prm["dt"]
+    R0, Val = orc.assemble(p, A0, np.zeros_like(A0), D0)
+    dA = rng.standard_normal((p.nNo, 3))
+    R1 = orc.assemble(p, A0 + am * dA, np.zeros_like(A0), D0 + af * beta * dt * dt * dA)[0]
+    K = _lelas_K(p, Val)
+    pred = K @ dA.ravel()
+    assert np.allclose((R1 - R0).ravel(), pred, rtol=1e-9, atol=1e-10 * np.abs(pred).max())
+    # the body force enters as -rho f per unit volume: at rest and undeformed
+    # the residual sums to -rho f V (V = 4)
+    Rf = orc.assemble(p, np.zeros_like(A0), np.zeros_like(A0), np.zeros_like(A0))[0]
+    assert np.allclose(Rf.sum(0), -4.0 * np.array([0.5, -1.0, 2.0]), rtol=1e-12)
