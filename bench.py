@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--only", choices=["all", "mixed", "fp64"], default="all",
                     help="time one precision only (profiling runs)")
-    ap.add_argument("--workload", choices=["struct", "fluid", "cep", "lelas", "adjoint"],
+    ap.add_argument("--workload", choices=["struct", "fluid", "cep", "lelas", "heatf", "adjoint"],
                     default="struct")
     ap.add_argument("--fd-dirs", type=int, default=4,
                     help="adjoint workload: random directions of the central-FD check")
@@ -94,6 +94,8 @@ def workload(args):
         if args.small:
             return problems.cep_slab(27, 27, 6, nsteps=args.steps, A=52.0)
         return problems.cep_slab(nsteps=args.steps, A=52.0)
+    if args.workload == "heatf":
+        return problems.heatf_cylinder(h=0.08 if args.small else args.fluid_h, nsteps=args.steps)
     if args.workload == "lelas":
         if args.small:
             return problems.lelas_beam(24, 6, 6, nsteps=args.steps)
@@ -107,11 +109,39 @@ def is_fluid(p):
     return p.dof == 4
 
 
+def is_heatf(p):
+    from svfsi_gb300 import problems
+    return p.phys == problems.PHYS_HEATF
+
+
+def compared_field(p, state):
+    """The unknown compared between the mixed and FP64 runs: D (solids),
+    Y (fluid, CEP) or the temperature column of Y (HEATF)."""
+    if is_heatf(p):
+        return state[1][:, p.s]
+    return state[1] if (is_fluid(p) or is_cep(p)) else state[2]
+
+
 def is_cep(p):
     return bool(getattr(p, "cep", None))
 
 
+def l2_note(p):
+    """What keeps the timed steps from running out of a warm L2 (129 MB)."""
+    v32, v64 = p.nnz * p.dof ** 2 * 4 / 1e6, p.nnz * p.dof ** 2 * 8 / 1e6
+    if v32 > 129.0:
+        return f"inputs larger than L2 (FP32 Val {v32:.0f} MB, FP64 Val {v64:.0f} MB)"
+    per_el = (13 * 8 + 64 + 16) * p.nEl / 1e6  # geometry table, element->CSR map, IEN
+    return (f"per-step working set larger than L2: every assembly streams the element geometry, "
+            f"element->CSR map and IEN ({per_el:.0f} MB) and the state; FP32 Val {v32:.0f} MB")
+
+
 def workload_desc(p):
+    if is_heatf(p):
+        return (f"{p.name}: heat carried by a prescribed Poiseuille flow (HEATF3D, peak 30, "
+                f"conductivity 0.1, T = 1 on the inlet), {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
+                f"{p.nnz:,}, GMRES+diag, dt 1e-3, {p.maxItr} Newton iterations per step (the "
+                f"discontinuity-capturing fixed point converges linearly)")
     if is_cep(p):
         return (f"{p.name}: monodomain Aliev-Panfilov (FE reaction step), Diso 0.1, stimulus "
                 f"+52 for 2 ms on the 1x1x2 corner block, {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
@@ -255,8 +285,8 @@ def run_gsls(args):
         if profile:
             L.gsls_profile_enable(0)
             cnt, tot = C.c_longlong(), C.c_double()
-            L.gsls_profile_read(b"gm_spmv_d3" if is_fluid(p) else b"cg_spmv", C.byref(cnt),
-                                C.byref(tot))
+            key = b"gm_spmv_d3" if is_fluid(p) else b"gm_spmv" if is_heatf(p) else b"cg_spmv"
+            L.gsls_profile_read(key, C.byref(cnt), C.byref(tot))
             acnt, atot = C.c_longlong(), C.c_double()
             L.gsls_profile_read(b"assembly", C.byref(acnt), C.byref(atot))
             prof = {"cg_spmv": (cnt.value, tot.value), "assembly": (acnt.value, atot.value)}
@@ -290,8 +320,7 @@ def run_gsls(args):
     profd = timed_run(fsils.PREC_MIXED, profile=True, nsteps=2, nwarm=1)
     ms_mixed = max_over_ranks(mixed["ms"]) / K
     ms_fp64 = max_over_ranks(fp64["ms"]) / K
-    sidx = 1 if (is_fluid(p) or is_cep(p)) else 2  # compare Y (fluid, CEP) or D (struct)
-    D_m, D_f = mixed["state"][sidx], fp64["state"][sidx]
+    D_m, D_f = compared_field(p, mixed["state"]), compared_field(p, fp64["state"])
     rel_l2 = float(np.linalg.norm(D_m - D_f) / np.linalg.norm(D_f))
 
     # e2e through the public API with host buffers (pinned), H2D + D2H per step
@@ -328,6 +357,10 @@ def run_gsls(args):
         B = p.nnz * (9 * 4 + 4) + 8 * p.nNo + 2 * p.nNo * 3 * 4
         kname = "k_gm_spmv<3,float,float> (block-CSR SpMV on the K block of the NS solver)"
         tkey = "gm_spmv_d3_f32_fluid_cylinder"
+    elif is_heatf(p):
+        B = p.algorithmic_bytes(4, 4)["spmv"]
+        kname = "k_gm_spmv<1,float,float> (CSR SpMV of the GMRES Arnoldi step)"
+        tkey = f"gm_spmv_d1_f32_{p.name}"
     elif is_cep(p):
         B = p.algorithmic_bytes(4, 4)["spmv"]
         kname = "k_cg_spmv<1,float,float> (CSR SpMV + fused P.KP)"
@@ -351,12 +384,12 @@ def run_gsls(args):
         "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": ms_mixed,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 tangent+inner CG / f64 residual,Newton,reductions",
-        "data": ("synthetic: seeded Delaunay cylinder mesh, no external data" if is_fluid(p)
+        "data": ("synthetic: seeded Delaunay cylinder mesh, no external data"
+                 if (is_fluid(p) or is_heatf(p))
                  else "synthetic: Kuhn-split slab mesh, no external data" if is_cep(p)
                  else "synthetic: seeded Kuhn-split beam mesh, no external data"),
         "config": {"workload": workload_desc(p), "precision": "mixed",
-                   "l2": (f"inputs larger than L2 (FP32 Val {p.nnz * p.dof ** 2 * 4 / 1e6:.0f} MB, "
-                          f"FP64 Val {p.nnz * p.dof ** 2 * 8 / 1e6:.0f} MB)"),
+                   "l2": l2_note(p),
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "fp64": {"value": ms_fp64 / 1e3 / world, "ms_per_step": ms_fp64,
                  "newton_itr_per_step": fp64["newton"], "cg_itr_per_step": fp64["cg"],
@@ -364,7 +397,8 @@ def run_gsls(args):
         "mixed": {"newton_itr_per_step": mixed["newton"], "cg_itr_per_step": mixed["cg"],
                   "assembly_ms_per_newton": mixed["asm_ms"] / max(mixed["newton"], 1),
                   "all_solves_converged": bool(mixed["suc"])},
-        "ls_itr_note": ("NS outer iterations per step" if is_fluid(p) else "CG iterations per step"),
+        "ls_itr_note": ("NS outer iterations per step" if is_fluid(p)
+                        else "GMRES iterations per step" if is_heatf(p) else "CG iterations per step"),
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "rel_l2_mixed_vs_fp64": rel_l2,
         "roofline": roof,
@@ -400,7 +434,8 @@ def _colouring(p):
 
 def cpu_sample(p, threads):
     """Time, on the host cores with the oracle: one assembly, one diagonal
-    preconditioning and CG iterations (slope between 5 and 25 iterations)."""
+    preconditioning and Krylov iterations of the workload's solver (CG, or
+    GMRES Arnoldi steps; slope between 5 and 25 iterations)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     L = O.load()
@@ -411,11 +446,14 @@ def cpu_sample(p, threads):
     O.set_threads(threads)
     ncol, off, order = _colouring(p)
     rng = np.random.default_rng(0)
-    A = 1e-3 * rng.standard_normal((p.nNo, 3))
-    Y = 1e-3 * rng.standard_normal((p.nNo, 3))
-    D = 1e-3 * rng.standard_normal((p.nNo, 3))
-    R = np.zeros((p.nNo, 3))
-    Val = np.zeros((p.nnz, 9))
+    d, tD = p.dof, p.tDof
+    A = 1e-3 * rng.standard_normal((p.nNo, tD))
+    Y = 1e-3 * rng.standard_normal((p.nNo, tD))
+    if p.Y0 is not None:
+        Y += p.Y0
+    D = 1e-3 * rng.standard_normal((p.nNo, tD))
+    R = np.zeros((p.nNo, d))
+    Val = np.zeros((p.nnz, d * d))
     eqp = O.eqp_from(p)
     ien, x, rp, cp = O.i32(p.ien), O.f64(p.x), O.i32(p.rowPtr), O.i32(p.colPtr)
     t0 = time.perf_counter()
@@ -425,12 +463,14 @@ def cpu_sample(p, threads):
     t_asm = time.perf_counter() - t0
     s = O.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
     s.bc_create(1, p.dirichlet[0].nodes, 3, 0, np.zeros((p.dirichlet[0].nodes.size, 3)))
+    gm = p.LS_type == O.LS_TYPE_GMRES
     times = {}
     for m in (5, 25):
-        ls = O.ls_create(O.LS_TYPE_CG, relTol=1e-30, mItr=m)
+        ls = (O.ls_create(O.LS_TYPE_GMRES, relTol=1e-30, mItr=1, sD=m) if gm else
+              O.ls_create(O.LS_TYPE_CG, relTol=1e-30, mItr=m))
         Rc, Vc = R.copy(), Val.copy()
         t0 = time.perf_counter()
-        s.solve(ls, 3, Rc, Vc, O.PRECOND_FSILS)
+        s.solve(ls, d, Rc, Vc, O.PRECOND_FSILS)
         times[m] = time.perf_counter() - t0
     t_it = (times[25] - times[5]) / 20.0
     t_pre = max(times[5] - 5 * t_it, 0.0)
@@ -441,11 +481,13 @@ def cpu_baseline(p, newton, cg):
     threads = os.cpu_count() or 1
     t_asm, t_pre, t_it = cpu_sample(p, threads)
     per_step = newton * (t_asm + t_pre) + cg * t_it
+    kry = "GMRES" if is_heatf(p) else "CG"
     return {"value": per_step, "unit": "s/step", "cores": threads, "kind": "port",
             "sample": (f"oracle (C restatement, FP64, OpenMP {threads} threads) on the full mesh: "
-                       f"1 assembly {t_asm:.3f}s, 1 diag precond {t_pre:.3f}s, CG {t_it * 1e3:.2f} "
-                       f"ms/iter (5->25 iter slope); per step = {newton:.2f} Newton x (asm+precond) "
-                       f"+ {cg:.1f} CG iters, the counts of the FP64 GPU run of the same algorithm")}
+                       f"1 assembly {t_asm:.3f}s, 1 diag precond {t_pre:.3f}s, {kry} "
+                       f"{t_it * 1e3:.2f} ms/iter (5->25 iter slope); per step = {newton:.2f} Newton "
+                       f"x (asm+precond) + {cg:.1f} {kry} iters, the counts of the FP64 GPU run of "
+                       f"the same algorithm")}
 
 
 def cpu_sample_fluid(p, threads):

@@ -59,6 +59,8 @@ extern "C" {
 #define GSLS_PHYS_CEP 3
 #define GSLS_PHYS_FLUID 4
 #define GSLS_PHYS_LELAS 5  /* linear elasticity, Code/Source/svFSI/LELAS.f */
+#define GSLS_PHYS_HEATF 6  /* heat in a fluid (advection-diffusion), HEATF.f;
+                              velocity in state components 0..2 */
 
 /* Mirrors FSILS_subLsType, Code/Source/svFSILS/FSILS_STRUCT.h:162-191
    (Fortran LOGICAL stored as int32). */

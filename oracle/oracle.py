@@ -160,7 +160,7 @@ def lhsa(nNo, ien):
 
 def eqp_from(problem, eparam=None) -> EqP:
     p = EqP()
-    p.phys, p.dof, p.tDof, p.s = problem.phys, problem.dof, problem.tDof, 0
+    p.phys, p.dof, p.tDof, p.s = problem.phys, problem.dof, problem.tDof, getattr(problem, "s", 0)
     for k, v in problem.params.items():
         if k == "fb":
             for i in range(3):

@@ -115,7 +115,7 @@ void orc_doassem(int dof, int eNoN, const int *ptr, const double *lK,
 
 /* Equation parameters for one assembly call (one domain, constant props). */
 typedef struct {
-  int phys;      /* 1 HEATS, 2 STRUCT, 3 CEP, 4 FLUID, 5 LELAS */
+  int phys;      /* 1 HEATS, 2 STRUCT, 3 CEP, 4 FLUID, 5 LELAS, 6 HEATF */
   int dof, tDof, s; /* eq dof, total dof, 0-based start of this eq in tDof */
   double am, af, beta, gam, dt;
   double rho, cond, src;       /* HEATS: solid_density, conductivity, source */
@@ -145,6 +145,10 @@ void orc_elem_heats(const orc_eqp *p, const double xl[12], const double *al,
    tet4 element: lR(3,4), lK(9,4,4) */
 void orc_elem_lelas(const orc_eqp *p, const double xl[12], const double *al,
                     const double *dl, double lR[12], double lK[144]);
+/* HEATF3D, F/HEATF.f:116-205 (no mesh motion): velocity in state
+   components 0..2, temperature in component s; lR(1,4), lK(1,4,4) */
+void orc_elem_heatf(const orc_eqp *p, const double xl[12], const double *al,
+                    const double *yl, double lR[4], double lK[16]);
 void orc_elem_struct(const orc_eqp *p, double mu_e, const double xl[12],
                      const double *al, const double *yl, const double *dl,
                      double lR[12], double lK[144]);

@@ -429,6 +429,70 @@ void orc_elem_lelas(const orc_eqp *p, const double xl[12], const double *al,
   }
 }
 
+/* HEATF3D, F/HEATF.f:116-205 (no mesh motion), one tet4 element per
+   Gauss point as the reference: advection-diffusion of component s with the
+   velocity in components 0..2 of the state, SUPG-type stabilisation tauM =
+   ct4/sqrt(ct1/dt^2 + ct2 u.ks.u + ct3 nu^2 ks:ks), ct = (4, 1, 3, 1), and
+   the discontinuity-capturing diffusivity nu + |Td + u.Tx| / (2 sqrt(Tx.ks.Tx))
+   (ISZERO(Tx.ks.Tx) -> eps).  lR(1,4), lK(1,4,4). */
+void orc_elem_heatf(const orc_eqp *p, const double xl[12], const double *al,
+                    const double *yl, double lR[4], double lK[16]) {
+  static const double ct[4] = {4.0, 1.0, 3.0, 1.0};
+  const double eps = 2.220446049250313e-16;
+  double w4[4], N4[4][4], Nx[3][4], Jac, ks[3][3];
+  tet4_gauss(w4, N4);
+  gnn3k(xl, Nx, &Jac, ks);
+  for (int a = 0; a < 4; a++) lR[a] = 0.0;
+  for (int k = 0; k < 16; k++) lK[k] = 0.0;
+  const int i = p->s, tD = p->tDof;
+  const double dt = p->dt;
+  const double T1 = p->af * p->gam * dt;
+  const double amd = p->am / T1;
+  const double s = p->src;
+  for (int g = 0; g < 4; g++) {
+    const double w = w4[g] * Jac;
+    const double *N = N4[g];
+    const double wl = w * T1;
+    double nu = p->cond;
+    double u[3] = {0, 0, 0}, Tx[3] = {0, 0, 0}, Td = -s;
+    for (int a = 0; a < 4; a++) {
+      u[0] = u[0] + N[a] * yl[a * tD + 0];
+      u[1] = u[1] + N[a] * yl[a * tD + 1];
+      u[2] = u[2] + N[a] * yl[a * tD + 2];
+      Td = Td + N[a] * al[a * tD + i];
+      Tx[0] = Tx[0] + Nx[0][a] * yl[a * tD + i];
+      Tx[1] = Tx[1] + Nx[1][a] * yl[a * tD + i];
+      Tx[2] = Tx[2] + Nx[2][a] * yl[a * tD + i];
+    }
+    const double kU = u[0] * u[0] * ks[0][0] + u[1] * u[0] * ks[1][0] + u[2] * u[0] * ks[2][0] +
+                      u[0] * u[1] * ks[0][1] + u[1] * u[1] * ks[1][1] + u[2] * u[1] * ks[2][1] +
+                      u[0] * u[2] * ks[0][2] + u[1] * u[2] * ks[1][2] + u[2] * u[2] * ks[2][2];
+    const double kS = ks[0][0] * ks[0][0] + ks[1][0] * ks[1][0] + ks[2][0] * ks[2][0] +
+                      ks[0][1] * ks[0][1] + ks[1][1] * ks[1][1] + ks[2][1] * ks[2][1] +
+                      ks[0][2] * ks[0][2] + ks[1][2] * ks[1][2] + ks[2][2] * ks[2][2];
+    double nTx = ks[0][0] * Tx[0] * Tx[0] + ks[1][1] * Tx[1] * Tx[1] + ks[2][2] * Tx[2] * Tx[2] +
+                 (ks[0][1] + ks[1][0]) * Tx[0] * Tx[1] + (ks[0][2] + ks[2][0]) * Tx[0] * Tx[2] +
+                 (ks[1][2] + ks[2][1]) * Tx[1] * Tx[2];
+    if (iszero(nTx)) nTx = eps;
+    const double udTx = u[0] * Tx[0] + u[1] * Tx[1] + u[2] * Tx[2];
+    double Tp = fabs(Td + udTx);
+    nu = nu + 0.5 * Tp / sqrt(nTx);
+    const double tauM = ct[3] / sqrt((ct[0] / (dt * dt)) + ct[1] * kU + ct[2] * nu * nu * kS);
+    Tp = -tauM * (Td + udTx);
+    double udNx[4];
+    for (int a = 0; a < 4; a++) udNx[a] = u[0] * Nx[0][a] + u[1] * Nx[1][a] + u[2] * Nx[2][a];
+    for (int a = 0; a < 4; a++) {
+      lR[a] = lR[a] + w * (N[a] * (Td + udTx) +
+                           (Nx[0][a] * Tx[0] + Nx[1][a] * Tx[1] + Nx[2][a] * Tx[2]) * nu -
+                           udNx[a] * Tp);
+      for (int b = 0; b < 4; b++)
+        lK[a * 4 + b] = lK[a * 4 + b] +
+                        wl * (nu * (Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b]) +
+                              (N[a] + tauM * udNx[a]) * (N[b] * amd + udNx[b]));
+    }
+  }
+}
+
 /* CEP3D, F/CEP.f:136-266, isotropic D = Diso I (no fibres, no
    electromechanical coupling), one tet4 element. */
 void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12], const double *al,
@@ -751,6 +815,10 @@ int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
       double lR[12], lK[144];
       orc_elem_lelas(p, xl, al, dl, lR, lK);
       orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+    } else if (p->phys == 6) {
+      double lR[4], lK[16];
+      orc_elem_heatf(p, xl, al, yl, lR, lK);
+      orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
     } else {
       return -2;
     }
@@ -803,6 +871,10 @@ int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
         double lR[12], lK[144];
         orc_elem_lelas(p, xl, al, dl, lR, lK);
         orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+      } else if (p->phys == 6) {
+        double lR[4], lK[16];
+        orc_elem_heatf(p, xl, al, yl, lR, lK);
+        orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
       }
     }
   }

@@ -18,7 +18,7 @@ LS_TYPE_CG, LS_TYPE_GMRES, LS_TYPE_NS, LS_TYPE_BICGS = 798, 797, 796, 795
 PRECOND_FSILS, PRECOND_RCS = 701, 709
 BC_TYPE_DIR, BC_TYPE_NEU = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-PHYS_HEATS, PHYS_STRUCT, PHYS_CEP, PHYS_FLUID, PHYS_LELAS = 1, 2, 3, 4, 5
+PHYS_HEATS, PHYS_STRUCT, PHYS_CEP, PHYS_FLUID, PHYS_LELAS, PHYS_HEATF = 1, 2, 3, 4, 5, 6
 
 
 class SubLs(C.Structure):

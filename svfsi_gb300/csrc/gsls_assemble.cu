@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
 
 #include "gsls_asm_fluid.cuh"
 #include "gsls_asm_lelas.cuh"
+#include "gsls_asm_heatf.cuh"
 
 namespace gsls {
 
@@ -279,6 +280,13 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
         k_asm_fluid<float><<<nb, kAsmThreads, 0, st>>>(A);
       else
         k_asm_fluid<double><<<nb, kAsmThreads, 0, st>>>(A);
+    } else if (p->phys == GSLS_PHYS_HEATF) {
+      if (dof != 1 || p->tDof < 4 || p->s < 3 || p->s >= p->tDof || !(p->dt > 0.0))
+        return GSLS_ERR_ARG;
+      if (mixed)
+        k_asm_heatf<float><<<nb, kAsmThreads, 0, st>>>(A);
+      else
+        k_asm_heatf<double><<<nb, kAsmThreads, 0, st>>>(A);
     } else if (p->phys == GSLS_PHYS_LELAS) {
       if (dof != 3 || p->s + 3 > p->tDof || !Dg || !(p->elM > 0.0) || !(p->nu > -1.0) ||
           !(p->nu < 0.5) || !(p->dt > 0.0))

@@ -13,7 +13,8 @@ conventions.  The workloads follow the five benchmark configurations:
 * ``cep_slab``     -- Aliev-Panfilov monodomain on a 10x10x2 slab.
 
 and, on the same boundary, ``lelas_beam`` -- linear elastodynamics of the
-struct beam.
+struct beam -- and ``heatf_cylinder`` -- heat carried by a prescribed
+Poiseuille flow in the fluid cylinder.
 """
 from __future__ import annotations
 
@@ -22,7 +23,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import meshgen
-from ._lib import (LS_TYPE_CG, LS_TYPE_NS, PHYS_CEP, PHYS_FLUID, PHYS_HEATS, PHYS_LELAS, PHYS_STRUCT, PREC_FP64,
+from ._lib import (LS_TYPE_CG, LS_TYPE_GMRES, LS_TYPE_NS, PHYS_CEP, PHYS_FLUID, PHYS_HEATF, PHYS_HEATS,
+                   PHYS_LELAS, PHYS_STRUCT, PREC_FP64,
                    PRECOND_FSILS, PRECOND_RCS, EqParams, EqSolver)
 
 SEED = 20261203
@@ -79,6 +81,8 @@ class Problem:
     eparam: np.ndarray | None = None
     cep: dict | None = None         # cell model and stimulus (CEP only)
     stim: np.ndarray | None = None  # per-node stimulus flag (CEP only)
+    s: int = 0                      # first unknown of this equation in the state
+    Y0: np.ndarray | None = None    # initial Y (nNo, tDof), e.g. a prescribed velocity
 
     @property
     def nNo(self):
@@ -94,7 +98,7 @@ class Problem:
 
     def eq_params(self) -> EqParams:
         p = EqParams()
-        p.phys, p.dof, p.tDof, p.s = self.phys, self.dof, self.tDof, 0
+        p.phys, p.dof, p.tDof, p.s = self.phys, self.dof, self.tDof, self.s
         for k, v in self.params.items():
             if k == "fb":
                 for i in range(3):
@@ -116,7 +120,7 @@ class Problem:
 
     def initial_state(self):
         z = np.zeros((self.nNo, self.tDof))
-        Y = z.copy()
+        Y = z.copy() if self.Y0 is None else np.array(self.Y0, dtype=float)
         if self.cep:
             Y[:, 0] = self.cep["V0"]  # resting potential of the cell model
         return z.copy(), Y, z.copy()
@@ -236,6 +240,31 @@ def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float 
                    dirichlet=[DirBC(inlet, -u_max, gx=gx, nV=nV), DirBC(wall, 0.0)],
                    LS_type=LS_TYPE_NS, prec=PRECOND_RCS, ls_relTol=1e-2, ls_sD=100, minItr=1,
                    maxItr=12, tol=1e-10, nsteps=nsteps)
+
+
+def heatf_cylinder(h: float = 0.027, nsteps: int = 10, R: float = 0.5, L: float = 5.0,
+                   u_max: float = 30.0, cond: float = 0.1, dt: float = 1e-3,
+                   T0_linear: bool = False) -> Problem:
+    """Heat transported by a prescribed Poiseuille flow (HEATF3D) in the fluid
+    cylinder: state (u, v, w, p, T) with the velocity u_z = u_max (1 - r^2/R^2)
+    held in components 0..2 and the temperature the equation's unknown
+    (component 4); conductivity 0.1, no source, T = 1 on the inlet, T = 0
+    initially (T0_linear: T = 1 - z/L), insulated wall and open outlet,
+    dt 1e-3, first-order
+    generalized-alpha (rho_inf 0.2), GMRES + diagonal preconditioner (the
+    reference's default for heatF), Newton to 1e-8."""
+    x, ien, info = meshgen.cylinder(R, L, h)
+    rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
+    am, af, beta, gam = genalpha(0.2, second_order=False)
+    params = dict(am=am, af=af, beta=beta, gam=gam, dt=dt, cond=cond, src=0.0)
+    Y0 = np.zeros((x.shape[0], 5))
+    Y0[:, 2] = u_max * np.clip(1.0 - (x[:, 0] ** 2 + x[:, 1] ** 2) / (R * R), 0.0, None)
+    if T0_linear:
+        Y0[:, 4] = 1.0 - x[:, 2] / L
+    return Problem(name=f"heatf_cylinder_h{h:g}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
+                   phys=PHYS_HEATF, dof=1, tDof=5, s=4, params=params,
+                   dirichlet=[DirBC(info["inlet"], 1.0)], LS_type=LS_TYPE_GMRES,
+                   prec=PRECOND_FSILS, minItr=1, maxItr=10, tol=1e-8, nsteps=nsteps, Y0=Y0)
 
 
 def make_lhs_arrays(p: Problem):

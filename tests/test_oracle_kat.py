@@ -537,3 +537,35 @@ def test_lelas_tangent_is_residual_derivative(orc):
     # the residual sums to -rho f V (V = 4)
     Rf = orc.assemble(p, np.zeros_like(A0), np.zeros_like(A0), np.zeros_like(A0))[0]
     assert np.allclose(Rf.sum(0), -4.0 * np.array([0.5, -1.0, 2.0]), rtol=1e-12)
+
+
+def test_heatf_reduces_to_heats_without_flow(orc):
+    """HEATF3D with no velocity, no source and dT/dt = 0 is the heat
+    equation with unit density: the same residual and tangent as HEATS3D."""
+    pf = problems.heatf_cylinder(h=0.2, nsteps=1)
+    rng = np.random.default_rng(3)
+    T = rng.standard_normal(pf.nNo)
+    Y = np.zeros((pf.nNo, 5))
+    Y[:, 4] = T
+    Rf, Vf = orc.assemble(pf, np.zeros_like(Y), Y)
+    ph = problems.heats_cube(2)
+    ph.x, ph.ien, ph.rowPtr, ph.colPtr = pf.x, pf.ien, pf.rowPtr, pf.colPtr
+    ph.params = dict(pf.params, rho=1.0)
+    Rh, Vh = orc.assemble(ph, np.zeros((pf.nNo, 1)), T.reshape(-1, 1))
+    assert np.allclose(Rf, Rh, rtol=1e-13, atol=1e-13 * np.abs(Rh).max())
+    assert np.allclose(Vf, Vh, rtol=1e-13, atol=1e-13 * np.abs(Vh).max())
+
+
+def test_heatf_linear_profile_across_the_flow_is_steady(orc):
+    """A linear temperature T = a.x with a orthogonal to a constant velocity
+    is a steady solution (u.grad T = 0, no diffusion term at interior nodes):
+    the residual vanishes away from the boundary."""
+    p = problems.heatf_cylinder(h=0.15, nsteps=1)
+    Y = np.zeros((p.nNo, 5))
+    Y[:, 2] = 3.0                               # u = (0, 0, 3)
+    Y[:, 4] = 0.7 * p.x[:, 0] - 0.2 * p.x[:, 1]  # grad T = (0.7, -0.2, 0)
+    R, _ = orc.assemble(p, np.zeros_like(Y), Y)
+    r = np.hypot(p.x[:, 0], p.x[:, 1])
+    interior = (r < 0.5 - 1e-9) & (p.x[:, 2] > 1e-9) & (p.x[:, 2] < 5.0 - 1e-9)
+    assert interior.sum() > 10
+    assert np.abs(R[interior]).max() < 1e-12 * np.abs(R).max()
