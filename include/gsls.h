@@ -283,6 +283,22 @@ int gsls_eq_get_cep_state(gsls_eq *eq, double *Xion);
 
 /* Advance one time step. */
 int gsls_eq_step(gsls_eq *eq, gsls_step_info *info);
+
+/* Restart file of one equation in the reference's layout
+   (Code/Source/svFSI/OUTPUT.f:132-232 WRITERESTART, read back as
+   INITIALIZE.f:508-621 INITFROMBIN; record length INITIALIZE.f:152-163),
+   serial form: one direct-access record of
+     stamp(7) = (1, 1, 1, nNo, 0, tDof, dFlag), cTS      int32
+     time, cpu_time, eq%iNorm                           float64
+     Y(tDof,nNo), A(tDof,nNo) [, D(tDof,nNo) if dFlag]  float64
+     [Xion(2,nNo) for CEP]                              float64
+   in native byte order, no record markers.  The state written is the one
+   after the last step (the reference's Yn, An, Dn at WRITERESTART).
+   Reading checks the stamp as INITFROMBIN does (an error names the first
+   field that differs) and restores the state, the simulation time, the
+   Newton normalisation eq%iNorm and the cell state. */
+int gsls_eq_write_restart(gsls_eq *eq, const char *path, int cTS, double cpu_time);
+int gsls_eq_read_restart(gsls_eq *eq, const char *path, int *cTS, double *cpu_time);
 /* Per-element parameter update (host, original element order). */
 int gsls_eq_set_eparam(gsls_eq *eq, const double *eparam);
 

@@ -115,6 +115,8 @@ SIGNATURES = {
     "gsls_eq_step": (C.c_int, [C.c_void_p, C.POINTER(StepInfo)]),
     "gsls_eq_set_cep": (C.c_int, [C.c_void_p, C.POINTER(CepParams), C.c_int, c_int_p]),
     "gsls_eq_get_cep_state": (C.c_int, [C.c_void_p, c_double_p]),
+    "gsls_eq_write_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_double]),
+    "gsls_eq_read_restart": (C.c_int, [C.c_void_p, C.c_char_p, c_int_p, c_double_p]),
     "gsls_eq_set_eparam": (C.c_int, [C.c_void_p, c_double_p]),
     "gsls_adjoint_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "gsls_adjoint_backward": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p,

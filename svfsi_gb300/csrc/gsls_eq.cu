@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -400,6 +401,102 @@ int gsls_eq_set_cep(gsls_eq *eq, const gsls_cep_params *c, int nStim, const int 
   eq->has_cep = true;
   eq->cep_first = true;
   eq->time = 0.0;
+  return GSLS_OK;
+}
+
+static int restart_fields(const gsls_eq *eq, int stamp[7], size_t *nstate) {
+  stamp[0] = 1;                   // processors
+  stamp[1] = 1;                   // equations
+  stamp[2] = 1;                   // meshes
+  stamp[3] = eq->nNo;             // tnNo
+  stamp[4] = 0;                   // cplBC%nX
+  stamp[5] = eq->p.tDof;          // tDof
+  stamp[6] = eq->dFlag ? 1 : 0;   // dFlag
+  *nstate = (size_t)eq->nNo * eq->p.tDof;
+  return GSLS_OK;
+}
+
+int gsls_eq_write_restart(gsls_eq *eq, const char *path, int cTS, double cpu_time) {
+  if (!eq || !path) return GSLS_ERR_ARG;
+  int stamp[7];
+  size_t ns;
+  restart_fields(eq, stamp, &ns);
+  std::vector<double> Y(ns), A(ns), D(eq->dFlag ? ns : 0), X(eq->has_cep ? 2 * (size_t)eq->nNo : 0);
+  cudaStream_t st = eq->lhs->stream;
+  GSLS_CUDA(cudaMemcpyAsync(A.data(), eq->st[0].p, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+  GSLS_CUDA(cudaMemcpyAsync(Y.data(), eq->st[1].p, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+  if (eq->dFlag)
+    GSLS_CUDA(cudaMemcpyAsync(D.data(), eq->st[2].p, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+  if (eq->has_cep)
+    GSLS_CUDA(cudaMemcpyAsync(X.data(), eq->Xion.p, sizeof(double) * X.size(), cudaMemcpyDeviceToHost, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  FILE *f = fopen(path, "wb");
+  if (!f) {
+    set_error("restart: cannot open the file for writing");
+    return GSLS_ERR_ARG;
+  }
+  const double hd[3] = {eq->time, cpu_time, eq->eq_iNorm};
+  bool ok = fwrite(stamp, sizeof(int), 7, f) == 7 && fwrite(&cTS, sizeof(int), 1, f) == 1 &&
+            fwrite(hd, sizeof(double), 3, f) == 3 && fwrite(Y.data(), sizeof(double), ns, f) == ns &&
+            fwrite(A.data(), sizeof(double), ns, f) == ns;
+  if (ok && eq->dFlag) ok = fwrite(D.data(), sizeof(double), ns, f) == ns;
+  if (ok && eq->has_cep) ok = fwrite(X.data(), sizeof(double), X.size(), f) == X.size();
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) {
+    set_error("restart: write failed");
+    return GSLS_ERR_ARG;
+  }
+  return GSLS_OK;
+}
+
+int gsls_eq_read_restart(gsls_eq *eq, const char *path, int *cTS, double *cpu_time) {
+  if (!eq || !path) return GSLS_ERR_ARG;
+  int stamp[7], ts[7], c = 0;
+  size_t ns;
+  restart_fields(eq, stamp, &ns);
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    set_error("restart: cannot open the file");
+    return GSLS_ERR_ARG;
+  }
+  double hd[3];
+  bool ok = fread(ts, sizeof(int), 7, f) == 7 && fread(&c, sizeof(int), 1, f) == 1 &&
+            fread(hd, sizeof(double), 3, f) == 3;
+  static const char *what[7] = {"Number of processors", "Number of equations", "Number of meshes",
+                                "Number of nodes", "Number of cplBC%x", "Number of dof",
+                                "dFlag specification"};
+  for (int k = 0; ok && k < 7; k++)
+    if (ts[k] != stamp[k]) {
+      fclose(f);
+      char msg[160];
+      snprintf(msg, sizeof(msg), "restart: %s <%d> in the file differs from the equation's <%d>",
+               what[k], ts[k], stamp[k]);
+      set_error(msg);
+      return GSLS_ERR_ARG;
+    }
+  std::vector<double> Y(ns), A(ns), D(eq->dFlag ? ns : 0), X(eq->has_cep ? 2 * (size_t)eq->nNo : 0);
+  ok = ok && fread(Y.data(), sizeof(double), ns, f) == ns && fread(A.data(), sizeof(double), ns, f) == ns;
+  if (ok && eq->dFlag) ok = fread(D.data(), sizeof(double), ns, f) == ns;
+  if (ok && eq->has_cep) ok = fread(X.data(), sizeof(double), X.size(), f) == X.size();
+  fclose(f);
+  if (!ok) {
+    set_error("restart: the file is shorter than the equation's record");
+    return GSLS_ERR_ARG;
+  }
+  cudaStream_t st = eq->lhs->stream;
+  GSLS_CUDA(cudaMemcpyAsync(eq->st[0].p, A.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, st));
+  GSLS_CUDA(cudaMemcpyAsync(eq->st[1].p, Y.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, st));
+  if (eq->dFlag)
+    GSLS_CUDA(cudaMemcpyAsync(eq->st[2].p, D.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, st));
+  if (eq->has_cep) {
+    GSLS_CUDA(cudaMemcpyAsync(eq->Xion.p, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, st));
+    eq->cep_first = false;
+  }
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  eq->time = hd[0];
+  eq->eq_iNorm = hd[2];
+  if (cTS) *cTS = c;
+  if (cpu_time) *cpu_time = hd[1];
   return GSLS_OK;
 }
 

@@ -195,6 +195,18 @@ class Equation:
         check(_lib.load().gsls_eq_step(self.h, C.byref(info)), "gsls_eq_step")
         return info
 
+    def write_restart(self, path, cTS: int, cpu_time: float = 0.0):
+        """Restart record in the reference's layout (WRITERESTART)."""
+        check(_lib.load().gsls_eq_write_restart(self.h, str(path).encode(), int(cTS),
+                                                float(cpu_time)), "gsls_eq_write_restart")
+
+    def read_restart(self, path):
+        """Restore state, time and eq%iNorm (INITFROMBIN); returns (cTS, cpu_time)."""
+        c, t = C.c_int(), C.c_double()
+        check(_lib.load().gsls_eq_read_restart(self.h, str(path).encode(), C.byref(c), C.byref(t)),
+              "gsls_eq_read_restart")
+        return c.value, t.value
+
     def set_cep(self, cep: dict, stim_nodes0):
         """Aliev-Panfilov reaction step (gsls_eq_set_cep); stim_nodes0 0-based."""
         c = _lib.CepParams()
