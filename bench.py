@@ -290,6 +290,10 @@ def run_gsls(args):
             acnt, atot = C.c_longlong(), C.c_double()
             L.gsls_profile_read(b"assembly", C.byref(acnt), C.byref(atot))
             prof = {"cg_spmv": (cnt.value, tot.value), "assembly": (acnt.value, atot.value)}
+            for extra in (b"cg_update", b"cg_pupdate"):
+                ec, et = C.c_longlong(), C.c_double()
+                if L.gsls_profile_read(extra, C.byref(ec), C.byref(et)) == 0 and ec.value:
+                    prof[extra.decode()] = (ec.value, et.value)
         state = eq.get_state()
         res = dict(ms=ms, launches=launches, prof=prof, state=state,
                    newton=np.mean([i.newton_itr for i in timed]),

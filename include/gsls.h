@@ -309,8 +309,10 @@ long long gsls_launch_count(void);
    clock per call in ls%callD).  When enabled, the library brackets its
    dominant launches with CUDA events on its own stream and accumulates,
    per name, the number of launches that did work and their device time:
-   "cg_spmv" (SpMV + fused dot of one CG iteration), "assembly" (all colour
-   launches of one assembly).  Off by default. */
+   "cg_spmv" (SpMV + fused dot of one CG iteration), "cg_update" (X, R and
+   |R|^2), "cg_pupdate" (direction update), "gm_spmv"/"gm_spmv_d3" (GMRES
+   Arnoldi SpMV), "assembly" (all colour launches of one assembly).  Off by
+   default; profiled solves run without graphs or programmatic launch. */
 int gsls_profile_enable(int on);
 int gsls_profile_reset(void);
 int gsls_profile_read(const char *name, long long *count, double *total_ms);

@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(int nNo, const int *__rest
   const AT bsa = block_sum_t<AT>(dot, sha);
   double bs = double(bsa);
   double tot;
-  if (grid_reduce_last<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
+  if (grid_reduce_last1<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
     S->errO = S->err;
     S->dot = tot;
     S->alpha = S->errO / tot;
@@ -349,24 +349,74 @@ template <class XT, bool FUSED>
 __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_update(size_t n, CgVecs v, KrylovScalars *S,
                                                            double *partials, unsigned *ticket) {
   cudaGridDependencySynchronize();
-  if (*(volatile int *)&S->done) return;
   using AT = XT;
   __shared__ double sh[32];
   __shared__ AT sha[32];
-  const int par = S->itr & 1;
-  const XT *__restrict__ P = (const XT *)(FUSED ? (par ? v.P0 : v.P1) : v.P0);
   XT *__restrict__ X = (XT *)v.X;
   XT *__restrict__ R = (XT *)v.R;
   const XT *__restrict__ KP = (const XT *)v.KP;
-  const AT alpha = AT(S->alpha);
   AT acc = AT(0);
   size_t k0 = 0;
-  if constexpr (sizeof(XT) == 4) {
+  constexpr bool kEarly = sizeof(XT) == 4 && !FUSED;
+  if constexpr (kEarly) {
+    // the first float4 of each vector is requested before the done flag and
+    // alpha, so that the loads' latency overlaps the scalar reads
+    const size_t n4 = n / 4, t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nt = (size_t)gridDim.x * blockDim.x;
+    float4 *__restrict__ X4 = reinterpret_cast<float4 *>(X);
+    float4 *__restrict__ R4 = reinterpret_cast<float4 *>(R);
+    const float4 *__restrict__ P4 = reinterpret_cast<const float4 *>(v.P0);
+    const float4 *__restrict__ K4 = reinterpret_cast<const float4 *>(KP);
+    float4 xa = make_float4(0.f, 0.f, 0.f, 0.f), ra = xa, pa = xa, qa = xa;
+    if (t0 < n4) {
+      xa = X4[t0];
+      ra = R4[t0];
+      pa = P4[t0];
+      qa = K4[t0];
+    }
+    if (*(volatile int *)&S->done) return;
+    const AT alpha = AT(S->alpha);
+    for (size_t k = t0; k < n4; k += nt) {
+      float4 x, r, p, q;
+      if (k == t0) {
+        x = xa;
+        r = ra;
+        p = pa;
+        q = qa;
+      } else {
+        x = X4[k];
+        r = R4[k];
+        p = P4[k];
+        q = K4[k];
+      }
+      x.x = fmaf(alpha, p.x, x.x);
+      x.y = fmaf(alpha, p.y, x.y);
+      x.z = fmaf(alpha, p.z, x.z);
+      x.w = fmaf(alpha, p.w, x.w);
+      r.x = fmaf(-alpha, q.x, r.x);
+      r.y = fmaf(-alpha, q.y, r.y);
+      r.z = fmaf(-alpha, q.z, r.z);
+      r.w = fmaf(-alpha, q.w, r.w);
+      X4[k] = x;
+      R4[k] = r;
+      acc = fmaf(r.x, r.x, acc);
+      acc = fmaf(r.y, r.y, acc);
+      acc = fmaf(r.z, r.z, acc);
+      acc = fmaf(r.w, r.w, acc);
+    }
+    k0 = n4 * 4;
+  } else {
+    if (*(volatile int *)&S->done) return;
+  }
+  const int par = S->itr & 1;
+  const XT *__restrict__ P = (const XT *)(FUSED ? (par ? v.P0 : v.P1) : v.P0);
+  const AT alpha = AT(S->alpha);
+  if constexpr (sizeof(XT) == 4 && FUSED) {
     const size_t n4 = n / 4;
-    float4 *X4 = reinterpret_cast<float4 *>(X);
-    float4 *R4 = reinterpret_cast<float4 *>(R);
-    const float4 *P4 = reinterpret_cast<const float4 *>(P);
-    const float4 *K4 = reinterpret_cast<const float4 *>(KP);
+    float4 *__restrict__ X4 = reinterpret_cast<float4 *>(X);
+    float4 *__restrict__ R4 = reinterpret_cast<float4 *>(R);
+    const float4 *__restrict__ P4 = reinterpret_cast<const float4 *>(P);
+    const float4 *__restrict__ K4 = reinterpret_cast<const float4 *>(KP);
     for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4;
          k += (size_t)gridDim.x * blockDim.x) {
       float4 x = X4[k], r = R4[k];
@@ -398,7 +448,7 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_update(size_t n, CgVecs v
   const AT bsa = block_sum_t<AT>(acc, sha);
   double bs = double(bsa);
   double tot;
-  if (grid_reduce_last<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
+  if (grid_reduce_last1<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
     S->err = tot;
     S->beta = tot / S->errO;
     S->itr += 1;
@@ -419,19 +469,25 @@ template <class XT>
 __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_pupdate(size_t n, CgVecs v,
                                                             const KrylovScalars *S) {
   cudaGridDependencySynchronize();
-  if (*(volatile const int *)&S->done) return;
-  const XT beta = XT(S->beta);
   XT *__restrict__ P = (XT *)v.P0;
   const XT *__restrict__ R = (const XT *)v.R;
   size_t k0 = 0;
   if constexpr (sizeof(XT) == 4) {
-    const size_t n4 = n / 4;
-    float4 *P4 = reinterpret_cast<float4 *>(P);
-    const float4 *R4 = reinterpret_cast<const float4 *>(R);
-    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4;
-         k += (size_t)gridDim.x * blockDim.x) {
-      float4 p = P4[k];
-      const float4 r = R4[k];
+    // first float4 requested before the done flag and beta (as k_cg_update)
+    const size_t n4 = n / 4, t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nt = (size_t)gridDim.x * blockDim.x;
+    float4 *__restrict__ P4 = reinterpret_cast<float4 *>(P);
+    const float4 *__restrict__ R4 = reinterpret_cast<const float4 *>(R);
+    float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), ra = pa;
+    if (t0 < n4) {
+      pa = P4[t0];
+      ra = R4[t0];
+    }
+    if (*(volatile const int *)&S->done) return;
+    const XT beta = XT(S->beta);
+    for (size_t k = t0; k < n4; k += nt) {
+      float4 p = (k == t0) ? pa : P4[k];
+      const float4 r = (k == t0) ? ra : R4[k];
       p.x = fmaf(beta, p.x, r.x);
       p.y = fmaf(beta, p.y, r.y);
       p.z = fmaf(beta, p.z, r.z);
@@ -439,7 +495,10 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_pupdate(size_t n, CgVecs 
       P4[k] = p;
     }
     k0 = n4 * 4;
+  } else {
+    if (*(volatile const int *)&S->done) return;
   }
+  const XT beta = XT(S->beta);
   for (size_t k = k0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (size_t)gridDim.x * blockDim.x)
     P[k] = fma(beta, P[k], R[k]);
@@ -760,7 +819,7 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
   unsigned *tk = ws.ticket.as<unsigned>();
   const int zz = zigzag_on();
   for (int b = 0; b < n_iter; b++) {
-    if (prof) cudaEventRecord(prof_event(ev_base + 2 * b), st);
+    if (prof) cudaEventRecord(prof_event(ev_base + 4 * b), st);
     // programmatic dependent launch: each kernel's blocks may be scheduled
     // while its predecessor drains; they wait (cudaGridDependencySynchronize)
     // for its completion before reading anything it wrote
@@ -788,16 +847,18 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
                                    zz));
     }
     GSLS_CHECK_LAUNCH();
-    if (prof) cudaEventRecord(prof_event(ev_base + 2 * b + 1), st);
+    if (prof) cudaEventRecord(prof_event(ev_base + 4 * b + 1), st);
     cfg.gridDim = dim3(G2);
     cfg.blockDim = dim3(kUpdThreads);
     GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_update<XT, FUSED>, nv, v, S, part, tk));
     GSLS_CHECK_LAUNCH();
+    if (prof) cudaEventRecord(prof_event(ev_base + 4 * b + 2), st);
     if (!FUSED) {
       cfg.gridDim = dim3(G3);
       GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_pupdate<XT>, nv, v, (const KrylovScalars *)S));
       GSLS_CHECK_LAUNCH();
     }
+    if (prof) cudaEventRecord(prof_event(ev_base + 4 * b + 3), st);
   }
   return GSLS_OK;
 }
@@ -891,13 +952,19 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
     if (prof) {
       // only the launches that did work (one per completed iteration)
       const int worked = ws.h_scal->itr - itr_before;
-      double ms = 0.0;
+      double ms = 0.0, mu = 0.0, mp = 0.0;
       for (int b = 0; b < worked && b < B; b++) {
         float t = 0.f;
-        cudaEventElapsedTime(&t, prof_event(2 * b), prof_event(2 * b + 1));
+        cudaEventElapsedTime(&t, prof_event(4 * b), prof_event(4 * b + 1));
         ms += t;
+        cudaEventElapsedTime(&t, prof_event(4 * b + 1), prof_event(4 * b + 2));
+        mu += t;
+        cudaEventElapsedTime(&t, prof_event(4 * b + 2), prof_event(4 * b + 3));
+        mp += t;
       }
       prof_add("cg_spmv", worked, ms);
+      prof_add("cg_update", worked, mu);
+      prof_add("cg_pupdate", worked, mp);
     }
   }
   k_scale_out<D, XT><<<G, kThreads, 0, st>>>(nNo, R, (const XT *)v.X, Wc);

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(VT) == 4 ? (U > 4 ? 4 : 6) : 
   const AT bsa = block_sum_t<AT>(dot, sha);
   double bs = double(bsa);
   double tot;
-  if (grid_reduce_last<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
+  if (grid_reduce_last1<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
     S->errO = S->err;
     S->dot = tot;
     S->alpha = S->errO / tot;
