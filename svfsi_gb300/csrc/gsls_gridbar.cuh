@@ -17,8 +17,15 @@ struct GridBar {
 constexpr unsigned kBarSpin = 1u << 24;
 
 // Barrier number `epoch` (1, 2, ...) of the launch: every block adds one
-// arrival and waits until all nblk * epoch arrivals are in; no reset, so
-// the last arriver has nothing more to publish.
+// arrival (release at GPU scope) and thread 0 polls the count with acquire
+// loads until all nblk * epoch arrivals are in, then releases its block
+// with a block barrier; no reset, so the last arriver has nothing more to
+// publish.  The error word is polled every 32 iterations.
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ bool grid_bar(GridBar *b, unsigned nblk, unsigned &epoch) {
   __shared__ int s_ok;
   __syncthreads();
@@ -26,22 +33,21 @@ __device__ __forceinline__ bool grid_bar(GridBar *b, unsigned nblk, unsigned &ep
   if (threadIdx.x == 0) {
     int ok = 1;
     const unsigned target = epoch * nblk;
-    __threadfence();
-    atomicAdd(&b->count, 1u);
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&b->count), "r"(1u) : "memory");
     unsigned it = 0;
-    while (*(volatile unsigned *)&b->count < target) {
-      if (*(volatile int *)&b->err) {
+    while (ld_acquire_gpu(&b->count) < target) {
+      ++it;
+      if ((it & 31u) == 0u && *(volatile int *)&b->err) {
         ok = 0;
         break;
       }
-      if (++it > kBarSpin) {
+      if (it > kBarSpin) {
         atomicExch(&b->err, 1);
         ok = 0;
         break;
       }
-      __nanosleep(20);
+      if (it > 64u) __nanosleep(20);
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();

@@ -259,11 +259,21 @@ __device__ __forceinline__ bool grid_reduce_last(const double *vals, double *par
   return true;
 }
 
+// Ticket increment with acquire-release semantics at GPU scope: the
+// caller's earlier writes are visible to whoever later acquires the ticket,
+// and the caller sees the writes released by earlier increments.
+__device__ __forceinline__ unsigned atomic_add_acq_rel(unsigned *p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 // Single-level form of grid_reduce_last for grids of a few hundred blocks
-// (the resident grids of the CG kernels): one fence and one ticket per
+// (the resident grids of the CG kernels): one acquire-release ticket per
 // block, and the last block sums all partials in block order -- one memory
-// round trip less on the critical path than the two-level form.  Uses
-// ticket[0] only (reset by the last block).
+// round trip less on the critical path than the two-level form.  The last
+// block's other threads read the partials after the barrier that follows
+// thread 0's acquire.  Uses ticket[0] only (reset by the last block).
 template <int NV>
 __device__ __forceinline__ bool grid_reduce_last1(const double *vals, double *partials,
                                                   unsigned *ticket, double *out, double *sh) {
@@ -272,12 +282,10 @@ __device__ __forceinline__ bool grid_reduce_last1(const double *vals, double *pa
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; k++) partials[(size_t)k * G + blockIdx.x] = vals[k];
-    __threadfence();
-    last = (atomicAdd(ticket, 1u) == (unsigned)G - 1) ? 1 : 0;
+    last = (atomic_add_acq_rel(ticket, 1u) == (unsigned)G - 1) ? 1 : 0;
   }
   __syncthreads();
   if (!last) return false;
-  __threadfence();
 #pragma unroll
   for (int k = 0; k < NV; k++) {
     double s = 0.0;
