@@ -195,6 +195,15 @@ __device__ __forceinline__ double block_sum(double v, double *sh /*[32]*/) {
   return v;
 }
 
+// Ticket increment with acquire-release semantics at GPU scope: the
+// caller's earlier writes are visible to whoever later acquires the ticket,
+// and the caller sees the writes released by earlier increments.
+__device__ __forceinline__ unsigned atomic_add_acq_rel(unsigned *p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 // Deterministic grid reduction of NV values per block.  Every block calls it
 // with its block sums in thread 0 (vals[k]); returns true in exactly one
 // block (the last to arrive), whose thread 0 holds the totals in out[k].
@@ -217,13 +226,11 @@ __device__ __forceinline__ bool grid_reduce_last(const double *vals, double *par
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; k++) partials[(size_t)k * G + blockIdx.x] = vals[k];
-    __threadfence();
-    const unsigned t = atomicAdd(ticket + 1 + g, 1u);
+    const unsigned t = atomic_add_acq_rel(ticket + 1 + g, 1u);
     stage = (t == (unsigned)gsz - 1) ? 1 : 0;
   }
   __syncthreads();
   if (stage == 0) return false;
-  __threadfence();
   // last block of group g: fixed-order sum of the group's partials
   double gs[NV];
 #pragma unroll
@@ -239,13 +246,11 @@ __device__ __forceinline__ bool grid_reduce_last(const double *vals, double *par
 #pragma unroll
     for (int k = 0; k < NV; k++) gpart[(size_t)k * ngroups + g] = gs[k];
     ticket[1 + g] = 0u;
-    __threadfence();
-    const unsigned t = atomicAdd(ticket, 1u);
+    const unsigned t = atomic_add_acq_rel(ticket, 1u);
     stage = (t == (unsigned)ngroups - 1) ? 2 : 1;
   }
   __syncthreads();
   if (stage != 2) return false;
-  __threadfence();
 #pragma unroll
   for (int k = 0; k < NV; k++) {
     double s = 0.0;
@@ -257,15 +262,6 @@ __device__ __forceinline__ bool grid_reduce_last(const double *vals, double *par
   }
   if (threadIdx.x == 0) *ticket = 0u;
   return true;
-}
-
-// Ticket increment with acquire-release semantics at GPU scope: the
-// caller's earlier writes are visible to whoever later acquires the ticket,
-// and the caller sees the writes released by earlier increments.
-__device__ __forceinline__ unsigned atomic_add_acq_rel(unsigned *p, unsigned v) {
-  unsigned old;
-  asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
 }
 
 // Single-level form of grid_reduce_last for grids of a few hundred blocks
