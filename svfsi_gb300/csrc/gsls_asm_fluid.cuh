@@ -26,6 +26,7 @@ namespace gsls {
 
 template <class TT>
 __global__ void __launch_bounds__(kAsmThreads) k_asm_fluid(AsmArgs A) {
+  asm_colour_start();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.nColorEl) return;
   const int e = A.el0 + t;
@@ -172,6 +173,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_fluid(AsmArgs A) {
       for (int b = 0; b < 4; b++) G[a][b] += c1 * vN[b] + c2 * (uN[b] + upN[b]) + c3 * upN[b];
     }
   }
+  asm_colour_scatter();
 #pragma unroll
   for (int a = 0; a < 4; a++)
 #pragma unroll

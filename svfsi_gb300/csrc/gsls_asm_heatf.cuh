@@ -18,6 +18,7 @@ namespace gsls {
 
 template <class VT>
 __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
+  asm_colour_start();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.nColorEl) return;
   const int e = A.el0 + t;
@@ -108,6 +109,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
       for (int b = 0; b < 4; b++) lK[a][b] += wn * NxN[a][b] + ta[a] * tb[b];
   }
   VT *Val = reinterpret_cast<VT *>(A.Val);
+  asm_colour_scatter();
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     A.R[n4[a]] += lR[a];

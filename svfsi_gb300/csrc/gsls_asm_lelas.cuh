@@ -18,6 +18,7 @@ namespace gsls {
 
 template <class VT>
 __global__ void __launch_bounds__(kAsmThreads) k_asm_lelas(AsmArgs A) {
+  asm_colour_start();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.nColorEl) return;
   const int e = A.el0 + t;
@@ -52,6 +53,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_lelas(AsmArgs A) {
   const double Sxy = mu * ed[3], Syz = mu * ed[4], Sxz = mu * ed[5];
 
   // ---- residual (FP64)
+  asm_colour_scatter();
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     double m[3];

@@ -50,6 +50,7 @@ __device__ __forceinline__ double jm23(double J) {
 // the FP64 variant stays at its natural register count
 template <class VT>
 __global__ void __launch_bounds__(kAsmThreads, sizeof(VT) == 4 ? 3 : 1) k_asm_struct(AsmArgs A) {
+  asm_colour_start();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.nColorEl) return;
   using AT = VT;
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(kAsmThreads, sizeof(VT) == 4 ? 3 : 1) k_asm_st
   }
 
   // ---- residual (FP64): lR(a,c) = W Nx_a.P(c,:) + w sum_b M_ab inert_b - w rho fb N_a
+  asm_colour_scatter();
   {
     double P[3][3];
 #pragma unroll

