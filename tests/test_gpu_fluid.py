@@ -138,6 +138,42 @@ def test_ns_solve_matches_oracle(gsls, orc, tight):
         assert rel(R, Ro) < 20 * kw["relTol"]
 
 
+@pytest.mark.parametrize("relTol", [None, 1e-4])
+def test_ns_solve_two_row_slots_matches_oracle(gsls, orc, relTol):
+    """A 46,928-node cylinder: the persistent Schur CG gives every 4-lane
+    group two row slots (the second one partly past the last row) and visits
+    them last to first on odd iterations; 3 (loose) and 678 (1e-4) Schur
+    iterations in the oracle."""
+    p = problems.fluid_cylinder(h=0.045, nsteps=1)
+    assert p.nNo > 152 * 256
+    A, Y = _state(p, seed=5)
+    R0, V0 = orc.assemble(p, A, Y)
+    faces = _fluid_faces(p)
+    lhs = _lhs(p, len(faces))
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, len(faces))
+    for k, nodes in enumerate(faces):
+        fsils.FSILS_BC_CREATE(lhs, k + 1, nodes.size, 3, fsils.BC_TYPE_DIR, nodes + 1,
+                              np.zeros((nodes.size, 3)))
+        s.bc_create(k + 1, nodes, 3, 0, np.zeros((nodes.size, 3)))
+    kw = dict(dimKry=100)
+    if relTol:
+        kw["relTol"] = relTol
+    ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_NS, **kw)
+    ols = orc.ls_create(orc.LS_TYPE_NS, sD=100, relTol=relTol)
+    R, Val = R0.copy(), V0.copy()
+    fsils.FSILS_SOLVE(lhs, ls, 4, R, Val, fsils.PRECOND_RCS)
+    Ro, Vo = R0.copy(), V0.copy()
+    s.solve(ols, 4, Ro, Vo, orc.PRECOND_RCS)
+    assert ls.RI.suc == ols.RI.suc == 1
+    if relTol is None:
+        assert ls.RI.itr == ols.RI.itr
+        assert ls.CG.itr == ols.CG.itr
+        assert rel(R, Ro) < 1e-8
+    else:
+        assert abs(ls.RI.itr - ols.RI.itr) <= 2
+        assert rel(R, Ro) < 20 * relTol
+
+
 def test_fluid_steps_fp64(gsls, orc):
     """Converged implicit steps (Newton to 1e-10) land on the oracle's state."""
     p = _cyl(nsteps=3)
