@@ -3,7 +3,9 @@
 neo-Hookean elastodynamics workload (4x1x1 beam, 176x44x44 hexes -> 2,044,416
 tet4, 358,425 nodes, 5,233,801 3x3 CSR blocks; CG + diagonal preconditioner),
 mixed precision (FP32 tangent + FP32 inner CG, FP64 residual/Newton) beside
-the plain FP64 GPU path, with the relative L2 distance between the two.
+the plain FP64 GPU path, with the relative L2 distance between the two,
+and the HBM roofline of the dominant SpMV on both paths (`roofline` for the
+FP32 values of the mixed path, `roofline_fp64` for the FP64 one).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gsls|reference]
                   [--workload struct|fluid|cep|lelas|adjoint]
@@ -322,6 +324,7 @@ def run_gsls(args):
     # kernel-level timing (CUDA events around every CG SpMV) in a separate,
     # shorter run so that the headline numbers carry no event overhead
     profd = timed_run(fsils.PREC_MIXED, profile=True, nsteps=2, nwarm=1)
+    profd64 = timed_run(fsils.PREC_FP64, profile=True, nsteps=1, nwarm=1)
     ms_mixed = max_over_ranks(mixed["ms"]) / K
     ms_fp64 = max_over_ranks(fp64["ms"]) / K
     D_m, D_f = compared_field(p, mixed["state"]), compared_field(p, fp64["state"])
@@ -354,34 +357,42 @@ def run_gsls(args):
     state_bytes = 3 * p.nNo * p.tDof * 8
 
     # roofline of the dominant kernel: the CG SpMV + fused dot (struct) or
-    # the GMRES SpMV on the 3x3 K block (fluid), FP32 values
-    cnt, tot_ms = profd["prof"]["cg_spmv"]
+    # the GMRES SpMV on the 3x3 K block (fluid); FP32 values on the mixed
+    # path, FP64 on the drop-in one
     peak, peak_kind = peaks()
-    if is_fluid(p):
-        B = p.nnz * (9 * 4 + 4) + 8 * p.nNo + 2 * p.nNo * 3 * 4
-        kname = "k_gm_spmv<3,float,float> (block-CSR SpMV on the K block of the NS solver)"
-        tkey = "gm_spmv_d3_f32_fluid_cylinder"
-    elif is_heatf(p):
-        B = p.algorithmic_bytes(4, 4)["spmv"]
-        kname = "k_gm_spmv<1,float,float> (CSR SpMV of the GMRES Arnoldi step)"
-        tkey = f"gm_spmv_d1_f32_{p.name}"
-    elif is_cep(p):
-        B = p.algorithmic_bytes(4, 4)["spmv"]
-        kname = "k_cg_spmv<1,float,float> (CSR SpMV + fused P.KP)"
-        tkey = "cg_spmv_d1_f32_cep_slab"
-    else:
-        B = p.algorithmic_bytes(4, 4)["spmv"]
-        kname = ("k_cg_spmv_sell<3,float,float,8> (sliced block-ELL SpMV + fused P.KP, "
-                 "zig-zag order; the first batch of each solve runs k_cg_spmv on the CSR)")
-        tkey = f"cg_spmv_sell_d3_f32_{p.name}"
-    avg_s = (tot_ms / max(cnt, 1)) / 1e3
-    achieved = B / avg_s / 1e9 if cnt else None
-    roof = {"kernel": kname,
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None,
-            "peak_source": f"{peak_kind} hbm_gbs", "bytes_per_launch": B,
-            "avg_launch_us": avg_s * 1e6, "launches": cnt,
-            "traffic": traffic_from_profiles(tkey)}
+
+    def roofline(prof, s):
+        cnt, tot_ms = prof["cg_spmv"]
+        t = "float" if s == 4 else "double"
+        if is_fluid(p):
+            B = p.nnz * (9 * s + 4) + 8 * p.nNo + 2 * p.nNo * 3 * s
+            kname = f"k_gm_spmv<3,{t},{t}> (block-CSR SpMV on the K block of the NS solver)"
+            tkey = f"gm_spmv_d3_f{8 * s}_fluid_cylinder"
+        elif is_heatf(p):
+            B = p.algorithmic_bytes(s, s)["spmv"]
+            kname = f"k_gm_spmv<1,{t},{t}> (CSR SpMV of the GMRES Arnoldi step)"
+            tkey = f"gm_spmv_d1_f{8 * s}_{p.name}"
+        elif is_cep(p):
+            B = p.algorithmic_bytes(s, s)["spmv"]
+            kname = f"k_cg_spmv<1,{t},{t}> (CSR SpMV + fused P.KP)"
+            tkey = f"cg_spmv_d1_f{8 * s}_cep_slab"
+        else:
+            B = p.algorithmic_bytes(s, s)["spmv"]
+            kname = (f"k_cg_spmv_sell<3,{t},{t},{8 if s == 4 else 4}> (sliced block-ELL SpMV + "
+                     "fused P.KP, zig-zag order; the first batch of each solve runs k_cg_spmv "
+                     "on the CSR)")
+            tkey = f"cg_spmv_sell_d3_f{8 * s}_{p.name}"
+        avg_s = (tot_ms / max(cnt, 1)) / 1e3
+        achieved = B / avg_s / 1e9 if cnt else None
+        return {"kernel": kname,
+                "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "peak_source": f"{peak_kind} hbm_gbs", "bytes_per_launch": B,
+                "avg_launch_us": avg_s * 1e6, "launches": cnt,
+                "traffic": traffic_from_profiles(tkey)}
+
+    roof = roofline(profd["prof"], 4)
+    roof64 = roofline(profd64["prof"], 8)
 
     out = {
         "metric": METRIC, "value": job_value(ms_mixed / 1e3, world), "unit": "s/step",
@@ -406,6 +417,7 @@ def run_gsls(args):
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "rel_l2_mixed_vs_fp64": rel_l2,
         "roofline": roof,
+        "roofline_fp64": roof64,
         "e2e": {"value": e2e_s / world, "unit": "s/step", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes},
         "gpu_launches": int(mixed["launches"]),
