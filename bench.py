@@ -393,6 +393,23 @@ def run_gsls(args):
 
     roof = roofline(profd["prof"], 4)
     roof64 = roofline(profd64["prof"], 8)
+    # the FP64 SpMV issues one FP64 FMA per matrix entry; GB300 runs FP64 at
+    # ~1/74 of FP32, so its roof is the FP64 pipe when that takes longer
+    # than the HBM stream (measured live by the library's probe kernel)
+    rate = C.c_double()
+    _lib.check(L.gsls_fp64_fma_rate(C.byref(rate)), "gsls_fp64_fma_rate")
+    d = 3 if (is_fluid(p) or p.dof == 3) else 1
+    fmas = d * d * p.nnz
+    if roof64["achieved"]:
+        avg_s = roof64["avg_launch_us"] / 1e6
+        t_fma, t_hbm = fmas / rate.value, roof64["bytes_per_launch"] / (peak * 1e9)
+        hbm = {k: roof64[k] for k in ("achieved", "peak", "unit", "frac", "peak_source", "traffic")}
+        if t_fma > t_hbm:
+            roof64.update({"bound": "fp64", "achieved": 2 * fmas / avg_s / 1e12,
+                           "peak": 2 * rate.value / 1e12, "unit": "TFLOP/s",
+                           "frac": t_fma / avg_s,
+                           "peak_source": "measured FP64 FMA rate (gsls_fp64_fma_rate)",
+                           "fma_per_launch": fmas, "hbm": hbm})
 
     out = {
         "metric": METRIC, "value": job_value(ms_mixed / 1e3, world), "unit": "s/step",

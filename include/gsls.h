@@ -316,6 +316,12 @@ long long gsls_launch_count(void);
 int gsls_profile_enable(int on);
 int gsls_profile_reset(void);
 int gsls_profile_read(const char *name, long long *count, double *total_ms);
+/* FP64 FMA throughput of the current device (FMAs per second), measured
+   with a short probe kernel (8 independent FMA chains per thread, 4 blocks
+   of 256 per SM, CUDA events): the compute roof of the FP64 drop-in path,
+   whose SpMV issues one FP64 FMA per matrix entry.  No counterpart in the
+   reference. */
+int gsls_fp64_fma_rate(double *fma_per_s);
 
 /* ---- discrete adjoint (forward/backward pair) --------------------------
    Gradient of an objective of the final state with respect to the

@@ -128,6 +128,7 @@ SIGNATURES = {
     "gsls_profile_enable": (C.c_int, [C.c_int]),
     "gsls_profile_reset": (C.c_int, []),
     "gsls_profile_read": (C.c_int, [C.c_char_p, C.POINTER(C.c_longlong), c_double_p]),
+    "gsls_fp64_fma_rate": (C.c_int, [c_double_p]),
 }
 
 _LIB = None

@@ -303,6 +303,24 @@ __global__ void k_row_of(const int *rowPtr, int nNo, int *rowOf) {
     for (int j = rowPtr[i]; j < rowPtr[i + 1]; j++) rowOf[j] = i;
 }
 
+// FP64 FMA throughput probe: 8 independent chains per thread, one store per
+// thread into a buffer of exactly grid * block doubles.
+__global__ void __launch_bounds__(256) k_dfma_probe(double *out, int iters) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) a[k] = 1e-9 * (t + k);
+  const double b = 0.9999999, c = 1e-7;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = fma(a[k], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += a[k];
+  out[t] = s;
+}
+
 }  // namespace gsls
 
 using namespace gsls;
@@ -310,6 +328,38 @@ using namespace gsls;
 extern "C" {
 
 int gsls_version(void) { return GSLS_VERSION; }
+
+int gsls_fp64_fma_rate(double *fma_per_s) {
+  if (!fma_per_s) return GSLS_ERR_ARG;
+  const int threads = 256, blocks = 4 * num_sms(), iters = 4000;
+  const size_t n = (size_t)blocks * threads;
+  double *d = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = GSLS_OK;
+  float ms = 0.0f;
+  if (cudaMalloc(&d, n * sizeof(double)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    rc = GSLS_ERR_CUDA;
+  } else {
+    for (int r = 0; r < 3; r++) k_dfma_probe<<<blocks, threads, 0, st>>>(d, iters);
+    cudaEventRecord(e0, st);
+    k_dfma_probe<<<blocks, threads, 0, st>>>(d, iters);
+    cudaEventRecord(e1, st);
+    count_launch_n(4);
+    if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.0f)
+      rc = GSLS_ERR_CUDA;
+  }
+  if (rc == GSLS_OK) *fma_per_s = 8.0 * iters * (double)n / (ms * 1e-3);
+  else set_error("gsls_fp64_fma_rate: CUDA error");
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (d) cudaFree(d);
+  return rc;
+}
 
 const char *gsls_last_error(void) { return g_err.c_str(); }
 

@@ -421,3 +421,13 @@ def test_cg_block_sizes_matches_oracle(gsls, orc, dof, mixed):
         assert abs(ls.RI.itr - ols.RI.itr) <= 1
         assert rel(R, Ro) < 1e-7
     assert ls.RI.suc == 1
+
+
+def test_fp64_fma_rate_probe(gsls):
+    """The FP64 FMA probe (the compute roof of the FP64 SpMV) returns a
+    positive rate of a plausible size and counts its launches."""
+    n0 = gsls.gsls_launch_count()
+    r = C.c_double()
+    _lib.check(gsls.gsls_fp64_fma_rate(C.byref(r)), "gsls_fp64_fma_rate")
+    assert 1e10 < r.value < 1e14
+    assert gsls.gsls_launch_count() - n0 == 4
