@@ -224,6 +224,9 @@ typedef struct {
 
 int gsls_eq_create(gsls_eq **eq, gsls_mesh *mesh, const gsls_eq_params *p,
                    const gsls_eq_solver *sv);
+/* Frees the equation and releases the LS faces its Dirichlet sets claimed
+   on the lhs (faces 1 .. number of sets), so that the next equation on the
+   same lhs and mesh can claim them. */
 int gsls_eq_free(gsls_eq *eq);
 
 /* Strong Dirichlet BC on a node list (1-based): component c of the

@@ -266,7 +266,12 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
 
 int gsls_eq_free(gsls_eq *eq) {
   if (!eq) return GSLS_ERR_ARG;
-  cudaStreamSynchronize(eq->lhs->stream);
+  gsls_lhs *lhs = eq->lhs;
+  cudaStreamSynchronize(lhs->stream);
+  // release the LS faces this equation's Dirichlet sets claimed (faces 1 ..
+  // nextFace), so that a later equation on the same lhs can claim them
+  for (int k = 0; k < eq->nextFace && k < lhs->nFaces; k++) lhs->faces[k].foC = false;
+  lhs->ws.mask_dof = -1;  // the cached Dirichlet mask was built from them
   delete eq;
   return GSLS_OK;
 }

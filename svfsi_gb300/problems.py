@@ -275,10 +275,18 @@ def make_lhs_arrays(p: Problem):
 
 def build_equation(p: Problem, precision=PREC_FP64):
     """LHS + mesh + equation on the GPU for a Problem."""
-    from .fsils import Equation, Mesh, FSILS_LHS_CREATE
+    from .fsils import Mesh, FSILS_LHS_CREATE
     g, rp1, cp1 = make_lhs_arrays(p)
     lhs = FSILS_LHS_CREATE(p.nNo, p.nNo, p.nnz, g, rp1, cp1, max(1, len(p.dirichlet)))
     mesh = Mesh(lhs, p.ien, p.x)
+    return lhs, mesh, equation_on(p, mesh, precision)
+
+
+def equation_on(p: Problem, mesh, precision=PREC_FP64):
+    """A fresh equation of the Problem (parameters, boundary conditions,
+    initial state) on an existing mesh; the previous equation on the mesh
+    must have been freed (it holds the lhs faces of its Dirichlet sets)."""
+    from .fsils import Equation
     prm = p.eq_params()
     eq = Equation(mesh, prm, p.eq_solver(precision))
     if p.eparam is not None:
@@ -291,4 +299,4 @@ def build_equation(p: Problem, precision=PREC_FP64):
         eq.set_cep(p.cep, np.nonzero(p.stim)[0])
     Ao, Yo, Do = p.initial_state()
     eq.set_state(Ao, Yo, Do)
-    return lhs, mesh, eq
+    return eq

@@ -431,3 +431,29 @@ def test_fp64_fma_rate_probe(gsls):
     _lib.check(gsls.gsls_fp64_fma_rate(C.byref(r)), "gsls_fp64_fma_rate")
     assert 1e10 < r.value < 1e14
     assert gsls.gsls_launch_count() - n0 == 4
+
+
+def test_next_equation_on_the_same_lhs_claims_the_freed_faces(gsls):
+    """gsls_eq_free releases the LS faces of its Dirichlet sets: a second
+    equation on the same lhs and mesh can be set up and steps bit for bit
+    like the first."""
+    p = problems.struct_beam(8, 2, 2, nsteps=1)
+    lhs, mesh, eq = problems.build_equation(p)
+    eq.step()
+    D1 = eq.get_state()[2]
+    eq.free()
+    eq2 = fsils.Equation(mesh, p.eq_params(), p.eq_solver())
+    for d in p.dirichlet:
+        eq2.add_dirichlet(d.nodes, d.g, d.gx, d.mask, d.nV)
+    for t in p.traction:
+        eq2.add_traction(t.faces, t.h)
+    eq2.set_state(*p.initial_state())
+    eq2.step()
+    assert np.array_equal(eq2.get_state()[2], D1)
+    # a second live equation finds no free face
+    eq3 = fsils.Equation(mesh, p.eq_params(), p.eq_solver())
+    with pytest.raises(_lib.GslsError, match="face"):
+        for d in p.dirichlet:
+            eq3.add_dirichlet(d.nodes, d.g, d.gx, d.mask, d.nV)
+    eq3.free()
+    eq2.free()
