@@ -303,11 +303,11 @@ __global__ void __launch_bounds__(kNT) k_ns_split(int nNo, const double *__restr
   }
 }
 
-// DEPART (NSSOLVER.f:237-305) for nsd = 3.  Also writes the second Schur
-// operand packed four to a block for the persistent CG: A2 = (Gt, mL).
+// DEPART (NSSOLVER.f:237-305) for nsd = 3.  Also writes the Schur operands
+// packed four to a block for the persistent CG: A1 = (mG, 0), A2 = (Gt, mL).
 template <class VT>
 __global__ void k_depart(int nnz, const VT *__restrict__ Val, const int *__restrict__ tpos, VT *mK,
-                         VT *mG, VT *mD, VT *mL, VT *Gt, VT *A2) {
+                         VT *mG, VT *mD, VT *mL, VT *Gt, VT *A1, VT *A2) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nnz; j += gridDim.x * blockDim.x) {
     const VT *t = Val + (size_t)j * 16;
     VT *k = mK + (size_t)j * 9;
@@ -322,8 +322,10 @@ __global__ void k_depart(int nnz, const VT *__restrict__ Val, const int *__restr
       mG[(size_t)j * 3 + m] = g;
       mD[(size_t)j * 3 + m] = t[12 + m];
       Gt[(size_t)l * 3 + m] = -g;
+      A1[(size_t)j * 4 + m] = g;
       A2[(size_t)l * 4 + m] = -g;
     }
+    A1[(size_t)j * 4 + 3] = VT(0);
     mL[j] = t[15];
     A2[(size_t)j * 4 + 3] = t[15];
   }
@@ -743,7 +745,7 @@ template <class VT, class XT>
 struct SchurArgs {
   int nNo;
   const int *rowPtr, *colPtr;
-  const VT *A1, *A2;              // mG (3) and (Gt, mL) (4) per CSR block
+  const VT *A1, *A2;              // (mG, 0) and (Gt, mL) per CSR block
   XT *X, *Pa, *Pb, *R, *SP, *GP;  // Pa holds the initial direction; GP 4 per node
   double *part;                   // 2 * gridDim.x
   GridBar *bar;
@@ -843,8 +845,10 @@ __global__ void __launch_bounds__(kPT, 1) k_schur_persistent(SchurArgs<VT, XT> A
             const int col = scol[jl];
             const size_t j = (size_t)(jl + dl);
             pv[u] = AT(c2 * (__ldcg(Pold + col) + c1 * __ldcg(A.R + col)));
+            VT a4[4];
+            V4<VT>::ldg(A.A1 + j * 4, a4);
 #pragma unroll
-            for (int m = 0; m < 3; m++) gv[u][m] = AT(__ldg(A.A1 + j * 3 + m));
+            for (int m = 0; m < 3; m++) gv[u][m] = AT(a4[m]);
           } else {
             pv[u] = AT(0);
 #pragma unroll
@@ -994,7 +998,7 @@ static size_t schur_geometry(const gsls_lhs *lhs, int nblk, int *K_out) {
 // CGRAD_SCHUR on P (in: right-hand side, out: solution)
 template <class VT, class XT>
 static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, const VT *mL,
-                    const VT *A2, XT *P, XT *Rs, XT *Ps, XT *Pb, XT *SP, XT *GP,
+                    const VT *A1, const VT *A2, XT *P, XT *Rs, XT *Ps, XT *Pb, XT *SP, XT *GP,
                     XT *GP4, SchurScal *sc, SchurScal *h_sc, GridBar *db) {
   cudaStream_t st = lhs->stream;
   const int nNo = lhs->nNo, G = lhs->grid;
@@ -1029,7 +1033,7 @@ static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, 
     } else {
       GSLS_TRY(lhs->ws.partials.alloc(sizeof(double) * ((size_t)2 * nblk + 64) + 64));
       GSLS_CUDA(cudaMemsetAsync(db, 0, sizeof(GridBar), st));
-      SchurArgs<VT, XT> a{nNo, rp, cp, mG, A2, P, Ps, Pb, Rs, SP, GP4,
+      SchurArgs<VT, XT> a{nNo, rp, cp, A1, A2, P, Ps, Pb, Rs, SP, GP4,
                           lhs->ws.partials.as<double>(), db, sc, K, zigzag_on()};
       void *args[] = {&a};
       GSLS_CUDA(cudaLaunchCooperativeKernel((const void *)k_schur_persistent<VT, XT>, dim3(nblk),
@@ -1102,9 +1106,10 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
   GridBar *bar = reinterpret_cast<GridBar *>(dsc + 96);
   const size_t m9 = (size_t)nnz * 9, m3 = (size_t)nnz * 3;
   const size_t m1 = ((size_t)nnz + 15) & ~(size_t)15;
-  GSLS_TRY(ws.ns_mat.alloc(sizeof(VT) * (m9 + 4 * m3 + m1 + 4 * (size_t)nnz) + 256));
+  GSLS_TRY(ws.ns_mat.alloc(sizeof(VT) * (m9 + 4 * m3 + m1 + 8 * (size_t)nnz) + 256));
   VT *mK = ws.ns_mat.as<VT>(), *mG = mK + m9, *mD = mG + m3, *Gt = mD + m3, *mL = Gt + m3;
-  VT *A2 = reinterpret_cast<VT *>((reinterpret_cast<uintptr_t>(mL + m1) + 63) & ~(uintptr_t)63);
+  VT *A1 = reinterpret_cast<VT *>((reinterpret_cast<uintptr_t>(mL + m1) + 63) & ~(uintptr_t)63);
+  VT *A2 = A1 + 4 * (size_t)nnz;
   // the GMRES workspace may grow ws.partials: size it for both up front
   const int Gd = num_sms() * 2;
   const int sD = ls->GM.sD > 0 ? ls->GM.sD : 1;
@@ -1118,7 +1123,7 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
   k_ns_split<XT><<<G, kNT, 0, st>>>(nNo, R, Rmi, Rci, Rm, Rc, part, tk, dsc);
   GSLS_CHECK_LAUNCH();
   k_depart<VT><<<grid_for(nnz, G * 4), kNT, 0, st>>>(nnz, Val, lhs->d_tpos.as<int>(), mK, mG, mD, mL,
-                                                      Gt, A2);
+                                                      Gt, A1, A2);
   GSLS_CHECK_LAUNCH();
   double n2[2];
   GSLS_CUDA(cudaMemcpyAsync(n2, dsc, sizeof(n2), cudaMemcpyDeviceToHost, st));
@@ -1152,7 +1157,7 @@ static int ns_t(gsls_lhs *lhs, gsls_ls *ls, const VT *Val, double *R, const doub
     part = ws.partials.as<double>();
     k_ns_vs<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mD, Ui, Rc, Pi, nullptr);
     GSLS_CHECK_LAUNCH();
-    GSLS_TRY((schur_cg<VT, XT>(lhs, &ls->CG, mG, Gt, mL, A2, Pi, Rs, Ps, Pb, SP, GP, GP4, sc,
+    GSLS_TRY((schur_cg<VT, XT>(lhs, &ls->CG, mG, Gt, mL, A1, A2, Pi, Rs, Ps, Pb, SP, GP, GP4, sc,
                                &h_sc, bar)));
     k_ns_sv<VT, XT><<<G, kNT, 0, st>>>(nNo, rp, cp, mG, Pi, MUiB, Rm, MUiBB, nullptr);
     GSLS_CHECK_LAUNCH();
