@@ -151,7 +151,7 @@ __device__ __forceinline__ void ap_f(T x0, T x1, T fext, T &f0, T &f1) {
 
 // Reaction step of CEPINTEG for every node: Xion(1) = Yo(v) (after the
 // first pass), nt substeps of AP_INTEGFE / AP_INTEGRK with the stimulus
-// window of CEPINTEGL, then Yo(v) = Xion(1).  T = float in mixed mode.
+// window of CEPINTEGL, then Yo(v) = Xion(1); run in FP64 (T = double).
 template <class T>
 __global__ void k_cep_ionic(int nNo, int tDof, int s, double *__restrict__ Yo,
                             double *__restrict__ Xion, const int *__restrict__ stim, int first,
@@ -571,14 +571,13 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     long long icl = (long long)floor(t1 / c.CL);
     if (icl < 0) icl = 0;
     const double Ts = c.Ts + (double)icl * c.CL, Te = Ts + c.Td;
-    if (valp == GSLS_PREC_MIXED)
-      k_cep_ionic<float><<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, Yo, eq->Xion.as<double>(),
-                                                   eq->stim.as<int>(), eq->cep_first ? 1 : 0,
-                                                   c.ode, nt, c.dt_ode, t1, Ts, Te, c.A);
-    else
-      k_cep_ionic<double><<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, Yo, eq->Xion.as<double>(),
-                                                    eq->stim.as<int>(), eq->cep_first ? 1 : 0,
-                                                    c.ode, nt, c.dt_ode, t1, Ts, Te, c.A);
+    // FP64 in both precisions: the reaction step sets the state that the
+    // Newton loop starts from, so its rounding is not refined away (an FP32
+    // step left the mixed state 1.2e-8 from the FP64 one); it is ~20 FP64
+    // operations per node and substep
+    k_cep_ionic<double><<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, Yo, eq->Xion.as<double>(),
+                                                  eq->stim.as<int>(), eq->cep_first ? 1 : 0,
+                                                  c.ode, nt, c.dt_ode, t1, Ts, Te, c.A);
     GSLS_CHECK_LAUNCH();
     eq->cep_first = false;
   }

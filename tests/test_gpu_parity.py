@@ -274,9 +274,11 @@ def test_cep_steps(gsls, orc, precision, ode, A):
     _, Y, _ = eq.get_state()
     _, Yo, _ = oeq.state()
     X = eq.get_cep_state()
-    tol = 1e-10 if precision == "fp64" else 1e-6
+    # the reaction step runs in FP64 on both paths; the mixed path's FP32
+    # tangent and inner CG are refined by the FP64 Newton residual
+    tol = 1e-10 if precision == "fp64" else 1e-8
     assert rel(Y, Yo) < tol
-    assert rel(X[:, 1], oeq.Xion[:, 1]) < (1e-9 if precision == "fp64" else 1e-5)
+    assert rel(X[:, 1], oeq.Xion[:, 1]) < (1e-9 if precision == "fp64" else 1e-8)
     if A > 0:
         assert Y.max() > -60.0  # the stimulated corner depolarised well above rest (-80 mV)
 
