@@ -146,6 +146,13 @@ class Mesh:
             _lib.load().gsls_mesh_free(self.h)
             self.h = None
 
+    def __del__(self):
+        # the Lhs outlives this mesh: self.lhs keeps it referenced
+        try:
+            self.free()
+        except Exception:
+            pass
+
 
 class Equation:
     """Device-resident time integrator of one equation (gsls_eq)."""
@@ -237,6 +244,13 @@ class Equation:
         if self.h:
             _lib.load().gsls_eq_free(self.h)
             self.h = None
+
+    def __del__(self):
+        # the Mesh and Lhs outlive this equation: self.mesh keeps them referenced
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class Tape:
