@@ -193,7 +193,20 @@ typedef struct {
                            STRUCT C10, CEP Diso, HEATS conductivity */
   double elM, nu;   /* LELAS elasticity modulus and Poisson ratio (body
                        force f_x, f_y, f_z in fb) */
+  /* FLUID viscosity model (GETVISCOSITY, Code/Source/svFSI/FLUID.f:1690-1739;
+     READVISCMODEL, READFILES.f:2875-2925): GSLS_VISC_CONST uses mu_f;
+     GSLS_VISC_CY (Carreau-Yasuda): mu_f = high shear-rate limit, mu_o = low
+     shear-rate limit, vlam = lambda, va = a, vn = power-law index n;
+     GSLS_VISC_CASSON: mu_f = asymptotic viscosity parameter, mu_o = yield
+     stress parameter, vlam = low shear-rate threshold (0.5 by default in
+     the reference's input). */
+  int viscType;
+  double mu_o, vlam, va, vn;
 } gsls_eq_params;
+
+#define GSLS_VISC_CONST 0
+#define GSLS_VISC_CY 1
+#define GSLS_VISC_CASSON 2
 
 /* Assemble R(dof,nNo) (double) and Val(dof*dof,nnz) (double or float per
    val_prec) on device arrays from device state arrays Ag/Yg/Dg(tDof,nNo).

@@ -40,7 +40,8 @@ class EqP(C.Structure):
                 ("dmp", C.c_double), ("fb", C.c_double * 3), ("Diso", C.c_double),
                 ("mu_f", C.c_double), ("ctM", C.c_double),
                 ("ctC", C.c_double), ("eparam", c_double_p), ("elM", C.c_double),
-                ("nu", C.c_double)]
+                ("nu", C.c_double), ("viscType", C.c_int), ("mu_o", C.c_double),
+                ("vlam", C.c_double), ("va", C.c_double), ("vn", C.c_double)]
 
 
 class DirBC(C.Structure):

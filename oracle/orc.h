@@ -126,6 +126,9 @@ typedef struct {
   double ctM, ctC;             /* FLUID stabilisation constants */
   const double *eparam;        /* optional per-element parameter (mu or Diso) */
   double elM, nu;              /* LELAS elasticity modulus, Poisson ratio (f in fb) */
+  int viscType;                /* FLUID viscosity: 0 constant (mu_f), 1 Carreau-Yasuda,
+                                  2 Casson (F/FLUID.f:1690-1739) */
+  double mu_o, vlam, va, vn;   /* mu_o, lam, a, n of the model (mu_i = mu_f) */
 } orc_eqp;
 
 int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,

@@ -192,6 +192,38 @@ static int iszero(double v) {
    uxx, d2u2, es_x, mu_x and rS are identically zero and are left out; no
    mesh motion.  al, yl: tDof x 4 (u, v, w, p first); lR[a*4+i]; lK[(a*4+b)*16
    + r*4 + c] with the reference's lK(k,a,b), k = r*4 + c + 1. */
+/* GETVISCOSITY, F/FLUID.f:1690-1739: mu, mu_s and mu_x = d mu / d gamma
+   at shear rate gam; the Casson model raises gam to its threshold lam. */
+static void orc_getviscosity(const orc_eqp *p, double *gam, double *mu, double *mu_s,
+                             double *mu_x) {
+  if (p->viscType == 1) {
+    const double mu_i = p->mu_f, mu_o = p->mu_o, lam = p->vlam, a = p->va, n = p->vn;
+    double T1 = 1.0 + pow(lam * (*gam), a);
+    double T2 = pow(T1, (n - 1.0) / a);
+    *mu = mu_i + (mu_o - mu_i) * T2;
+    *mu_s = mu_i;
+    T1 = T2 / T1;
+    T2 = pow(lam, a) * pow(*gam, a - 1.0) * T1;
+    *mu_x = (mu_o - mu_i) * (n - 1.0) * T2;
+  } else if (p->viscType == 2) {
+    const double mu_i = p->mu_f, lam = p->vlam;
+    double mu_o = p->mu_o;
+    if (*gam < lam) {
+      mu_o = mu_o / sqrt(lam);
+      *gam = lam;
+    } else {
+      mu_o = mu_o / sqrt(*gam);
+    }
+    *mu = (mu_i + mu_o) * (mu_i + mu_o);
+    *mu_s = mu_i * mu_i;
+    *mu_x = 2.0 * mu_o * (mu_o + mu_i) / (*gam);
+  } else {
+    *mu = p->mu_f;
+    *mu_s = *mu;
+    *mu_x = 0.0;
+  }
+}
+
 void orc_elem_fluid(const orc_eqp *p, const double xl[12], const double *al,
                     const double *yl, double lR[16], double lK[256]) {
   double w4[4], N4[4][4], Nx[3][4], Jac, Kxi[3][3];
@@ -201,7 +233,7 @@ void orc_elem_fluid(const orc_eqp *p, const double xl[12], const double *al,
   for (int k = 0; k < 256; k++) lK[k] = 0.0;
   const int tD = p->tDof;
   const double ctM = p->ctM, ctC = p->ctC;
-  const double rho = p->rho, mu = p->mu_f;
+  const double rho = p->rho;
   const double f[3] = {p->fb[0], p->fb[1], p->fb[2]};
   const double T1c = p->af * p->gam * p->dt;
   const double amd = p->am / T1c;
@@ -236,7 +268,19 @@ void orc_elem_fluid(const orc_eqp *p, const double xl[12], const double *al,
       for (int a = 0; a < 4; a++)
         for (int i = 0; i < 3; i++)
           esNx[i][a] = es[0][i] * Nx[0][a] + es[1][i] * Nx[1][a] + es[2][i] * Nx[2][a];
-      const double mu_g = 0.0;
+      /* shear rate (2 e_ij e_ij)^(1/2) and the viscosity model, F/FLUID.f:358-373;
+         mu_x(:) = mu_g es_x . es vanishes for tet4 (no second derivatives) */
+      double gam = 0.0;
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) gam = gam + es[i][j] * es[i][j];
+      gam = sqrt(0.5 * gam);
+      double mu, mu_s, mu_g;
+      orc_getviscosity(p, &gam, &mu, &mu_s, &mu_g);
+      (void)mu_s;
+      if (iszero(gam))
+        mu_g = 0.0;
+      else
+        mu_g = mu_g / gam;
       const double kT = 4.0 * pow(ctM / p->dt, 2.0);
       double kU = 0.0, kS = 0.0;
       for (int j = 0; j < 3; j++)

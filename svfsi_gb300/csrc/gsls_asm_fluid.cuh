@@ -1,14 +1,17 @@
 // FLUID3D_M + FLUID3D_C (Code/Source/svFSI/FLUID.f:192-560, 813-1084) for
-// P1-P1 tet4 with VMS stabilisation and constant viscosity, one element per
-// thread.  Included by gsls_assemble.cu (needs AsmArgs, c_rule, adj_det3,
-// kAsmThreads).
+// P1-P1 tet4 with VMS stabilisation, one element per thread, with the
+// constant, Carreau-Yasuda or Casson viscosity of GETVISCOSITY
+// (FLUID.f:1690-1739).  Included by gsls_assemble.cu (needs AsmArgs,
+// c_rule, adj_det3, kAsmThreads).
 //
 // Same quantities as the reference, arranged for GB300:
 //  * the momentum and continuity passes of CONSTRUCT_FLUID run over the same
 //    four Gauss points with the same basis (GETTHOODFS, FS.f:270-286) and
 //    write disjoint entries, so they are fused into one point loop;
 //  * tet4 gradients are constant and the second derivatives vanish, so
-//    uxx, d2u2, es_x, mu_x and rS are zero (constant viscosity: mu_g = 0);
+//    uxx, d2u2, es_x, mu_x and rS are zero; the shear rate, mu and mu_g are
+//    element constants, and the viscosity model adds
+//    4 wl mu_g esNx_i(a) esNx_j(b) to Kuu (zero for constant viscosity);
 //  * the residual (u, ud, p, tauM, tauC, tauB, up, rM, lR) is FP64 at every
 //    Gauss point; the tangent runs in TT and is rebuilt per block (a,b) from
 //    eleven per-point factors (tauM, tauC, tauB, u.Nx_a, up.Nx_a):
@@ -24,7 +27,36 @@
 
 namespace gsls {
 
-template <class TT>
+// GETVISCOSITY (FLUID.f:1690-1739) for the Carreau-Yasuda and Casson models:
+// mu and mu_x = d mu / d gamma at shear rate gam (Casson raises gam to its
+// threshold lam first)
+__device__ __forceinline__ void visc_model(const AsmArgs &A, double &gam, double &mu,
+                                           double &mu_x) {
+  if (A.viscType == GSLS_VISC_CY) {
+    const double mi = A.mu_f, mo = A.mu_o, lam = A.vlam, a = A.va, n = A.vn;
+    double T1 = 1.0 + pow(lam * gam, a);
+    double T2 = pow(T1, (n - 1.0) / a);
+    mu = mi + (mo - mi) * T2;
+    T1 = T2 / T1;
+    T2 = pow(lam, a) * pow(gam, a - 1.0) * T1;
+    mu_x = (mo - mi) * (n - 1.0) * T2;
+  } else {
+    const double mi = A.mu_f, lam = A.vlam;
+    double mo;
+    if (gam < lam) {
+      mo = A.mu_o / sqrt(lam);
+      gam = lam;
+    } else {
+      mo = A.mu_o / sqrt(gam);
+    }
+    mu = (mi + mo) * (mi + mo);
+    mu_x = 2.0 * mo * (mo + mi) / gam;
+  }
+}
+
+// NN: a shear-rate dependent viscosity (Carreau-Yasuda or Casson); the
+// constant-viscosity kernel carries none of its terms
+template <class TT, bool NN>
 __global__ void __launch_bounds__(kAsmThreads) k_asm_fluid(AsmArgs A) {
   asm_colour_start();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -68,7 +100,21 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_fluid(AsmArgs A) {
 #pragma unroll
     for (int j = 0; j < 3; j++) es[i][j] = ux[i][j] + ux[j][i];
 
-  const double rho = A.rho, mu = A.mu_f;
+  // shear rate (2 e_ij e_ij)^(1/2), FLUID.f:358-373, and the viscosity
+  double mu = A.mu_f, mu_g = 0.0;
+  if (NN) {
+    double gam = 0.0;
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) gam += es[i][j] * es[i][j];
+    gam = sqrt(0.5 * gam);
+    double mu_x;
+    visc_model(A, gam, mu, mu_x);
+    // ISZERO (MATFUN.f:763-780): |x| < eps^2
+    mu_g = (fabs(gam) < 4.930380657631324e-32) ? 0.0 : mu_x / gam;
+  }
+  const double rho = A.rho;
   const double T1c = A.af * A.gam * A.dt;
   const double amd = A.am / T1c;
   const double wl = w * T1c, wr = w * rho;
@@ -187,6 +233,14 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_fluid(AsmArgs A) {
 #pragma unroll
     for (int a = 0; a < 4; a++) Nxa[i][a] = TT(Nx[i][a]);
   TT *Val = reinterpret_cast<TT *>(A.Val);
+  // esNx_i(a) = sum_k es(k,i) Nx_k(a) for the term 4 mu_g esNx_i(a) esNx_j(b)
+  const TT g4 = TT(4.0 * mu_g);
+  TT eN[3][4];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+      eN[i][a] = NN ? TT(es[0][i] * Nx[0][a] + es[1][i] * Nx[1][a] + es[2][i] * Nx[2][a]) : TT(0);
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     const int4 m4 = A.map[(size_t)e * 4 + a];
@@ -201,6 +255,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_fluid(AsmArgs A) {
 #pragma unroll
         for (int j = 0; j < 3; j++)
           blk[i * 4 + j] = wlt * (mu4 * Nxa[i][b] * Nxa[j][a] + SC * Nxa[i][a] * Nxa[j][b] +
+                                  (NN ? g4 * eN[i][a] * eN[j][b] : TT(0)) +
                                   (i == j ? S : TT(0)));
         blk[i * 4 + 3] = -wlt * (Nxa[i][a] * TT(c_rule.Ns[b]) - rh * Nxa[i][b] * Q[a]);
         blk[12 + i] = wlt * (TT(c_rule.Ns[a]) * Nxa[i][b] + rh * Nxa[i][a] * Vc[b]);

@@ -81,6 +81,8 @@ struct AsmArgs {
   double fb[3];
   double mu_f, ctM, ctC;
   double lam_le, mu_le;  // LELAS Lame parameters
+  int viscType;          // FLUID viscosity model (GSLS_VISC_*)
+  double mu_o, vlam, va, vn;
   const int4 *ien;
   const int4 *map;  // 4 int4 per element: map[e*4 + a] = (b0..b3)
   const double *x;
@@ -273,6 +275,19 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   A.mu_f = p->mu_f;
   A.ctM = p->ctM;
   A.ctC = p->ctC;
+  if (p->phys == GSLS_PHYS_FLUID &&
+      (p->viscType < GSLS_VISC_CONST || p->viscType > GSLS_VISC_CASSON ||
+       (p->viscType == GSLS_VISC_CY && !(p->va > 0.0)) ||
+       (p->viscType == GSLS_VISC_CASSON && !(p->vlam > 0.0)))) {
+    set_error("assembly: unknown viscosity model or a <= 0 (Carreau-Yasuda) / "
+              "threshold <= 0 (Casson)");
+    return GSLS_ERR_ARG;
+  }
+  A.viscType = p->viscType;
+  A.mu_o = p->mu_o;
+  A.vlam = p->vlam;
+  A.va = p->va;
+  A.vn = p->vn;
   if (p->phys == GSLS_PHYS_LELAS) {
     // F/LELAS.f:166-167
     A.lam_le = p->elM * p->nu / (1.0 + p->nu) / (1.0 - 2.0 * p->nu);
@@ -312,10 +327,13 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
         GSLS_TRY(asm_launch(k_asm_struct<double>, nb, st, A, pdl));
     } else if (p->phys == GSLS_PHYS_FLUID) {
       if (dof != 4 || p->s + 4 > p->tDof || !(p->rho > 0.0) || !(p->dt > 0.0)) return GSLS_ERR_ARG;
+      const bool nn = (p->viscType != GSLS_VISC_CONST);
       if (mixed)
-        GSLS_TRY(asm_launch(k_asm_fluid<float>, nb, st, A, pdl));
+        GSLS_TRY(asm_launch(nn ? k_asm_fluid<float, true> : k_asm_fluid<float, false>, nb, st, A,
+                            pdl));
       else
-        GSLS_TRY(asm_launch(k_asm_fluid<double>, nb, st, A, pdl));
+        GSLS_TRY(asm_launch(nn ? k_asm_fluid<double, true> : k_asm_fluid<double, false>, nb, st,
+                            A, pdl));
     } else if (p->phys == GSLS_PHYS_HEATF) {
       if (dof != 1 || p->tDof < 4 || p->s < 3 || p->s >= p->tDof || !(p->dt > 0.0))
         return GSLS_ERR_ARG;

@@ -216,21 +216,47 @@ def cep_slab(nx: int = 135, ny: int = 135, nz: int = 27, nsteps: int = 5000,
                    cep=cep, stim=stim)
 
 
+VISC_CONST, VISC_CY, VISC_CASSON = 0, 1, 2
+
+
+def viscosity_params(model: str = "constant", mu: float = 0.04, mu_o: float = 0.0,
+                     lam: float = 0.0, a: float = 0.0, n: float = 0.0) -> dict:
+    """Equation parameters of a viscosity model as READVISCMODEL reads them
+    (F/READFILES.f:2875-2925): "constant" (mu), "carreau-yasuda" (mu = high
+    shear-rate limit, mu_o = low shear-rate limit, lam, a, n) or "cassons"
+    (mu = asymptotic viscosity parameter, mu_o = yield stress parameter, lam
+    = low shear-rate threshold, 0.5 when not given)."""
+    m = model.lower()
+    if m in ("constant", "const", "newtonian"):
+        return dict(viscType=VISC_CONST, mu_f=mu)
+    if m in ("carreau-yasuda", "cy"):
+        if mu > mu_o:
+            raise ValueError("Carreau-Yasuda: the high shear-rate viscosity must not exceed "
+                             "the low shear-rate one")
+        return dict(viscType=VISC_CY, mu_f=mu, mu_o=mu_o, vlam=lam, va=a, vn=n)
+    if m in ("cassons", "cass"):
+        return dict(viscType=VISC_CASSON, mu_f=mu, mu_o=mu_o, vlam=lam if lam > 0 else 0.5)
+    raise ValueError(f"undefined viscosity model {model!r}")
+
+
 def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float = 5.0,
                    u_max: float = 30.0, rho: float = 1.06, mu: float = 0.04,
-                   dt: float = 1e-3) -> Problem:
+                   dt: float = 1e-3, viscosity: dict | None = None) -> Problem:
     """Config: cylinder R=0.5, L=5 (seeded Delaunay cross-section), rho 1.06,
     mu 0.04, parabolic inlet with peak u_max at z=0 (value -u_max along the
     outward normal -z, profile of BCINI), no-slip wall, traction-free outlet
     (p = 0 Neumann: no term), dt 1e-3, NS solver with RCS preconditioning and
     Krylov dimension 100 (outer tolerance 1e-2, inner GMRES 1e-2 and Schur CG
     0.2 as LS_CREATE sets them), Newton to 1e-10 (a converged implicit step:
-    ~8 iterations).  Fluid starts at rest."""
+    ~8 iterations).  Fluid starts at rest.  ``viscosity``: the result of
+    ``viscosity_params`` (default: constant mu)."""
     x, ien, info = meshgen.cylinder(R, L, h)
     rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
     am, af, beta, gam = genalpha(0.2, second_order=False)
     params = dict(am=am, af=af, beta=beta, gam=gam, dt=dt, rho=rho, mu_f=mu, ctM=1.0, ctC=36.0,
                   fb=(0.0, 0.0, 0.0))
+    if viscosity:
+        params.update(viscosity)
     inlet, wall = info["inlet"], info["wall"]
     perim = np.intersect1d(inlet, wall)
     gx = meshgen.parabolic_profile(x, info["inlet_faces"], inlet, perim)

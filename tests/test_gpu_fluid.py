@@ -237,3 +237,56 @@ def test_ns_solve_coupled_outlet_matches_oracle(gsls, orc):
     assert ls.RI.suc == ols.RI.suc
     assert ls.RI.itr == ols.RI.itr
     assert rel(R, Ro) < 1e-8
+
+
+_MODELS = {"cy": dict(model="cy", mu=0.0035, mu_o=0.16, lam=8.2, a=0.64, n=0.2128),
+           "cassons": dict(model="cassons", mu=0.0536, mu_o=0.4, lam=0.5)}
+
+
+@pytest.mark.parametrize("model", ["cy", "cassons"])
+def test_fluid_viscosity_model_assembly(gsls, orc, model):
+    """Carreau-Yasuda and Casson viscosity (GETVISCOSITY): FP64 assembly at
+    1e-12 and the FP32 tangent at 1e-5 against the oracle."""
+    torch = pytest.importorskip("torch")
+    p = problems.fluid_cylinder(h=0.1, nsteps=1, viscosity=problems.viscosity_params(**_MODELS[model]))
+    A, Y = _state(p, seed=4)
+    R0, V0 = orc.assemble(p, A, Y)
+    lhs = _lhs(p, 1)
+    mesh = fsils.Mesh(lhs, p.ien, p.x)
+    R, Val = mesh.assemble(p.eq_params(), A, Y, np.zeros_like(Y), p.dof)
+    assert rel(R, R0) < 1e-12
+    assert rel(Val, V0) < 1e-12
+    dA = torch.tensor(A, device="cuda")
+    dY = torch.tensor(Y, device="cuda")
+    dR = torch.zeros((p.nNo, 4), dtype=torch.float64, device="cuda")
+    dV = torch.zeros((p.nnz, 16), dtype=torch.float32, device="cuda")
+    prm = p.eq_params()
+    _lib.check(gsls.gsls_assemble_dev(mesh.h, C.byref(prm), C.c_void_p(dA.data_ptr()),
+                                      C.c_void_p(dY.data_ptr()), C.c_void_p(torch.zeros_like(dY).data_ptr()),
+                                      C.c_void_p(dR.data_ptr()), C.c_void_p(dV.data_ptr()),
+                                      fsils.PREC_MIXED))
+    torch.cuda.synchronize()
+    assert rel(dR.cpu().numpy(), R0) < 1e-12
+    assert rel(dV.cpu().numpy().astype(np.float64), V0) < 1e-5
+
+
+@pytest.mark.parametrize("model", ["cy", "cassons"])
+def test_fluid_viscosity_model_steps(gsls, orc, model):
+    """Two converged steps of the shear-thinning fluid (Newton to 1e-10,
+    RCS + NS solver) land on the oracle's state."""
+    p = problems.fluid_cylinder(h=0.1, nsteps=2, viscosity=problems.viscosity_params(**_MODELS[model]))
+    lhs, mesh, eq = problems.build_equation(p)
+    oeq = orc.OracleEquation(p)
+    for _ in range(p.nsteps):
+        gi = eq.step()
+        oi = oeq.step()
+        assert gi.last_suc == 1 and oi.last_suc == 1
+    assert rel(eq.get_state()[1], oeq.state()[1]) < 1e-8
+
+
+def test_unknown_viscosity_model_is_rejected(gsls):
+    p = problems.fluid_cylinder(h=0.2, nsteps=1)
+    p.params["viscType"] = 7
+    lhs, mesh, eq = problems.build_equation(p)
+    with pytest.raises(_lib.GslsError, match="viscosity"):
+        eq.step()

@@ -569,3 +569,81 @@ def test_heatf_linear_profile_across_the_flow_is_steady(orc):
     interior = (r < 0.5 - 1e-9) & (p.x[:, 2] > 1e-9) & (p.x[:, 2] < 5.0 - 1e-9)
     assert interior.sum() > 10
     assert np.abs(R[interior]).max() < 1e-12 * np.abs(R).max()
+
+
+def _cy_mu(g, mi, mo, lam, a, n):
+    """Carreau-Yasuda viscosity and d mu / d gamma, written from the model:
+    mu = mi + (mo - mi) (1 + (lam g)^a)^((n - 1)/a)."""
+    T = 1.0 + (lam * g) ** a
+    mu = mi + (mo - mi) * T ** ((n - 1.0) / a)
+    dmu = (mo - mi) * (n - 1.0) * T ** ((n - 1.0) / a - 1.0) * lam ** a * g ** (a - 1.0)
+    return mu, dmu
+
+
+def _casson_mu(g, mi, mo, lam):
+    """Casson viscosity (sqrt(mi) form of the input) and d mu / d gamma, with
+    the shear rate held at the threshold lam below it."""
+    g = max(g, lam)
+    r = mo / np.sqrt(g)
+    return (mi + r) ** 2, 2.0 * r * (r + mi) / g, g
+
+
+@pytest.mark.parametrize("model", ["cy", "cassons", "cassons_above_threshold"])
+def test_fluid_viscosity_models(orc, model):
+    """tet4 velocity gradients are element constants, so with a shear-rate
+    dependent viscosity (GETVISCOSITY) the element residual equals the
+    constant-viscosity residual at mu(gamma_e), and the tangent differs from
+    it by 4 wl mu_g esNx_i(a) esNx_j(b) (mu_g = mu'(gamma)/gamma)."""
+    p = _fluid_box(1)
+    rng = np.random.default_rng(7)
+    xl = _unit_tet() + 0.1 * rng.standard_normal((4, 3))
+    yl = rng.standard_normal((4, 4))
+    al = rng.standard_normal((4, 4))
+    G = np.linalg.inv((xl[:3] - xl[3]).T)          # G[a, i] = d xi_a / d x_i
+    Nx = np.zeros((3, 4))                          # Nx[i, a] = d N_a / d x_i
+    Nx[:, :3] = G.T
+    Nx[:, 3] = -G.T.sum(axis=1)
+    ux = Nx @ yl[:, :3]                            # ux[i, j] = d u_j / d x_i
+    es = ux + ux.T
+    gam = np.sqrt(0.5 * np.sum(es * es))
+    if model == "cy":
+        vp = problems.viscosity_params("cy", mu=0.0035, mu_o=0.16, lam=8.2, a=0.64, n=0.2128)
+        mu, dmu = _cy_mu(gam, 0.0035, 0.16, 8.2, 0.64, 0.2128)
+        g_used = gam
+    else:
+        lam = gam * (1.5 if model == "cassons" else 0.5)
+        vp = problems.viscosity_params("cassons", mu=0.0536, mu_o=0.4, lam=lam)
+        mu, dmu, g_used = _casson_mu(gam, 0.0536, 0.4, lam)
+    mu_g = dmu / g_used
+
+    def elem(params):
+        eqp = orc.eqp_from(p)
+        for k, v in params.items():
+            setattr(eqp, k, v)
+        lR, lK = np.zeros(16), np.zeros(256)
+        orc.load().orc_elem_fluid(C.byref(eqp), orc.dp(orc.f64(xl.ravel())), orc.dp(orc.f64(al.ravel())),
+                                  orc.dp(orc.f64(yl.ravel())), orc.dp(lR), orc.dp(lK))
+        return lR, lK
+
+    R1, K1 = elem(vp)
+    R0, K0 = elem(problems.viscosity_params("constant", mu=mu))
+    assert np.allclose(R1, R0, rtol=1e-12, atol=1e-12 * np.abs(R0).max())
+    prm = p.params
+    wl = abs(np.linalg.det((xl[:3] - xl[3]).T)) / 24.0 * prm["af"] * prm["gam"] * prm["dt"]
+    esNx = es.T @ Nx                               # esNx[i, a] = sum_k es[k, i] Nx[k, a]
+    for a in range(4):
+        for b in range(4):
+            d = (K1 - K0)[(a * 4 + b) * 16:(a * 4 + b + 1) * 16].reshape(4, 4)
+            ref = 4 * wl * mu_g * np.outer(esNx[:, a], esNx[:, b])
+            assert np.allclose(d[:3, :3], ref, rtol=1e-9, atol=1e-12 * np.abs(K0).max())
+            assert np.abs(d[3, :]).max() <= 1e-12 * np.abs(K0).max()
+            assert np.abs(d[:3, 3]).max() <= 1e-12 * np.abs(K0).max()
+
+
+def test_viscosity_params_follow_the_input_rules():
+    assert problems.viscosity_params("newtonian", mu=0.04) == {"viscType": 0, "mu_f": 0.04}
+    assert problems.viscosity_params("cass", mu=1.0, mu_o=2.0)["vlam"] == 0.5
+    with pytest.raises(ValueError):
+        problems.viscosity_params("cy", mu=0.2, mu_o=0.1, lam=1, a=1, n=0.5)
+    with pytest.raises(ValueError):
+        problems.viscosity_params("power-law")
