@@ -258,6 +258,13 @@ int gsls_eq_add_dirichlet(gsls_eq *eq, int nNo, const int *gNodes,
 int gsls_eq_add_dirichlet_nv(gsls_eq *eq, int nNo, const int *gNodes,
                              const double *gx, const double *nV, double g,
                              int mask);
+/* Neumann BC of value g on tri3 faces (fIEN 1-based, 3 x nFel) of a HEATF
+   equation: BASSEMNEUBC with BHEATF (Code/Source/svFSI/EQASSEM.f:90-192,
+   HEATF.f:289-319) at every Newton iteration, h = -g (SETBCNEUL,
+   SETBC.f:300) and the backflow term min(u.n, 0) T with its tangent; the
+   outward normal is oriented away from the parent element's fourth node
+   (GNNB, NN.f:1856-1990).  Other physics: GSLS_ERR_UNSUPPORTED. */
+int gsls_eq_add_neumann(gsls_eq *eq, int nFel, const int *fIEN, double g);
 /* Constant traction h on tri3 faces (fIEN 1-based, 3 x nFel), integrated
    as SETBCTRACL does (Code/Source/svFSI/SETBC.f:319-416). */
 int gsls_eq_add_traction(gsls_eq *eq, int nFel, const int *fIEN,

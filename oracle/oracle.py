@@ -58,6 +58,10 @@ class CepP(C.Structure):
                 ("Td", C.c_double), ("CL", C.c_double), ("Ksac", C.c_double)]
 
 
+class NeuBC(C.Structure):
+    _fields_ = [("nFel", C.c_int), ("fIEN", c_int_p), ("g", C.c_double)]
+
+
 class Eq(C.Structure):
     _fields_ = [("p", EqP), ("nNo", C.c_int), ("nEl", C.c_int), ("IEN", c_int_p),
                 ("x", c_double_p), ("rowPtr", c_int_p), ("colPtr", c_int_p), ("nnz", C.c_int),
@@ -72,7 +76,7 @@ class Eq(C.Structure):
                 ("An", c_double_p), ("Yn", c_double_p), ("Dn", c_double_p),
                 ("eq_iNorm", C.c_double), ("eq_pNorm", C.c_double),
                 ("cep", CepP), ("stim", c_int_p), ("Xion", c_double_p), ("time", C.c_double),
-                ("cep_ipass_done", C.c_int)]
+                ("cep_ipass_done", C.c_int), ("nNeu", C.c_int), ("neu", C.POINTER(NeuBC))]
 
 
 class StepInfo(C.Structure):
@@ -286,6 +290,15 @@ class OracleEquation:
         keep(tr)
         eq.nTrac = len(p.traction)
         eq.trac = C.cast(tr, C.POINTER(TracBC))
+        neus = getattr(p, "neumann", [])
+        nb = (NeuBC * max(1, len(neus)))()
+        for k, nf in enumerate(neus):
+            nb[k].nFel = nf.faces.shape[0]
+            nb[k].fIEN = ip(keep(i32(nf.faces)))
+            nb[k].g = nf.g
+        keep(nb)
+        eq.nNeu = len(neus)
+        eq.neu = C.cast(nb, C.POINTER(NeuBC))
         eq.LS_type, eq.prec = p.LS_type, p.prec
         eq.ls_relTol, eq.ls_absTol, eq.ls_mItr, eq.ls_sD = p.ls_relTol, p.ls_absTol, p.ls_mItr, p.ls_sD
         eq.ls_relTolIn[0] = eq.ls_relTolIn[1] = -1.0

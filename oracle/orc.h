@@ -159,6 +159,12 @@ void orc_pk2cc_nhk(double C10, double Kpen, const double F[9], double S[9],
                    double Dm[36]);
 void orc_traction(int dof, int nFel, const int *fIEN, const double *x,
                   const double h[3], double *R);
+/* BASSEMNEUBC with BHEATF (F/EQASSEM.f:90-192, F/HEATF.f:289-319) on tri3
+   faces: h = -g (F/SETBC.f:300), outward normal from the parent element
+   (GNNB, F/NN.f:1856-1990), into R(1,nNo) and the scalar CSR Val */
+void orc_bheatf(const orc_eqp *p, int nFel, const int *fIEN, double g, int nEl,
+                const int *IEN, const double *x, const double *Yg, const int *rowPtr,
+                const int *colPtr, double *R, double *Val);
 
 /* CEP3D with isotropic diffusivity, F/CEP.f:136-266 (no fibres) */
 void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12],
@@ -200,6 +206,13 @@ typedef struct {
   double h[3];
 } orc_tracbc;
 
+/* Neumann face set of a HEATF equation: value g (BASSEMNEUBC + BHEATF) */
+typedef struct {
+  int nFel;
+  const int *fIEN;    /* 3 x nFel, 0-based */
+  double g;
+} orc_neubc;
+
 typedef struct {
   orc_eqp p;
   int nNo, nEl;
@@ -224,6 +237,7 @@ typedef struct {
   double *Xion;
   double time;
   int cep_ipass_done;
+  int nNeu; const orc_neubc *neu;  /* HEATF Neumann faces */
 } orc_eq;
 
 typedef struct {

@@ -927,6 +927,77 @@ int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
 
 /* SETBCTRACL for tri3 faces with a constant traction vector h,
    F/SETBC.f:319-416; 3-point rule F/NN.f:416-422, w = 1/6. */
+void orc_bheatf(const orc_eqp *p, int nFel, const int *fIEN, double g, int nEl,
+                const int *IEN, const double *x, const double *Yg, const int *rowPtr,
+                const int *colPtr, double *R, double *Val) {
+  const int tD = p->tDof;
+  const double h = -g;
+  const double s = 2.0 / 3.0, t = 1.0 / 6.0;
+  const double xi[3][2] = {{t, t}, {s, t}, {t, s}};
+  for (int f = 0; f < nFel; f++) {
+    const int *q = fIEN + 3 * f;
+    /* the element holding the face, and its node off the face */
+    int inner = -1;
+    for (int e = 0; e < nEl && inner < 0; e++) {
+      int hit = 0, other = -1;
+      for (int a = 0; a < 4; a++) {
+        const int v = IEN[4 * e + a];
+        if (v == q[0] || v == q[1] || v == q[2])
+          hit++;
+        else if (other < 0)
+          other = v;
+      }
+      if (hit == 3) inner = other;
+    }
+    if (inner < 0) continue;
+    /* GNNB for tri3: n = (x1 - x3) x (x2 - x3), pointing away from the
+       element's other node */
+    double e1[3], e2[3], n[3], v[3];
+    for (int i = 0; i < 3; i++) {
+      e1[i] = x[3 * q[0] + i] - x[3 * q[2] + i];
+      e2[i] = x[3 * q[1] + i] - x[3 * q[2] + i];
+      v[i] = x[3 * q[0] + i] - x[3 * inner + i];
+    }
+    n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    if (n[0] * v[0] + n[1] * v[1] + n[2] * v[2] < 0.0)
+      for (int i = 0; i < 3; i++) n[i] = -n[i];
+    const double Jac = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    double nV[3];
+    for (int i = 0; i < 3; i++) nV[i] = n[i] / Jac;
+    double lR[3] = {0, 0, 0}, lK[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int gp = 0; gp < 3; gp++) {
+      const double N[3] = {xi[gp][0], xi[gp][1], 1.0 - xi[gp][0] - xi[gp][1]};
+      const double w = (1.0 / 6.0) * Jac;
+      const double wl = w * p->af * p->gam * p->dt;
+      double y[4] = {0, 0, 0, 0};
+      for (int a = 0; a < 3; a++) {
+        for (int i = 0; i < 3; i++) y[i] = y[i] + N[a] * Yg[(size_t)q[a] * tD + i];
+        y[3] = y[3] + N[a] * Yg[(size_t)q[a] * tD + p->s];
+      }
+      double udn = 0.0;
+      for (int i = 0; i < 3; i++) udn = udn + y[i] * nV[i];
+      udn = 0.5 * (udn - fabs(udn));
+      const double T1 = h - udn * y[3];
+      for (int a = 0; a < 3; a++) {
+        lR[a] = lR[a] + w * N[a] * T1;
+        for (int b = 0; b < 3; b++) lK[3 * a + b] = lK[3 * a + b] - wl * N[a] * N[b] * udn;
+      }
+    }
+    /* DOASSEM for the face element */
+    for (int a = 0; a < 3; a++) {
+      R[q[a]] += lR[a];
+      for (int b = 0; b < 3; b++)
+        for (int j = rowPtr[q[a]]; j < rowPtr[q[a] + 1]; j++)
+          if (colPtr[j] == q[b]) {
+            Val[j] += lK[3 * a + b];
+            break;
+          }
+    }
+  }
+}
+
 void orc_traction(int dof, int nFel, const int *fIEN, const double *x,
                   const double h[3], double *R) {
   const double s = 2.0 / 3.0, t = 1.0 / 6.0;
@@ -1085,6 +1156,10 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
     /* SETBCNEU (traction) */
     for (int t = 0; t < eq->nTrac; t++)
       orc_traction(dof, eq->trac[t].nFel, eq->trac[t].fIEN, eq->x, eq->trac[t].h, R);
+    /* BASSEMNEUBC (HEATF Neumann faces) */
+    for (int k = 0; k < eq->nNeu; k++)
+      orc_bheatf(&eq->p, eq->neu[k].nFel, eq->neu[k].fIEN, eq->neu[k].g, eq->nEl, eq->IEN,
+                 eq->x, Yg, eq->rowPtr, eq->colPtr, R, Val);
     /* LSSOLVE */
     rc = orc_solve(lhs, &ls, dof, R, Val, eq->prec, incL, res);
     if (rc) break;

@@ -110,6 +110,7 @@ SIGNATURES = {
     "gsls_eq_add_dirichlet_nv": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_double_p, c_double_p,
                                            C.c_double, C.c_int]),
     "gsls_eq_add_traction": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_double_p]),
+    "gsls_eq_add_neumann": (C.c_int, [C.c_void_p, C.c_int, c_int_p, C.c_double]),
     "gsls_eq_set_state": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p]),
     "gsls_eq_get_state": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p]),
     "gsls_eq_state_dev": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),

@@ -500,6 +500,16 @@ int mesh_mass(gsls_mesh *m, const double *zeros, double *R, double *Val) {
   return GSLS_OK;
 }
 
+// host copies for boundary-face setup: IEN (0-based, colour order, 4 per
+// element) and the coordinates (3 per node)
+int mesh_host_geometry(gsls_mesh *m, const int **ien, int *nEl, std::vector<double> &x) {
+  *ien = m->h_ien.data();
+  *nEl = m->nEl;
+  x.resize((size_t)m->nNo * 3);
+  GSLS_CUDA(cudaMemcpy(x.data(), m->d_x.p, sizeof(double) * x.size(), cudaMemcpyDeviceToHost));
+  return GSLS_OK;
+}
+
 // colour-order index -> original element index
 const int *mesh_perm(gsls_mesh *m, int *nEl) {
   *nEl = m->nEl;

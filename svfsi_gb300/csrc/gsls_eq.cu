@@ -20,6 +20,7 @@ int mesh_dRdp(gsls_mesh *m, const gsls_eq_params *p, const double *Yg, const dou
               const double *lam, double *out, double scale);
 int mesh_mass(gsls_mesh *m, const double *zeros, double *R, double *Val);
 const int *mesh_perm(gsls_mesh *m, int *nEl);
+int mesh_host_geometry(gsls_mesh *m, const int **ien, int *nEl, std::vector<double> &x);
 int mesh_set_eparam(gsls_mesh *m, const double *eparam);
 int mesh_check_error(gsls_mesh *m);
 gsls_lhs *mesh_lhs(gsls_mesh *m);
@@ -44,6 +45,15 @@ struct gsls_eq {
     int mask = 0;
   };
   std::vector<Dir *> dirs;
+  // HEATF Neumann face sets (BASSEMNEUBC with BHEATF), faces in colour order
+  struct Neu {
+    gsls::DevBuf fien;      // int, 3 per face (0-based nodes)
+    gsls::DevBuf geo;       // double, 4 per face: outward unit normal, |n|
+    gsls::DevBuf pos;       // int, 9 per face: CSR position of (a, b)
+    std::vector<int> coff;  // colour offsets
+    double h = 0.0;         // SETBCNEUL's nodal value -g
+  };
+  std::vector<Neu *> neus;
   int nextFace = 0;
   double eq_iNorm = 0.0, eq_pNorm = 0.0;
   // CEP cell model
@@ -55,6 +65,7 @@ struct gsls_eq {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   ~gsls_eq() {
     for (auto *d : dirs) delete d;
+    for (auto *n : neus) delete n;
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
   }
@@ -137,6 +148,56 @@ __global__ void k_picc(int nNo, int tDof, int s, int dof, double c1, double c2,
     An[k] = An[k] - r;
     Yn[k] = Yn[k] - r * c1;
     Dn[k] = Dn[k] - r * c2;
+  }
+}
+
+// BASSEMNEUBC + BHEATF (Code/Source/svFSI/EQASSEM.f:90-192, HEATF.f:289-319)
+// on tri3 faces, one face per thread, faces of one colour share no node:
+// at the 3 points of the face rule (w = 1/6, GNN's xi table, NN.f:416-422)
+// y = sum N_a y_a, udn = min(u.n, 0) and
+//   lR(a)   += w N_a (h - udn T),  lK(a,b) -= w af gam dt N_a N_b udn
+// with w = 1/6 |n| and h = -g (SETBCNEUL, SETBC.f:300).
+template <class VT>
+__global__ void k_bheatf(int nF, int f0, const int *__restrict__ fien,
+                         const double *__restrict__ geo, const int *__restrict__ pos,
+                         const double *__restrict__ Yg, int tDof, int s, double h, double T1,
+                         double *R, VT *Val) {
+  const int f = f0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= f0 + nF) return;
+  const int n[3] = {fien[3 * f], fien[3 * f + 1], fien[3 * f + 2]};
+  const double nv[3] = {geo[4 * f], geo[4 * f + 1], geo[4 * f + 2]}, Jac = geo[4 * f + 3];
+  double yl[3][4];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) yl[a][i] = Yg[(size_t)n[a] * tDof + i];
+    yl[a][3] = Yg[(size_t)n[a] * tDof + s];
+  }
+  const double xs = 2.0 / 3.0, xt = 1.0 / 6.0;
+  const double xi[3][2] = {{xt, xt}, {xs, xt}, {xt, xs}};
+  const double w = Jac / 6.0, wl = w * T1;
+  double lR[3] = {0, 0, 0}, lK[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+  for (int g = 0; g < 3; g++) {
+    const double N[3] = {xi[g][0], xi[g][1], 1.0 - xi[g][0] - xi[g][1]};
+    double y[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) y[c] = N[0] * yl[0][c] + N[1] * yl[1][c] + N[2] * yl[2][c];
+    double udn = y[0] * nv[0] + y[1] * nv[1] + y[2] * nv[2];
+    udn = 0.5 * (udn - fabs(udn));
+    const double T1r = h - udn * y[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      lR[a] += w * N[a] * T1r;
+#pragma unroll
+      for (int b = 0; b < 3; b++) lK[a][b] -= wl * N[a] * N[b] * udn;
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    R[n[a]] += lR[a];
+#pragma unroll
+    for (int b = 0; b < 3; b++) Val[pos[9 * f + 3 * a + b]] += VT(lK[a][b]);
   }
 }
 
@@ -325,6 +386,126 @@ int gsls_eq_add_dirichlet_nv(gsls_eq *eq, int nNo, const int *gNodes, const doub
   }
   GSLS_CUDA(cudaStreamSynchronize(lhs->stream));
   eq->dirs.push_back(d);
+  return GSLS_OK;
+}
+
+int gsls_eq_add_neumann(gsls_eq *eq, int nFel, const int *fIEN, double g) {
+  if (!eq || nFel < 0 || (nFel > 0 && !fIEN)) return GSLS_ERR_ARG;
+  if (eq->p.phys != GSLS_PHYS_HEATF) {
+    set_error("gsls_eq_add_neumann: only the HEATF boundary term (BHEATF) is built");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  gsls_lhs *lhs = eq->lhs;
+  const int *ien = nullptr;
+  int nEl = 0;
+  std::vector<double> x;
+  GSLS_TRY(mesh_host_geometry(eq->mesh, &ien, &nEl, x));
+  const int nNo = eq->nNo;
+  // elements of the face nodes (node -> elements, face nodes only)
+  std::vector<char> onF(nNo, 0);
+  std::vector<int> fn((size_t)3 * nFel);
+  for (size_t k = 0; k < fn.size(); k++) {
+    fn[k] = fIEN[k] - 1;
+    if (fn[k] < 0 || fn[k] >= nNo) {
+      set_error("gsls_eq_add_neumann: face node out of range");
+      return GSLS_ERR_ARG;
+    }
+    onF[fn[k]] = 1;
+  }
+  std::vector<std::vector<int>> elOf(nNo);
+  for (int e = 0; e < nEl; e++)
+    for (int a = 0; a < 4; a++)
+      if (onF[ien[4 * e + a]]) elOf[ien[4 * e + a]].push_back(e);
+  std::vector<double> geo((size_t)4 * nFel);
+  std::vector<int> pos((size_t)9 * nFel);
+  const std::vector<int> &rp = lhs->h_rowPtr, &cp = lhs->h_colPtr;
+  for (int f = 0; f < nFel; f++) {
+    const int *q = &fn[(size_t)3 * f];
+    // parent element and its node off the face (GNNB, NN.f:1856-1990)
+    int inner = -1;
+    for (int e : elOf[q[0]]) {
+      int hit = 0, other = -1;
+      for (int a = 0; a < 4; a++) {
+        const int v = ien[4 * e + a];
+        if (v == q[0] || v == q[1] || v == q[2]) hit++;
+        else if (other < 0) other = v;
+      }
+      if (hit == 3) {
+        inner = other;
+        break;
+      }
+    }
+    if (inner < 0) {
+      set_error("gsls_eq_add_neumann: a face is not a face of any element");
+      return GSLS_ERR_ARG;
+    }
+    double e1[3], e2[3], n[3], v[3];
+    for (int i = 0; i < 3; i++) {
+      e1[i] = x[3 * q[0] + i] - x[3 * q[2] + i];
+      e2[i] = x[3 * q[1] + i] - x[3 * q[2] + i];
+      v[i] = x[3 * q[0] + i] - x[3 * inner + i];
+    }
+    n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    if (n[0] * v[0] + n[1] * v[1] + n[2] * v[2] < 0.0)
+      for (int i = 0; i < 3; i++) n[i] = -n[i];
+    const double J = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int i = 0; i < 3; i++) geo[(size_t)4 * f + i] = n[i] / J;
+    geo[(size_t)4 * f + 3] = J;
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) {
+        const int *lo = cp.data() + rp[q[a]], *hi = cp.data() + rp[q[a] + 1];
+        const int *it = std::lower_bound(lo, hi, q[b]);
+        if (it == hi || *it != q[b]) {
+          set_error("gsls_eq_add_neumann: face node pair missing from the CSR graph");
+          return GSLS_ERR_ARG;
+        }
+        pos[(size_t)9 * f + 3 * a + b] = (int)(it - cp.data());
+      }
+  }
+  // colouring: a face takes one colour above the highest colour already at
+  // any of its nodes, so faces of one colour share no node
+  std::vector<int> col(nFel, -1), last(nNo, -1);
+  int ncol = 0;
+  for (int f = 0; f < nFel; f++) {
+    int c = 0;
+    for (int a = 0; a < 3; a++) c = std::max(c, last[fn[(size_t)3 * f + a]] + 1);
+    col[f] = c;
+    for (int a = 0; a < 3; a++) last[fn[(size_t)3 * f + a]] = c;
+    ncol = std::max(ncol, c + 1);
+  }
+  auto *nf = new gsls_eq::Neu();
+  nf->h = -g;
+  nf->coff.assign(ncol + 1, 0);
+  for (int f = 0; f < nFel; f++) nf->coff[col[f] + 1]++;
+  for (int c = 0; c < ncol; c++) nf->coff[c + 1] += nf->coff[c];
+  std::vector<int> at(nf->coff.begin(), nf->coff.end() - 1);
+  std::vector<int> fs((size_t)3 * nFel), ps((size_t)9 * nFel);
+  std::vector<double> gs((size_t)4 * nFel);
+  for (int f = 0; f < nFel; f++) {
+    const int k = at[col[f]]++;
+    for (int a = 0; a < 3; a++) fs[(size_t)3 * k + a] = fn[(size_t)3 * f + a];
+    for (int a = 0; a < 9; a++) ps[(size_t)9 * k + a] = pos[(size_t)9 * f + a];
+    for (int a = 0; a < 4; a++) gs[(size_t)4 * k + a] = geo[(size_t)4 * f + a];
+  }
+  const size_t nb = nFel > 0 ? nFel : 1;
+  int rc = GSLS_OK;
+  if (nf->fien.alloc(sizeof(int) * 3 * nb) != GSLS_OK || nf->pos.alloc(sizeof(int) * 9 * nb) != GSLS_OK ||
+      nf->geo.alloc(sizeof(double) * 4 * nb) != GSLS_OK) {
+    rc = GSLS_ERR_CUDA;
+  } else if (nFel > 0 &&
+             (cudaMemcpy(nf->fien.p, fs.data(), sizeof(int) * fs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(nf->pos.p, ps.data(), sizeof(int) * ps.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(nf->geo.p, gs.data(), sizeof(double) * gs.size(), cudaMemcpyHostToDevice) != cudaSuccess)) {
+    rc = GSLS_ERR_CUDA;
+  }
+  if (rc != GSLS_OK) {
+    delete nf;
+    set_error("gsls_eq_add_neumann: device copy failed");
+    return rc;
+  }
+  eq->neus.push_back(nf);
   return GSLS_OK;
 }
 
@@ -611,6 +792,22 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     if (eq->has_trac) {
       k_axpy1<<<nblk(nr), kT, 0, st>>>(nr, eq->R.as<double>(), eq->Ftrac.as<double>());
       GSLS_CHECK_LAUNCH();
+    }
+    for (auto *nf : eq->neus) {
+      const double T1 = p.af * p.gam * p.dt;
+      for (size_t c = 0; c + 1 < nf->coff.size(); c++) {
+        const int f0 = nf->coff[c], n = nf->coff[c + 1] - f0;
+        if (n <= 0) continue;
+        if (valp == GSLS_PREC_MIXED)
+          k_bheatf<float><<<(n + 127) / 128, 128, 0, st>>>(
+              n, f0, nf->fien.as<int>(), nf->geo.as<double>(), nf->pos.as<int>(), Yg, tD, p.s,
+              nf->h, T1, eq->R.as<double>(), eq->Val.as<float>());
+        else
+          k_bheatf<double><<<(n + 127) / 128, 128, 0, st>>>(
+              n, f0, nf->fien.as<int>(), nf->geo.as<double>(), nf->pos.as<int>(), Yg, tD, p.s,
+              nf->h, T1, eq->R.as<double>(), eq->Val.as<double>());
+        GSLS_CHECK_LAUNCH();
+      }
     }
     cudaEventRecord(eq->e1, st);
     auto t0 = std::chrono::steady_clock::now();

@@ -177,6 +177,12 @@ class Equation:
                                                    float(g), int(mask)),
               "gsls_eq_add_dirichlet_nv")
 
+    def add_neumann(self, faces0, g):
+        """Neumann BC of value g on tri3 faces (HEATF: BASSEMNEUBC + BHEATF)."""
+        f1 = _i32(np.asarray(faces0) + 1)
+        check(_lib.load().gsls_eq_add_neumann(self.h, f1.shape[0], _ip(f1), float(g)),
+              "gsls_eq_add_neumann")
+
     def add_traction(self, faces0, h):
         f1 = _i32(np.asarray(faces0) + 1)
         hh = _f64(h)

@@ -55,6 +55,12 @@ class TracBC:
 
 
 @dataclass
+class NeuBC:
+    faces: np.ndarray   # (nFel, 3) 0-based
+    g: float            # Neumann value (HEATF: flux g, backflow term added)
+
+
+@dataclass
 class Problem:
     name: str
     x: np.ndarray
@@ -67,6 +73,7 @@ class Problem:
     params: dict
     dirichlet: list = field(default_factory=list)
     traction: list = field(default_factory=list)
+    neumann: list = field(default_factory=list)
     LS_type: int = LS_TYPE_CG
     prec: int = PRECOND_FSILS
     ls_relTol: float = -1.0
@@ -321,6 +328,8 @@ def equation_on(p: Problem, mesh, precision=PREC_FP64):
         eq.add_dirichlet(d.nodes, d.g, d.gx, d.mask, d.nV)
     for t in p.traction:
         eq.add_traction(t.faces, t.h)
+    for nf in p.neumann:
+        eq.add_neumann(nf.faces, nf.g)
     if p.cep:
         eq.set_cep(p.cep, np.nonzero(p.stim)[0])
     Ao, Yo, Do = p.initial_state()

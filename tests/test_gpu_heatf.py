@@ -20,7 +20,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from svfsi_gb300 import _lib, fsils, problems
+from svfsi_gb300 import _lib, fsils, meshgen, problems
 
 pytestmark = pytest.mark.gpu
 
@@ -102,3 +102,35 @@ def test_heatf_steps(gsls, orc, precision):
     dT, dTo = Y[:, 4] - q.Y0[:, 4], Yo[:, 4] - q.Y0[:, 4]
     assert np.abs(dTo).max() > 1e-4  # the temperature moved
     assert rel(dT, dTo) < (1e-9 if precision == "fp64" else 1e-4)
+
+
+@pytest.mark.parametrize("u_max,g", [(-3.0, 0.0), (3.0, 0.5)])
+def test_heatf_outlet_neumann_face(gsls, orc, u_max, g):
+    """A Neumann face on the outlet plane z = 5 (BASSEMNEUBC + BHEATF): with
+    the flow reversed the backflow term min(u.n, 0) T and its tangent act,
+    with forward flow the flux -g alone; the temperature change of one step
+    (2 Newton iterations, GMRES(20)) matches the oracle to 1e-9 and differs
+    from the step without the face."""
+    def run(with_face):
+        p = problems.heatf_cylinder(h=0.2, nsteps=1, u_max=u_max, cond=1.0, T0_linear=True)
+        p.maxItr, p.ls_sD, p.ls_mItr, p.ls_relTol = 2, 20, 20, 1e-12
+        if with_face:
+            p.neumann = [problems.NeuBC(meshgen.faces_on_plane(p.x, p.ien, 2, 5.0), g)]
+        _, _, eq = problems.build_equation(p)
+        oeq = orc.OracleEquation(p)
+        oeq.set_state(*p.initial_state())
+        eq.step()
+        oeq.step()
+        return (eq.get_state()[1][:, 4] - p.Y0[:, 4], oeq.state()[1][:, 4] - p.Y0[:, 4])
+
+    dT, dTo = run(True)
+    assert rel(dT, dTo) < 1e-9
+    dT0, _ = run(False)
+    assert rel(dT, dT0) > 1e-6
+
+
+def test_neumann_face_of_other_physics_is_unsupported(gsls):
+    p = problems.heats_cube(3, nsteps=1)
+    _, _, eq = problems.build_equation(p)
+    with pytest.raises(_lib.GslsError, match="BHEATF"):
+        eq.add_neumann(meshgen.faces_on_plane(p.x, p.ien, 0, 1.0), 1.0)

@@ -647,3 +647,38 @@ def test_viscosity_params_follow_the_input_rules():
         problems.viscosity_params("cy", mu=0.2, mu_o=0.1, lam=1, a=1, n=0.5)
     with pytest.raises(ValueError):
         problems.viscosity_params("power-law")
+
+
+def test_bheatf_uniform_state_kat(orc):
+    """BHEATF on one face of the unit tet with uniform velocity and
+    temperature: every node gets area/3 (h - min(u.n, 0) T) with h = -g, the
+    outward normal points away from the fourth node, and the tangent is
+    -wl udn M_face (row sums area/3 af gam dt (-udn))."""
+    x = _unit_tet()
+    ien = np.array([[0, 1, 2, 3]], np.int32)
+    rp, cp = meshgen.csr_from_ien(4, ien)
+    p = problems.heatf_cylinder(h=0.5, nsteps=1)  # parameters only
+    eqp = orc.eqp_from(p)
+    # face (x1, x2, x4) = (1,0,0), (0,1,0), (0,0,0) lies in z = 0; its outward
+    # normal is -z, away from x3 = (0,0,1)
+    face = np.array([[0, 1, 3]], np.int32)
+    T, g = 2.0, 0.3
+    for uz, udn in ((1.0, -1.0), (-1.0, 0.0)):    # u.n = -uz
+        Y = np.zeros((4, 5))
+        Y[:, 2] = uz
+        Y[:, 4] = T
+        R = np.zeros(4)
+        Val = np.zeros(cp.size)
+        orc.load().orc_bheatf(C.byref(eqp), 1, orc.ip(orc.i32(face.ravel())), C.c_double(g), 1,
+                              orc.ip(orc.i32(ien.ravel())), orc.dp(orc.f64(x.ravel())),
+                              orc.dp(orc.f64(Y.ravel())), orc.ip(orc.i32(rp)), orc.ip(orc.i32(cp)),
+                              orc.dp(R), orc.dp(Val))
+        area = 0.5
+        exp = area / 3.0 * (-g - udn * T)
+        assert np.allclose(R[[0, 1, 3]], exp, rtol=1e-14, atol=1e-15)
+        assert R[2] == 0.0
+        T1 = eqp.af * eqp.gam * eqp.dt
+        rows = np.zeros(4)
+        for i in range(4):
+            rows[i] = Val[rp[i]:rp[i + 1]].sum()
+        assert np.allclose(rows[[0, 1, 3]], area / 3.0 * T1 * (-udn), rtol=1e-14, atol=1e-16)
