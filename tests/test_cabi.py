@@ -64,3 +64,38 @@ def test_ls_create_rejects_unknown_type(libpath):
     from svfsi_gb300 import _lib, fsils
     with pytest.raises(_lib.GslsError):
         fsils.FSILS_LS_CREATE(123)
+
+
+_MIRRORS = {"EqParams": "gsls_eq_params", "EqSolver": "gsls_eq_solver", "CepParams": "gsls_cep_params",
+            "Ls": "gsls_ls", "SubLs": "gsls_sub_ls", "StepInfo": "gsls_step_info",
+            "AdjPoint": "gsls_adj_point"}
+
+
+def test_ctypes_mirrors_match_the_header_layout(tmp_path):
+    """Every ctypes structure of the Python mirror has the size and field
+    offsets that a C compiler gives the header's struct (a probe compiled
+    with gcc against include/gsls.h)."""
+    import shutil
+    import subprocess
+    from svfsi_gb300 import _lib
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "gsls.h"', "int main(void) {"]
+    expect = []
+    for py, c in _MIRRORS.items():
+        cls = getattr(_lib, py)
+        lines.append(f'  printf("%zu\\n", sizeof({c}));')
+        expect.append((py, "sizeof", C.sizeof(cls)))
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({c}, {f}));')
+            expect.append((py, f, getattr(cls, f).offset))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert len(got) == len(expect)
+    for (py, f, off), g in zip(expect, got):
+        assert off == int(g), (py, f, off, g)
