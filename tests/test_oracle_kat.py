@@ -682,3 +682,35 @@ def test_bheatf_uniform_state_kat(orc):
         for i in range(4):
             rows[i] = Val[rp[i]:rp[i + 1]].sum()
         assert np.allclose(rows[[0, 1, 3]], area / 3.0 * T1 * (-udn), rtol=1e-14, atol=1e-16)
+
+
+def test_oracle_ctypes_mirrors_match_its_header(orc, tmp_path):
+    """The oracle's ctypes structures have the size and field offsets that a
+    C compiler gives oracle/orc.h (gcc probe)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    mirrors = {"SubLs": "orc_subls", "Ls": "orc_ls", "EqP": "orc_eqp", "DirBC": "orc_dirbc",
+               "TracBC": "orc_tracbc", "CepP": "orc_cep", "NeuBC": "orc_neubc", "Eq": "orc_eq",
+               "StepInfo": "orc_stepinfo"}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "orc.h"', "int main(void) {"]
+    expect = []
+    for py, c in mirrors.items():
+        cls = getattr(orc, py)
+        lines.append(f'  printf("%zu\\n", sizeof({c}));')
+        expect.append((py, "sizeof", C.sizeof(cls)))
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({c}, {f}));')
+            expect.append((py, f, getattr(cls, f).offset))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = Path(__file__).resolve().parents[1] / "oracle"
+    subprocess.run(["gcc", "-std=c99", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert len(got) == len(expect)
+    for (py, f, off), g in zip(expect, got):
+        assert off == int(g), (py, f, off, g)
