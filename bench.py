@@ -16,9 +16,14 @@ format with its own roofline kernel (the GMRES block SpMV on the K block);
 cep the monodomain slab, lelas linear elastodynamics on the beam mesh,
 adjoint the discrete adjoint of the beam with a finite-difference check.
 
---impl reference times the CPU restatement of the reference's algorithm
-(oracle/, OpenMP over all host cores) on the same workload.  N > 1 runs
-independent replicas (the path does not shard across GPUs), one per rank.
+--impl reference times W + K real implicit steps of the CPU restatement of the
+reference's algorithm (oracle/, coloured OpenMP assembly and OpenMP Krylov
+over all host cores) on the same workload from its initial state.  The
+default run also steps the oracle beside the GPU for a few steps (the
+cpu_baseline sample) and reports the error of the FP64 and the mixed GPU
+solution against the oracle's on the full mesh, with the Newton counts of
+all three.  N > 1 runs independent replicas (the path does not shard across
+GPUs), one per rank.
 """
 from __future__ import annotations
 
@@ -60,6 +65,11 @@ def parse():
                     help="adjoint workload: relative step of the central differences")
     ap.add_argument("--fluid-h", type=float, default=0.027,
                     help="cylinder mesh spacing (profiling captures use a coarser mesh)")
+    ap.add_argument("--cep-amplitude", type=float, default=-52.0,
+                    help="cep workload: stimulus amplitude (the configuration's is -52)")
+    ap.add_argument("--parity-steps", type=int, default=None,
+                    help="implicit steps run by the oracle beside the GPU for the "
+                         "cpu_baseline and the error against the oracle (default per workload)")
     return ap.parse_args()
 
 
@@ -91,11 +101,12 @@ def workload(args):
     if args.workload == "fluid":
         return problems.fluid_cylinder(h=0.08 if args.small else args.fluid_h, nsteps=args.steps)
     if args.workload == "cep":
-        # the stimulus amplitude of the configuration is -52 (AP sign: no upstroke);
-        # +52 is timed so that the front propagates and the CG works at full range
+        # the configured stimulus amplitude is -52 (under the Aliev-Panfilov
+        # sign convention it hyperpolarises the corner: no upstroke);
+        # --cep-amplitude 52 times a propagating front instead
         if args.small:
-            return problems.cep_slab(27, 27, 6, nsteps=args.steps, A=52.0)
-        return problems.cep_slab(nsteps=args.steps, A=52.0)
+            return problems.cep_slab(27, 27, 6, nsteps=args.steps, A=args.cep_amplitude)
+        return problems.cep_slab(nsteps=args.steps, A=args.cep_amplitude)
     if args.workload == "heatf":
         return problems.heatf_cylinder(h=0.08 if args.small else args.fluid_h, nsteps=args.steps)
     if args.workload == "lelas":
@@ -128,6 +139,12 @@ def is_cep(p):
     return bool(getattr(p, "cep", None))
 
 
+def compared_name(p):
+    if is_heatf(p):
+        return "Y[:, temperature]"
+    return "Y (velocity, pressure)" if is_fluid(p) else "Y (potential)" if is_cep(p) else "D"
+
+
 def l2_note(p):
     """What keeps the timed steps from running out of a warm L2 (129 MB)."""
     v32, v64 = p.nnz * p.dof ** 2 * 4 / 1e6, p.nnz * p.dof ** 2 * 8 / 1e6
@@ -146,8 +163,8 @@ def workload_desc(p):
                 f"discontinuity-capturing fixed point converges linearly)")
     if is_cep(p):
         return (f"{p.name}: monodomain Aliev-Panfilov (FE reaction step), Diso 0.1, stimulus "
-                f"+52 for 2 ms on the 1x1x2 corner block, {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
-                f"{p.nnz:,}, CG+diag, dt 0.01, Newton tol 1e-6")
+                f"{p.cep['A']:+g} for 2 ms on the 1x1x2 corner block, {p.nEl:,} tet4, {p.nNo:,} "
+                f"nodes, nnz {p.nnz:,}, CG+diag, dt 0.01, Newton tol 1e-6")
     if is_fluid(p):
         return (f"{p.name}: VMS incompressible Navier-Stokes (rho 1.06, mu 0.04, parabolic "
                 f"inlet peak 30, impulsive start), {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
@@ -310,6 +327,19 @@ def run_gsls(args):
     def max_over_ranks(v):
         return max_over_ranks_(v, world, "cuda")
 
+    def gpu_steps(precision, n):
+        """n implicit steps from the initial state: (state, [(Newton, Krylov)])."""
+        lhs, mesh, eq = problems.build_equation(p, precision=precision)
+        counts = []
+        for _ in range(n):
+            i = eq.step()
+            counts.append((int(i.newton_itr), int(i.ls_itr_total)))
+        st = eq.get_state()
+        eq.free()
+        mesh.free()
+        lhs.free()
+        return st, counts
+
     if args.only != "all":
         r = timed_run(fsils.PREC_MIXED if args.only == "mixed" else fsils.PREC_FP64, profile=True)
         if rank == 0:
@@ -440,9 +470,33 @@ def run_gsls(args):
         "gpu_launches": int(mixed["launches"]),
         "clocks": clk,
     }
-    if rank == 0 and not args.no_cpu and not is_cep(p):
-        out["cpu_baseline"] = (cpu_baseline_fluid(p, fp64["newton"]) if is_fluid(p)
-                               else cpu_baseline(p, fp64["newton"], fp64["cg"]))
+    if rank == 0 and world == 1 and not args.no_cpu:
+        # the oracle's own implicit steps of the workload (timed: the CPU
+        # baseline) and the same steps on the GPU in both precisions: the
+        # error of each against the oracle's FP64 solution on the full mesh
+        n = args.parity_steps or PARITY_STEPS[args.workload]
+        threads = os.cpu_count() or 1
+        so, secs, co = oracle_steps(p, n, threads)
+        s64, c64 = gpu_steps(fsils.PREC_FP64, n)
+        smx, cmx = gpu_steps(fsils.PREC_MIXED, n)
+        ref = compared_field(p, so)
+        nref = float(np.linalg.norm(ref))
+        e64 = float(np.linalg.norm(compared_field(p, s64) - ref)) / nref
+        emx = float(np.linalg.norm(compared_field(p, smx) - ref)) / nref
+        out["rel_l2_fp64_vs_oracle"] = e64
+        out["rel_l2_mixed_vs_oracle"] = emx
+        out["parity_vs_oracle"] = {
+            "steps": n, "field": compared_name(p), "norm_oracle": nref,
+            "newton_oracle": [c[0] for c in co], "newton_fp64": [c[0] for c in c64],
+            "newton_mixed": [c[0] for c in cmx],
+            "ls_itr_oracle": [c[1] for c in co], "ls_itr_fp64": [c[1] for c in c64],
+            "ls_itr_mixed": [c[1] for c in cmx],
+            "newton_counts_equal": ([c[0] for c in co] == [c[0] for c in c64] ==
+                                    [c[0] for c in cmx])}
+        out["cpu_baseline"] = {"value": float(sum(secs) / len(secs)), "unit": "s/step",
+                               "cores": threads, "kind": "port",
+                               "sample": oracle_sample_desc(p, n, threads, co, 1),
+                               "step_s": secs}
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -451,176 +505,79 @@ def run_gsls(args):
 
 
 # ---------------------------------------------------------------------------
-def _colouring(p):
-    """Conflict-free element colouring of a Kuhn beam: hex parity (8) x tet
-    type (6); hexes of equal parity share no node."""
-    h = np.arange(p.nEl) // 6
-    t6 = np.arange(p.nEl) % 6
-    xs = np.unique(p.x[:, 0]).size - 1
-    ys = np.unique(p.x[:, 1]).size - 1
-    i, j, k = h % xs, (h // xs) % ys, h // (xs * ys)
-    col = ((i % 2) + 2 * (j % 2) + 4 * (k % 2)) * 6 + t6
-    order = np.argsort(col, kind="stable").astype(np.int32)
-    off = np.concatenate([[0], np.cumsum(np.bincount(col, minlength=48))]).astype(np.int32)
-    return 48, off, order
+# CPU side: real implicit steps of the oracle (the C restatement of the
+# reference's algorithm, FP64), assembled colour by colour with OpenMP and
+# solved with OpenMP SpMVs and reductions on all host threads.
+
+# implicit steps the oracle runs beside the GPU in the default bench run: the
+# cpu_baseline sample and the full-size error against the oracle's solution
+PARITY_STEPS = {"struct": 2, "lelas": 2, "fluid": 1, "heatf": 2, "cep": 20}
 
 
-def cpu_sample(p, threads):
-    """Time, on the host cores with the oracle: one assembly, one diagonal
-    preconditioning and Krylov iterations of the workload's solver (CG, or
-    GMRES Arnoldi steps; slope between 5 and 25 iterations)."""
+def oracle_steps(p, nsteps, threads, warm=0):
+    """Run warm + nsteps implicit steps of the workload on the oracle from
+    its initial state.  Returns the final state (A, Y, D), the seconds of
+    each of the last nsteps steps and their (Newton, Krylov) counts."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
-    L = O.load()
-    L.orc_assemble_colored.argtypes = [C.POINTER(O.EqP), C.c_int, C.c_int, O.c_int_p,
-                                       O.c_double_p, O.c_double_p, O.c_double_p, O.c_double_p,
-                                       O.c_int_p, O.c_int_p, O.c_double_p, O.c_double_p, C.c_int,
-                                       O.c_int_p, O.c_int_p]
     O.set_threads(threads)
-    ncol, off, order = _colouring(p)
-    rng = np.random.default_rng(0)
-    d, tD = p.dof, p.tDof
-    A = 1e-3 * rng.standard_normal((p.nNo, tD))
-    Y = 1e-3 * rng.standard_normal((p.nNo, tD))
-    if p.Y0 is not None:
-        Y += p.Y0
-    D = 1e-3 * rng.standard_normal((p.nNo, tD))
-    R = np.zeros((p.nNo, d))
-    Val = np.zeros((p.nnz, d * d))
-    eqp = O.eqp_from(p)
-    ien, x, rp, cp = O.i32(p.ien), O.f64(p.x), O.i32(p.rowPtr), O.i32(p.colPtr)
-    t0 = time.perf_counter()
-    L.orc_assemble_colored(C.byref(eqp), p.nNo, p.nEl, O.ip(ien), O.dp(x), O.dp(A), O.dp(Y),
-                           O.dp(D), O.ip(rp), O.ip(cp), O.dp(R), O.dp(Val), ncol, O.ip(off),
-                           O.ip(order))
-    t_asm = time.perf_counter() - t0
-    s = O.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
-    s.bc_create(1, p.dirichlet[0].nodes, 3, 0, np.zeros((p.dirichlet[0].nodes.size, 3)))
-    gm = p.LS_type == O.LS_TYPE_GMRES
-    times = {}
-    for m in (5, 25):
-        ls = (O.ls_create(O.LS_TYPE_GMRES, relTol=1e-30, mItr=1, sD=m) if gm else
-              O.ls_create(O.LS_TYPE_CG, relTol=1e-30, mItr=m))
-        Rc, Vc = R.copy(), Val.copy()
+    eq = O.OracleEquation(p, colored=True)
+    eq.set_state(*p.initial_state())
+    secs, counts = [], []
+    for k in range(warm + nsteps):
         t0 = time.perf_counter()
-        s.solve(ls, d, Rc, Vc, O.PRECOND_FSILS)
-        times[m] = time.perf_counter() - t0
-    t_it = (times[25] - times[5]) / 20.0
-    t_pre = max(times[5] - 5 * t_it, 0.0)
-    return t_asm, t_pre, t_it
+        info = eq.step()
+        dt = time.perf_counter() - t0
+        if k >= warm:
+            secs.append(dt)
+            counts.append((int(info.newton_itr), int(info.ls_itr_total)))
+    return eq.state(), secs, counts
 
 
-def cpu_baseline(p, newton, cg):
-    threads = os.cpu_count() or 1
-    t_asm, t_pre, t_it = cpu_sample(p, threads)
-    per_step = newton * (t_asm + t_pre) + cg * t_it
-    kry = "GMRES" if is_heatf(p) else "CG"
-    return {"value": per_step, "unit": "s/step", "cores": threads, "kind": "port",
-            "sample": (f"oracle (C restatement, FP64, OpenMP {threads} threads) on the full mesh: "
-                       f"1 assembly {t_asm:.3f}s, 1 diag precond {t_pre:.3f}s, {kry} "
-                       f"{t_it * 1e3:.2f} ms/iter (5->25 iter slope); per step = {newton:.2f} Newton "
-                       f"x (asm+precond) + {cg:.1f} {kry} iters, the counts of the FP64 GPU run of "
-                       f"the same algorithm")}
+def krylov_name(p):
+    return "NS outer" if is_fluid(p) else "GMRES" if is_heatf(p) else "CG"
 
 
-def cpu_sample_fluid(p, threads):
-    """Time, on the host cores with the oracle: one fluid assembly (one
-    thread, element loop) and one RCS + NS solve of that system with the
-    workload's solver settings (OpenMP SpMV)."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle as O
-    O.set_threads(threads)
-    rng = np.random.default_rng(0)
-    Y = np.zeros((p.nNo, 4))
-    Y[:, 2] = 30.0 * np.clip(1.0 - (p.x[:, 0] ** 2 + p.x[:, 1] ** 2) / 0.25, 0.0, None)
-    Y[:, 3] = rng.standard_normal(p.nNo)
-    A = 1e3 * rng.standard_normal((p.nNo, 4))
-    t0 = time.perf_counter()
-    R, Val = O.assemble(p, A, Y)
-    t_asm = time.perf_counter() - t0
-    s = O.OracleSolver(p.nNo, p.rowPtr, p.colPtr, len(p.dirichlet))
-    for k, d in enumerate(p.dirichlet):
-        s.bc_create(k + 1, d.nodes, 3, 0, np.zeros((d.nodes.size, 3)))
-    ls = O.ls_create(O.LS_TYPE_NS, relTol=p.ls_relTol, sD=p.ls_sD)
-    t0 = time.perf_counter()
-    s.solve(ls, 4, R, Val, O.PRECOND_RCS)
-    t_solve = time.perf_counter() - t0
-    return t_asm, t_solve
-
-
-def cpu_baseline_fluid(p, newton):
-    threads = os.cpu_count() or 1
-    t_asm, t_solve = cpu_sample_fluid(p, threads)
-    return {"value": newton * (t_asm + t_solve), "unit": "s/step", "cores": threads,
-            "kind": "port",
-            "sample": (f"oracle (C restatement, FP64) on the full mesh: 1 assembly {t_asm:.2f}s "
-                       f"(1 thread), 1 RCS + NS solve {t_solve:.2f}s (OpenMP {threads} threads "
-                       f"in the SpMVs); per step = {newton:.2f} Newton x (asm + solve), the "
-                       f"count of the FP64 GPU run")}
+def oracle_sample_desc(p, n, threads, counts, first):
+    newton = [c[0] for c in counts]
+    ls = [c[1] for c in counts]
+    return (f"{n} implicit steps (steps {first}..{first + n - 1} of the workload) run in full "
+            f"by the oracle (C restatement of the reference's algorithm, FP64; coloured OpenMP "
+            f"assembly, OpenMP SpMV/reductions) on {threads} host threads: Newton iterations "
+            f"per step {newton}, {krylov_name(p)} iterations per step {ls}")
 
 
 def run_reference(args):
+    """The reference arm: the oracle's own implicit steps of the workload on
+    the host cores, W untimed then K timed, from the workload's initial
+    state (no counts borrowed from the GPU run)."""
     rank, local, world = dist_env()
     if rank != 0:
         return
     p = workload(args)
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle as O
     threads = os.cpu_count() or 1
-    O.set_threads(threads)
-    if is_fluid(p):
-        vals = []
-        for k in range(args.warmup + args.steps):
-            t_asm, t_solve = cpu_sample_fluid(p, threads)
-            if k >= args.warmup:
-                vals.append(REF_NEWTON_FLUID * (t_asm + t_solve))
-        v = statistics.median(vals)
-        print(json.dumps({
-            "metric": METRIC, "value": v, "unit": "s/step", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-            "data": "synthetic: seeded Delaunay cylinder mesh, no external data",
-            "config": {"workload": workload_desc(p), "precision": "fp64 (reference CPU)"},
-            "cpu_baseline": {"value": v, "unit": "s/step", "cores": threads, "kind": "port",
-                             "sample": (f"per step: {REF_NEWTON_FLUID} Newton x (1 assembly + 1 "
-                                        f"RCS + NS solve) on the full mesh")},
-            "e2e": {"value": v, "unit": "s/step", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}))
-        return
-    # Newton / CG counts of this workload's first step, by the CPU oracle itself
-    if args.small:
-        eq = O.OracleEquation(p)
-        info = eq.step()
-        newton, cg = info.newton_itr, info.ls_itr_total
-        src = "first step run in full by the oracle"
-    else:
-        newton, cg = REF_COUNTS
-        src = ("Newton/CG counts per step of this workload (first steps, identical algorithm, "
-               "recorded from the parity-checked GPU FP64 run)")
-    vals = []
-    for k in range(args.warmup + args.steps):
-        t_asm, t_pre, t_it = cpu_sample(p, threads)
-        if k >= args.warmup:
-            vals.append(newton * (t_asm + t_pre) + cg * t_it)
-    v = statistics.median(vals)
+    t0 = time.perf_counter()
+    _, secs, counts = oracle_steps(p, args.steps, threads, warm=args.warmup)
+    wall = time.perf_counter() - t0
+    v = float(sum(secs) / len(secs))
+    sample = oracle_sample_desc(p, args.steps, threads, counts, args.warmup + 1)
+    data = ("synthetic: seeded Delaunay cylinder mesh, no external data"
+            if (is_fluid(p) or is_heatf(p))
+            else "synthetic: Kuhn-split slab mesh, no external data" if is_cep(p)
+            else "synthetic: seeded Kuhn-split beam mesh, no external data")
     out = {"metric": METRIC, "value": v, "unit": "s/step", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-           "data": "synthetic: seeded Kuhn-split beam mesh, no external data",
+           "data": data,
            "config": {"workload": workload_desc(p), "precision": "fp64 (reference CPU)"},
            "cpu_baseline": {"value": v, "unit": "s/step", "cores": threads, "kind": "port",
-                            "sample": (f"per step: 1 colored OpenMP assembly + 1 diag precond + "
-                                       f"CG per-iteration time from 5->25 iterations, scaled by "
-                                       f"{newton} Newton and {cg} CG iterations per step ({src})")},
+                            "sample": sample},
+           "oracle": {"newton_itr_per_step": float(np.mean([c[0] for c in counts])),
+                      "ls_itr_per_step": float(np.mean([c[1] for c in counts])),
+                      "ls_itr_note": f"{krylov_name(p)} iterations per step",
+                      "timed_s": float(sum(secs)), "wall_s_with_warmup": wall},
            "e2e": {"value": v, "unit": "s/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
-
-
-# Newton iterations and total CG iterations per step of the full-size beam
-# (FP64 path), used to scale the CPU sample in the reference arm.
-REF_COUNTS = (5.0, 1911.4)
-# Newton iterations per step of the full-size cylinder (FP64 path)
-REF_NEWTON_FLUID = 7.0
 
 
 def run_adjoint(args):

@@ -76,7 +76,8 @@ class Eq(C.Structure):
                 ("An", c_double_p), ("Yn", c_double_p), ("Dn", c_double_p),
                 ("eq_iNorm", C.c_double), ("eq_pNorm", C.c_double),
                 ("cep", CepP), ("stim", c_int_p), ("Xion", c_double_p), ("time", C.c_double),
-                ("cep_ipass_done", C.c_int), ("nNeu", C.c_int), ("neu", C.POINTER(NeuBC))]
+                ("cep_ipass_done", C.c_int), ("nNeu", C.c_int), ("neu", C.POINTER(NeuBC)),
+                ("ncolor", C.c_int), ("color_off", c_int_p), ("color_order", c_int_p)]
 
 
 class StepInfo(C.Structure):
@@ -128,6 +129,8 @@ def load():
                                    c_double_p]
         L.orc_eq_step.argtypes = [C.POINTER(Eq), C.POINTER(StepInfo)]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_color_elements.restype = C.c_int
+        L.orc_color_elements.argtypes = [C.c_int, C.c_int, c_int_p, c_int_p, c_int_p]
         _L = L
     return _L
 
@@ -246,10 +249,23 @@ def ls_create(LS_type, relTol=None, absTol=None, mItr=None, sD=None) -> Ls:
     return ls
 
 
-class OracleEquation:
-    """Time stepping of a Problem on the oracle (orc_eq_step)."""
+def color_elements(nNo, ien):
+    """Greedy conflict-free element colouring (orc_color_elements):
+    returns (ncolor, color_off[ncolor+1], order[nEl])."""
+    ien = i32(ien)
+    off = np.zeros(65, np.int32)
+    order = np.zeros(max(ien.shape[0], 1), np.int32)
+    nc = load().orc_color_elements(nNo, ien.shape[0], ip(ien), ip(off), ip(order))
+    assert nc > 0, nc
+    return nc, off[:nc + 1].copy(), order[:ien.shape[0]].copy()
 
-    def __init__(self, problem, eparam=None):
+
+class OracleEquation:
+    """Time stepping of a Problem on the oracle (orc_eq_step).  colored:
+    assemble colour by colour with OpenMP (the multi-core CPU baseline);
+    otherwise the serial element loop."""
+
+    def __init__(self, problem, eparam=None, colored=False):
         self.P = problem
         p = problem
         self._keep = []
@@ -319,6 +335,11 @@ class OracleEquation:
             self.Xion[:, 0] = c["V0"]
             self.Xion[:, 1] = c["X20"]
         eq.Xion = dp(self.Xion)
+        if colored:
+            nc, off, order = color_elements(p.nNo, p.ien)
+            eq.ncolor = nc
+            eq.color_off = ip(keep(off))
+            eq.color_order = ip(keep(order))
         self.eq = eq
 
     def set_state(self, Ao, Yo, Do):

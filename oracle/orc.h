@@ -238,7 +238,17 @@ typedef struct {
   double time;
   int cep_ipass_done;
   int nNeu; const orc_neubc *neu;  /* HEATF Neumann faces */
+  /* optional element colouring for the multi-core CPU baseline: ncolor > 0
+     runs each colour's elements with OpenMP (orc_assemble_colored); 0 keeps
+     the serial element loop of GLOBALEQASSEM */
+  int ncolor; const int *color_off; const int *color_order;
 } orc_eq;
+
+/* Greedy element colouring: elements of one colour share no node.  Writes
+   color_off[ncolor+1] (at most 65 entries) and order[nEl] (element ids
+   colour by colour, ascending within a colour); returns ncolor (<= 64) or
+   -1 when 64 colours do not suffice. */
+int orc_color_elements(int nNo, int nEl, const int *IEN, int *color_off, int *order);
 
 typedef struct {
   int newton_itr;

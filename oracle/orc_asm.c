@@ -911,6 +911,10 @@ int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
         double lR[4], lK[16];
         orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso, xl, al, yl, lR, lK);
         orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
+      } else if (p->phys == 4) {
+        double lR[16], lK[256];
+        orc_elem_fluid(p, xl, al, yl, lR, lK);
+        orc_doassem(4, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
       } else if (p->phys == 5) {
         double lR[12], lK[144];
         orc_elem_lelas(p, xl, al, dl, lR, lK);
@@ -923,6 +927,37 @@ int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
     }
   }
   return 0;
+}
+
+int orc_color_elements(int nNo, int nEl, const int *IEN, int *color_off, int *order) {
+  /* one 64-bit mask of used colours per node; an element takes the lowest
+     colour free at all four of its nodes */
+  unsigned long long *used = (unsigned long long *)xcalloc((size_t)nNo, sizeof(*used));
+  unsigned char *col = (unsigned char *)xcalloc((size_t)(nEl > 0 ? nEl : 1), 1);
+  int ncolor = 0;
+  for (int e = 0; e < nEl; e++) {
+    unsigned long long m = 0;
+    for (int a = 0; a < 4; a++) m |= used[IEN[(size_t)e * 4 + a]];
+    if (m == ~0ULL) {
+      free(used);
+      free(col);
+      return -1;
+    }
+    int c = 0;
+    while ((m >> c) & 1ULL) c++;
+    col[e] = (unsigned char)c;
+    for (int a = 0; a < 4; a++) used[IEN[(size_t)e * 4 + a]] |= 1ULL << c;
+    if (c + 1 > ncolor) ncolor = c + 1;
+  }
+  for (int c = 0; c <= ncolor; c++) color_off[c] = 0;
+  for (int e = 0; e < nEl; e++) color_off[col[e] + 1]++;
+  for (int c = 0; c < ncolor; c++) color_off[c + 1] += color_off[c];
+  int fill[64];
+  for (int c = 0; c < ncolor; c++) fill[c] = color_off[c];
+  for (int e = 0; e < nEl; e++) order[fill[col[e]]++] = e;
+  free(used);
+  free(col);
+  return ncolor;
 }
 
 /* SETBCTRACL for tri3 faces with a constant traction vector h,
@@ -1076,6 +1111,7 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
      Xion(1) = Yo(v) (not on the first pass), integrate the cell model from
      time-dt over dt, Yo(v) = Xion(1) */
   if (eq->p.phys == 3) {
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
     for (int a = 0; a < nNo; a++) {
       double X[2];
       X[0] = eq->cep_ipass_done ? eq->Yo[(size_t)a * tD + eq->p.s] : eq->Xion[(size_t)a * 2];
@@ -1143,6 +1179,7 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
   while (!ok) {
     /* PICI */
     itr++;
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
     for (size_t k = 0; k < nS; k++) {
       Ag[k] = eq->Ao[k] * (1.0 - am) + eq->An[k] * am;
       Yg[k] = eq->Yo[k] * (1.0 - af) + eq->Yn[k] * af;
@@ -1151,7 +1188,12 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
     /* LSALLOC */
     memset(R, 0, sizeof(double) * (size_t)nNo * dof);
     memset(Val, 0, sizeof(double) * (size_t)eq->nnz * dof * dof);
-    rc = orc_assemble(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr, eq->colPtr, R, Val);
+    if (eq->ncolor > 0)
+      rc = orc_assemble_colored(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr,
+                                eq->colPtr, R, Val, eq->ncolor, eq->color_off, eq->color_order);
+    else
+      rc = orc_assemble(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr,
+                        eq->colPtr, R, Val);
     if (rc) break;
     /* SETBCNEU (traction) */
     for (int t = 0; t < eq->nTrac; t++)

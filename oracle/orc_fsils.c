@@ -193,8 +193,21 @@ double orc_dotv(int dof, int nNo, const double *U, const double *V) {
   double s = 0.0;
   const size_t n = (size_t)dof * nNo;
   if (g_threads > 1) {
-#pragma omp parallel for reduction(+ : s) schedule(static) num_threads(g_threads)
-    for (long long i = 0; i < (long long)n; i++) s += U[i] * V[i];
+    /* fixed chunks, partial sums added in chunk order: the same bits on
+       every run for a given thread count (an OpenMP reduction clause
+       combines the partials in arrival order) */
+    enum { kMaxChunks = 256 };
+    double part[kMaxChunks];
+    const int nt = g_threads < kMaxChunks ? g_threads : kMaxChunks;
+    const size_t chunk = (n + (size_t)nt - 1) / (size_t)nt;
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int t = 0; t < nt; t++) {
+      const size_t i0 = (size_t)t * chunk, i1 = i0 + chunk < n ? i0 + chunk : n;
+      double a = 0.0;
+      for (size_t i = i0; i < i1; i++) a += U[i] * V[i];
+      part[t] = a;
+    }
+    for (int t = 0; t < nt; t++) s += part[t];
     return s;
   }
   for (int i = 0; i < nNo; i++) {

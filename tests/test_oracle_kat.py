@@ -714,3 +714,32 @@ def test_oracle_ctypes_mirrors_match_its_header(orc, tmp_path):
     assert len(got) == len(expect)
     for (py, f, off), g in zip(expect, got):
         assert off == int(g), (py, f, off, g)
+
+
+@pytest.mark.parametrize("case", ["struct", "fluid"])
+def test_coloured_oracle_step_matches_serial(orc, case):
+    """The timed CPU baseline assembles colour by colour with OpenMP: the
+    colouring is conflict-free (no two elements of a colour share a node) and
+    the coloured steps equal the serial element loop to rounding, with the
+    same Newton and Krylov counts."""
+    if case == "struct":
+        p = problems.struct_beam(12, 3, 3, nsteps=2)
+    else:
+        p = problems.fluid_cylinder(h=0.12, nsteps=1)
+    nc, off, order = orc.color_elements(p.nNo, p.ien)
+    assert off[0] == 0 and off[-1] == p.nEl
+    assert np.array_equal(np.sort(order), np.arange(p.nEl))
+    for c in range(nc):
+        nodes = p.ien[order[off[c]:off[c + 1]]].ravel()
+        assert np.unique(nodes).size == nodes.size
+    orc.set_threads(4)
+    a, b = orc.OracleEquation(p), orc.OracleEquation(p, colored=True)
+    for eq in (a, b):
+        eq.set_state(*p.initial_state())
+    for _ in range(p.nsteps):
+        ia, ib = a.step(), b.step()
+        assert (ia.newton_itr, ia.ls_itr_total) == (ib.newton_itr, ib.ls_itr_total)
+    k = 2 if case == "struct" else 1
+    fa, fb = a.state()[k], b.state()[k]
+    assert np.linalg.norm(fa - fb) <= 1e-12 * np.linalg.norm(fa)
+    orc.set_threads(1)
