@@ -128,11 +128,14 @@ def is_heatf(p):
 
 
 def compared_field(p, state):
-    """The unknown compared between the mixed and FP64 runs: D (solids),
-    Y (fluid, CEP) or the temperature column of Y (HEATF)."""
+    """The unknown compared between runs: D (solids), Y (fluid), the
+    potential's departure from rest (CEP) or the temperature column of Y
+    (HEATF)."""
     if is_heatf(p):
         return state[1][:, p.s]
-    return state[1] if (is_fluid(p) or is_cep(p)) else state[2]
+    if is_cep(p):
+        return state[1] - p.cep["V0"]
+    return state[1] if is_fluid(p) else state[2]
 
 
 def is_cep(p):
@@ -142,7 +145,8 @@ def is_cep(p):
 def compared_name(p):
     if is_heatf(p):
         return "Y[:, temperature]"
-    return "Y (velocity, pressure)" if is_fluid(p) else "Y (potential)" if is_cep(p) else "D"
+    return ("Y (velocity, pressure)" if is_fluid(p) else "Y - V_rest (potential)" if is_cep(p)
+            else "D")
 
 
 def l2_note(p):

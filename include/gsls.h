@@ -82,8 +82,16 @@ typedef struct gsls_eq gsls_eq;     /* one equation's time integrator */
 /* ------------------------------------------------------------------------ */
 /* Library */
 
-/* Select the CUDA device for this process. */
+/* Select the CUDA device for this process (and place gsls_dot_noalloc's
+   fixed scratch array on it). */
 int gsls_init(int device);
+/* No counterpart in the reference.  Poll limit of the grid barrier that
+   the persistent Schur-complement CG of the NS solver waits on between its
+   phases (0 = the default, 2^24 polls: seconds).  When a wait reaches the
+   limit the kernel sets an error word, every block leaves, and the solve
+   returns GSLS_ERR_CUDA with the CUDA context intact.  A test hook for the
+   timeout path; a small limit makes waits expire on healthy launches. */
+int gsls_set_wait_limit(unsigned polls);
 /* Library version (GSLS_VERSION). */
 int gsls_version(void);
 /* Human-readable text for the last error of this thread. */
@@ -141,13 +149,18 @@ int gsls_dot_dev(gsls_lhs *lhs, int dof, const double *du, const double *dv,
 /* No counterpart in the reference.  Dot product of two device vectors of
    length n (result on the host), for callers that cannot call cudaMalloc:
    it allocates no device memory.  Its reduction scratch is a fixed
-   ~139 KB array in the library's device image, held by every GPU that
-   loads the library until the process exits; n <= 67,108,864, larger n is
-   rejected with GSLS_ERR_ARG.  The first call on a device resolves the
-   array's address (cudaGetSymbolAddress) with that device current; make it
-   before any stream capture.  All calls share the array: calls that
-   overlap on the GPU (other streams, other host threads) race.  stream is
-   a cudaStream_t (NULL = the default stream). */
+   137,476-byte array in the library's device image; n <= 67,108,864,
+   larger n is rejected with GSLS_ERR_ARG.  CUDA loads modules lazily, so
+   the array is placed on a device when its address is first resolved
+   (cudaGetSymbolAddress, with that device current): gsls_init does this
+   for the device it selects, and the array then stays until the process
+   exits.  Without gsls_init the first gsls_dot_noalloc call on a device
+   does it; make that call before any stream capture and before a pool
+   takes the whole heap (or set CUDA_MODULE_LOADING=EAGER).  The address is
+   kept for the process: after cudaDeviceReset call gsls_init again.  All
+   calls share the array: calls that overlap on the GPU (other streams,
+   other host threads) race.  stream is a cudaStream_t (NULL = the default
+   stream). */
 int gsls_dot_noalloc(long long n, const double *du, const double *dv,
                      double *result, void *stream);
 int gsls_norm_dev(gsls_lhs *lhs, int dof, const double *du, double *result);

@@ -74,6 +74,7 @@ class StepInfo(C.Structure):
 SIGNATURES = {
     "gsls_init": (C.c_int, [C.c_int]),
     "gsls_version": (C.c_int, []),
+    "gsls_set_wait_limit": (C.c_int, [C.c_uint]),
     "gsls_last_error": (C.c_char_p, []),
     "gsls_lhs_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, c_int_p,
                                   c_int_p, c_int_p, C.c_int]),

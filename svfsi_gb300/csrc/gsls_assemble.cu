@@ -33,6 +33,12 @@ struct gsls_mesh {
   bool bad_jac = false;           // a zero or non-finite element Jacobian
   const double *eparam_src = nullptr;
   bool has_eparam = false;
+  // HEATS/CEP operators (built on the first heat/CEP assembly, rebuilt after
+  // a new per-element parameter): the assembled mass sum_e w M_ab, the
+  // assembled conduction sum_e W nu_e Nx_a.Nx_b (nu_e = 1 without a
+  // per-element parameter) as FP64 scalar CSR, and sum_e w Ns_a per node
+  gsls::DevBuf d_linM, d_linK, d_linB;
+  bool lin_ready = false;
 };
 
 namespace gsls {
@@ -206,6 +212,104 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// HEATS3D and isotropic CEP3D are linear in the state with mesh-constant
+// element matrices: with m_e(a,b) = w M_ab (mass) and k_e(a,b) = W Nx_a.Nx_b
+// (conduction; W = 4w), the element terms above are
+//   lR(a)   = rho sum_b m_e(a,b) al_b + nu sum_b k_e(a,b) yl_b - rho s w Ns_a
+//   lK(a,b) = am rho m_e(a,b) + T1 nu k_e(a,b)            (T1 = af gam dt)
+// so DOASSEM's sums over elements are the assembled operators Mg = sum m_e,
+// Kg = sum nu_e k_e and b = sum w Ns, built once per mesh (one colour launch
+// each, k_lin_build), and every Newton assembly is one row-parallel pass:
+//   R = rho Mg Ag + nu Kg Yg - rho s b,   Val = am rho Mg + T1 nu Kg
+// (k_asm_lin).  The sums are regrouped, not changed: FP64 results agree
+// with the element-by-element loop to rounding.
+__global__ void __launch_bounds__(kAsmThreads) k_lin_build(AsmArgs A, double *Mg, double *Kg,
+                                                           double *Bg) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.nColorEl) return;
+  const int e = A.el0 + t;
+  const int4 nd = A.ien[e];
+  const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
+  double Nx[3][4];
+  const double Jac = load_geo(A, e, Nx);
+  const double w = c_rule.w * Jac;
+  const double Wn = 4.0 * w * (A.eparam ? A.eparam[e] : 1.0);
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    Bg[n4[a]] += w * c_rule.Ns[a];
+    const int4 mp = A.map[(size_t)e * 4 + a];
+    const int pos[4] = {mp.x, mp.y, mp.z, mp.w};
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      Mg[pos[b]] += w * c_rule.M[a][b];
+      Kg[pos[b]] += Wn * (Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b]);
+    }
+  }
+}
+
+// 16 lanes per CSR row (tet4 rows hold ~15 entries), entries strided by
+// 16, the row sum by a fixed shuffle tree: deterministic.
+constexpr int kLinLanes = 16;
+template <class VT>
+__global__ void __launch_bounds__(256) k_asm_lin(int nNo, const int *__restrict__ rowPtr,
+                                                 const int *__restrict__ colPtr,
+                                                 const double *__restrict__ Mg,
+                                                 const double *__restrict__ Kg,
+                                                 const double *__restrict__ Bg,
+                                                 const double *__restrict__ Ag,
+                                                 const double *__restrict__ Yg, int tDof, int s,
+                                                 double rho, double nu, double rs, double cM,
+                                                 double cK, double *__restrict__ R,
+                                                 VT *__restrict__ Val) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = (int)(g / kLinLanes), l = (int)(g % kLinLanes);
+  double r = 0.0;
+  if (row < nNo) {
+    const int j0 = __ldg(rowPtr + row), j1 = __ldg(rowPtr + row + 1);
+    for (int j = j0 + l; j < j1; j += kLinLanes) {
+      const double m = __ldcs(Mg + j), k = __ldcs(Kg + j);
+      const size_t c = (size_t)__ldcs(colPtr + j) * tDof + s;
+      __stcs(Val + j, VT(cM * m + cK * k));
+      r += rho * m * __ldg(Ag + c) + nu * k * __ldg(Yg + c);
+    }
+  }
+#pragma unroll
+  for (int o = kLinLanes / 2; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o, kLinLanes);
+  if (row < nNo && l == 0) R[row] = r - rs * Bg[row];
+}
+
+static int lin_prepare(gsls_mesh *m, AsmArgs A) {
+  if (m->lin_ready) return GSLS_OK;
+  gsls_lhs *lhs = m->lhs;
+  cudaStream_t st = lhs->stream;
+  GSLS_TRY(m->d_linM.alloc(sizeof(double) * (size_t)lhs->nnz));
+  GSLS_TRY(m->d_linK.alloc(sizeof(double) * (size_t)lhs->nnz));
+  GSLS_TRY(m->d_linB.alloc(sizeof(double) * (size_t)lhs->nNo));
+  GSLS_CUDA(cudaMemsetAsync(m->d_linM.p, 0, sizeof(double) * (size_t)lhs->nnz, st));
+  GSLS_CUDA(cudaMemsetAsync(m->d_linK.p, 0, sizeof(double) * (size_t)lhs->nnz, st));
+  GSLS_CUDA(cudaMemsetAsync(m->d_linB.p, 0, sizeof(double) * (size_t)lhs->nNo, st));
+  for (int c = 0; c < m->ncolors; c++) {
+    A.el0 = m->color_off[c];
+    A.nColorEl = m->color_off[c + 1] - m->color_off[c];
+    if (A.nColorEl <= 0) continue;
+    k_lin_build<<<(A.nColorEl + kAsmThreads - 1) / kAsmThreads, kAsmThreads, 0, st>>>(
+        A, m->d_linM.as<double>(), m->d_linK.as<double>(), m->d_linB.as<double>());
+    GSLS_CHECK_LAUNCH();
+  }
+  m->lin_ready = true;
+  return GSLS_OK;
+}
+
+// GSLS_HEATS_ASM=element keeps the per-Newton element loop (k_asm_heats)
+static bool lin_on() {
+  static const bool on = [] {
+    const char *e = getenv("GSLS_HEATS_ASM");
+    return !(e && strcmp(e, "element") == 0);
+  }();
+  return on;
+}
+
 }  // namespace gsls
 
 #include "gsls_asm_fluid.cuh"
@@ -246,8 +350,6 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   cudaStream_t st = lhs->stream;
   const int dof = p->dof;
   const size_t vbytes = (size_t)lhs->nnz * dof * dof * (val_prec == GSLS_PREC_MIXED ? 4 : 8);
-  GSLS_CUDA(cudaMemsetAsync(R, 0, sizeof(double) * (size_t)lhs->nNo * dof, st));
-  GSLS_CUDA(cudaMemsetAsync(Val, 0, vbytes, st));
   AsmArgs A;
   memset(&A, 0, sizeof(A));
   A.tDof = p->tDof;
@@ -306,6 +408,29 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   A.Val = Val;
   A.err = m->d_err.as<int>();
   const bool mixed = (val_prec == GSLS_PREC_MIXED);
+  if ((p->phys == GSLS_PHYS_HEATS || p->phys == GSLS_PHYS_CEP) && lin_on()) {
+    if (dof != 1) return GSLS_ERR_ARG;
+    GSLS_TRY(lin_prepare(m, A));
+    const double T1 = A.af * A.gam * A.dt;
+    const double nu = A.eparam ? 1.0 : A.cond;  // a per-element nu is inside Kg
+    const long long nt = (long long)lhs->nNo * kLinLanes;
+    const int nb = (int)((nt + 255) / 256);
+    const int *rp = lhs->d_rowPtr.as<int>(), *cp = lhs->d_colPtr.as<int>();
+    if (mixed)
+      k_asm_lin<float><<<nb, 256, 0, st>>>(lhs->nNo, rp, cp, m->d_linM.as<double>(),
+                                           m->d_linK.as<double>(), m->d_linB.as<double>(), Ag,
+                                           Yg, A.tDof, A.s, A.rho, nu, A.rho * A.src,
+                                           A.am * A.rho, T1 * nu, R, static_cast<float *>(Val));
+    else
+      k_asm_lin<double><<<nb, 256, 0, st>>>(lhs->nNo, rp, cp, m->d_linM.as<double>(),
+                                            m->d_linK.as<double>(), m->d_linB.as<double>(), Ag,
+                                            Yg, A.tDof, A.s, A.rho, nu, A.rho * A.src,
+                                            A.am * A.rho, T1 * nu, R, static_cast<double *>(Val));
+    GSLS_CHECK_LAUNCH();
+    return GSLS_OK;
+  }
+  GSLS_CUDA(cudaMemsetAsync(R, 0, sizeof(double) * (size_t)lhs->nNo * dof, st));
+  GSLS_CUDA(cudaMemsetAsync(Val, 0, vbytes, st));
   for (int c = 0; c < m->ncolors; c++) {
     A.el0 = m->color_off[c];
     A.nColorEl = m->color_off[c + 1] - m->color_off[c];
@@ -517,6 +642,7 @@ const int *mesh_perm(gsls_mesh *m, int *nEl) {
 }
 
 int mesh_set_eparam(gsls_mesh *m, const double *eparam) {
+  m->lin_ready = false;  // the heat/CEP conduction operator holds the parameter
   if (!eparam) {
     m->has_eparam = false;
     return GSLS_OK;

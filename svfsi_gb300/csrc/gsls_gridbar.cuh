@@ -1,8 +1,10 @@
 // Grid-wide barrier and reductions of the persistent (cooperative) Krylov
-// kernels.  Every wait is bounded: after kBarSpin polls (each a 20 ns sleep
-// plus an L2 round trip: seconds at most) the waiting block sets the error
-// word and returns false, and every other block leaves at its next poll, so
-// a launch that lost a block ends with an error status instead of hanging.
+// kernels.  Every wait is bounded: after `limit` polls (kBarSpinDefault
+// unless set, each a 20 ns sleep plus an L2 round trip: seconds at most; the
+// host can lower it with gsls_set_wait_limit) the waiting block sets the
+// error word and returns false, and every other block leaves at its next
+// poll or at its own limit, so a launch that lost a block ends with an
+// error status instead of hanging.
 #pragma once
 
 #include "gsls_internal.cuh"
@@ -14,7 +16,6 @@ struct GridBar {
   unsigned pad;
   int err, pad2;
 };
-constexpr unsigned kBarSpin = 1u << 24;
 
 // Barrier number `epoch` (1, 2, ...) of the launch: every block adds one
 // arrival (release at GPU scope) and thread 0 polls the count with acquire
@@ -26,7 +27,8 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ bool grid_bar(GridBar *b, unsigned nblk, unsigned &epoch) {
+__device__ __forceinline__ bool grid_bar(GridBar *b, unsigned nblk, unsigned &epoch,
+                                         unsigned limit) {
   __shared__ int s_ok;
   __syncthreads();
   epoch += 1;
@@ -41,7 +43,7 @@ __device__ __forceinline__ bool grid_bar(GridBar *b, unsigned nblk, unsigned &ep
         ok = 0;
         break;
       }
-      if (it > kBarSpin) {
+      if (it > limit) {
         atomicExch(&b->err, 1);
         ok = 0;
         break;

@@ -38,6 +38,12 @@ int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 void count_launch();
 void count_launch_n(int n);
 int num_sms();
+// gsls_noalloc.cu: place gsls_dot_noalloc's scratch array on the current
+// device and resolve its address (called by gsls_init)
+int noalloc_prepare_device();
+// poll limit of the grid barriers of the persistent kernels (gsls_set_wait_limit)
+constexpr unsigned kBarSpinDefault = 1u << 24;
+unsigned wait_limit();
 // Zig-zag traversal of the Krylov SpMVs: a matrix larger than L2 streamed in
 // the same order every iteration leaves L2 holding its tail, which the next
 // forward pass evicts before reaching it; reversing the row order every

@@ -323,6 +323,11 @@ __global__ void __launch_bounds__(256) k_dfma_probe(double *out, int iters) {
 
 }  // namespace gsls
 
+namespace gsls {
+static std::atomic<unsigned> g_wait_limit{kBarSpinDefault};
+unsigned wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+}  // namespace gsls
+
 using namespace gsls;
 
 extern "C" {
@@ -390,10 +395,17 @@ int gsls_profile_read(const char *name, long long *count, double *total_ms) {
   return GSLS_OK;
 }
 
+int gsls_set_wait_limit(unsigned polls) {
+  g_wait_limit.store(polls ? polls : kBarSpinDefault, std::memory_order_relaxed);
+  return GSLS_OK;
+}
+
 int gsls_init(int device) {
   GSLS_CUDA(cudaSetDevice(device));
   GSLS_CUDA(cudaFree(0));
-  return GSLS_OK;
+  // place the fixed scratch array of gsls_dot_noalloc on this device now
+  // (lazy module loading would otherwise place it on its first call)
+  return noalloc_prepare_device();
 }
 
 int gsls_lhs_create(gsls_lhs **out, int gnNo, int nNo, int nnz, const int *gNodes,

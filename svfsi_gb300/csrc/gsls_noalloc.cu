@@ -5,10 +5,16 @@
 // allocation may be made.  The reduction scratch -- one partial sum per
 // block, the group sums of the two-level reduction, the result slot and the
 // arrival counters -- lives in a file-scope __device__ array of fixed size
-// (about 139 KB), which every GPU that loads this library holds until the
-// process exits.  Host code cannot use the array's name as a device
-// address; its address is resolved with cudaGetSymbolAddress once per
-// device, with that device current, on the first call made on it.
+// (137,476 bytes), which every GPU that loads this translation unit's
+// module holds until the process exits.  CUDA loads modules lazily by
+// default, so the array is placed on a device when its address is first
+// resolved: gsls_init does that for the device it selects, so that a
+// caller whose pool then takes the whole heap still finds the array in
+// place.  Host code cannot use the array's name as a device address; its
+// address is resolved with cudaGetSymbolAddress once per device, with that
+// device current (in gsls_init, or else on the first call on the device),
+// and kept for the life of the process: after a cudaDeviceReset, call
+// gsls_init again, which resolves it anew.
 #include <mutex>
 
 #include "gsls_internal.cuh"
@@ -25,6 +31,7 @@ constexpr size_t kNaResultOff = sizeof(double) * (kNaMaxBlocks + kNaMaxGroups);
 constexpr size_t kNaTicketOff = kNaResultOff + 256;
 constexpr size_t kNaTicketBytes = sizeof(unsigned) * (1 + kNaMaxGroups);
 constexpr size_t kNaBytes = kNaTicketOff + kNaTicketBytes;
+static_assert(kNaBytes == 137476, "scratch size as documented in include/gsls.h");
 
 static __device__ __align__(256) unsigned char g_na_scratch[kNaBytes];
 
@@ -49,8 +56,9 @@ __global__ void __launch_bounds__(kNaThreads) k_dot_chunked(long long n, const d
 static std::mutex g_na_mu;
 static unsigned char *g_na_ptr[64] = {};
 
-// Device address of the scratch array on the current device (resolved once).
-static int na_scratch(unsigned char **out) {
+// Device address of the scratch array on the current device: resolved on
+// the first use on a device (or always, with refresh) and kept.
+static int na_scratch(unsigned char **out, bool refresh) {
   int dev = 0;
   GSLS_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) {
@@ -58,15 +66,19 @@ static int na_scratch(unsigned char **out) {
     return GSLS_ERR_ARG;
   }
   std::lock_guard<std::mutex> lk(g_na_mu);
-  if (!g_na_ptr[dev]) {
+  if (refresh || !g_na_ptr[dev]) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_na_scratch)", __FILE__, __LINE__);
     g_na_ptr[dev] = static_cast<unsigned char *>(p);
   }
-  *out = g_na_ptr[dev];
+  if (out) *out = g_na_ptr[dev];
   return GSLS_OK;
 }
+
+// Called by gsls_init with the selected device current: loads this module
+// on the device (placing the scratch array) and resolves its address.
+int noalloc_prepare_device() { return na_scratch(nullptr, true); }
 
 }  // namespace gsls
 
@@ -84,7 +96,7 @@ extern "C" int gsls_dot_noalloc(long long n, const double *du, const double *dv,
     return GSLS_ERR_ARG;
   }
   unsigned char *scratch = nullptr;
-  GSLS_TRY(na_scratch(&scratch));
+  GSLS_TRY(na_scratch(&scratch, false));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // the array keeps the previous call's contents: the arrival counters must
   // start at zero (a completed call leaves them at zero; clear regardless)

@@ -752,6 +752,7 @@ struct SchurArgs {
   SchurScal *sc;
   int K;                          // rows per 4-lane group (row slots)
   int zz;                         // reverse the row-slot order on odd iterations
+  unsigned spin;                  // poll limit of the grid barrier
 };
 
 constexpr int kPT = 1024;
@@ -870,7 +871,7 @@ __global__ void __launch_bounds__(kPT, 1) k_schur_persistent(SchurArgs<VT, XT> A
         __stcg(Pnew + i, pown);
       }
     }
-    if (!(ok = grid_bar(A.bar, nblk, epoch))) break;
+    if (!(ok = grid_bar(A.bar, nblk, epoch, A.spin))) break;
     // phase 2: SP = mL P - Gt GP; dot = P.SP
     AT dloc = AT(0);
     for (int kk = 0; kk < K; kk++) {
@@ -925,7 +926,7 @@ __global__ void __launch_bounds__(kPT, 1) k_schur_persistent(SchurArgs<VT, XT> A
       const double bs = block_sum(double(dloc), sh);
       if (threadIdx.x == 0) __stcg(A.part + blockIdx.x, bs);
     }
-    if (!(ok = grid_bar(A.bar, nblk, epoch))) break;
+    if (!(ok = grid_bar(A.bar, nblk, epoch, A.spin))) break;
     // phase 3: X, R and |R|^2
     const double dot = sum_partials(A.part, nblk, sh);
     errO = err;
@@ -942,7 +943,7 @@ __global__ void __launch_bounds__(kPT, 1) k_schur_persistent(SchurArgs<VT, XT> A
       const double bs = block_sum(eloc, sh);
       if (threadIdx.x == 0) __stcg(A.part + nblk + blockIdx.x, bs);
     }
-    if (!(ok = grid_bar(A.bar, nblk, epoch))) break;
+    if (!(ok = grid_bar(A.bar, nblk, epoch, A.spin))) break;
     double e = sqrt(sum_partials(A.part + nblk, nblk, sh));
     e = e * e;
     err = e;
@@ -1034,7 +1035,8 @@ static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, 
       GSLS_TRY(lhs->ws.partials.alloc(sizeof(double) * ((size_t)2 * nblk + 64) + 64));
       GSLS_CUDA(cudaMemsetAsync(db, 0, sizeof(GridBar), st));
       SchurArgs<VT, XT> a{nNo, rp, cp, A1, A2, P, Ps, Pb, Rs, SP, GP4,
-                          lhs->ws.partials.as<double>(), db, sc, K, zigzag_on()};
+                          lhs->ws.partials.as<double>(), db, sc, K, zigzag_on(),
+                          wait_limit()};
       void *args[] = {&a};
       GSLS_CUDA(cudaLaunchCooperativeKernel((const void *)k_schur_persistent<VT, XT>, dim3(nblk),
                                             dim3(kPT), args, smem, st));
