@@ -313,7 +313,7 @@ def run_gsls(args):
             acnt, atot = C.c_longlong(), C.c_double()
             L.gsls_profile_read(b"assembly", C.byref(acnt), C.byref(atot))
             prof = {"cg_spmv": (cnt.value, tot.value), "assembly": (acnt.value, atot.value)}
-            for extra in (b"cg_update", b"cg_pupdate"):
+            for extra in (b"cg_update", b"cg_pupdate", b"schur", b"schur_calls"):
                 ec, et = C.c_longlong(), C.c_double()
                 if L.gsls_profile_read(extra, C.byref(ec), C.byref(et)) == 0 and ec.value:
                     prof[extra.decode()] = (ec.value, et.value)
@@ -427,6 +427,36 @@ def run_gsls(args):
 
     roof = roofline(profd["prof"], 4)
     roof64 = roofline(profd64["prof"], 8)
+    l2rate = None
+    if is_fluid(p):
+        # the NS solver's time is the Schur-complement CG (one persistent
+        # launch per call, its operator L2-resident): its roof is the L2
+        # read bandwidth, measured live
+        r = C.c_double()
+        _lib.check(L.gsls_l2_read_rate(C.byref(r)), "gsls_l2_read_rate")
+        l2rate = r.value / 1e9
+
+        def schur_roof(prof, s):
+            cnt, tot_ms = prof.get("schur", (0, 0.0))
+            calls, _ = prof.get("schur_calls", (0, 0.0))
+            t = "float" if s == 4 else "double"
+            B = p.nnz * (7 * s + 4) + 4 * p.nNo + 16 * p.nNo * s
+            it_s = (tot_ms / max(cnt, 1)) / 1e3
+            ach = B / it_s / 1e9 if cnt else None
+            return {"kernel": f"k_schur_persistent<{t},{t}> (CGRAD_SCHUR: every CG iteration "
+                              "of one call in one cooperative launch, 3 grid barriers per "
+                              "iteration)",
+                    "bound": "l2", "achieved": ach, "peak": l2rate, "unit": "GB/s",
+                    "frac": (ach / l2rate) if ach else None,
+                    "peak_source": "measured L2 read bandwidth (gsls_l2_read_rate)",
+                    "bytes_per_iteration": B, "avg_iteration_us": it_s * 1e6,
+                    "iterations": cnt, "launches": calls,
+                    "note": "per CG iteration: operator mG, Gt, mL and columns "
+                            "(nnz (7 s + 4) B) + 16 vector passes; time = launch time / "
+                            "iterations of the call"}
+
+        roof_gm, roof_gm64 = roof, roof64
+        roof, roof64 = schur_roof(profd["prof"], 4), schur_roof(profd64["prof"], 8)
     # the FP64 SpMV issues one FP64 FMA per matrix entry; GB300 runs FP64 at
     # ~1/74 of FP32, so its roof is the FP64 pipe when that takes longer
     # than the HBM stream (measured live by the library's probe kernel)
@@ -434,7 +464,7 @@ def run_gsls(args):
     _lib.check(L.gsls_fp64_fma_rate(C.byref(rate)), "gsls_fp64_fma_rate")
     d = 3 if (is_fluid(p) or p.dof == 3) else 1
     fmas = d * d * p.nnz
-    if roof64["achieved"]:
+    if roof64["achieved"] and not is_fluid(p):
         avg_s = roof64["avg_launch_us"] / 1e6
         t_fma, t_hbm = fmas / rate.value, roof64["bytes_per_launch"] / (peak * 1e9)
         hbm = {k: roof64[k] for k in ("achieved", "peak", "unit", "frac", "peak_source", "traffic")}
@@ -474,6 +504,9 @@ def run_gsls(args):
         "gpu_launches": int(mixed["launches"]),
         "clocks": clk,
     }
+    if is_fluid(p):
+        out["roofline_gm_spmv"] = roof_gm
+        out["roofline_gm_spmv_fp64"] = roof_gm64
     if rank == 0 and world == 1 and not args.no_cpu:
         # the oracle's own implicit steps of the workload (timed: the CPU
         # baseline) and the same steps on the GPU in both precisions: the

@@ -215,6 +215,9 @@ typedef struct {
      the reference's input). */
   int viscType;
   double mu_o, vlam, va, vn;
+  double bstab;     /* FLUID backflow stabilisation coefficient of the
+                       Neumann faces (BFLUID, backflow_stab; the reference's
+                       input default is 0.2, READFILES.f:1089-1091) */
 } gsls_eq_params;
 
 #define GSLS_VISC_CONST 0
@@ -271,12 +274,15 @@ int gsls_eq_add_dirichlet(gsls_eq *eq, int nNo, const int *gNodes,
 int gsls_eq_add_dirichlet_nv(gsls_eq *eq, int nNo, const int *gNodes,
                              const double *gx, const double *nV, double g,
                              int mask);
-/* Neumann BC of value g on tri3 faces (fIEN 1-based, 3 x nFel) of a HEATF
-   equation: BASSEMNEUBC with BHEATF (Code/Source/svFSI/EQASSEM.f:90-192,
-   HEATF.f:289-319) at every Newton iteration, h = -g (SETBCNEUL,
-   SETBC.f:300) and the backflow term min(u.n, 0) T with its tangent; the
-   outward normal is oriented away from the parent element's fourth node
-   (GNNB, NN.f:1856-1990).  Other physics: GSLS_ERR_UNSUPPORTED. */
+/* Neumann BC of value g on tri3 faces (fIEN 1-based, 3 x nFel), applied
+   by BASSEMNEUBC (Code/Source/svFSI/EQASSEM.f:90-192) at every Newton
+   iteration with h = -g (SETBCNEUL, SETBC.f:300).  HEATF: BHEATF
+   (HEATF.f:289-319), the flux and the backflow term min(u.n, 0) T with its
+   tangent.  FLUID: BFLUID (FLUID.f:1280-1334), the traction h n and the
+   backflow stabilisation 1/2 bstab rho (u.n - |u.n|) u with its tangent on
+   the velocity diagonal.  The outward normal is oriented away from the
+   parent element's fourth node (GNNB, NN.f:1856-1990).  Other physics:
+   GSLS_ERR_UNSUPPORTED. */
 int gsls_eq_add_neumann(gsls_eq *eq, int nFel, const int *fIEN, double g);
 /* Constant traction h on tri3 faces (fIEN 1-based, 3 x nFel), integrated
    as SETBCTRACL does (Code/Source/svFSI/SETBC.f:319-416). */
@@ -358,6 +364,11 @@ int gsls_profile_read(const char *name, long long *count, double *total_ms);
    whose SpMV issues one FP64 FMA per matrix entry.  No counterpart in the
    reference. */
 int gsls_fp64_fma_rate(double *fma_per_s);
+/* No counterpart in the reference.  L2 read bandwidth of the device
+   (bytes/s): a 48 MiB buffer, resident in L2, swept 20 times by every
+   resident thread with 16-byte loads; the roof of kernels whose operator
+   stays in L2 between launches (the persistent Schur-complement CG). */
+int gsls_l2_read_rate(double *bytes_per_s);
 
 /* ---- discrete adjoint (forward/backward pair) --------------------------
    Gradient of an objective of the final state with respect to the

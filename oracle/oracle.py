@@ -41,7 +41,8 @@ class EqP(C.Structure):
                 ("mu_f", C.c_double), ("ctM", C.c_double),
                 ("ctC", C.c_double), ("eparam", c_double_p), ("elM", C.c_double),
                 ("nu", C.c_double), ("viscType", C.c_int), ("mu_o", C.c_double),
-                ("vlam", C.c_double), ("va", C.c_double), ("vn", C.c_double)]
+                ("vlam", C.c_double), ("va", C.c_double), ("vn", C.c_double),
+                ("bstab", C.c_double)]
 
 
 class DirBC(C.Structure):
@@ -128,6 +129,9 @@ def load():
         L.orc_genalpha.argtypes = [C.c_double, C.c_int, c_double_p, c_double_p, c_double_p,
                                    c_double_p]
         L.orc_eq_step.argtypes = [C.POINTER(Eq), C.POINTER(StepInfo)]
+        L.orc_bfluid.argtypes = [C.POINTER(EqP), C.c_int, c_int_p, C.c_double, C.c_int,
+                                 c_int_p, c_double_p, c_double_p, c_int_p, c_int_p,
+                                 c_double_p, c_double_p]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_color_elements.restype = C.c_int
         L.orc_color_elements.argtypes = [C.c_int, C.c_int, c_int_p, c_int_p, c_int_p]

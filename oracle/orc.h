@@ -129,6 +129,7 @@ typedef struct {
   int viscType;                /* FLUID viscosity: 0 constant (mu_f), 1 Carreau-Yasuda,
                                   2 Casson (F/FLUID.f:1690-1739) */
   double mu_o, vlam, va, vn;   /* mu_o, lam, a, n of the model (mu_i = mu_f) */
+  double bstab;                /* FLUID backflow_stab (F/READFILES.f:1089-1091) */
 } orc_eqp;
 
 int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
@@ -165,6 +166,15 @@ void orc_traction(int dof, int nFel, const int *fIEN, const double *x,
 void orc_bheatf(const orc_eqp *p, int nFel, const int *fIEN, double g, int nEl,
                 const int *IEN, const double *x, const double *Yg, const int *rowPtr,
                 const int *colPtr, double *R, double *Val);
+
+/* BASSEMNEUBC with BFLUID (F/EQASSEM.f:90-192, F/FLUID.f:1280-1334) on
+   tri3 faces of a fluid equation (dof 4, velocity at s..s+2): h = -g,
+   backflow coefficient p->bstab, into R(4,nNo) and Val(16,nnz) */
+void orc_bfluid(const orc_eqp *p, int nFel, const int *fIEN, double g, int nEl,
+                const int *IEN, const double *x, const double *Yg, const int *rowPtr,
+                const int *colPtr, double *R, double *Val);
+/* node of each face's parent element that is off the face (-1: none) */
+void orc_face_inner(int nFel, const int *fIEN, int nEl, const int *IEN, int *inner);
 
 /* CEP3D with isotropic diffusivity, F/CEP.f:136-266 (no fibres) */
 void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12],

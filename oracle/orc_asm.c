@@ -969,21 +969,12 @@ void orc_bheatf(const orc_eqp *p, int nFel, const int *fIEN, double g, int nEl,
   const double h = -g;
   const double s = 2.0 / 3.0, t = 1.0 / 6.0;
   const double xi[3][2] = {{t, t}, {s, t}, {t, s}};
+  int *innerv = (int *)xcalloc((size_t)(nFel > 0 ? nFel : 1), sizeof(int));
+  orc_face_inner(nFel, fIEN, nEl, IEN, innerv);
   for (int f = 0; f < nFel; f++) {
     const int *q = fIEN + 3 * f;
     /* the element holding the face, and its node off the face */
-    int inner = -1;
-    for (int e = 0; e < nEl && inner < 0; e++) {
-      int hit = 0, other = -1;
-      for (int a = 0; a < 4; a++) {
-        const int v = IEN[4 * e + a];
-        if (v == q[0] || v == q[1] || v == q[2])
-          hit++;
-        else if (other < 0)
-          other = v;
-      }
-      if (hit == 3) inner = other;
-    }
+    const int inner = innerv[f];
     if (inner < 0) continue;
     /* GNNB for tri3: n = (x1 - x3) x (x2 - x3), pointing away from the
        element's other node */
@@ -1031,6 +1022,110 @@ void orc_bheatf(const orc_eqp *p, int nFel, const int *fIEN, double g, int nEl,
           }
     }
   }
+  free(innerv);
+}
+
+void orc_face_inner(int nFel, const int *fIEN, int nEl, const int *IEN, int *inner) {
+  /* elements of each node that lies on a face (counting sort) */
+  int nNo = 0;
+  for (int k = 0; k < 4 * nEl; k++)
+    if (IEN[k] + 1 > nNo) nNo = IEN[k] + 1;
+  int *cnt = (int *)xcalloc((size_t)nNo + 1, sizeof(int));
+  char *onF = (char *)xcalloc((size_t)(nNo > 0 ? nNo : 1), 1);
+  for (int k = 0; k < 3 * nFel; k++) onF[fIEN[k]] = 1;
+  for (int k = 0; k < 4 * nEl; k++)
+    if (onF[IEN[k]]) cnt[IEN[k] + 1]++;
+  for (int v = 0; v < nNo; v++) cnt[v + 1] += cnt[v];
+  int *els = (int *)xcalloc((size_t)(cnt[nNo] > 0 ? cnt[nNo] : 1), sizeof(int));
+  int *fill = (int *)xcalloc((size_t)nNo + 1, sizeof(int));
+  memcpy(fill, cnt, sizeof(int) * ((size_t)nNo + 1));
+  for (int e = 0; e < nEl; e++)
+    for (int a = 0; a < 4; a++)
+      if (onF[IEN[4 * e + a]]) els[fill[IEN[4 * e + a]]++] = e;
+  for (int f = 0; f < nFel; f++) {
+    const int *q = fIEN + 3 * f;
+    inner[f] = -1;
+    for (int k = cnt[q[0]]; k < cnt[q[0] + 1] && inner[f] < 0; k++) {
+      const int e = els[k];
+      int hit = 0, other = -1;
+      for (int a = 0; a < 4; a++) {
+        const int v = IEN[4 * e + a];
+        if (v == q[0] || v == q[1] || v == q[2])
+          hit++;
+        else if (other < 0)
+          other = v;
+      }
+      if (hit == 3) inner[f] = other;
+    }
+  }
+  free(cnt);
+  free(onF);
+  free(els);
+  free(fill);
+}
+
+/* BFLUID (F/FLUID.f:1280-1334) through BASSEMNEUBC (F/EQASSEM.f:90-192):
+   at each point of the tri3 rule, udn = 1/2 bstab rho (u.n - |u.n|),
+   hc = h n + udn u, lR(i,a) -= w N_a hc_i and the velocity diagonal of
+   lK (entries 1, 6, 11 of the 4x4 block) -= w af gam dt N_a N_b udn. */
+void orc_bfluid(const orc_eqp *p, int nFel, const int *fIEN, double g, int nEl,
+                const int *IEN, const double *x, const double *Yg, const int *rowPtr,
+                const int *colPtr, double *R, double *Val) {
+  const int tD = p->tDof, s0 = p->s;
+  const double h = -g;
+  const double s = 2.0 / 3.0, t = 1.0 / 6.0;
+  const double xi[3][2] = {{t, t}, {s, t}, {t, s}};
+  int *innerv = (int *)xcalloc((size_t)(nFel > 0 ? nFel : 1), sizeof(int));
+  orc_face_inner(nFel, fIEN, nEl, IEN, innerv);
+  for (int f = 0; f < nFel; f++) {
+    const int *q = fIEN + 3 * f;
+    const int inner = innerv[f];
+    if (inner < 0) continue;
+    double e1[3], e2[3], n[3], v[3];
+    for (int i = 0; i < 3; i++) {
+      e1[i] = x[3 * q[0] + i] - x[3 * q[2] + i];
+      e2[i] = x[3 * q[1] + i] - x[3 * q[2] + i];
+      v[i] = x[3 * q[0] + i] - x[3 * inner + i];
+    }
+    n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    if (n[0] * v[0] + n[1] * v[1] + n[2] * v[2] < 0.0)
+      for (int i = 0; i < 3; i++) n[i] = -n[i];
+    const double Jac = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    double nV[3];
+    for (int i = 0; i < 3; i++) nV[i] = n[i] / Jac;
+    double lR[3][3] = {{0}}, lK[3][3] = {{0}};
+    for (int gp = 0; gp < 3; gp++) {
+      const double N[3] = {xi[gp][0], xi[gp][1], 1.0 - xi[gp][0] - xi[gp][1]};
+      const double w = (1.0 / 6.0) * Jac;
+      const double wl = w * p->af * p->gam * p->dt;
+      double u[3] = {0, 0, 0};
+      for (int a = 0; a < 3; a++)
+        for (int i = 0; i < 3; i++) u[i] = u[i] + N[a] * Yg[(size_t)q[a] * tD + s0 + i];
+      double udn = 0.0;
+      for (int i = 0; i < 3; i++) udn = udn + u[i] * nV[i];
+      udn = 0.5 * p->bstab * p->rho * (udn - fabs(udn));
+      double hc[3];
+      for (int i = 0; i < 3; i++) hc[i] = h * nV[i] + udn * u[i];
+      for (int a = 0; a < 3; a++) {
+        for (int i = 0; i < 3; i++) lR[a][i] = lR[a][i] - w * N[a] * hc[i];
+        for (int b = 0; b < 3; b++) lK[a][b] = lK[a][b] - wl * N[a] * N[b] * udn;
+      }
+    }
+    for (int a = 0; a < 3; a++) {
+      for (int i = 0; i < 3; i++) R[(size_t)q[a] * 4 + i] += lR[a][i];
+      for (int b = 0; b < 3; b++)
+        for (int j = rowPtr[q[a]]; j < rowPtr[q[a] + 1]; j++)
+          if (colPtr[j] == q[b]) {
+            Val[(size_t)j * 16 + 0] += lK[a][b];
+            Val[(size_t)j * 16 + 5] += lK[a][b];
+            Val[(size_t)j * 16 + 10] += lK[a][b];
+            break;
+          }
+    }
+  }
+  free(innerv);
 }
 
 void orc_traction(int dof, int nFel, const int *fIEN, const double *x,
@@ -1198,10 +1293,15 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
     /* SETBCNEU (traction) */
     for (int t = 0; t < eq->nTrac; t++)
       orc_traction(dof, eq->trac[t].nFel, eq->trac[t].fIEN, eq->x, eq->trac[t].h, R);
-    /* BASSEMNEUBC (HEATF Neumann faces) */
-    for (int k = 0; k < eq->nNeu; k++)
-      orc_bheatf(&eq->p, eq->neu[k].nFel, eq->neu[k].fIEN, eq->neu[k].g, eq->nEl, eq->IEN,
-                 eq->x, Yg, eq->rowPtr, eq->colPtr, R, Val);
+    /* BASSEMNEUBC (Neumann faces: BFLUID for a fluid, BHEATF for HEATF) */
+    for (int k = 0; k < eq->nNeu; k++) {
+      if (eq->p.phys == 4)
+        orc_bfluid(&eq->p, eq->neu[k].nFel, eq->neu[k].fIEN, eq->neu[k].g, eq->nEl, eq->IEN,
+                   eq->x, Yg, eq->rowPtr, eq->colPtr, R, Val);
+      else
+        orc_bheatf(&eq->p, eq->neu[k].nFel, eq->neu[k].fIEN, eq->neu[k].g, eq->nEl, eq->IEN,
+                   eq->x, Yg, eq->rowPtr, eq->colPtr, R, Val);
+    }
     /* LSSOLVE */
     rc = orc_solve(lhs, &ls, dof, R, Val, eq->prec, incL, res);
     if (rc) break;

@@ -43,7 +43,7 @@ class EqParams(C.Structure):
                 ("mu_f", C.c_double), ("ctM", C.c_double), ("ctC", C.c_double),
                 ("eparam", c_double_p), ("elM", C.c_double), ("nu", C.c_double),
                 ("viscType", C.c_int), ("mu_o", C.c_double), ("vlam", C.c_double),
-                ("va", C.c_double), ("vn", C.c_double)]
+                ("va", C.c_double), ("vn", C.c_double), ("bstab", C.c_double)]
 
 
 class EqSolver(C.Structure):
@@ -133,6 +133,7 @@ SIGNATURES = {
     "gsls_profile_reset": (C.c_int, []),
     "gsls_profile_read": (C.c_int, [C.c_char_p, C.POINTER(C.c_longlong), c_double_p]),
     "gsls_fp64_fma_rate": (C.c_int, [c_double_p]),
+    "gsls_l2_read_rate": (C.c_int, [c_double_p]),
 }
 
 _LIB = None

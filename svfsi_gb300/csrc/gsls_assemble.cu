@@ -38,6 +38,7 @@ struct gsls_mesh {
   // assembled conduction sum_e W nu_e Nx_a.Nx_b (nu_e = 1 without a
   // per-element parameter) as FP64 scalar CSR, and sum_e w Ns_a per node
   gsls::DevBuf d_linM, d_linK, d_linB;
+  gsls::DevBuf d_linM32, d_linK32;  // FP32 copies for the mixed-precision tangent
   bool lin_ready = false;
 };
 
@@ -249,34 +250,50 @@ __global__ void __launch_bounds__(kAsmThreads) k_lin_build(AsmArgs A, double *Mg
 }
 
 // 16 lanes per CSR row (tet4 rows hold ~15 entries), entries strided by
-// 16, the row sum by a fixed shuffle tree: deterministic.
+// 16, the row sums by a fixed shuffle tree: deterministic.  GB300 runs FP64
+// at ~1/74 of the FP32 rate, so a pass over the operators is FP64-bound
+// before it is HBM-bound: the residual takes two FP64 FMAs per entry
+// (rM = sum m Ag, rK = sum k Yg; R = rho rM + nu rK - rs b) and the FP32
+// tangent is formed from FP32 copies of the operators (Val = cM m + cK k in
+// VT; the FP64 tangent from the FP64 operators).
 constexpr int kLinLanes = 16;
 template <class VT>
 __global__ void __launch_bounds__(256) k_asm_lin(int nNo, const int *__restrict__ rowPtr,
                                                  const int *__restrict__ colPtr,
                                                  const double *__restrict__ Mg,
                                                  const double *__restrict__ Kg,
+                                                 const VT *__restrict__ Mt,
+                                                 const VT *__restrict__ Kt,
                                                  const double *__restrict__ Bg,
                                                  const double *__restrict__ Ag,
                                                  const double *__restrict__ Yg, int tDof, int s,
-                                                 double rho, double nu, double rs, double cM,
-                                                 double cK, double *__restrict__ R,
-                                                 VT *__restrict__ Val) {
+                                                 double rho, double nu, double rs, VT cM, VT cK,
+                                                 double *__restrict__ R, VT *__restrict__ Val) {
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int row = (int)(g / kLinLanes), l = (int)(g % kLinLanes);
-  double r = 0.0;
+  double rM = 0.0, rK = 0.0;
   if (row < nNo) {
     const int j0 = __ldg(rowPtr + row), j1 = __ldg(rowPtr + row + 1);
     for (int j = j0 + l; j < j1; j += kLinLanes) {
       const double m = __ldcs(Mg + j), k = __ldcs(Kg + j);
       const size_t c = (size_t)__ldcs(colPtr + j) * tDof + s;
-      __stcs(Val + j, VT(cM * m + cK * k));
-      r += rho * m * __ldg(Ag + c) + nu * k * __ldg(Yg + c);
+      __stcs(Val + j, cM * __ldcs(Mt + j) + cK * __ldcs(Kt + j));
+      rM = fma(m, __ldg(Ag + c), rM);
+      rK = fma(k, __ldg(Yg + c), rK);
     }
   }
 #pragma unroll
-  for (int o = kLinLanes / 2; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o, kLinLanes);
-  if (row < nNo && l == 0) R[row] = r - rs * Bg[row];
+  for (int o = kLinLanes / 2; o > 0; o >>= 1) {
+    rM += __shfl_xor_sync(0xffffffffu, rM, o, kLinLanes);
+    rK += __shfl_xor_sync(0xffffffffu, rK, o, kLinLanes);
+  }
+  if (row < nNo && l == 0) R[row] = rho * rM + nu * rK - rs * Bg[row];
+}
+
+__global__ void k_f64_to_f32(size_t n, const double *__restrict__ a, float *__restrict__ b) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    b[k] = (float)a[k];
 }
 
 static int lin_prepare(gsls_mesh *m, AsmArgs A) {
@@ -297,6 +314,13 @@ static int lin_prepare(gsls_mesh *m, AsmArgs A) {
         A, m->d_linM.as<double>(), m->d_linK.as<double>(), m->d_linB.as<double>());
     GSLS_CHECK_LAUNCH();
   }
+  GSLS_TRY(m->d_linM32.alloc(sizeof(float) * (size_t)lhs->nnz));
+  GSLS_TRY(m->d_linK32.alloc(sizeof(float) * (size_t)lhs->nnz));
+  const int nb = 4 * num_sms();
+  k_f64_to_f32<<<nb, 256, 0, st>>>(lhs->nnz, m->d_linM.as<double>(), m->d_linM32.as<float>());
+  GSLS_CHECK_LAUNCH();
+  k_f64_to_f32<<<nb, 256, 0, st>>>(lhs->nnz, m->d_linK.as<double>(), m->d_linK32.as<float>());
+  GSLS_CHECK_LAUNCH();
   m->lin_ready = true;
   return GSLS_OK;
 }
@@ -416,15 +440,16 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
     const long long nt = (long long)lhs->nNo * kLinLanes;
     const int nb = (int)((nt + 255) / 256);
     const int *rp = lhs->d_rowPtr.as<int>(), *cp = lhs->d_colPtr.as<int>();
+    const double *M = m->d_linM.as<double>(), *K = m->d_linK.as<double>();
     if (mixed)
-      k_asm_lin<float><<<nb, 256, 0, st>>>(lhs->nNo, rp, cp, m->d_linM.as<double>(),
-                                           m->d_linK.as<double>(), m->d_linB.as<double>(), Ag,
+      k_asm_lin<float><<<nb, 256, 0, st>>>(lhs->nNo, rp, cp, M, K, m->d_linM32.as<float>(),
+                                           m->d_linK32.as<float>(), m->d_linB.as<double>(), Ag,
                                            Yg, A.tDof, A.s, A.rho, nu, A.rho * A.src,
-                                           A.am * A.rho, T1 * nu, R, static_cast<float *>(Val));
+                                           float(A.am * A.rho), float(T1 * nu), R,
+                                           static_cast<float *>(Val));
     else
-      k_asm_lin<double><<<nb, 256, 0, st>>>(lhs->nNo, rp, cp, m->d_linM.as<double>(),
-                                            m->d_linK.as<double>(), m->d_linB.as<double>(), Ag,
-                                            Yg, A.tDof, A.s, A.rho, nu, A.rho * A.src,
+      k_asm_lin<double><<<nb, 256, 0, st>>>(lhs->nNo, rp, cp, M, K, M, K, m->d_linB.as<double>(),
+                                            Ag, Yg, A.tDof, A.s, A.rho, nu, A.rho * A.src,
                                             A.am * A.rho, T1 * nu, R, static_cast<double *>(Val));
     GSLS_CHECK_LAUNCH();
     return GSLS_OK;

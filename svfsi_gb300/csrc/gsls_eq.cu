@@ -201,6 +201,61 @@ __global__ void k_bheatf(int nF, int f0, const int *__restrict__ fien,
   }
 }
 
+// BASSEMNEUBC + BFLUID (Code/Source/svFSI/EQASSEM.f:90-192, FLUID.f:
+// 1280-1334) on the tri3 faces of a fluid equation (dof 4, velocity at
+// s..s+2), one face per thread, colours as for BHEATF: at each of the 3
+// points udn = 1/2 bstab rho (u.n - |u.n|) (backflow only), hc = h n + udn u,
+//   lR(i,a) -= w N_a hc_i,   lK(a,b)[i,i] -= w af gam dt N_a N_b udn (i < 3)
+// (entries 1, 6, 11 of the reference's 4x4 block), h = -g.
+template <class VT>
+__global__ void k_bfluid(int nF, int f0, const int *__restrict__ fien,
+                         const double *__restrict__ geo, const int *__restrict__ pos,
+                         const double *__restrict__ Yg, int tDof, int s, double h, double T1,
+                         double brho, double *R, VT *Val) {
+  const int f = f0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= f0 + nF) return;
+  const int n[3] = {fien[3 * f], fien[3 * f + 1], fien[3 * f + 2]};
+  const double nv[3] = {geo[4 * f], geo[4 * f + 1], geo[4 * f + 2]}, Jac = geo[4 * f + 3];
+  double ul[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) ul[a][i] = Yg[(size_t)n[a] * tDof + s + i];
+  const double xs = 2.0 / 3.0, xt = 1.0 / 6.0;
+  const double xi[3][2] = {{xt, xt}, {xs, xt}, {xt, xs}};
+  const double w = Jac / 6.0, wl = w * T1;
+  double lR[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, lK[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+  for (int g = 0; g < 3; g++) {
+    const double N[3] = {xi[g][0], xi[g][1], 1.0 - xi[g][0] - xi[g][1]};
+    double u[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) u[i] = N[0] * ul[0][i] + N[1] * ul[1][i] + N[2] * ul[2][i];
+    double udn = u[0] * nv[0] + u[1] * nv[1] + u[2] * nv[2];
+    udn = 0.5 * brho * (udn - fabs(udn));
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) lR[a][i] -= w * N[a] * (h * nv[i] + udn * u[i]);
+#pragma unroll
+      for (int b = 0; b < 3; b++) lK[a][b] -= wl * N[a] * N[b] * udn;
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) R[(size_t)n[a] * 4 + i] += lR[a][i];
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+      VT *blk = Val + (size_t)pos[9 * f + 3 * a + b] * 16;
+      const VT k = VT(lK[a][b]);
+      blk[0] += k;
+      blk[5] += k;
+      blk[10] += k;
+    }
+  }
+}
+
 // Aliev-Panfilov right-hand side (AP_GETF, Code/Source/svFSI/CEPMOD_AP.f:
 // 255-267) with the parameters of PARAMS_AP.f:53-86, in precision T.
 template <class T>
@@ -391,8 +446,9 @@ int gsls_eq_add_dirichlet_nv(gsls_eq *eq, int nNo, const int *gNodes, const doub
 
 int gsls_eq_add_neumann(gsls_eq *eq, int nFel, const int *fIEN, double g) {
   if (!eq || nFel < 0 || (nFel > 0 && !fIEN)) return GSLS_ERR_ARG;
-  if (eq->p.phys != GSLS_PHYS_HEATF) {
-    set_error("gsls_eq_add_neumann: only the HEATF boundary term (BHEATF) is built");
+  if (eq->p.phys != GSLS_PHYS_HEATF && eq->p.phys != GSLS_PHYS_FLUID) {
+    set_error("gsls_eq_add_neumann: only the HEATF (BHEATF) and FLUID (BFLUID) boundary "
+              "terms are built");
     return GSLS_ERR_UNSUPPORTED;
   }
   gsls_lhs *lhs = eq->lhs;
@@ -798,14 +854,25 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
       for (size_t c = 0; c + 1 < nf->coff.size(); c++) {
         const int f0 = nf->coff[c], n = nf->coff[c + 1] - f0;
         if (n <= 0) continue;
-        if (valp == GSLS_PREC_MIXED)
+        if (p.phys == GSLS_PHYS_FLUID) {
+          const double brho = p.bstab * p.rho;
+          if (valp == GSLS_PREC_MIXED)
+            k_bfluid<float><<<(n + 127) / 128, 128, 0, st>>>(
+                n, f0, nf->fien.as<int>(), nf->geo.as<double>(), nf->pos.as<int>(), Yg, tD,
+                p.s, nf->h, T1, brho, eq->R.as<double>(), eq->Val.as<float>());
+          else
+            k_bfluid<double><<<(n + 127) / 128, 128, 0, st>>>(
+                n, f0, nf->fien.as<int>(), nf->geo.as<double>(), nf->pos.as<int>(), Yg, tD,
+                p.s, nf->h, T1, brho, eq->R.as<double>(), eq->Val.as<double>());
+        } else if (valp == GSLS_PREC_MIXED) {
           k_bheatf<float><<<(n + 127) / 128, 128, 0, st>>>(
               n, f0, nf->fien.as<int>(), nf->geo.as<double>(), nf->pos.as<int>(), Yg, tD, p.s,
               nf->h, T1, eq->R.as<double>(), eq->Val.as<float>());
-        else
+        } else {
           k_bheatf<double><<<(n + 127) / 128, 128, 0, st>>>(
               n, f0, nf->fien.as<int>(), nf->geo.as<double>(), nf->pos.as<int>(), Yg, tD, p.s,
               nf->h, T1, eq->R.as<double>(), eq->Val.as<double>());
+        }
         GSLS_CHECK_LAUNCH();
       }
     }

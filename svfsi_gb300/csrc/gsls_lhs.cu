@@ -321,6 +321,21 @@ __global__ void __launch_bounds__(256) k_dfma_probe(double *out, int iters) {
   out[t] = s;
 }
 
+// L2 read-bandwidth probe: every block sweeps the whole L2-resident buffer
+// (float4 loads, each block from its own starting offset), `passes` times;
+// one sum per thread stored into out[grid * block].
+__global__ void __launch_bounds__(512) k_l2_probe(const float4 *__restrict__ buf, size_t n4,
+                                                  int passes, float *out) {
+  float acc = 0.f;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (int p = 0; p < passes; p++)
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += stride) {
+      const float4 v = __ldcg(buf + k);
+      acc += v.x + v.y + v.z + v.w;
+    }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
 }  // namespace gsls
 
 namespace gsls {
@@ -363,6 +378,43 @@ int gsls_fp64_fma_rate(double *fma_per_s) {
   if (e1) cudaEventDestroy(e1);
   if (st) cudaStreamDestroy(st);
   if (d) cudaFree(d);
+  return rc;
+}
+
+int gsls_l2_read_rate(double *bytes_per_s) {
+  if (!bytes_per_s) return GSLS_ERR_ARG;
+  const int threads = 512, blocks = 2 * num_sms(), passes = 20;
+  const size_t bytes = (size_t)48 << 20;  // 48 MiB: well inside the 129 MB L2
+  const size_t n4 = bytes / 16;
+  float4 *buf = nullptr;
+  float *out = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = GSLS_OK;
+  float ms = 0.0f;
+  if (cudaMalloc(&buf, bytes) != cudaSuccess ||
+      cudaMalloc(&out, sizeof(float) * (size_t)blocks * threads) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
+      cudaMemsetAsync(buf, 0, bytes, st) != cudaSuccess) {
+    rc = GSLS_ERR_CUDA;
+  } else {
+    for (int r = 0; r < 3; r++) k_l2_probe<<<blocks, threads, 0, st>>>(buf, n4, 2, out);
+    cudaEventRecord(e0, st);
+    k_l2_probe<<<blocks, threads, 0, st>>>(buf, n4, passes, out);
+    cudaEventRecord(e1, st);
+    count_launch_n(4);
+    if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.0f)
+      rc = GSLS_ERR_CUDA;
+  }
+  if (rc == GSLS_OK) *bytes_per_s = (double)passes * (double)bytes / (ms * 1e-3);
+  else set_error("gsls_l2_read_rate: CUDA error");
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (out) cudaFree(out);
+  if (buf) cudaFree(buf);
   return rc;
 }
 

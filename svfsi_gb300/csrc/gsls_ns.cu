@@ -1038,11 +1038,28 @@ static int schur_cg(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *mG, const VT *Gt, 
                           lhs->ws.partials.as<double>(), db, sc, K, zigzag_on(),
                           wait_limit()};
       void *args[] = {&a};
+      const bool prof = prof_on();
+      cudaEvent_t pe0 = nullptr, pe1 = nullptr;
+      if (prof) {
+        GSLS_CUDA(cudaEventCreate(&pe0));
+        GSLS_CUDA(cudaEventCreate(&pe1));
+        GSLS_CUDA(cudaEventRecord(pe0, st));
+      }
       GSLS_CUDA(cudaLaunchCooperativeKernel((const void *)k_schur_persistent<VT, XT>, dim3(nblk),
                                             dim3(kPT), args, smem, st));
       GSLS_CHECK_LAUNCH();
+      if (prof) GSLS_CUDA(cudaEventRecord(pe1, st));
       GSLS_CUDA(cudaMemcpyAsync(h_sc, sc, sizeof(SchurScal), cudaMemcpyDeviceToHost, st));
       GSLS_CUDA(cudaStreamSynchronize(st));
+      if (prof) {
+        // per CG iteration: count = iterations of this call
+        float ms = 0.f;
+        GSLS_CUDA(cudaEventElapsedTime(&ms, pe0, pe1));
+        prof_add("schur", h_sc->itr, ms);
+        prof_add("schur_calls", 1, ms);
+        cudaEventDestroy(pe0);
+        cudaEventDestroy(pe1);
+      }
       if (h_sc->done == 4) {
         set_error("NS: grid barrier of the Schur-complement CG timed out");
         return GSLS_ERR_CUDA;

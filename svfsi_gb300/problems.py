@@ -251,8 +251,9 @@ def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float 
                    dt: float = 1e-3, viscosity: dict | None = None) -> Problem:
     """Config: cylinder R=0.5, L=5 (seeded Delaunay cross-section), rho 1.06,
     mu 0.04, parabolic inlet with peak u_max at z=0 (value -u_max along the
-    outward normal -z, profile of BCINI), no-slip wall, traction-free outlet
-    (p = 0 Neumann: no term), dt 1e-3, NS solver with RCS preconditioning and
+    outward normal -z, profile of BCINI), no-slip wall, outlet z = L a
+    Neumann face of value 0 (p = 0; BFLUID adds its backflow stabilisation,
+    coefficient 0.2, where u.n < 0), dt 1e-3, NS solver with RCS preconditioning and
     Krylov dimension 100 (outer tolerance 1e-2, inner GMRES 1e-2 and Schur CG
     0.2 as LS_CREATE sets them), Newton to 1e-10 (a converged implicit step:
     ~8 iterations).  Fluid starts at rest.  ``viscosity``: the result of
@@ -261,7 +262,7 @@ def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float 
     rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
     am, af, beta, gam = genalpha(0.2, second_order=False)
     params = dict(am=am, af=af, beta=beta, gam=gam, dt=dt, rho=rho, mu_f=mu, ctM=1.0, ctC=36.0,
-                  fb=(0.0, 0.0, 0.0))
+                  fb=(0.0, 0.0, 0.0), bstab=0.2)
     if viscosity:
         params.update(viscosity)
     inlet, wall = info["inlet"], info["wall"]
@@ -271,6 +272,7 @@ def fluid_cylinder(h: float = 0.027, nsteps: int = 20, R: float = 0.5, L: float 
     return Problem(name=f"fluid_cylinder_h{h:g}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
                    phys=PHYS_FLUID, dof=4, tDof=4, params=params,
                    dirichlet=[DirBC(inlet, -u_max, gx=gx, nV=nV), DirBC(wall, 0.0)],
+                   neumann=[NeuBC(meshgen.faces_on_plane(x, ien, 2, L), 0.0)],
                    LS_type=LS_TYPE_NS, prec=PRECOND_RCS, ls_relTol=1e-2, ls_sD=100, minItr=1,
                    maxItr=12, tol=1e-10, nsteps=nsteps)
 

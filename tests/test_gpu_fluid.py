@@ -290,3 +290,40 @@ def test_unknown_viscosity_model_is_rejected(gsls):
     lhs, mesh, eq = problems.build_equation(p)
     with pytest.raises(_lib.GslsError, match="viscosity"):
         eq.step()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fluid_outlet_backflow_face_matches_oracle(gsls, orc, precision):
+    """The outlet z = L is a Neumann face (p = 0) with BFLUID's backflow
+    stabilisation (bstab 0.2).  The initial axial velocity 30 (1 - r^2/R^2)
+    - 12 flows back in through the outer part of the outlet, so the backflow
+    term and its tangent act: two converged steps land on the oracle's state
+    (FP64 1e-9, mixed 1e-8) and differ from the same steps without it."""
+    def case(bstab):
+        p = _cyl(nsteps=2)
+        p.params["bstab"] = bstab
+        r2 = p.x[:, 0] ** 2 + p.x[:, 1] ** 2
+        Y0 = np.zeros((p.nNo, 4))
+        Y0[:, 2] = 30.0 * (1.0 - r2 / 0.25) - 12.0
+        p.Y0 = Y0
+        return p
+
+    p = case(0.2)
+    out = meshgen.nodes_on_plane(p.x, 2, 5.0)
+    assert (p.Y0[out, 2] < 0).any() and (p.Y0[out, 2] > 0).any()
+    prec = fsils.PREC_FP64 if precision == "fp64" else fsils.PREC_MIXED
+    lhs, mesh, eq = problems.build_equation(p, precision=prec)
+    oeq = orc.OracleEquation(p)
+    oeq.set_state(*p.initial_state())
+    for _ in range(p.nsteps):
+        gi = eq.step()
+        oi = oeq.step()
+        assert gi.last_suc == 1 and oi.last_suc == 1
+    Y, Yo = eq.get_state()[1], oeq.state()[1]
+    assert rel(Y, Yo) < (1e-9 if precision == "fp64" else 1e-8)
+    q = case(0.0)
+    oq = orc.OracleEquation(q)
+    oq.set_state(*q.initial_state())
+    for _ in range(q.nsteps):
+        oq.step()
+    assert rel(oq.state()[1], Yo) > 1e-6

@@ -743,3 +743,42 @@ def test_coloured_oracle_step_matches_serial(orc, case):
     fa, fb = a.state()[k], b.state()[k]
     assert np.linalg.norm(fa - fb) <= 1e-12 * np.linalg.norm(fa)
     orc.set_threads(1)
+
+
+def test_bfluid_uniform_state_kat(orc):
+    """BFLUID on one face of the unit tet with a uniform velocity: every face
+    node gets -area/3 (h + udn u.n) n with h = -g and udn = bstab rho
+    min(u.n, 0) (backflow only); the velocity diagonal of the tangent has row
+    sums -area/3 af gam dt udn, the pressure row and column stay zero."""
+    x = _unit_tet()
+    ien = np.array([[0, 1, 2, 3]], np.int32)
+    rp, cp = meshgen.csr_from_ien(4, ien)
+    p = problems.fluid_cylinder(h=0.5, nsteps=1)   # parameters only
+    eqp = orc.eqp_from(p)
+    assert eqp.bstab == 0.2
+    face = np.array([[0, 1, 3]], np.int32)          # z = 0, outward normal -z
+    g = 0.7
+    for uz in (1.0, -2.0):                          # u.n = -uz: backflow for uz > 0
+        Y = np.zeros((4, 4))
+        Y[:, 2] = uz
+        R = np.zeros((4, 4))
+        Val = np.zeros((cp.size, 16))
+        orc.load().orc_bfluid(C.byref(eqp), 1, orc.ip(orc.i32(face.ravel())), C.c_double(g), 1,
+                              orc.ip(orc.i32(ien.ravel())), orc.dp(orc.f64(x.ravel())),
+                              orc.dp(orc.f64(Y.ravel())), orc.ip(orc.i32(rp)), orc.ip(orc.i32(cp)),
+                              orc.dp(R), orc.dp(Val))
+        area, un = 0.5, -uz
+        udn = eqp.bstab * eqp.rho * min(un, 0.0)
+        # hc = h n + udn u = (h + udn * (u.n)) n, with n = -e_z and u = -un n
+        exp_z = -area / 3.0 * (-g + udn * un) * (-1.0)
+        assert np.allclose(R[[0, 1, 3], 2], exp_z, rtol=1e-14, atol=1e-15)
+        assert np.abs(R[[0, 1, 3]][:, [0, 1, 3]]).max() <= 1e-15
+        assert np.all(R[2] == 0.0)
+        T1 = eqp.af * eqp.gam * eqp.dt
+        for i in range(4):
+            rows = Val[rp[i]:rp[i + 1]].sum(axis=0).reshape(4, 4)
+            want = 0.0 if i == 2 else -area / 3.0 * T1 * udn
+            assert np.allclose(np.diag(rows)[:3], want, rtol=1e-14, atol=1e-16)
+            off = rows.copy()
+            np.fill_diagonal(off, 0.0)
+            assert np.all(off == 0.0) and rows[3, 3] == 0.0
