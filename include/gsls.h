@@ -106,7 +106,10 @@ const char *gsls_last_error(void);
 int gsls_lhs_create(gsls_lhs **lhs, int gnNo, int nNo, int nnz,
                     const int *gNodes, const int *rowPtr, const int *colPtr,
                     int nFaces);
-/* Replaces FSILS_LHS_FREE, Code/Source/svFSILS/LHS.f:295-325. */
+/* Replaces FSILS_LHS_FREE, Code/Source/svFSILS/LHS.f:295-325.  Meshes,
+   equations and tapes built on the lhs may still be freed afterwards, in
+   any order (their free calls then touch no lhs); no other call on them is
+   valid once their lhs is freed. */
 int gsls_lhs_free(gsls_lhs *lhs);
 
 /* Replaces FSILS_BC_CREATE, Code/Source/svFSILS/BC.f:50-121: faIn 1-based,
@@ -385,6 +388,22 @@ int gsls_adjoint_forward(gsls_eq *eq, int nsteps, int every, gsls_tape **tape);
 int gsls_adjoint_backward(gsls_tape *tape, const double *Abar, const double *Ybar,
                           const double *Dbar, double *grad);
 int gsls_tape_free(gsls_tape *tape);
+
+/* Activation-time adjoint of a CEP equation (monodomain, forward-Euler
+   cell step; config: per-element diffusivity by gsls_eq_set_eparam).  The
+   smoothed activation time of node a over the nsteps steps is
+     T_a = sum_n dt (1 - s(V_n(a))),  s(V) = 1 / (1 + exp(-(V - vth) / vw))
+   (vw > 0; T_a tends to the first crossing of vth as vw -> 0 for a node
+   that depolarises once and stays up over the window).  The forward call
+   steps eq as gsls_eq_step does, checkpointing the state and the cell
+   state every `every` steps, and returns T (host, nNo).  The backward call
+   takes dJ/dT (host, nNo) and writes dJ/dDiso_e (host, nEl, original
+   element order): each reverse step adds dJ/dV_n, reverses the diffusion
+   solve (transpose solve + dR/dDiso) and the cell step's substeps.  eq is
+   left at step N.  New capability (the reference has no adjoint); FP64. */
+int gsls_cep_adjoint_forward(gsls_eq *eq, int nsteps, int every, double vth, double vw,
+                             double *T, gsls_tape **tape);
+int gsls_cep_adjoint_backward(gsls_tape *tape, const double *Tbar, double *grad);
 
 /* Linearisation point of one step: old and new state (device, tDof x nNo). */
 typedef struct {

@@ -125,6 +125,9 @@ SIGNATURES = {
     "gsls_adjoint_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "gsls_adjoint_backward": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p,
                                         c_double_p]),
+    "gsls_cep_adjoint_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
+                                           c_double_p, C.POINTER(C.c_void_p)]),
+    "gsls_cep_adjoint_backward": (C.c_int, [C.c_void_p, c_double_p, c_double_p]),
     "gsls_tape_free": (C.c_int, [C.c_void_p]),
     "gsls_adjoint_solve": (C.c_int, [C.c_void_p, C.POINTER(AdjPoint), C.c_void_p, C.c_void_p]),
     "gsls_dRdp": (C.c_int, [C.c_void_p, C.POINTER(AdjPoint), C.c_void_p, C.c_void_p]),

@@ -771,6 +771,7 @@ int gsls_mesh_create(gsls_mesh **out, gsls_lhs *lhs, int nEl, int eNoN, const in
   }
   gsls_mesh *m = new gsls_mesh();
   m->lhs = lhs;
+  lhs_attach(lhs, &m->lhs);
   m->nEl = nEl;
   m->nNo = nNo;
   m->ncolors = ncol;
@@ -839,7 +840,12 @@ int gsls_mesh_create(gsls_mesh **out, gsls_lhs *lhs, int nEl, int eNoN, const in
 
 int gsls_mesh_free(gsls_mesh *m) {
   if (!m) return GSLS_ERR_ARG;
-  if (m->lhs) cudaStreamSynchronize(m->lhs->stream);
+  if (m->lhs) {
+    cudaStreamSynchronize(m->lhs->stream);
+    lhs_detach(m->lhs, &m->lhs);
+  } else {
+    cudaDeviceSynchronize();  // its lhs (and stream) is gone already
+  }
   delete m;
   return GSLS_OK;
 }

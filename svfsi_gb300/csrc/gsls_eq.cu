@@ -310,6 +310,18 @@ __global__ void k_cep_ionic(int nNo, int tDof, int s, double *__restrict__ Yo,
   }
 }
 
+// Substeps and stimulus window of the reaction step that starts at t1
+// (CEPINTEG, Code/Source/svFSI/CEPION.f:166-314: nt = NINT(dt/cep%dt), the
+// stimulus repeats every CL from Ts for Td)
+static void cep_window(const gsls_eq *eq, double t1, int *nt, double *Ts, double *Te) {
+  const gsls_cep_params &c = eq->cep;
+  *nt = (int)llround(eq->p.dt / c.dt_ode);
+  long long icl = (long long)floor(t1 / c.CL);
+  if (icl < 0) icl = 0;
+  *Ts = c.Ts + (double)icl * c.CL;
+  *Te = *Ts + c.Td;
+}
+
 // Xion(1) = Yn(v) after the Newton loop (PICC for CEP, PIC.f:232-238)
 __global__ void k_cep_sync(int nNo, int tDof, int s, const double *__restrict__ Yn,
                            double *__restrict__ Xion) {
@@ -337,6 +349,7 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
   gsls_eq *eq = new gsls_eq();
   eq->mesh = mesh;
   eq->lhs = mesh_lhs(mesh);
+  lhs_attach(eq->lhs, &eq->lhs);
   eq->p = *p;
   eq->p.eparam = nullptr;
   eq->sv = *sv;
@@ -383,11 +396,16 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
 int gsls_eq_free(gsls_eq *eq) {
   if (!eq) return GSLS_ERR_ARG;
   gsls_lhs *lhs = eq->lhs;
-  cudaStreamSynchronize(lhs->stream);
-  // release the LS faces this equation's Dirichlet sets claimed (faces 1 ..
-  // nextFace), so that a later equation on the same lhs can claim them
-  for (int k = 0; k < eq->nextFace && k < lhs->nFaces; k++) lhs->faces[k].foC = false;
-  lhs->ws.mask_dof = -1;  // the cached Dirichlet mask was built from them
+  if (lhs) {
+    cudaStreamSynchronize(lhs->stream);
+    // release the LS faces this equation's Dirichlet sets claimed (faces 1
+    // .. nextFace), so that a later equation on the same lhs can claim them
+    for (int k = 0; k < eq->nextFace && k < lhs->nFaces; k++) lhs->faces[k].foC = false;
+    lhs->ws.mask_dof = -1;  // the cached Dirichlet mask was built from them
+    lhs_detach(lhs, &eq->lhs);
+  } else {
+    cudaDeviceSynchronize();  // its lhs (and stream) is gone already
+  }
   delete eq;
   return GSLS_OK;
 }
@@ -804,10 +822,9 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     }
     const gsls_cep_params &c = eq->cep;
     const double t1 = eq->time - p.dt;
-    const int nt = (int)llround(p.dt / c.dt_ode);
-    long long icl = (long long)floor(t1 / c.CL);
-    if (icl < 0) icl = 0;
-    const double Ts = c.Ts + (double)icl * c.CL, Te = Ts + c.Td;
+    int nt;
+    double Ts, Te;
+    cep_window(eq, t1, &nt, &Ts, &Te);
     // FP64 in both precisions: the reaction step sets the state that the
     // Newton loop starts from, so its rounding is not refined away (an FP32
     // step left the mixed state 1.2e-8 from the FP64 one); it is ~20 FP64
@@ -957,6 +974,14 @@ struct gsls_tape {
     double iN = 0.0, pN = 0.0, time = 0.0;
   };
   std::vector<Ck *> ck;
+  // CEP (monodomain): cell state at each checkpoint, the first-pass flag of
+  // CEPINTEG, and the smoothed activation-time objective's pieces
+  bool cep = false;
+  double vth = 0.0, vw = 1.0;
+  std::vector<gsls::DevBuf *> ckX;  // Xion (2 x nNo) per checkpoint
+  std::vector<int> ckFirst;
+  gsls::DevBuf segX;    // Xion of one recomputed segment ((every+1) x 2 x nNo)
+  gsls::DevBuf Tact, Tbar, x2bar, yp, xp;
   gsls::DevBuf seg;     // states of one recomputed segment ((every+1) x 3 x ns)
   gsls::DevBuf last;    // final state, restored after the backward pass
   gsls::DevBuf M, Mz;   // mass CSR values; zeros / scratch (nNo)
@@ -965,6 +990,7 @@ struct gsls_tape {
   gsls::DevBuf grad;    // per-element gradient (colour order)
   ~gsls_tape() {
     for (auto *c : ck) delete c;
+    for (auto *x : ckX) delete x;
   }
 };
 
@@ -1117,16 +1143,114 @@ static int adj_reverse_step(gsls_tape *t, const double *so, const double *sn) {
   // dJ/dp -= (dR/dp)^T lambda at (Yg, Dg)
   GSLS_TRY(mesh_dRdp(eq->mesh, &p, eq->st[7].as<double>(), eq->st[8].as<double>(), lam,
                      t->grad.as<double>(), -1.0));
-  AdjCoef c{p.dt, p.gam, p.beta, p.am, p.af, p.rho, p.dmp, eq->dFlag ? 1 : 0};
+  // CEP3D is HEATS3D with unit density (the assembly sets it so)
+  const double rho = (p.phys == GSLS_PHYS_CEP) ? 1.0 : p.rho;
+  AdjCoef c{p.dt, p.gam, p.beta, p.am, p.af, rho, p.dmp, eq->dFlag ? 1 : 0};
   k_adj_update<<<nblk(nr), kT, 0, st>>>(nr, c, g, Kl, lhs->ws.mask.as<double>(), Ab, Yb, Db);
   GSLS_CHECK_LAUNCH();
   return GSLS_OK;
 }
 
-static int adj_check(gsls_eq *eq) {
+// ---------------------------------------------------------------------------
+// Activation-time adjoint of the monodomain model (CEP).  The activation
+// time of node a is the first time its potential crosses a threshold: a
+// step function of the state, with no useful derivative.  The objective is
+// built on the smoothed activation time
+//   T_a = sum_{n=1..N} dt (1 - s(V_n(a))),   s(V) = 1 / (1 + exp(-(V - vth)/vw))
+// (the time spent below threshold; T_a -> the activation time as vw -> 0
+// for a node that depolarises once and stays up over the window), and the
+// caller's J(T) enters through dJ/dT.  Step n of the forward model is the
+// operator split of CEPINTEG: the cell step (forward Euler substeps of the
+// Aliev-Panfilov model, per node) takes (V, X2) to (V', X2'), then the
+// implicit diffusion step (CEP3D, linear in the state) runs from (A, V').
+// One reverse step: add dJ/dV_n = -dt Tbar s'(V_n); reverse the diffusion
+// step (the HEATS reverse step at the post-cell-step state; dR/dD_e for
+// the gradient); reverse the cell step per node with the transposed
+// Jacobians of its substeps, recomputed from the stored pre-step state.
+__device__ __forceinline__ double act_sig(double V, double vth, double vw) {
+  return 1.0 / (1.0 + exp(-(V - vth) / vw));
+}
+
+__global__ void k_act_accum(int nNo, int tDof, int s, const double *__restrict__ Y, double dt,
+                            double vth, double vw, double *__restrict__ T) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x)
+    T[a] += dt * (1.0 - act_sig(Y[(size_t)a * tDof + s], vth, vw));
+}
+
+// Ybar(a) += -dt Tbar(a) s'(V(a)), s' = s (1 - s) / vw
+__global__ void k_act_src(int nNo, int tDof, int s, const double *__restrict__ Y,
+                          const double *__restrict__ Tbar, double dt, double vth, double vw,
+                          double *__restrict__ Ybar) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x) {
+    const double g = act_sig(Y[(size_t)a * tDof + s], vth, vw);
+    Ybar[a] -= dt * Tbar[a] * g * (1.0 - g) / vw;
+  }
+}
+
+// Reverse of the forward-Euler cell step of k_cep_ionic at (V, X2) =
+// (Yin or Xin(1) on the first pass, Xin(2)): Ybar (cotangent of V' on
+// entry, of V on exit) and X2bar (of X2' on entry, of X2 on exit).  With
+// X0 = (V - Voffset)/Vscale, each substep X <- X + h f(X) has the Jacobian
+// I + h df/dX of AP_GETF's right-hand side
+//   f0 = X0 (c (X0 - alpha)(1 - X0) - X1) + fext,
+//   f1 = (a + mu1 X1/(mu2 + X0)) (-X1 - c X0 (X0 - b - 1)).
+constexpr int kCepMaxSub = 32;
+__global__ void k_cep_ionic_rev(int nNo, int tDof, int s, const double *__restrict__ Yin,
+                                const double *__restrict__ Xin, const int *__restrict__ stim,
+                                int first, int nt, double dt_ode, double t1, double Ts, double Te,
+                                double A, double *__restrict__ Ybar, double *__restrict__ X2bar) {
+  const double Vscale = 100.0, Tscale = 12.9, Voffset = -80.0;
+  const double c = 8.0, alpha = 1e-2, aa = 2e-3, b = 0.15, mu1 = 0.2, mu2 = 0.3;
+  const double eps = 2.220446049250313e-16;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x) {
+    const double V = first ? Xin[2 * (size_t)a] : Yin[(size_t)a * tDof + s];
+    const bool st = stim && stim[a];
+    const double h = dt_ode / Tscale;
+    double X0s[kCepMaxSub], X1s[kCepMaxSub];
+    double x0 = V, x1 = Xin[2 * (size_t)a + 1];
+    for (int i = 0; i < nt; i++) {
+      const double t = t1 + (double)i * dt_ode;
+      const double Istim = (st && t >= Ts - eps && t <= Te + eps) ? A : 0.0;
+      const double fext = Istim * Tscale / Vscale;
+      double X0 = (x0 - Voffset) / Vscale, X1 = x1, f0, f1;
+      X0s[i] = X0;
+      X1s[i] = X1;
+      ap_f<double>(X0, X1, fext, f0, f1);
+      x0 = (X0 + h * f0) * Vscale + Voffset;
+      x1 = X1 + h * f1;
+    }
+    double B0 = Ybar[a] * Vscale, B1 = X2bar[a];
+    for (int i = nt - 1; i >= 0; i--) {
+      const double X0 = X0s[i], X1 = X1s[i];
+      const double d00 = c * (X0 - alpha) * (1.0 - X0) - X1 + c * X0 * (1.0 + alpha - 2.0 * X0);
+      const double d01 = -X0;
+      const double gg = aa + mu1 * X1 / (mu2 + X0);
+      const double q = -X1 - c * X0 * (X0 - b - 1.0);
+      const double dg0 = -mu1 * X1 / ((mu2 + X0) * (mu2 + X0)), dg1 = mu1 / (mu2 + X0);
+      const double dq0 = -c * (2.0 * X0 - b - 1.0), dq1 = -1.0;
+      const double d10 = dg0 * q + gg * dq0, d11 = dg1 * q + gg * dq1;
+      const double n0 = B0 * (1.0 + h * d00) + B1 * h * d10;
+      const double n1 = B0 * h * d01 + B1 * (1.0 + h * d11);
+      B0 = n0;
+      B1 = n1;
+    }
+    // on the first pass V came from Xion(1), not from the state
+    Ybar[a] = first ? 0.0 : B0 / Vscale;
+    X2bar[a] = B1;
+  }
+}
+
+static int adj_check(gsls_eq *eq, bool cep = false) {
   const gsls_eq_params &p = eq->p;
-  if (p.phys != GSLS_PHYS_STRUCT && p.phys != GSLS_PHYS_HEATS) {
-    set_error("adjoint: built for STRUCT and HEATS equations");
+  if (cep ? (p.phys != GSLS_PHYS_CEP)
+          : (p.phys != GSLS_PHYS_STRUCT && p.phys != GSLS_PHYS_HEATS)) {
+    set_error(cep ? "adjoint: the activation-time adjoint is built for CEP equations"
+                  : "adjoint: built for STRUCT and HEATS equations (CEP: "
+                    "gsls_cep_adjoint_forward/backward)");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  if (cep && (!eq->has_cep || eq->cep.ode != 0)) {
+    set_error("adjoint: CEP needs gsls_eq_set_cep with the forward-Euler cell step");
     return GSLS_ERR_UNSUPPORTED;
   }
   if (p.s != 0 || p.tDof != p.dof) {
@@ -1230,7 +1354,8 @@ int gsls_adjoint_backward(gsls_tape *t, const double *Abar, const double *Ybar,
 
 int gsls_tape_free(gsls_tape *t) {
   if (!t) return GSLS_ERR_ARG;
-  cudaStreamSynchronize(t->eq->lhs->stream);
+  // the equation may be gone already (callers free in any order)
+  cudaDeviceSynchronize();
   delete t;
   return GSLS_OK;
 }
@@ -1247,6 +1372,165 @@ int gsls_adjoint_solve(gsls_eq *eq, const gsls_adj_point *pt, const double *dRhs
   GSLS_TRY(tape_alloc(&t));
   GSLS_TRY(adj_solve_at(&t, pt->Ao, pt->Yo, pt->Do, pt->An, pt->Yn, pt->Dn, dRhs, dLambda));
   GSLS_CUDA(cudaStreamSynchronize(eq->lhs->stream));
+  return GSLS_OK;
+}
+
+int gsls_cep_adjoint_forward(gsls_eq *eq, int nsteps, int every, double vth, double vw,
+                             double *T, gsls_tape **out) {
+  if (!eq || !out || !T || nsteps < 1 || every < 1 || !(vw > 0.0)) return GSLS_ERR_ARG;
+  GSLS_TRY(adj_check(eq, true));
+  int nt;
+  double Ts, Te;
+  cep_window(eq, eq->time, &nt, &Ts, &Te);
+  if (nt < 1 || nt > kCepMaxSub) {
+    set_error("adjoint: CEP cell step needs 1..32 substeps per time step");
+    return GSLS_ERR_UNSUPPORTED;
+  }
+  cudaStream_t st = eq->lhs->stream;
+  const int nNo = eq->nNo;
+  const size_t ns = (size_t)nNo * eq->p.tDof, nx = 2 * (size_t)nNo;
+  gsls_tape *t = new gsls_tape();
+  t->eq = eq;
+  t->nsteps = nsteps;
+  t->every = every;
+  t->nseg = (nsteps + every - 1) / every;
+  t->cep = true;
+  t->vth = vth;
+  t->vw = vw;
+  int rc = tape_alloc(t);
+  if (rc == GSLS_OK &&
+      ((rc = t->segX.alloc(sizeof(double) * nx * (size_t)(every + 1))) != GSLS_OK ||
+       (rc = t->Tact.alloc(sizeof(double) * (size_t)nNo)) != GSLS_OK ||
+       (rc = t->Tbar.alloc(sizeof(double) * (size_t)nNo)) != GSLS_OK ||
+       (rc = t->x2bar.alloc(sizeof(double) * (size_t)nNo)) != GSLS_OK ||
+       (rc = t->yp.alloc(sizeof(double) * 3 * ns)) != GSLS_OK ||
+       (rc = t->xp.alloc(sizeof(double) * nx * 2)) != GSLS_OK))
+    rc = GSLS_ERR_NOMEM;
+  if (rc == GSLS_OK && cudaMemsetAsync(t->Tact.p, 0, sizeof(double) * nNo, st) != cudaSuccess)
+    rc = GSLS_ERR_CUDA;
+  for (int n = 0; rc == GSLS_OK && n < nsteps; n++) {
+    if (n % every == 0) {
+      auto *c = new gsls_tape::Ck();
+      t->ck.push_back(c);
+      auto *x = new DevBuf();
+      t->ckX.push_back(x);
+      t->ckFirst.push_back(eq->cep_first ? 1 : 0);
+      if ((rc = c->st.alloc(sizeof(double) * 3 * ns)) != GSLS_OK ||
+          (rc = x->alloc(sizeof(double) * nx)) != GSLS_OK)
+        break;
+      if ((rc = save_state(eq, c->st.as<double>())) != GSLS_OK) break;
+      if (cudaMemcpyAsync(x->p, eq->Xion.p, sizeof(double) * nx, cudaMemcpyDeviceToDevice, st) !=
+          cudaSuccess) {
+        rc = GSLS_ERR_CUDA;
+        break;
+      }
+      c->iN = eq->eq_iNorm;
+      c->pN = eq->eq_pNorm;
+      c->time = eq->time;
+    }
+    gsls_step_info info;
+    if ((rc = gsls_eq_step(eq, &info)) != GSLS_OK) break;
+    k_act_accum<<<nblk(nNo), kT, 0, st>>>(nNo, eq->p.tDof, eq->p.s, eq->st[1].as<double>(),
+                                          eq->p.dt, vth, vw, t->Tact.as<double>());
+    if (cudaGetLastError() != cudaSuccess) rc = GSLS_ERR_CUDA;
+  }
+  if (rc == GSLS_OK) rc = save_state(eq, t->last.as<double>());
+  if (rc == GSLS_OK &&
+      (cudaMemcpyAsync(t->xp.as<double>() + nx, eq->Xion.p, sizeof(double) * nx,
+                       cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+       cudaMemcpyAsync(T, t->Tact.p, sizeof(double) * nNo, cudaMemcpyDeviceToHost, st) !=
+           cudaSuccess ||
+       cudaStreamSynchronize(st) != cudaSuccess))
+    rc = GSLS_ERR_CUDA;
+  if (rc != GSLS_OK) {
+    if (rc == GSLS_ERR_CUDA) set_error("adjoint: CEP forward failed");
+    delete t;
+    return rc;
+  }
+  *out = t;
+  return GSLS_OK;
+}
+
+int gsls_cep_adjoint_backward(gsls_tape *t, const double *Tbar, double *grad) {
+  if (!t || !Tbar || !grad || !t->cep) return GSLS_ERR_ARG;
+  gsls_eq *eq = t->eq;
+  gsls_lhs *lhs = eq->lhs;
+  cudaStream_t st = lhs->stream;
+  const gsls_eq_params &p = eq->p;
+  const int nNo = eq->nNo, tD = p.tDof;
+  const size_t ns = (size_t)nNo * tD, nr = (size_t)nNo * p.dof, nx = 2 * (size_t)nNo;
+  int nEl = 0;
+  const int *perm = mesh_perm(eq->mesh, &nEl);
+  double *cot = t->cot.as<double>();
+  double *Yb = cot + nr;
+  GSLS_CUDA(cudaMemsetAsync(cot, 0, sizeof(double) * 3 * nr, st));
+  GSLS_CUDA(cudaMemsetAsync(t->x2bar.p, 0, sizeof(double) * (size_t)nNo, st));
+  GSLS_CUDA(cudaMemsetAsync(t->grad.p, 0, sizeof(double) * (size_t)nEl, st));
+  GSLS_CUDA(cudaMemcpyAsync(t->Tbar.p, Tbar, sizeof(double) * (size_t)nNo, cudaMemcpyHostToDevice,
+                            st));
+  const double iN_end = eq->eq_iNorm, pN_end = eq->eq_pNorm, time_end = eq->time;
+  const bool first_end = eq->cep_first;
+  const gsls_cep_params &c = eq->cep;
+  double *seg = t->seg.as<double>(), *segX = t->segX.as<double>();
+  double *so = t->yp.as<double>(), *xs = t->xp.as<double>();
+  for (int sgi = t->nseg - 1; sgi >= 0; sgi--) {
+    const int n0 = sgi * t->every, n1 = std::min(n0 + t->every, t->nsteps);
+    gsls_tape::Ck *ck = t->ck[sgi];
+    GSLS_TRY(load_state(eq, ck->st.as<double>()));
+    GSLS_CUDA(cudaMemcpyAsync(eq->Xion.p, t->ckX[sgi]->p, sizeof(double) * nx,
+                              cudaMemcpyDeviceToDevice, st));
+    eq->eq_iNorm = ck->iN;
+    eq->eq_pNorm = ck->pN;
+    eq->time = ck->time;
+    eq->cep_first = t->ckFirst[sgi] != 0;
+    GSLS_TRY(save_state(eq, seg));
+    GSLS_CUDA(cudaMemcpyAsync(segX, eq->Xion.p, sizeof(double) * nx, cudaMemcpyDeviceToDevice, st));
+    for (int k = 1; k <= n1 - n0; k++) {
+      gsls_step_info info;
+      GSLS_TRY(gsls_eq_step(eq, &info));
+      GSLS_TRY(save_state(eq, seg + (size_t)k * 3 * ns));
+      GSLS_CUDA(cudaMemcpyAsync(segX + (size_t)k * nx, eq->Xion.p, sizeof(double) * nx,
+                                cudaMemcpyDeviceToDevice, st));
+    }
+    for (int k = n1 - n0; k >= 1; k--) {
+      const double *sp = seg + (size_t)(k - 1) * 3 * ns, *sn = seg + (size_t)k * 3 * ns;
+      const int first = (k == 1) ? t->ckFirst[sgi] : 0;
+      const double t1 = ck->time + (double)(k - 1) * p.dt;
+      int nt;
+      double Ts, Te;
+      cep_window(eq, t1, &nt, &Ts, &Te);
+      // objective term of the state after step k
+      k_act_src<<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, sn + ns, t->Tbar.as<double>(), p.dt,
+                                          t->vth, t->vw, Yb);
+      GSLS_CHECK_LAUNCH();
+      // post-cell-step state of step k: (A_{k-1}, V', D_{k-1})
+      GSLS_CUDA(cudaMemcpyAsync(so, sp, sizeof(double) * 3 * ns, cudaMemcpyDeviceToDevice, st));
+      GSLS_CUDA(cudaMemcpyAsync(xs, segX + (size_t)(k - 1) * nx, sizeof(double) * nx,
+                                cudaMemcpyDeviceToDevice, st));
+      k_cep_ionic<double><<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, so + ns, xs, eq->stim.as<int>(),
+                                                    first, c.ode, nt, c.dt_ode, t1, Ts, Te, c.A);
+      GSLS_CHECK_LAUNCH();
+      // the diffusion step, then the cell step, in reverse
+      GSLS_TRY(adj_reverse_step(t, so, sn));
+      k_cep_ionic_rev<<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, sp + ns, segX + (size_t)(k - 1) * nx,
+                                                eq->stim.as<int>(), first, nt, c.dt_ode, t1, Ts,
+                                                Te, c.A, Yb, t->x2bar.as<double>());
+      GSLS_CHECK_LAUNCH();
+    }
+  }
+  // leave the equation at its final state
+  GSLS_TRY(load_state(eq, t->last.as<double>()));
+  GSLS_CUDA(cudaMemcpyAsync(eq->Xion.p, t->xp.as<double>() + nx, sizeof(double) * nx,
+                            cudaMemcpyDeviceToDevice, st));
+  eq->eq_iNorm = iN_end;
+  eq->eq_pNorm = pN_end;
+  eq->time = time_end;
+  eq->cep_first = first_end;
+  std::vector<double> g((size_t)nEl);
+  GSLS_CUDA(cudaMemcpyAsync(g.data(), t->grad.p, sizeof(double) * (size_t)nEl,
+                            cudaMemcpyDeviceToHost, st));
+  GSLS_CUDA(cudaStreamSynchronize(st));
+  for (int k = 0; k < nEl; k++) grad[perm[k]] = g[k];
   return GSLS_OK;
 }
 

@@ -176,7 +176,25 @@ struct gsls_lhs {
   int grid = 0;          // fixed reduction grid (deterministic sums)
   gsls::Workspace ws;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // the `lhs` fields of the meshes and equations bound to this lhs:
+  // gsls_lhs_free sets them to null, so that freeing those objects later
+  // (in any order) touches no freed lhs
+  std::vector<gsls_lhs **> deps;
 };
+
+namespace gsls {
+inline void lhs_attach(gsls_lhs *lhs, gsls_lhs **ref) {
+  if (lhs) lhs->deps.push_back(ref);
+}
+inline void lhs_detach(gsls_lhs *lhs, gsls_lhs **ref) {
+  if (!lhs) return;
+  for (size_t k = 0; k < lhs->deps.size(); k++)
+    if (lhs->deps[k] == ref) {
+      lhs->deps.erase(lhs->deps.begin() + (long)k);
+      return;
+    }
+}
+}  // namespace gsls
 
 namespace gsls {
 

@@ -545,6 +545,7 @@ int gsls_lhs_create(gsls_lhs **out, int gnNo, int nNo, int nnz, const int *gNode
 int gsls_lhs_free(gsls_lhs *lhs) {
   if (!lhs) return GSLS_ERR_ARG;
   if (lhs->stream) cudaStreamSynchronize(lhs->stream);
+  for (gsls_lhs **ref : lhs->deps) *ref = nullptr;
   if (lhs->ws.h_scal) cudaFreeHost(lhs->ws.h_scal);
   if (lhs->ws.cg_graph) cudaGraphExecDestroy(lhs->ws.cg_graph);
   if (lhs->ws.cg_graph_s) cudaGraphExecDestroy(lhs->ws.cg_graph_s);

@@ -241,6 +241,16 @@ class Equation:
               "gsls_adjoint_forward")
         return Tape(h, self)
 
+    def cep_adjoint_forward(self, nsteps, every=5, vth=-30.0, vw=5.0):
+        """CEP: take nsteps steps with checkpoints; returns (T, CepTape) with
+        T the smoothed activation time per node (gsls_cep_adjoint_forward)."""
+        h = C.c_void_p()
+        T = np.zeros(self.nNo)
+        check(_lib.load().gsls_cep_adjoint_forward(self.h, int(nsteps), int(every), float(vth),
+                                                   float(vw), _dp(T), C.byref(h)),
+              "gsls_cep_adjoint_forward")
+        return T, CepTape(h, self)
+
     def set_eparam(self, ep):
         e = None if ep is None else _f64(ep)
         check(_lib.load().gsls_eq_set_eparam(self.h, _dp(e) if e is not None else None),
@@ -286,3 +296,15 @@ class Tape:
             self.free()
         except Exception:
             pass
+
+
+class CepTape(Tape):
+    """Checkpoints of a CEP activation-time forward run."""
+
+    def backward(self, Tbar):
+        """dJ/dDiso (nEl) from dJ/dT (nNo)."""
+        g = np.zeros(self.eq.mesh.nEl)
+        tb = _f64(Tbar)
+        check(_lib.load().gsls_cep_adjoint_backward(self.h, _dp(tb), _dp(g)),
+              "gsls_cep_adjoint_backward")
+        return g

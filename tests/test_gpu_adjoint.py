@@ -160,3 +160,95 @@ def test_adjoint_solve_and_dRdp_building_blocks(gsls):
     gh = g.cpu().numpy()
     assert np.allclose(Kl[free], gh[free], rtol=1e-8, atol=1e-8 * np.abs(gh).max())
     assert np.abs(lh[~free]).max() == 0.0
+
+
+# ---------------------------------------------------------------------------
+# CEP: gradient of an activation-time mismatch with respect to the
+# per-element diffusivity.  A planar front (stimulus +52 on x <= 1.5: under
+# the Aliev-Panfilov sign convention -52 would hyperpolarise and nothing
+# would activate) crosses a 24x24x2-hex slab, D_e = exp(0.2 N(0,1)),
+# dt = dt_ode = 0.1 ms, 120 steps.  T_a = sum_n dt (1 - s(V_n(a))) with
+# s(V) = 1/(1 + exp(-(V + 30)/5)), J = 1/2 |T - T*|^2, T* from a run with
+# D_e perturbed by exp(0.05 N(0,1)).
+
+CEP_VTH, CEP_VW = -30.0, 5.0
+
+
+def _cep(nsteps=120):
+    p = problems.cep_slab(24, 24, 2, nsteps=nsteps, A=52.0, Diso=1.0)
+    p.stim = (p.x[:, 0] <= 1.5).astype(np.int32)
+    p.params["dt"] = 0.1
+    p.cep["dt_ode"] = 0.1
+    p.tol, p.maxItr, p.ls_relTol = 1e-13, 8, 1e-11
+    rng = np.random.default_rng(9)
+    ep = np.exp(0.2 * rng.standard_normal(p.nEl))
+    return p, ep
+
+
+def _act(Y):
+    return 1.0 - 1.0 / (1.0 + np.exp(-(Y - CEP_VTH) / CEP_VW))
+
+
+def _cep_T_gpu(p, ep):
+    lhs, mesh, eq = problems.build_equation(p)
+    eq.set_eparam(ep)
+    T = np.zeros(p.nNo)
+    for _ in range(p.nsteps):
+        eq.step()
+        T += p.params["dt"] * _act(eq.get_state()[1][:, 0])
+    eq.free()
+    mesh.free()
+    lhs.free()
+    return T
+
+
+def _cep_T_oracle(orc, p, ep):
+    eq = orc.OracleEquation(p, eparam=ep)
+    eq.set_state(*p.initial_state())
+    T = np.zeros(p.nNo)
+    for _ in range(p.nsteps):
+        eq.step()
+        T += p.params["dt"] * _act(eq.state()[1][:, 0])
+    return T
+
+
+def test_cep_activation_adjoint_matches_fd(gsls, orc):
+    p, ep = _cep()
+    rng = np.random.default_rng(31)
+    Tstar = _cep_T_gpu(p, ep * np.exp(0.05 * rng.standard_normal(p.nEl)))
+    lhs, mesh, eq = problems.build_equation(p)
+    eq.set_eparam(ep)
+    T, tape = eq.cep_adjoint_forward(p.nsteps, every=25, vth=CEP_VTH, vw=CEP_VW)
+    # the front crossed part of the slab: activation times spread over the run
+    assert T.min() < 2.0 and np.percentile(T, 50) < 0.9 * p.nsteps * p.params["dt"]
+    assert np.allclose(T, _cep_T_gpu(p, ep), rtol=0, atol=1e-12 * T.max())
+    YN = eq.get_state()[1].copy()
+    grad = tape.backward(T - Tstar)
+    tape.free()
+    assert np.array_equal(eq.get_state()[1], YN)       # left at step N
+
+    def J(Tx):
+        d = Tx - Tstar
+        return 0.5 * float(d @ d)
+
+    errs = []
+    for k in range(2):
+        r = rng.standard_normal(p.nEl)
+        r /= np.linalg.norm(r)
+        dp = ep * r
+        fd = (J(_cep_T_gpu(p, ep + FD_H * dp)) - J(_cep_T_gpu(p, ep - FD_H * dp))) / (2 * FD_H)
+        ad = float(grad @ dp)
+        errs.append(abs(fd - ad) / abs(ad))
+        if k == 0:
+            # and against finite differences of the oracle's own steps
+            fdo = (J(_cep_T_oracle(orc, p, ep + FD_H * dp)) -
+                   J(_cep_T_oracle(orc, p, ep - FD_H * dp))) / (2 * FD_H)
+            assert abs(fdo - ad) <= 1e-5 * abs(ad), (fdo, ad)
+    assert max(errs) <= 1e-5, errs
+
+
+def test_cep_adjoint_rejects_other_physics(gsls):
+    p = problems.heats_cube(3, nsteps=1)
+    lhs, mesh, eq = problems.build_equation(p)
+    with pytest.raises(Exception, match="CEP"):
+        eq.cep_adjoint_forward(1)
