@@ -67,6 +67,8 @@ def parse():
                     help="cylinder mesh spacing (profiling captures use a coarser mesh)")
     ap.add_argument("--cep-amplitude", type=float, default=-52.0,
                     help="cep workload: stimulus amplitude (the configuration's is -52)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations' legs of the default run")
     ap.add_argument("--parity-steps", type=int, default=None,
                     help="implicit steps run by the oracle beside the GPU for the "
                          "cpu_baseline and the error against the oracle (default per workload)")
@@ -534,11 +536,73 @@ def run_gsls(args):
                                "cores": threads, "kind": "port",
                                "sample": oracle_sample_desc(p, n, threads, co, 1),
                                "step_s": secs}
+    if (rank == 0 and world == 1 and not args.no_cpu and not args.no_configs and not args.small
+            and args.workload == "struct"):
+        out["configs"] = config_legs(L, problems, fsils, torch)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def config_legs(L, problems, fsils, torch):
+    """The other benchmark configurations, run briefly beside the headline
+    one: the heat cube (20^3 hexes, 48,000 tets), the monodomain slab
+    (135x135x27 hexes, 2,952,450 tets, stimulus -52) and the VMS cylinder
+    (h 0.027, 1,225,440 tets).  For each, the oracle's first n_par implicit
+    steps from the initial state beside the FP64 and mixed GPU steps (error
+    of each against the oracle, Newton counts), then n_time more GPU steps
+    per precision timed with CUDA events on the library's stream."""
+    threads = os.cpu_count() or 1
+    legs = [("heats_cube_20", lambda: problems.heats_cube(20, nsteps=20), 10, 10),
+            ("cep_slab_135x135x27", lambda: problems.cep_slab(nsteps=100, A=-52.0), 20, 50),
+            ("fluid_cylinder_h0.027", lambda: problems.fluid_cylinder(h=0.027, nsteps=4), 1, 3)]
+    res = {}
+    for name, make, n_par, n_time in legs:
+        p = make()
+        so, secs, co = oracle_steps(p, n_par, threads)
+        ref = compared_field(p, so)
+        nref = float(np.linalg.norm(ref))
+        leg = {"workload": workload_desc(p) if (is_fluid(p) or is_cep(p)) else
+               (f"{p.name}: HEATS3D, conductivity 1, rho 1, T = 1 at x = 0 and 0 at x = 1, "
+                f"{p.nEl:,} tet4, {p.nNo:,} nodes, nnz {p.nnz:,}, CG+diag relTol 1e-10, dt 0.01"),
+               "oracle": {"s_per_step": float(sum(secs) / len(secs)), "cores": threads,
+                          "steps": n_par, "newton": [c[0] for c in co],
+                          "ls_itr": [c[1] for c in co], "kind": "port"}}
+        fields = {}
+        for prec, key in ((fsils.PREC_FP64, "fp64"), (fsils.PREC_MIXED, "mixed")):
+            lhs, mesh, eq = problems.build_equation(p, precision=prec)
+            stream = torch.cuda.ExternalStream(L.gsls_get_stream(lhs.h))
+            newton = [int(eq.step().newton_itr) for _ in range(n_par)]
+            st = eq.get_state()
+            leg[f"rel_l2_{key}_vs_oracle"] = float(np.linalg.norm(compared_field(p, st) - ref)) / nref
+            leg[f"newton_{key}"] = newton
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            infos = [eq.step() for _ in range(n_time)]
+            ev1.record(stream)
+            ev1.synchronize()
+            leg[f"{key}_s_per_step"] = ev0.elapsed_time(ev1) / 1e3 / n_time
+            leg[f"{key}_newton_per_step"] = float(np.mean([i.newton_itr for i in infos]))
+            leg[f"{key}_ls_itr_per_step"] = float(np.mean([i.ls_itr_total for i in infos]))
+            leg[f"{key}_assembly_ms_per_newton"] = float(
+                np.mean([i.t_assembly_ms for i in infos]) / max(leg[f"{key}_newton_per_step"], 1))
+            fields[key] = compared_field(p, eq.get_state())
+            eq.free()
+            mesh.free()
+            lhs.free()
+        leg["speedup_mixed_vs_fp64"] = leg["fp64_s_per_step"] / leg["mixed_s_per_step"]
+        leg["rel_l2_mixed_vs_fp64"] = float(np.linalg.norm(fields["mixed"] - fields["fp64"]) /
+                                            max(np.linalg.norm(fields["fp64"]), 1e-300))
+        leg["newton_counts_equal"] = (leg["newton_fp64"] == leg["newton_mixed"] ==
+                                      leg["oracle"]["newton"])
+        leg["timed"] = (f"steps {n_par + 1}..{n_par + n_time} of the workload per precision "
+                        f"(CUDA events); the error columns compare steps 1..{n_par} with the "
+                        f"oracle's (field: {compared_name(p)})")
+        res[name] = leg
+    return res
 
 
 # ---------------------------------------------------------------------------

@@ -249,14 +249,16 @@ __global__ void __launch_bounds__(kAsmThreads) k_lin_build(AsmArgs A, double *Mg
   }
 }
 
-// 16 lanes per CSR row (tet4 rows hold ~15 entries), entries strided by
-// 16, the row sums by a fixed shuffle tree: deterministic.  GB300 runs FP64
-// at ~1/74 of the FP32 rate, so a pass over the operators is FP64-bound
+// 4 lanes per CSR row (tet4 rows hold ~15 entries), entries strided by 4,
+// the row sums by a fixed two-step shuffle tree: deterministic.  GB300 runs
+// FP64 at ~1/74 of the FP32 rate, so a pass over the operators is FP64-bound
 // before it is HBM-bound: the residual takes two FP64 FMAs per entry
-// (rM = sum m Ag, rK = sum k Yg; R = rho rM + nu rK - rs b) and the FP32
-// tangent is formed from FP32 copies of the operators (Val = cM m + cK k in
-// VT; the FP64 tangent from the FP64 operators).
-constexpr int kLinLanes = 16;
+// (rM = sum m Ag, rK = sum k Yg; R = rho rM + nu rK - rs b), the lane sums
+// 2 x 2 FP64 adds per lane (16 lanes per row spent 8x that in the tree and
+// ran 4x slower), and the FP32 tangent is formed from FP32 copies of the
+// operators (Val = cM m + cK k in VT; the FP64 tangent from the FP64
+// operators).
+constexpr int kLinLanes = 4;
 template <class VT>
 __global__ void __launch_bounds__(256) k_asm_lin(int nNo, const int *__restrict__ rowPtr,
                                                  const int *__restrict__ colPtr,

@@ -1485,9 +1485,13 @@ int gsls_cep_adjoint_backward(gsls_tape *t, const double *Tbar, double *grad) {
     eq->cep_first = t->ckFirst[sgi] != 0;
     GSLS_TRY(save_state(eq, seg));
     GSLS_CUDA(cudaMemcpyAsync(segX, eq->Xion.p, sizeof(double) * nx, cudaMemcpyDeviceToDevice, st));
+    // start time of each step's cell step, as the step computes it (the
+    // stimulus window test is exact: recompute nothing differently)
+    std::vector<double> t1s((size_t)(n1 - n0) + 1, 0.0);
     for (int k = 1; k <= n1 - n0; k++) {
       gsls_step_info info;
       GSLS_TRY(gsls_eq_step(eq, &info));
+      t1s[(size_t)k] = eq->time - p.dt;
       GSLS_TRY(save_state(eq, seg + (size_t)k * 3 * ns));
       GSLS_CUDA(cudaMemcpyAsync(segX + (size_t)k * nx, eq->Xion.p, sizeof(double) * nx,
                                 cudaMemcpyDeviceToDevice, st));
@@ -1495,7 +1499,7 @@ int gsls_cep_adjoint_backward(gsls_tape *t, const double *Tbar, double *grad) {
     for (int k = n1 - n0; k >= 1; k--) {
       const double *sp = seg + (size_t)(k - 1) * 3 * ns, *sn = seg + (size_t)k * 3 * ns;
       const int first = (k == 1) ? t->ckFirst[sgi] : 0;
-      const double t1 = ck->time + (double)(k - 1) * p.dt;
+      const double t1 = t1s[(size_t)k];
       int nt;
       double Ts, Te;
       cep_window(eq, t1, &nt, &Ts, &Te);

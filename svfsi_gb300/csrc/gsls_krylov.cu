@@ -519,6 +519,22 @@ __global__ void k_scale_out(int nNo, double *__restrict__ Rout, const XT *__rest
 
 // ---------------------------------------------------------------------------
 // Diagonal preconditioner (PRECONDDIAG, Code/Source/svFSILS/PRECOND.f:50-145)
+
+// 1/sqrt(a) for a > 0 in FP64 by Newton-Raphson on f(y) = 1/y^2 - a
+// (y <- y (3 - a y^2) / 2, quadratic convergence) from the FP32 estimate:
+// two steps take the ~1e-7 start to the FP64 rounding level with 8 FP64
+// operations, where a division and a square root cost several times that on
+// GB300's FP64 pipe (~1/74 of the FP32 rate).  Outside the FP32 normal range
+// the plain FP64 expression is used.
+__device__ __forceinline__ double rsqrt_nr(double a) {
+  if (!(a > 1e-36 && a < 1e36)) return 1.0 / sqrt(a);
+  double y = (double)rsqrtf((float)a);
+  const double h = 0.5 * a;
+  y = y * fma(-h * y, y, 1.5);
+  y = y * fma(-h * y, y, 1.5);
+  return y;
+}
+
 template <int D, class VT>
 __global__ void k_diag_w(int nNo, const int *__restrict__ diagPtr, const VT *__restrict__ Val,
                          const double *__restrict__ mask, double *__restrict__ W,
@@ -530,7 +546,7 @@ __global__ void k_diag_w(int nNo, const int *__restrict__ diagPtr, const VT *__r
     for (int k = 0; k < D; k++) {
       double w = double(Val[(size_t)d * DD + k * D + k]);
       if (w == 0.0) w = 1.0;
-      w = 1.0 / sqrt(fabs(w));
+      w = rsqrt_nr(fabs(w));
       w = w * mask[(size_t)i * D + k];
       W[(size_t)i * D + k] = w;
       Wf[(size_t)i * D + k] = float(w);
@@ -564,6 +580,23 @@ __global__ void __launch_bounds__(kThreads) k_scale_val(int nNo, const int *__re
         v[c] = VT(t);
       }
     }
+  }
+}
+
+// The same for scalar rows (D = 1): 4 lanes per row, entries strided by 4
+// (a lane per row walked 32 rows at once with uncoalesced loads: 4x slower)
+template <class VT, class WT>
+__global__ void __launch_bounds__(kThreads) k_scale_val1(int nNo, const int *__restrict__ rowPtr,
+                                                         const int *__restrict__ colPtr,
+                                                         VT *__restrict__ Val,
+                                                         const WT *__restrict__ W) {
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t nt = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = g; t < (size_t)nNo * 4; t += nt) {
+    const int i = (int)(t >> 2), l = (int)(t & 3);
+    const WT wr = W[i];
+    const int re = rowPtr[i + 1];
+    for (int j = rowPtr[i] + l; j < re; j += 4) Val[j] = VT((WT(Val[j]) * wr) * W[colPtr[j]]);
   }
 }
 
@@ -605,12 +638,21 @@ static int precond_diag_t(gsls_lhs *lhs, VT *Val, double *R, double *W) {
   k_diag_w<D, VT><<<blocks_for(nNo, num_sms() * 8), kThreads, 0, st>>>(
       nNo, lhs->d_diagPtr.as<int>(), Val, lhs->ws.mask.as<double>(), W, Wf, R);
   GSLS_CHECK_LAUNCH();
-  if (sizeof(VT) == 4)
+  if (D == 1) {
+    const int nb = blocks_for((size_t)nNo * 4, num_sms() * 8);
+    if (sizeof(VT) == 4)
+      k_scale_val1<VT, float><<<nb, kThreads, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
+                                                       lhs->d_colPtr.as<int>(), Val, Wf);
+    else
+      k_scale_val1<VT, double><<<nb, kThreads, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(),
+                                                        lhs->d_colPtr.as<int>(), Val, W);
+  } else if (sizeof(VT) == 4) {
     k_scale_val<D, VT, float><<<lhs->grid, kThreads, 0, st>>>(
         nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, Wf);
-  else
+  } else {
     k_scale_val<D, VT, double><<<lhs->grid, kThreads, 0, st>>>(
         nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, W);
+  }
   GSLS_CHECK_LAUNCH();
   return GSLS_OK;
 }

@@ -239,10 +239,12 @@ def test_cep_activation_adjoint_matches_fd(gsls, orc):
         fd = (J(_cep_T_gpu(p, ep + FD_H * dp)) - J(_cep_T_gpu(p, ep - FD_H * dp))) / (2 * FD_H)
         ad = float(grad @ dp)
         errs.append(abs(fd - ad) / abs(ad))
+        print(f"CEP adjoint direction {k}: fd {fd:.12e} adjoint {ad:.12e} rel {errs[-1]:.2e}")
         if k == 0:
             # and against finite differences of the oracle's own steps
             fdo = (J(_cep_T_oracle(orc, p, ep + FD_H * dp)) -
                    J(_cep_T_oracle(orc, p, ep - FD_H * dp))) / (2 * FD_H)
+            print(f"CEP adjoint oracle fd {fdo:.12e}")
             assert abs(fdo - ad) <= 1e-5 * abs(ad), (fdo, ad)
     assert max(errs) <= 1e-5, errs
 
