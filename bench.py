@@ -137,18 +137,23 @@ def compared_field(p, state):
         return state[1][:, p.s]
     if is_cep(p):
         return state[1] - p.cep["V0"]
-    return state[1] if is_fluid(p) else state[2]
+    return state[1] if (is_fluid(p) or is_heats(p)) else state[2]
 
 
 def is_cep(p):
     return bool(getattr(p, "cep", None))
 
 
+def is_heats(p):
+    from svfsi_gb300 import problems
+    return p.phys == problems.PHYS_HEATS
+
+
 def compared_name(p):
     if is_heatf(p):
         return "Y[:, temperature]"
     return ("Y (velocity, pressure)" if is_fluid(p) else "Y - V_rest (potential)" if is_cep(p)
-            else "D")
+            else "Y (temperature)" if is_heats(p) else "D")
 
 
 def l2_note(p):
@@ -538,7 +543,10 @@ def run_gsls(args):
                                "step_s": secs}
     if (rank == 0 and world == 1 and not args.no_cpu and not args.no_configs and not args.small
             and args.workload == "struct"):
-        out["configs"] = config_legs(L, problems, fsils, torch)
+        try:
+            out["configs"] = config_legs(L, problems, fsils, torch)
+        except Exception as e:  # the headline line is printed regardless
+            out["configs"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

@@ -546,7 +546,13 @@ __global__ void k_diag_w(int nNo, const int *__restrict__ diagPtr, const VT *__r
     for (int k = 0; k < D; k++) {
       double w = double(Val[(size_t)d * DD + k * D + k]);
       if (w == 0.0) w = 1.0;
-      w = rsqrt_nr(fabs(w));
+      // the FP64 drop-in keeps the reference's expression (rounding-
+      // sensitive Krylov counts follow it); the mixed path takes the
+      // Newton form
+      if constexpr (sizeof(VT) == 8)
+        w = 1.0 / sqrt(fabs(w));
+      else
+        w = rsqrt_nr(fabs(w));
       w = w * mask[(size_t)i * D + k];
       W[(size_t)i * D + k] = w;
       Wf[(size_t)i * D + k] = float(w);
