@@ -61,6 +61,8 @@ extern "C" {
 #define GSLS_PHYS_LELAS 5  /* linear elasticity, Code/Source/svFSI/LELAS.f */
 #define GSLS_PHYS_HEATF 6  /* heat in a fluid (advection-diffusion), HEATF.f;
                               velocity in state components 0..2 */
+#define GSLS_PHYS_USTRUCT 7 /* velocity-pressure nonlinear solid, USTRUCT.f
+                              (tet4, equal order, VMS; dof 4: v, p) */
 
 /* Mirrors FSILS_subLsType, Code/Source/svFSILS/FSILS_STRUCT.h:162-191
    (Fortran LOGICAL stored as int32). */
@@ -221,6 +223,10 @@ typedef struct {
   double bstab;     /* FLUID backflow stabilisation coefficient of the
                        Neumann faces (BFLUID, backflow_stab; the reference's
                        input default is 0.2, READFILES.f:1089-1091) */
+  int volType;      /* USTRUCT volumetric penalty of GVOLPEN
+                       (MATMODELS.f:1020-1070): 0 quadratic, 1 ST91, 2 M94;
+                       USTRUCT also reads rho, C10 (neo-Hookean), Kpen
+                       (0: incompressible), visc, fb, elM, nu, ctM, ctC */
 } gsls_eq_params;
 
 #define GSLS_VISC_CONST 0

@@ -42,7 +42,7 @@ class EqP(C.Structure):
                 ("ctC", C.c_double), ("eparam", c_double_p), ("elM", C.c_double),
                 ("nu", C.c_double), ("viscType", C.c_int), ("mu_o", C.c_double),
                 ("vlam", C.c_double), ("va", C.c_double), ("vn", C.c_double),
-                ("bstab", C.c_double)]
+                ("bstab", C.c_double), ("volType", C.c_int)]
 
 
 class DirBC(C.Structure):
@@ -78,7 +78,8 @@ class Eq(C.Structure):
                 ("eq_iNorm", C.c_double), ("eq_pNorm", C.c_double),
                 ("cep", CepP), ("stim", c_int_p), ("Xion", c_double_p), ("time", C.c_double),
                 ("cep_ipass_done", C.c_int), ("nNeu", C.c_int), ("neu", C.POINTER(NeuBC)),
-                ("ncolor", C.c_int), ("color_off", c_int_p), ("color_order", c_int_p)]
+                ("ncolor", C.c_int), ("color_off", c_int_p), ("color_order", c_int_p),
+                ("Ad", c_double_p)]
 
 
 class StepInfo(C.Structure):
@@ -123,6 +124,8 @@ def load():
                                       c_double_p, c_double_p, c_double_p, c_double_p]
         L.orc_elem_fluid.argtypes = [C.POINTER(EqP), c_double_p, c_double_p, c_double_p,
                                      c_double_p, c_double_p]
+        L.orc_elem_ustruct.argtypes = [C.POINTER(EqP), c_double_p, c_double_p, c_double_p,
+                                       c_double_p, c_double_p, c_double_p, c_double_p]
         L.orc_ge.restype = C.c_int
         L.orc_ge.argtypes = [C.c_int, C.c_int, c_double_p, c_double_p]
         L.orc_pk2cc_nhk.argtypes = [C.c_double, C.c_double, c_double_p, c_double_p, c_double_p]
@@ -339,6 +342,9 @@ class OracleEquation:
             self.Xion[:, 0] = c["V0"]
             self.Xion[:, 1] = c["X20"]
         eq.Xion = dp(self.Xion)
+        self.Ad = keep(np.zeros((p.nNo, 3)))
+        if p.phys == 7:
+            eq.Ad = dp(self.Ad)
         if colored:
             nc, off, order = color_elements(p.nNo, p.ien)
             eq.ncolor = nc

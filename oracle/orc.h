@@ -115,7 +115,7 @@ void orc_doassem(int dof, int eNoN, const int *ptr, const double *lK,
 
 /* Equation parameters for one assembly call (one domain, constant props). */
 typedef struct {
-  int phys;      /* 1 HEATS, 2 STRUCT, 3 CEP, 4 FLUID, 5 LELAS, 6 HEATF */
+  int phys;      /* 1 HEATS, 2 STRUCT, 3 CEP, 4 FLUID, 5 LELAS, 6 HEATF, 7 USTRUCT */
   int dof, tDof, s; /* eq dof, total dof, 0-based start of this eq in tDof */
   double am, af, beta, gam, dt;
   double rho, cond, src;       /* HEATS: solid_density, conductivity, source */
@@ -130,6 +130,7 @@ typedef struct {
                                   2 Casson (F/FLUID.f:1690-1739) */
   double mu_o, vlam, va, vn;   /* mu_o, lam, a, n of the model (mu_i = mu_f) */
   double bstab;                /* FLUID backflow_stab (F/READFILES.f:1089-1091) */
+  int volType;                 /* USTRUCT volumetric penalty: 0 Quad, 1 ST91, 2 M94 */
 } orc_eqp;
 
 int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
@@ -252,7 +253,22 @@ typedef struct {
      runs each colour's elements with OpenMP (orc_assemble_colored); 0 keeps
      the serial element loop of GLOBALEQASSEM */
   int ncolor; const int *color_off; const int *color_order;
+  /* USTRUCT (phys 7): Ad(3,nNo), the acceleration of the displacement
+     kept across steps (F/INITIALIZE.f:227-231); NULL otherwise */
+  double *Ad;
 } orc_eq;
+
+/* USTRUCT element (tet4, equal order, VMS): USTRUCT3D_M + USTRUCT3D_C,
+   F/USTRUCT.f:205-612, 880-1102 */
+void orc_elem_ustruct(const orc_eqp *p, const double xl[12], const double *al,
+                      const double *yl, const double *dl, double lR[16], double lK[256],
+                      double lKd[192]);
+/* CONSTRUCT_uSOLID + USTRUCT_DOASSEM (F/USTRUCT.f:39-203, 1419-1555):
+   R(4,nNo), Val(16,nnz), Kd(12,nnz) accumulated */
+int orc_assemble_ustruct(const orc_eqp *p, int nNo, int nEl, const int *IEN,
+                         const double *x, const double *Ag, const double *Yg,
+                         const double *Dg, const int *rowPtr, const int *colPtr,
+                         double *R, double *Val, double *Kd);
 
 /* Greedy element colouring: elements of one colour share no node.  Writes
    color_off[ncolor+1] (at most 65 entries) and order[nEl] (element ids

@@ -1195,11 +1195,33 @@ static void apply_dir(orc_eq *eq, double *lA, double *lY) {
   }
 }
 
+/* SETBCDIRL for ustruct (F/SETBC.f:133-175, plain Dirichlet): for each
+   constrained velocity component, Dn = gam dt Yn - (gam - 1) dt Ad + Do
+   and Ad = Yn */
+static void ust_dir(orc_eq *eq, const double *lY, double *lD) {
+  const int tD = eq->p.tDof, s = eq->p.s;
+  const double c1 = eq->p.gam * eq->p.dt, c2 = (eq->p.gam - 1.0) * eq->p.dt;
+  for (int ib = 0; ib < eq->nDir; ib++) {
+    const orc_dirbc *bc = &eq->dir[ib];
+    for (int a = 0; a < bc->nNo; a++) {
+      const int Ac = bc->nodes[a];
+      for (int i = 0; i < 3; i++) {
+        if (bc->mask && !((bc->mask >> i) & 1)) continue;
+        const size_t j = (size_t)Ac * tD + s + i;
+        lD[j] = c1 * lY[j] - c2 * eq->Ad[(size_t)Ac * 3 + i] + eq->Do[j];
+        eq->Ad[(size_t)Ac * 3 + i] = lY[j];
+      }
+    }
+  }
+}
+
 int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
   const int nNo = eq->nNo, tD = eq->p.tDof, dof = eq->p.dof;
   const size_t nS = (size_t)nNo * tD;
   const double dt = eq->p.dt, gam = eq->p.gam, beta = eq->p.beta;
   const int dFlag = (eq->p.phys == 2 || eq->p.phys == 5);
+  const int ust = (eq->p.phys == 7);
+  if (ust && (!eq->Ad || dof != 4 || eq->p.s != 0)) return -4;
   memset(info, 0, sizeof(*info));
   eq->time += dt;
   /* CEP: reaction step (CEPINTEG, F/CEPION.f:166-314, called from PICP):
@@ -1228,8 +1250,11 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
   } else {
     for (size_t k = 0; k < nS; k++) eq->Dn[k] = eq->Do[k];
   }
+  if (ust) /* ustruct: Ad = Ad (gam - 1)/gam, Dn = Do (F/PIC.f:111-116) */
+    for (size_t k = 0; k < (size_t)nNo * 3; k++) eq->Ad[k] = eq->Ad[k] * coef;
   /* SETBCDIR */
   apply_dir(eq, eq->An, eq->Yn);
+  if (ust) ust_dir(eq, eq->Yn, eq->Dn);
 
   /* LS structures: one face per Dirichlet BC (FSILSINI, F/BAFINI.f:468-513) */
   orc_lhs *lhs = orc_lhs_create(nNo, eq->nnz, eq->rowPtr, eq->colPtr, eq->nDir);
@@ -1265,6 +1290,8 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
   double *Dg = (double *)xcalloc(nS, sizeof(double));
   double *R = (double *)xcalloc((size_t)nNo * dof, sizeof(double));
   double *Val = (double *)xcalloc((size_t)eq->nnz * dof * dof, sizeof(double));
+  double *Kd = ust ? (double *)xcalloc((size_t)eq->nnz * 12, sizeof(double)) : NULL;
+  double *Rd = ust ? (double *)xcalloc((size_t)nNo * 3, sizeof(double)) : NULL;
   int *incL = (int *)xcalloc(eq->nDir > 0 ? eq->nDir : 1, sizeof(int));
   double *res = (double *)xcalloc(eq->nDir > 0 ? eq->nDir : 1, sizeof(double));
   for (int f = 0; f < eq->nDir; f++) incL[f] = 1;
@@ -1283,7 +1310,11 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
     /* LSALLOC */
     memset(R, 0, sizeof(double) * (size_t)nNo * dof);
     memset(Val, 0, sizeof(double) * (size_t)eq->nnz * dof * dof);
-    if (eq->ncolor > 0)
+    if (ust) {
+      memset(Kd, 0, sizeof(double) * (size_t)eq->nnz * 12);
+      rc = orc_assemble_ustruct(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr,
+                                eq->colPtr, R, Val, Kd);
+    } else if (eq->ncolor > 0)
       rc = orc_assemble_colored(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr,
                                 eq->colPtr, R, Val, eq->ncolor, eq->color_off, eq->color_order);
     else
@@ -1302,6 +1333,29 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
         orc_bheatf(&eq->p, eq->neu[k].nFel, eq->neu[k].fIEN, eq->neu[k].g, eq->nEl, eq->IEN,
                    eq->x, Yg, eq->rowPtr, eq->colPtr, R, Val);
     }
+    /* USTRUCTR (F/USTRUCT.f:1557-1637): on the first Newton iteration
+       Rd = amg Ad - Yg(velocity) and R -= Kd Rd / am; afterwards Rd = 0 */
+    if (ust) {
+      if (itr > 1) {
+        memset(Rd, 0, sizeof(double) * (size_t)nNo * 3);
+      } else {
+        const double amg = (gam - am) / (gam - 1.0), ami = 1.0 / am;
+        for (int a = 0; a < nNo; a++)
+          for (int i = 0; i < 3; i++)
+            Rd[(size_t)a * 3 + i] = amg * eq->Ad[(size_t)a * 3 + i] - Yg[(size_t)a * tD + i];
+        for (int a = 0; a < nNo; a++) {
+          double KU[4] = {0, 0, 0, 0};
+          for (int j = eq->rowPtr[a]; j < eq->rowPtr[a + 1]; j++) {
+            const int c = eq->colPtr[j];
+            const double *kd = Kd + (size_t)j * 12;
+            for (int r = 0; r < 4; r++)
+              KU[r] = KU[r] + kd[3 * r] * Rd[(size_t)c * 3] + kd[3 * r + 1] * Rd[(size_t)c * 3 + 1] +
+                      kd[3 * r + 2] * Rd[(size_t)c * 3 + 2];
+          }
+          for (int r = 0; r < 4; r++) R[(size_t)a * 4 + r] = R[(size_t)a * 4 + r] - ami * KU[r];
+        }
+      }
+    }
     /* LSSOLVE */
     rc = orc_solve(lhs, &ls, dof, R, Val, eq->prec, incL, res);
     if (rc) break;
@@ -1309,13 +1363,22 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
     info->last_suc = ls.RI.suc;
     /* PICC */
     const double c1 = gam * dt, c2 = beta * dt * dt;
+    if (ust) { /* F/PIC.f:185-196 */
+      const double c3 = 1.0 / am, c4 = af * c1 * c3;
+      for (int a = 0; a < nNo; a++)
+        for (int i = 0; i < 3; i++) {
+          const double dU = Rd[(size_t)a * 3 + i] * c3 + R[(size_t)a * 4 + i] * c4;
+          eq->Ad[(size_t)a * 3 + i] = eq->Ad[(size_t)a * 3 + i] - dU;
+          eq->Dn[(size_t)a * tD + i] = eq->Dn[(size_t)a * tD + i] - dU * c1;
+        }
+    }
     for (int a = 0; a < nNo; a++)
       for (int c = 0; c < dof; c++) {
         const double r = R[(size_t)a * dof + c];
         const size_t k = (size_t)a * tD + eq->p.s + c;
         eq->An[k] = eq->An[k] - r;
         eq->Yn[k] = eq->Yn[k] - r * c1;
-        eq->Dn[k] = eq->Dn[k] - r * c2;
+        if (!ust) eq->Dn[k] = eq->Dn[k] - r * c2;
       }
     if (ls.RI.iNorm == 0.0) ls.RI.iNorm = 2.220446049250313e-16;
     if (eq->eq_iNorm == 0.0) eq->eq_iNorm = ls.RI.iNorm;
@@ -1336,14 +1399,372 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
     for (int a = 0; a < nNo; a++) eq->Xion[(size_t)a * 2] = eq->Yn[(size_t)a * tD + eq->p.s];
   memcpy(eq->Ao, eq->An, nS * sizeof(double));
   memcpy(eq->Yo, eq->Yn, nS * sizeof(double));
-  if (dFlag) memcpy(eq->Do, eq->Dn, nS * sizeof(double));
+  if (dFlag || ust) memcpy(eq->Do, eq->Dn, nS * sizeof(double));
   orc_lhs_free(lhs);
   free(Ag);
   free(Yg);
   free(Dg);
   free(R);
   free(Val);
+  free(Kd);
+  free(Rd);
   free(incL);
   free(res);
   return rc;
+}
+
+/* ---------------------------------------------------------------------- */
+/* USTRUCT: velocity-pressure (mixed) nonlinear solid, F/USTRUCT.f.  The
+   tet4 mesh uses one function space for velocity and pressure (nFs = 1,
+   VMS stabilisation on), the neo-Hookean isochoric model (GETPK2CCdev,
+   F/MATMODELS.f:568-1016, without fibres or active coupling: Ja = 1) and
+   the volumetric penalty of GVOLPEN (F/MATMODELS.f:1020-1070); tauM/tauC
+   of GETTAU (F/MATMODELS.f:1073-1104).  lR(4,4), lK(16,4,4), lKd(12,4,4):
+   index [a*4+i], [(a*4+b)*16+k], [(a*4+b)*12+k]. */
+static void ust_gvolpen(const orc_eqp *p, double pr, double Ja, double *ro, double *bt,
+                        double *dro, double *dbt) {
+  *ro = p->rho / Ja;
+  *bt = 0.0;
+  *dbt = 0.0;
+  *dro = 0.0;
+  const double Kp = p->Kpen;
+  if (iszero(Kp)) return;
+  if (p->volType == 0) {        /* stVol_Quad */
+    const double r1 = 1.0 / (Kp - pr);
+    *ro = *ro * Kp * r1;
+    *bt = r1;
+    *dro = *ro * r1;
+    *dbt = r1 * r1;
+  } else if (p->volType == 1) { /* stVol_ST91 */
+    const double r1 = *ro / Kp, r2 = sqrt(pr * pr + Kp * Kp);
+    *ro = r1 * (pr + r2);
+    *bt = 1.0 / r2;
+    *dro = *ro * *bt;
+    *dbt = -*bt * pr / (pr * pr + Kp * Kp);
+  } else {                      /* stVol_M94 */
+    const double r1 = *ro / Kp, r2 = Kp + pr;
+    *ro = r1 * r2;
+    *bt = 1.0 / r2;
+    *dro = r1;
+    *dbt = -*bt * *bt;
+  }
+}
+
+static void ust_gettau(const orc_eqp *p, double detF, double Je, double *tauM, double *tauC) {
+  const double he = 0.5 * pow(Je, 1.0 / 3.0);
+  const double rho0 = p->rho, Em = p->elM, nu = p->nu;
+  const double mu = 0.5 * Em / (1.0 + nu);
+  double c;
+  if (iszero(nu - 0.5)) {
+    c = sqrt(mu / rho0);
+  } else {
+    const double lam = 2.0 * mu * nu / (1.0 - 2.0 * nu);
+    c = sqrt((lam + 2.0 * mu) / rho0);
+  }
+  *tauM = p->ctM * (he / c) * (detF / rho0);
+  *tauC = p->ctC * (he * c) * (rho0 / detF);
+}
+
+void orc_elem_ustruct(const orc_eqp *p, const double xl[12], const double *al,
+                      const double *yl, const double *dl, double lR[16], double lK[256],
+                      double lKd[192]) {
+  const int tD = p->tDof, s = p->s;
+  double w4[4], N4[4][4], Nx[3][4], Je, ksix[3][3];
+  tet4_gauss(w4, N4);
+  gnn3k(xl, Nx, &Je, ksix);
+  for (int k = 0; k < 16; k++) lR[k] = 0.0;
+  for (int k = 0; k < 256; k++) lK[k] = 0.0;
+  for (int k = 0; k < 192; k++) lKd[k] = 0.0;
+  const double mu = p->visc;
+  const double am = p->am, af = p->af * p->gam * p->dt, afm = af / am;
+  const double r13 = 1.0 / 3.0, r23 = 2.0 / 3.0;
+#define AL(c, a) al[(a) * tD + s + (c)]
+#define YL(c, a) yl[(a) * tD + s + (c)]
+#define DL(c, a) dl[(a) * tD + s + (c)]
+#define LK(k, a, b) lK[((a) * 4 + (b)) * 16 + (k) - 1]
+#define LKD(k, a, b) lKd[((a) * 4 + (b)) * 12 + (k) - 1]
+  /* kinematics are constant on a tet4 */
+  double vx[3][3] = {{0}}, F[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        vx[i][j] += Nx[j][a] * YL(i, a);
+        M3(F, i, j) += Nx[j][a] * DL(i, a);
+      }
+  const double Jac = det3(F);
+  double Fi[9];
+  inv3(F, Fi);
+  /* ---- Gauss integration 1: momentum, USTRUCT3D_M (F/USTRUCT.f:205-612) */
+  for (int g = 0; g < 4; g++) {
+    const double w = w4[g] * Je;
+    const double *Nw = N4[g];
+    double vd[3] = {-p->fb[0], -p->fb[1], -p->fb[2]};
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++) vd[i] = vd[i] + Nw[a] * AL(i, a);
+    double pr = 0.0, pd = 0.0;
+    for (int a = 0; a < 4; a++) {
+      pr = pr + Nw[a] * YL(3, a);
+      pd = pd + Nw[a] * AL(3, a);
+    }
+    /* GETPK2CCdev = GETPK2CC's neo-Hookean isochoric part (Kpen = 0) */
+    double Siso[9], Dm[36];
+    orc_pk2cc_nhk(p->C10, 0.0, F, Siso, Dm);
+    const double Ja = 1.0;
+    /* viscous contribution */
+    double VxFi[3][3], ddev[3][3], Svis[9];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        double t = 0.0;
+        for (int k = 0; k < 3; k++) t += vx[i][k] * M3(Fi, k, j);
+        VxFi[i][j] = t;
+      }
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) ddev[i][j] = 0.5 * (VxFi[i][j] + VxFi[j][i]);
+    {
+      const double tr = (ddev[0][0] + ddev[1][1] + ddev[2][2]) / 3.0;
+      for (int i = 0; i < 3; i++) ddev[i][i] -= tr;
+    }
+    {
+      double tmp[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          double t = 0.0;
+          for (int k = 0; k < 3; k++) t += ddev[i][k] * M3(Fi, j, k);
+          tmp[i][j] = t;
+        }
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          double t = 0.0;
+          for (int k = 0; k < 3; k++) t += M3(Fi, i, k) * tmp[k][j];
+          M3(Svis, i, j) = 2.0 * mu * Jac * t;
+        }
+    }
+    double rho, beta, drho, dbeta;
+    ust_gvolpen(p, pr, Ja, &rho, &beta, &drho, &dbeta);
+    double tauM, tauC;
+    ust_gettau(p, Jac, Je, &tauM, &tauC);
+    for (int k = 0; k < 9; k++) Siso[k] += Svis[k];
+    double Pdev[9];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        double t = 0.0;
+        for (int k = 0; k < 3; k++) t += M3(F, i, k) * M3(Siso, k, j);
+        M3(Pdev, i, j) = t;
+      }
+    double NxFi[3][4];
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++)
+        NxFi[i][a] = Nx[0][a] * M3(Fi, 0, i) + Nx[1][a] * M3(Fi, 1, i) + Nx[2][a] * M3(Fi, 2, i);
+    const double rC = beta * pd + VxFi[0][0] + VxFi[1][1] + VxFi[2][2];
+    const double rCl = -pr + tauC * rC;
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++) {
+        const double T1 = Jac * rho * vd[i] * Nw[a];
+        const double T2 = M3(Pdev, i, 0) * Nx[0][a] + M3(Pdev, i, 1) * Nx[1][a] +
+                          M3(Pdev, i, 2) * Nx[2][a];
+        const double T3 = Jac * rCl * NxFi[i][a];
+        lR[a * 4 + i] = lR[a * 4 + i] + w * (T1 + T2 + T3);
+      }
+    /* Bm(6,3,a): rows (11, 22, 33, 12, 23, 31) of the strain variation */
+    double Bm[6][3][4];
+    for (int a = 0; a < 4; a++)
+      for (int c = 0; c < 3; c++) {
+        Bm[0][c][a] = Nx[0][a] * M3(F, c, 0);
+        Bm[1][c][a] = Nx[1][a] * M3(F, c, 1);
+        Bm[2][c][a] = Nx[2][a] * M3(F, c, 2);
+        Bm[3][c][a] = Nx[0][a] * M3(F, c, 1) + M3(F, c, 0) * Nx[1][a];
+        Bm[4][c][a] = Nx[1][a] * M3(F, c, 2) + M3(F, c, 1) * Nx[2][a];
+        Bm[5][c][a] = Nx[2][a] * M3(F, c, 0) + M3(F, c, 2) * Nx[0][a];
+      }
+    double DdNx[3][4], VxNx[3][4];
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++) {
+        DdNx[i][a] = ddev[i][0] * NxFi[0][a] + ddev[i][1] * NxFi[1][a] + ddev[i][2] * NxFi[2][a];
+        VxNx[i][a] = VxFi[0][i] * NxFi[0][a] + VxFi[1][i] * NxFi[1][a] + VxFi[2][i] * NxFi[2][a];
+      }
+    for (int b = 0; b < 4; b++)
+      for (int a = 0; a < 4; a++) {
+        double NxSNx = 0.0;
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) NxSNx += Nx[i][a] * M3(Siso, i, j) * Nx[j][b];
+        double DBm[6][3];
+        for (int I = 0; I < 6; I++)
+          for (int c = 0; c < 3; c++) {
+            double t = 0.0;
+            for (int K = 0; K < 6; K++) t += Dm[I * 6 + K] * Bm[K][c][b];
+            DBm[I][c] = t;
+          }
+        const double NxNx = NxFi[0][a] * NxFi[0][b] + NxFi[1][a] * NxFi[1][b] +
+                            NxFi[2][a] * NxFi[2][b];
+        /* dM_r/dV_c + af/am dM_r/dU_c, r, c = 0..2 (lKd k = 3r+c+1,
+           lK k = 4r+c+1) */
+        for (int r = 0; r < 3; r++)
+          for (int c = 0; c < 3; c++) {
+            double BtDB = 0.0;
+            for (int I = 0; I < 6; I++) BtDB += Bm[I][r][a] * DBm[I][c];
+            const double T1 = Jac * rho * vd[r] * Nw[a] * NxFi[c][b];
+            const double T2 = -tauC * Jac * NxFi[r][a] * VxNx[c][b];
+            const double T3 = (r == c) ? 0.0
+                                       : Jac * rCl * (NxFi[r][a] * NxFi[c][b] - NxFi[c][a] * NxFi[r][b]);
+            const double Tv = (2.0 * (DdNx[r][a] * NxFi[c][b] - DdNx[r][b] * NxFi[c][a]) -
+                               (NxNx * VxFi[r][c] + NxFi[r][b] * VxNx[c][a] -
+                                r23 * NxFi[r][a] * VxNx[c][b])) * mu * Jac;
+            const double Ku = w * af * (T1 + T2 + T3 + Tv + BtDB + ((r == c) ? NxSNx : 0.0));
+            LKD(3 * r + c + 1, a, b) += Ku;
+            double T2k, Tvk;
+            if (r == c) {
+              const double T1m = am * Jac * rho * Nw[a] * Nw[b];
+              T2k = T1m + af * Jac * tauC * rho * NxFi[r][a] * NxFi[r][b];
+              Tvk = af * mu * Jac * (r13 * NxFi[r][a] * NxFi[r][b] + NxNx);
+            } else {
+              T2k = af * Jac * tauC * rho * NxFi[r][a] * NxFi[c][b];
+              Tvk = af * mu * Jac * (NxFi[c][a] * NxFi[r][b] - r23 * NxFi[r][a] * NxFi[c][b]);
+            }
+            LK(4 * r + c + 1, a, b) += w * (T2k + Tvk) + afm * Ku;
+          }
+      }
+    for (int b = 0; b < 4; b++)
+      for (int a = 0; a < 4; a++) {
+        const double T1 = am * tauC * beta + af * (tauC * dbeta * pd - 1.0);
+        for (int r = 0; r < 3; r++) {
+          const double T2 = T1 * NxFi[r][a] * Nw[b] + af * drho * vd[r] * Nw[a] * Nw[b];
+          LK(4 * r + 4, a, b) += w * Jac * T2;
+        }
+      }
+  }
+  /* ---- Gauss integration 2: continuity, USTRUCT3D_C (F/USTRUCT.f:880-1102) */
+  const double ctV = 36.0;
+  for (int g = 0; g < 4; g++) {
+    const double w = w4[g] * Je;
+    const double *Nw = N4[g], *Nq = N4[g];
+    double vd[3] = {-p->fb[0], -p->fb[1], -p->fb[2]};
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++) vd[i] = vd[i] + Nw[a] * AL(i, a);
+    double pr = 0.0, pd = 0.0, px[3] = {0, 0, 0};
+    for (int a = 0; a < 4; a++) {
+      pr = pr + Nq[a] * YL(3, a);
+      pd = pd + Nq[a] * AL(3, a);
+      for (int i = 0; i < 3; i++) px[i] = px[i] + Nx[i][a] * YL(3, a);
+    }
+    double rho, beta, drho, dbeta;
+    ust_gvolpen(p, pr, 1.0, &rho, &beta, &drho, &dbeta);
+    double tauM, tauC;
+    ust_gettau(p, Jac, Je, &tauM, &tauC);
+    {
+      double Kx[3][3], tmp[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          double t = 0.0;
+          for (int k = 0; k < 3; k++) t += ksix[i][k] * M3(Fi, k, j);
+          tmp[i][j] = t;
+        }
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          double t = 0.0;
+          for (int k = 0; k < 3; k++) t += M3(Fi, k, i) * tmp[k][j];
+          Kx[i][j] = t;
+        }
+      double tauV = 0.0;
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) tauV += Kx[i][j] * Kx[i][j];
+      tauV = ctV * mu * mu * tauV;
+      tauM = 1.0 / sqrt(tauV + pow(1.0 / tauM, 2.0));
+    }
+    double NwxFi[3][4], VxFi[3][3], PxFi[3];
+    for (int a = 0; a < 4; a++)
+      for (int i = 0; i < 3; i++)
+        NwxFi[i][a] = Nx[0][a] * M3(Fi, 0, i) + Nx[1][a] * M3(Fi, 1, i) + Nx[2][a] * M3(Fi, 2, i);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        VxFi[i][j] = vx[i][0] * M3(Fi, 0, j) + vx[i][1] * M3(Fi, 1, j) + vx[i][2] * M3(Fi, 2, j);
+    for (int i = 0; i < 3; i++) PxFi[i] = px[0] * M3(Fi, 0, i) + px[1] * M3(Fi, 1, i) + px[2] * M3(Fi, 2, i);
+    const double rC = beta * pd + VxFi[0][0] + VxFi[1][1] + VxFi[2][2];
+    double rM[3];
+    for (int i = 0; i < 3; i++) rM[i] = rho * vd[i] + PxFi[i];
+    double rMNqx[4], rMNwx[4], VxNwx[3][4];
+    for (int a = 0; a < 4; a++) {
+      rMNqx[a] = rM[0] * NwxFi[0][a] + rM[1] * NwxFi[1][a] + rM[2] * NwxFi[2][a];
+      lR[a * 4 + 3] = lR[a * 4 + 3] + w * Jac * (Nq[a] * rC + tauM * rMNqx[a]);
+    }
+    for (int a = 0; a < 4; a++) {
+      rMNwx[a] = rM[0] * NwxFi[0][a] + rM[1] * NwxFi[1][a] + rM[2] * NwxFi[2][a];
+      for (int i = 0; i < 3; i++)
+        VxNwx[i][a] = VxFi[0][i] * NwxFi[0][a] + VxFi[1][i] * NwxFi[1][a] + VxFi[2][i] * NwxFi[2][a];
+    }
+    for (int b = 0; b < 4; b++)
+      for (int a = 0; a < 4; a++) {
+        const double NxNx = NwxFi[0][a] * NwxFi[0][b] + NwxFi[1][a] * NwxFi[1][b] +
+                            NwxFi[2][a] * NwxFi[2][b];
+        for (int c = 0; c < 3; c++) {
+          const double T1 = Nq[a] * (rC * NwxFi[c][b] - VxNwx[c][b]);
+          const double T2 = tauM * (rMNqx[a] * NwxFi[c][b] - rMNwx[b] * NwxFi[c][a]);
+          const double T3 = -tauM * NxNx * PxFi[c];
+          const double Ku = w * af * Jac * (T1 + T2 + T3);
+          LKD(10 + c, a, b) += Ku;
+          const double T2k = (am * tauM * rho) * NwxFi[c][a] * Nw[b] + af * Nq[a] * NwxFi[c][b];
+          LK(13 + c, a, b) += w * Jac * T2k + afm * Ku;
+        }
+      }
+    for (int b = 0; b < 4; b++)
+      for (int a = 0; a < 4; a++) {
+        const double NxNx = NwxFi[0][a] * NwxFi[0][b] + NwxFi[1][a] * NwxFi[1][b] +
+                            NwxFi[2][a] * NwxFi[2][b];
+        const double T1 = (am * beta + af * dbeta * pd) * Nq[a] * Nq[b];
+        const double T2 = NwxFi[0][a] * vd[0] + NwxFi[1][a] * vd[1] + NwxFi[2][a] * vd[2];
+        const double T3 = T1 + af * tauM * (NxNx + drho * T2 * Nq[b]);
+        LK(16, a, b) += w * Jac * T3;
+      }
+  }
+#undef AL
+#undef YL
+#undef DL
+#undef LK
+#undef LKD
+}
+
+int orc_assemble_ustruct(const orc_eqp *p, int nNo, int nEl, const int *IEN,
+                         const double *x, const double *Ag, const double *Yg,
+                         const double *Dg, const int *rowPtr, const int *colPtr,
+                         double *R, double *Val, double *Kd) {
+  (void)nNo;
+  const int tD = p->tDof;
+  if (tD > 16 || p->dof != 4) return -1;
+  double xl[12], al[4 * 16], yl[4 * 16], dl[4 * 16], lR[16], lK[256], lKd[192];
+  for (int e = 0; e < nEl; e++) {
+    int ptr[4];
+    for (int a = 0; a < 4; a++) {
+      const int Ac = IEN[(size_t)e * 4 + a];
+      ptr[a] = Ac;
+      for (int i = 0; i < 3; i++) xl[a * 3 + i] = x[(size_t)Ac * 3 + i];
+      for (int i = 0; i < tD; i++) {
+        al[a * tD + i] = Ag[(size_t)Ac * tD + i];
+        yl[a * tD + i] = Yg[(size_t)Ac * tD + i];
+        dl[a * tD + i] = Dg[(size_t)Ac * tD + i];
+      }
+    }
+    orc_elem_ustruct(p, xl, al, yl, dl, lR, lK, lKd);
+    /* USTRUCT_DOASSEM with the identity node map of one mesh: every entry
+       of lK goes to Val, every entry of lKd to Kd, at the (a,b) block */
+    for (int a = 0; a < 4; a++) {
+      const int rowN = ptr[a];
+      for (int i = 0; i < 4; i++) R[(size_t)rowN * 4 + i] += lR[a * 4 + i];
+      for (int b = 0; b < 4; b++) {
+        const int colN = ptr[b];
+        int left = rowPtr[rowN], right = rowPtr[rowN + 1] - 1, q = -1;
+        while (left <= right) {
+          const int mid = (left + right) / 2;
+          if (colPtr[mid] == colN) {
+            q = mid;
+            break;
+          }
+          if (colPtr[mid] < colN) left = mid + 1;
+          else right = mid - 1;
+        }
+        if (q < 0) return -3;
+        for (int k = 0; k < 16; k++) Val[(size_t)q * 16 + k] += lK[(a * 4 + b) * 16 + k];
+        for (int k = 0; k < 12; k++) Kd[(size_t)q * 12 + k] += lKd[(a * 4 + b) * 12 + k];
+      }
+    }
+  }
+  return 0;
 }

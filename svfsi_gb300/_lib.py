@@ -19,6 +19,7 @@ PRECOND_FSILS, PRECOND_RCS = 701, 709
 BC_TYPE_DIR, BC_TYPE_NEU = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 PHYS_HEATS, PHYS_STRUCT, PHYS_CEP, PHYS_FLUID, PHYS_LELAS, PHYS_HEATF = 1, 2, 3, 4, 5, 6
+PHYS_USTRUCT = 7
 
 
 class SubLs(C.Structure):
@@ -43,7 +44,8 @@ class EqParams(C.Structure):
                 ("mu_f", C.c_double), ("ctM", C.c_double), ("ctC", C.c_double),
                 ("eparam", c_double_p), ("elM", C.c_double), ("nu", C.c_double),
                 ("viscType", C.c_int), ("mu_o", C.c_double), ("vlam", C.c_double),
-                ("va", C.c_double), ("vn", C.c_double), ("bstab", C.c_double)]
+                ("va", C.c_double), ("vn", C.c_double), ("bstab", C.c_double),
+                ("volType", C.c_int)]
 
 
 class EqSolver(C.Structure):

@@ -21,7 +21,8 @@ MODULE GSLS_C
   INTEGER(C_INT), PARAMETER :: GSLS_BC_TYPE_DIR = 0, GSLS_BC_TYPE_NEU = 1
   INTEGER(C_INT), PARAMETER :: GSLS_PREC_FP64 = 0, GSLS_PREC_MIXED = 1
   INTEGER(C_INT), PARAMETER :: GSLS_PHYS_HEATS = 1, GSLS_PHYS_STRUCT = 2, &
-       GSLS_PHYS_CEP = 3, GSLS_PHYS_FLUID = 4, GSLS_PHYS_LELAS = 5, GSLS_PHYS_HEATF = 6
+       GSLS_PHYS_CEP = 3, GSLS_PHYS_FLUID = 4, GSLS_PHYS_LELAS = 5, GSLS_PHYS_HEATF = 6, &
+       GSLS_PHYS_USTRUCT = 7
   INTEGER(C_INT), PARAMETER :: GSLS_VISC_CONST = 0, GSLS_VISC_CY = 1, GSLS_VISC_CASSON = 2
 
   ! FSILS_subLsType / FSILS_lsType (LOGICAL as C int)
@@ -46,6 +47,7 @@ MODULE GSLS_C
      INTEGER(C_INT) :: viscType
      REAL(C_DOUBLE) :: mu_o, vlam, va, vn
      REAL(C_DOUBLE) :: bstab
+     INTEGER(C_INT) :: volType
   END TYPE gsls_eq_params
 
   INTERFACE

@@ -99,6 +99,8 @@ CONTAINS
          p%phys = GSLS_PHYS_LELAS
       CASE (phys_heatF)
          p%phys = GSLS_PHYS_HEATF
+      CASE (phys_ustruct)
+         p%phys = GSLS_PHYS_USTRUCT
       CASE DEFAULT
          err = "GSLS_PARAMS: physics not on the GPU path"
       END SELECT
@@ -139,6 +141,14 @@ CONTAINS
       p%va = d%visc%a
       p%vn = d%visc%n
       p%bstab = d%prop(backflow_stab)
+      SELECT CASE (d%stM%volType)
+      CASE (stVol_Quad)
+         p%volType = 0
+      CASE (stVol_M94)
+         p%volType = 2
+      CASE DEFAULT
+         p%volType = 1
+      END SELECT
     END ASSOCIATE
   END SUBROUTINE GSLS_PARAMS
 

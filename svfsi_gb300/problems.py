@@ -24,7 +24,7 @@ import numpy as np
 
 from . import meshgen
 from ._lib import (LS_TYPE_CG, LS_TYPE_GMRES, LS_TYPE_NS, PHYS_CEP, PHYS_FLUID, PHYS_HEATF, PHYS_HEATS,
-                   PHYS_LELAS, PHYS_STRUCT, PREC_FP64,
+                   PHYS_LELAS, PHYS_STRUCT, PHYS_USTRUCT, PREC_FP64,
                    PRECOND_FSILS, PRECOND_RCS, EqParams, EqSolver)
 
 SEED = 20261203
@@ -200,6 +200,39 @@ def lelas_beam(nx: int = 176, ny: int = 44, nz: int = 44, nsteps: int = 10,
                    phys=PHYS_LELAS, dof=3, tDof=3, params=params,
                    dirichlet=[DirBC(clamp, 0.0)], traction=[TracBC(tface, tuple(traction))],
                    LS_type=LS_TYPE_CG, prec=PRECOND_FSILS, minItr=1, maxItr=10, tol=1e-8,
+                   nsteps=nsteps)
+
+
+VOL_QUAD, VOL_ST91, VOL_M94 = 0, 1, 2
+
+
+def ustruct_beam(nx: int = 24, ny: int = 6, nz: int = 6, nsteps: int = 10,
+                 E: float = 1e6, nu: float = 0.45, traction=(0.0, 0.0, -1e3),
+                 visc: float = 0.0, volType: int = VOL_ST91, ctM: float = 1e-3,
+                 ctC: float = 0.0) -> Problem:
+    """USTRUCT (velocity-pressure solid, F/USTRUCT.f) on the beam mesh:
+    state (v, p) with the displacement in D, neo-Hookean isochoric part
+    (C10 = mu/2) and the volumetric penalty volType (kappa = E/3(1-2nu),
+    0 for nu = 0.5: incompressible), rho 1, solid viscosity visc, VMS
+    stabilisation with the input defaults ctM 1e-3 and ctC 0
+    (F/READFILES.f:1099-1106), x = 0 clamped, constant traction on x = 4,
+    dt 1e-3, first-order generalized-alpha with rho_inf 0.2 (the reference
+    does not take the second-order am for ustruct, F/INITIALIZE.f:101-104),
+    GMRES + diagonal preconditioner (its default, F/READFILES.f:628)."""
+    x, ien = meshgen.kuhn_box(nx, ny, nz, 4.0, 1.0, 1.0)
+    rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
+    am, af, beta, gam = genalpha(0.2, second_order=False)
+    mu = E * 0.5 / (1.0 + nu)
+    kap = 0.0 if abs(nu - 0.5) < 1e-15 else E / (1.0 - 2.0 * nu) / 3.0
+    params = dict(am=am, af=af, beta=beta, gam=gam, dt=1e-3, rho=1.0, C10=0.5 * mu, Kpen=kap,
+                  visc=visc, fb=(0.0, 0.0, 0.0), elM=E, nu=nu, ctM=ctM, ctC=ctC,
+                  volType=volType)
+    clamp = meshgen.nodes_on_plane(x, 0, 0.0)
+    tface = meshgen.faces_on_plane(x, ien, 0, 4.0)
+    return Problem(name=f"ustruct_beam_{nx}x{ny}x{nz}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
+                   phys=PHYS_USTRUCT, dof=4, tDof=4, params=params,
+                   dirichlet=[DirBC(clamp, 0.0)], traction=[TracBC(tface, tuple(traction))],
+                   LS_type=LS_TYPE_GMRES, prec=PRECOND_FSILS, minItr=1, maxItr=10, tol=1e-8,
                    nsteps=nsteps)
 
 

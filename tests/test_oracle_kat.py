@@ -782,3 +782,75 @@ def test_bfluid_uniform_state_kat(orc):
             off = rows.copy()
             np.fill_diagonal(off, 0.0)
             assert np.all(off == 0.0) and rows[3, 3] == 0.0
+
+
+def _ustruct_elem(orc, eqp, xl, al, yl, dl):
+    lR, lK, lKd = np.zeros(16), np.zeros(256), np.zeros(192)
+    orc.load().orc_elem_ustruct(C.byref(eqp), orc.dp(orc.f64(xl.ravel())),
+                                orc.dp(orc.f64(al.ravel())), orc.dp(orc.f64(yl.ravel())),
+                                orc.dp(orc.f64(dl.ravel())), orc.dp(lR), orc.dp(lK), orc.dp(lKd))
+    return lR.reshape(4, 4), lK.reshape(4, 4, 4, 4), lKd.reshape(4, 4, 4, 3)
+
+
+@pytest.mark.parametrize("volType", [0, 1, 2])
+def test_ustruct_element_rest_and_momentum_tangent(orc, volType):
+    """USTRUCT element (USTRUCT3D_M/_C): zero residual at rest, and the
+    momentum rows of the tangents are the residual's derivatives (central
+    differences): lKd = af' dR/dD and lK = am dR/dA + af' dR/dY + (af'/am)
+    lKd, af' = af gam dt (the Newton increment moves A by 1, Y by af' and D
+    by af'^2/am).  The continuity rows also carry tau_M(J) and tau_C(J)
+    undifferentiated, as in the reference, so they are left out."""
+    p = problems.ustruct_beam(2, 1, 1, nu=0.4, volType=volType, ctC=0.0, visc=0.0)
+    eqp = orc.eqp_from(p)
+    xl = _unit_tet() * np.array([1.1, 0.9, 1.2])
+    z = np.zeros((4, 4))
+    lR, _, _ = _ustruct_elem(orc, eqp, xl, z, z, z)
+    assert np.abs(lR).max() <= 1e-15 * eqp.C10     # S(I) = 0 up to rounding
+    rng = np.random.default_rng(5)
+    st = [1e2 * rng.standard_normal((4, 4)), 1e-1 * rng.standard_normal((4, 4)),
+          1e-2 * rng.standard_normal((4, 4))]
+    st[1][:, 3] = 1e3 * rng.standard_normal(4)
+    st[2][:, 3] = 0.0
+    lR, lK, lKd = _ustruct_elem(orc, eqp, xl, *st)
+    afp = eqp.af * eqp.gam * eqp.dt
+    am = eqp.am
+
+    def d(which, b, c, h):
+        e = np.zeros((4, 4))
+        e[b, c] = h
+        P = [x + e if k == which else x for k, x in enumerate(st)]
+        M = [x - e if k == which else x for k, x in enumerate(st)]
+        return (_ustruct_elem(orc, eqp, xl, *P)[0] - _ustruct_elem(orc, eqp, xl, *M)[0]) / (2 * h)
+
+    sK = np.abs(lK[:, :, :3]).max()
+    for b in range(4):
+        for c in range(4):
+            h = 1e-3 if c == 3 else 1e-6
+            if c < 3:
+                kd = afp * d(2, b, c, 1e-7)
+                assert np.abs(kd[:, :3] - lKd[:, b, :3, c]).max() <= 1e-6 * np.abs(lKd).max()
+            mass = am * d(0, b, c, 1e-3) + afp * d(1, b, c, h)
+            want = lK[:, b, :3, c] - (afp / am * lKd[:, b, :3, c] if c < 3 else 0.0)
+            assert np.abs(mass[:, :3] - want).max() <= 1e-6 * sK, (b, c)
+
+
+def test_ustruct_oracle_steps_converge(orc):
+    """Three implicit USTRUCT steps of the oracle converge (Newton to 1e-8)
+    for the compressible (ST91) and the incompressible (Kpen = 0) solid,
+    and the beam bends the same way and by a similar amount as the STRUCT
+    formulation of the same problem."""
+    q = problems.struct_beam(12, 3, 3, nsteps=3)
+    eq = orc.OracleEquation(q)
+    eq.set_state(*q.initial_state())
+    for _ in range(3):
+        eq.step()
+    Ds = eq.state()[2]
+    for nu in (0.45, 0.5):
+        p = problems.ustruct_beam(12, 3, 3, nsteps=3, nu=nu)
+        eq = orc.OracleEquation(p)
+        eq.set_state(*p.initial_state())
+        for _ in range(3):
+            i = eq.step()
+            assert i.last_suc == 1 and i.r1_last <= p.tol * 10
+        Du = eq.state()[2][:, :3]
+        assert np.linalg.norm(Du - Ds) <= 0.2 * np.linalg.norm(Ds)
