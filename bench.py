@@ -57,7 +57,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--only", choices=["all", "mixed", "fp64"], default="all",
                     help="time one precision only (profiling runs)")
-    ap.add_argument("--workload", choices=["struct", "fluid", "cep", "lelas", "heatf", "adjoint"],
+    ap.add_argument("--workload",
+                    choices=["struct", "fluid", "cep", "lelas", "heatf", "ustruct", "adjoint"],
                     default="struct")
     ap.add_argument("--fd-dirs", type=int, default=4,
                     help="adjoint workload: random directions of the central-FD check")
@@ -100,6 +101,10 @@ def dist_env():
 
 def workload(args):
     from svfsi_gb300 import problems
+    if args.workload == "ustruct":
+        if args.small:
+            return problems.ustruct_beam(24, 6, 6, nsteps=args.steps)
+        return problems.ustruct_beam(**WORKLOAD, nsteps=args.steps)
     if args.workload == "fluid":
         return problems.fluid_cylinder(h=0.08 if args.small else args.fluid_h, nsteps=args.steps)
     if args.workload == "cep":
@@ -121,7 +126,8 @@ def workload(args):
 
 
 def is_fluid(p):
-    return p.dof == 4
+    from svfsi_gb300 import problems
+    return p.phys == problems.PHYS_FLUID
 
 
 def is_heatf(p):
@@ -142,6 +148,11 @@ def compared_field(p, state):
 
 def is_cep(p):
     return bool(getattr(p, "cep", None))
+
+
+def is_ust(p):
+    from svfsi_gb300 import problems
+    return p.phys == problems.PHYS_USTRUCT
 
 
 def is_heats(p):
@@ -181,6 +192,10 @@ def workload_desc(p):
                 f"inlet peak 30, impulsive start), {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
                 f"{p.nnz:,} 4x4 blocks, RCS + NS solver (sD 100, relTol 1e-2), dt 1e-3, Newton "
                 f"tol 1e-10")
+    if is_ust(p):
+        return (f"{p.name}: USTRUCT velocity-pressure neo-Hookean + ST91 solid (VMS, ctM 1e-3), "
+                f"E 1e6, nu 0.45, {p.nEl:,} tet4, {p.nNo:,} nodes, nnz {p.nnz:,} 4x4 blocks, "
+                f"GMRES+diag, dt 1e-3, Newton tol 1e-8")
     if p.phys == problems_phys_lelas():
         return (f"{p.name}: linear elastodynamics (LELAS3D, E 1e6, nu 0.45), {p.nEl:,} tet4, "
                 f"{p.nNo:,} nodes, nnz {p.nnz:,} 3x3 blocks, CG+diag, dt 1e-3, Newton tol 1e-8")
@@ -315,7 +330,8 @@ def run_gsls(args):
         if profile:
             L.gsls_profile_enable(0)
             cnt, tot = C.c_longlong(), C.c_double()
-            key = b"gm_spmv_d3" if is_fluid(p) else b"gm_spmv" if is_heatf(p) else b"cg_spmv"
+            key = (b"gm_spmv_d3" if is_fluid(p) else b"gm_spmv" if (is_heatf(p) or is_ust(p))
+                   else b"cg_spmv")
             L.gsls_profile_read(key, C.byref(cnt), C.byref(tot))
             acnt, atot = C.c_longlong(), C.c_double()
             L.gsls_profile_read(b"assembly", C.byref(acnt), C.byref(atot))
@@ -413,6 +429,10 @@ def run_gsls(args):
             B = p.algorithmic_bytes(s, s)["spmv"]
             kname = f"k_gm_spmv<1,{t},{t}> (CSR SpMV of the GMRES Arnoldi step)"
             tkey = f"gm_spmv_d1_f{8 * s}_{p.name}"
+        elif is_ust(p):
+            B = p.algorithmic_bytes(s, s)["spmv"]
+            kname = f"k_gm_spmv<4,{t},{t}> (block-CSR SpMV of the GMRES Arnoldi step, 4x4 blocks)"
+            tkey = f"gm_spmv_d4_f{8 * s}_{p.name}"
         elif is_cep(p):
             B = p.algorithmic_bytes(s, s)["spmv"]
             kname = f"k_cg_spmv<1,{t},{t}> (CSR SpMV + fused P.KP)"
@@ -469,7 +489,7 @@ def run_gsls(args):
     # than the HBM stream (measured live by the library's probe kernel)
     rate = C.c_double()
     _lib.check(L.gsls_fp64_fma_rate(C.byref(rate)), "gsls_fp64_fma_rate")
-    d = 3 if (is_fluid(p) or p.dof == 3) else 1
+    d = 3 if is_fluid(p) else p.dof
     fmas = d * d * p.nnz
     if roof64["achieved"] and not is_fluid(p):
         avg_s = roof64["avg_launch_us"] / 1e6
@@ -501,7 +521,8 @@ def run_gsls(args):
                   "assembly_ms_per_newton": mixed["asm_ms"] / max(mixed["newton"], 1),
                   "all_solves_converged": bool(mixed["suc"])},
         "ls_itr_note": ("NS outer iterations per step" if is_fluid(p)
-                        else "GMRES iterations per step" if is_heatf(p) else "CG iterations per step"),
+                        else "GMRES iterations per step" if (is_heatf(p) or is_ust(p))
+                        else "CG iterations per step"),
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "rel_l2_mixed_vs_fp64": rel_l2,
         "roofline": roof,
@@ -620,7 +641,7 @@ def config_legs(L, problems, fsils, torch):
 
 # implicit steps the oracle runs beside the GPU in the default bench run: the
 # cpu_baseline sample and the full-size error against the oracle's solution
-PARITY_STEPS = {"struct": 2, "lelas": 2, "fluid": 1, "heatf": 2, "cep": 20}
+PARITY_STEPS = {"struct": 2, "lelas": 2, "fluid": 1, "heatf": 2, "cep": 20, "ustruct": 1}
 
 
 def oracle_steps(p, nsteps, threads, warm=0):
@@ -644,7 +665,7 @@ def oracle_steps(p, nsteps, threads, warm=0):
 
 
 def krylov_name(p):
-    return "NS outer" if is_fluid(p) else "GMRES" if is_heatf(p) else "CG"
+    return "NS outer" if is_fluid(p) else "GMRES" if (is_heatf(p) or is_ust(p)) else "CG"
 
 
 def oracle_sample_desc(p, n, threads, counts, first):

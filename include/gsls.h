@@ -242,6 +242,15 @@ int gsls_assemble_dev(gsls_mesh *mesh, const gsls_eq_params *p,
 /* Same on host arrays (copies in and out). */
 int gsls_assemble(gsls_mesh *mesh, const gsls_eq_params *p, const double *Ag,
                   const double *Yg, const double *Dg, double *R, double *Val);
+/* USTRUCT (GSLS_PHYS_USTRUCT): CONSTRUCT_uSOLID with USTRUCT_DOASSEM
+   (Code/Source/svFSI/USTRUCT.f:39-203, 1419-1555) on device arrays: R(4,nNo)
+   and Val(16,nnz) as gsls_assemble_dev, and the displacement tangent
+   Kd(12,nnz) (double: rows v1..v3, p times columns d1..d3, row-major per
+   block) that USTRUCTR applies on the first Newton iteration.  All three
+   are overwritten. */
+int gsls_assemble_ustruct_dev(gsls_mesh *mesh, const gsls_eq_params *p,
+                              const double *dAg, const double *dYg, const double *dDg,
+                              double *dR, void *dVal, double *dKd, int val_prec);
 
 /* ------------------------------------------------------------------------ */
 /* Time integration of one equation (replaces the per-step work of

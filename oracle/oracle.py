@@ -126,6 +126,10 @@ def load():
                                      c_double_p, c_double_p]
         L.orc_elem_ustruct.argtypes = [C.POINTER(EqP), c_double_p, c_double_p, c_double_p,
                                        c_double_p, c_double_p, c_double_p, c_double_p]
+        L.orc_assemble_ustruct.argtypes = [C.POINTER(EqP), C.c_int, C.c_int, c_int_p,
+                                           c_double_p, c_double_p, c_double_p, c_double_p,
+                                           c_int_p, c_int_p, c_double_p, c_double_p,
+                                           c_double_p]
         L.orc_ge.restype = C.c_int
         L.orc_ge.argtypes = [C.c_int, C.c_int, c_double_p, c_double_p]
         L.orc_pk2cc_nhk.argtypes = [C.c_double, C.c_double, c_double_p, c_double_p, c_double_p]
@@ -203,6 +207,21 @@ def assemble(problem, Ag, Yg, Dg=None, eparam=None):
                         dp(Dg), ip(rp), ip(cp), dp(R), dp(Val))
     assert rc == 0, rc
     return R, Val
+
+
+def assemble_ustruct(problem, Ag, Yg, Dg):
+    """CONSTRUCT_uSOLID + USTRUCT_DOASSEM: (R(nNo,4), Val(nnz,16), Kd(nnz,12))."""
+    L = load()
+    p = eqp_from(problem)
+    R = np.zeros((problem.nNo, 4))
+    Val = np.zeros((problem.nnz, 16))
+    Kd = np.zeros((problem.nnz, 12))
+    ien, x, rp, cp = i32(problem.ien), f64(problem.x), i32(problem.rowPtr), i32(problem.colPtr)
+    Ag, Yg, Dg = f64(Ag), f64(Yg), f64(Dg)
+    rc = L.orc_assemble_ustruct(C.byref(p), problem.nNo, problem.nEl, ip(ien), dp(x), dp(Ag),
+                                dp(Yg), dp(Dg), ip(rp), ip(cp), dp(R), dp(Val), dp(Kd))
+    assert rc == 0, rc
+    return R, Val, Kd
 
 
 class OracleSolver:

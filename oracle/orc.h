@@ -269,6 +269,11 @@ int orc_assemble_ustruct(const orc_eqp *p, int nNo, int nEl, const int *IEN,
                          const double *x, const double *Ag, const double *Yg,
                          const double *Dg, const int *rowPtr, const int *colPtr,
                          double *R, double *Val, double *Kd);
+int orc_assemble_ustruct_colored(const orc_eqp *p, int nEl, const int *IEN, const double *x,
+                                 const double *Ag, const double *Yg, const double *Dg,
+                                 const int *rowPtr, const int *colPtr, double *R, double *Val,
+                                 double *Kd, int ncolor, const int *color_off,
+                                 const int *order);
 
 /* Greedy element colouring: elements of one colour share no node.  Writes
    color_off[ncolor+1] (at most 65 entries) and order[nEl] (element ids

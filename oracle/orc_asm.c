@@ -1312,8 +1312,13 @@ int orc_eq_step(orc_eq *eq, orc_stepinfo *info) {
     memset(Val, 0, sizeof(double) * (size_t)eq->nnz * dof * dof);
     if (ust) {
       memset(Kd, 0, sizeof(double) * (size_t)eq->nnz * 12);
-      rc = orc_assemble_ustruct(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr,
-                                eq->colPtr, R, Val, Kd);
+      if (eq->ncolor > 0)
+        rc = orc_assemble_ustruct_colored(&eq->p, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg,
+                                          eq->rowPtr, eq->colPtr, R, Val, Kd, eq->ncolor,
+                                          eq->color_off, eq->color_order);
+      else
+        rc = orc_assemble_ustruct(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr,
+                                  eq->colPtr, R, Val, Kd);
     } else if (eq->ncolor > 0)
       rc = orc_assemble_colored(&eq->p, nNo, eq->nEl, eq->IEN, eq->x, Ag, Yg, Dg, eq->rowPtr,
                                 eq->colPtr, R, Val, eq->ncolor, eq->color_off, eq->color_order);
@@ -1722,15 +1727,48 @@ void orc_elem_ustruct(const orc_eqp *p, const double xl[12], const double *al,
 #undef LKD
 }
 
+static int ust_elem_assemble(const orc_eqp *p, int e, const int *IEN, const double *x,
+                             const double *Ag, const double *Yg, const double *Dg,
+                             const int *rowPtr, const int *colPtr, double *R, double *Val,
+                             double *Kd);
+
 int orc_assemble_ustruct(const orc_eqp *p, int nNo, int nEl, const int *IEN,
                          const double *x, const double *Ag, const double *Yg,
                          const double *Dg, const int *rowPtr, const int *colPtr,
                          double *R, double *Val, double *Kd) {
   (void)nNo;
-  const int tD = p->tDof;
-  if (tD > 16 || p->dof != 4) return -1;
-  double xl[12], al[4 * 16], yl[4 * 16], dl[4 * 16], lR[16], lK[256], lKd[192];
+  if (p->tDof > 16 || p->dof != 4) return -1;
   for (int e = 0; e < nEl; e++) {
+    const int rc = ust_elem_assemble(p, e, IEN, x, Ag, Yg, Dg, rowPtr, colPtr, R, Val, Kd);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+/* The same colour by colour with OpenMP (the multi-core CPU baseline). */
+int orc_assemble_ustruct_colored(const orc_eqp *p, int nEl, const int *IEN, const double *x,
+                                 const double *Ag, const double *Yg, const double *Dg,
+                                 const int *rowPtr, const int *colPtr, double *R, double *Val,
+                                 double *Kd, int ncolor, const int *color_off,
+                                 const int *order) {
+  (void)nEl;
+  if (p->tDof > 16 || p->dof != 4) return -1;
+  int bad = 0;
+  for (int c = 0; c < ncolor; c++) {
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads()) reduction(| : bad)
+    for (int k = color_off[c]; k < color_off[c + 1]; k++)
+      bad |= ust_elem_assemble(p, order[k], IEN, x, Ag, Yg, Dg, rowPtr, colPtr, R, Val, Kd) != 0;
+  }
+  return bad ? -3 : 0;
+}
+
+static int ust_elem_assemble(const orc_eqp *p, int e, const int *IEN, const double *x,
+                             const double *Ag, const double *Yg, const double *Dg,
+                             const int *rowPtr, const int *colPtr, double *R, double *Val,
+                             double *Kd) {
+  const int tD = p->tDof;
+  double xl[12], al[4 * 16], yl[4 * 16], dl[4 * 16], lR[16], lK[256], lKd[192];
+  {
     int ptr[4];
     for (int a = 0; a < 4; a++) {
       const int Ac = IEN[(size_t)e * 4 + a];

@@ -103,6 +103,9 @@ SIGNATURES = {
     "gsls_mesh_ncolors": (C.c_int, [C.c_void_p]),
     "gsls_assemble_dev": (C.c_int, [C.c_void_p, C.POINTER(EqParams), C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "gsls_assemble_ustruct_dev": (C.c_int, [C.c_void_p, C.POINTER(EqParams), C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_int]),
     "gsls_assemble": (C.c_int, [C.c_void_p, C.POINTER(EqParams), c_double_p, c_double_p,
                                 c_double_p, c_double_p, c_double_p]),
     "gsls_eq_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.POINTER(EqParams),

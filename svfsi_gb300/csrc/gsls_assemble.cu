@@ -90,6 +90,8 @@ struct AsmArgs {
   double lam_le, mu_le;  // LELAS Lame parameters
   int viscType;          // FLUID viscosity model (GSLS_VISC_*)
   double mu_o, vlam, va, vn;
+  double E_s, nu_s;      // USTRUCT elasticity modulus and Poisson ratio (GETTAU)
+  int volType;           // USTRUCT volumetric penalty (GVOLPEN)
   const int4 *ien;
   const int4 *map;  // 4 int4 per element: map[e*4 + a] = (b0..b3)
   const double *x;
@@ -341,6 +343,7 @@ static bool lin_on() {
 #include "gsls_asm_fluid.cuh"
 #include "gsls_asm_lelas.cuh"
 #include "gsls_asm_heatf.cuh"
+#include "gsls_asm_ustruct.cuh"
 
 namespace gsls {
 
@@ -371,7 +374,7 @@ static int asm_launch(K kern, int nb, cudaStream_t st, const AsmArgs &A, bool pd
 // ---------------------------------------------------------------------------
 static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *Ag,
                            const double *Yg, const double *Dg, double *R, void *Val,
-                           int val_prec) {
+                           int val_prec, double *Kd = nullptr) {
   gsls_lhs *lhs = m->lhs;
   cudaStream_t st = lhs->stream;
   const int dof = p->dof;
@@ -416,6 +419,17 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   A.vlam = p->vlam;
   A.va = p->va;
   A.vn = p->vn;
+  A.E_s = p->elM;
+  A.nu_s = p->nu;
+  A.volType = p->volType;
+  if (p->phys == GSLS_PHYS_USTRUCT &&
+      (p->dof != 4 || p->s + 4 > p->tDof || !Dg || !Kd || !(p->am > 0.0) ||
+       !(p->rho > 0.0) || !(p->elM > 0.0) || p->volType < 0 || p->volType > 2 ||
+       !(p->ctM > 0.0))) {
+    set_error("assembly: USTRUCT needs dof 4, Dg, the Kd output, am, rho, elM > 0, "
+              "ctM > 0 and volType 0..2");
+    return GSLS_ERR_ARG;
+  }
   if (p->phys == GSLS_PHYS_LELAS) {
     // F/LELAS.f:166-167
     A.lam_le = p->elM * p->nu / (1.0 + p->nu) / (1.0 - 2.0 * p->nu);
@@ -458,6 +472,8 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   }
   GSLS_CUDA(cudaMemsetAsync(R, 0, sizeof(double) * (size_t)lhs->nNo * dof, st));
   GSLS_CUDA(cudaMemsetAsync(Val, 0, vbytes, st));
+  if (p->phys == GSLS_PHYS_USTRUCT)
+    GSLS_CUDA(cudaMemsetAsync(Kd, 0, sizeof(double) * 12 * (size_t)lhs->nnz, st));
   for (int c = 0; c < m->ncolors; c++) {
     A.el0 = m->color_off[c];
     A.nColorEl = m->color_off[c + 1] - m->color_off[c];
@@ -493,6 +509,11 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
         GSLS_TRY(asm_launch(k_asm_heatf<float>, nb, st, A, pdl));
       else
         GSLS_TRY(asm_launch(k_asm_heatf<double>, nb, st, A, pdl));
+    } else if (p->phys == GSLS_PHYS_USTRUCT) {
+      if (mixed)
+        k_asm_ustruct<float><<<nb, kAsmThreads, 0, st>>>(A, Kd);
+      else
+        k_asm_ustruct<double><<<nb, kAsmThreads, 0, st>>>(A, Kd);
     } else if (p->phys == GSLS_PHYS_LELAS) {
       if (dof != 3 || p->s + 3 > p->tDof || !Dg || !(p->elM > 0.0) || !(p->nu > -1.0) ||
           !(p->nu < 0.5) || !(p->dt > 0.0))
@@ -685,8 +706,8 @@ int mesh_set_eparam(gsls_mesh *m, const double *eparam) {
 }
 
 int assemble_dev(gsls_mesh *m, const gsls_eq_params *p, const double *Ag, const double *Yg,
-                 const double *Dg, double *R, void *Val, int val_prec) {
-  return launch_assembly(m, p, Ag, Yg, Dg, R, Val, val_prec);
+                 const double *Dg, double *R, void *Val, int val_prec, double *Kd) {
+  return launch_assembly(m, p, Ag, Yg, Dg, R, Val, val_prec, Kd);
 }
 
 gsls_lhs *mesh_lhs(gsls_mesh *m) { return m->lhs; }
@@ -859,7 +880,18 @@ int gsls_assemble_dev(gsls_mesh *m, const gsls_eq_params *p, const double *dAg,
                       int val_prec) {
   if (!m || !p || !dAg || !dYg || !dR || !dVal) return GSLS_ERR_ARG;
   GSLS_TRY(mesh_set_eparam(m, p->eparam));
-  GSLS_TRY(assemble_dev(m, p, dAg, dYg, dDg, dR, dVal, val_prec));
+  GSLS_TRY(assemble_dev(m, p, dAg, dYg, dDg, dR, dVal, val_prec, nullptr));
+  GSLS_CUDA(cudaStreamSynchronize(m->lhs->stream));
+  return mesh_check_error(m);
+}
+
+int gsls_assemble_ustruct_dev(gsls_mesh *m, const gsls_eq_params *p, const double *dAg,
+                              const double *dYg, const double *dDg, double *dR, void *dVal,
+                              double *dKd, int val_prec) {
+  if (!m || !p || !dAg || !dYg || !dDg || !dR || !dVal || !dKd ||
+      p->phys != GSLS_PHYS_USTRUCT)
+    return GSLS_ERR_ARG;
+  GSLS_TRY(assemble_dev(m, p, dAg, dYg, dDg, dR, dVal, val_prec, dKd));
   GSLS_CUDA(cudaStreamSynchronize(m->lhs->stream));
   return mesh_check_error(m);
 }

@@ -15,7 +15,7 @@
 
 namespace gsls {
 int assemble_dev(gsls_mesh *m, const gsls_eq_params *p, const double *Ag, const double *Yg,
-                 const double *Dg, double *R, void *Val, int val_prec);
+                 const double *Dg, double *R, void *Val, int val_prec, double *Kd = nullptr);
 int mesh_dRdp(gsls_mesh *m, const gsls_eq_params *p, const double *Yg, const double *Dg,
               const double *lam, double *out, double scale);
 int mesh_mass(gsls_mesh *m, const double *zeros, double *R, double *Val);
@@ -56,6 +56,10 @@ struct gsls_eq {
   std::vector<Neu *> neus;
   int nextFace = 0;
   double eq_iNorm = 0.0, eq_pNorm = 0.0;
+  // USTRUCT: Ad(3,nNo) kept across steps, Rd(3,nNo) and the displacement
+  // tangent Kd(12,nnz) of USTRUCTR (F/USTRUCT.f:1557-1637)
+  bool ust = false;
+  gsls::DevBuf Ad, Rd, Kd;
   // CEP cell model
   bool has_cep = false, cep_first = true;
   gsls_cep_params cep{};
@@ -256,6 +260,78 @@ __global__ void k_bfluid(int nF, int f0, const int *__restrict__ fien,
   }
 }
 
+// ---- USTRUCT step pieces (the reference's sstEq branches)
+__global__ void k_scale(size_t n, double *__restrict__ x, double c) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    x[k] = x[k] * c;
+}
+
+// SETBCDIRL for ustruct (Code/Source/svFSI/SETBC.f:133-175, plain
+// Dirichlet): on each constrained velocity component Dn = gam dt Yn -
+// (gam - 1) dt Ad + Do, then Ad = Yn
+__global__ void k_ust_dir(int n, const int *__restrict__ nodes, int mask, int tDof, int s,
+                          const double *__restrict__ Yn, const double *__restrict__ Do,
+                          double *__restrict__ Dn, double *__restrict__ Ad, double c1, double c2) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    const size_t Ac = nodes[a];
+    for (int i = 0; i < 3; i++) {
+      if (mask && !((mask >> i) & 1)) continue;
+      const size_t j = Ac * tDof + s + i;
+      Dn[j] = c1 * Yn[j] - c2 * Ad[Ac * 3 + i] + Do[j];
+      Ad[Ac * 3 + i] = Yn[j];
+    }
+  }
+}
+
+// USTRUCTR on the first Newton iteration: Rd = amg Ad - Yg(velocity),
+// R(:, a) -= ami sum_j Kd(:, j) Rd(col j)
+__global__ void k_ust_rd(int nNo, int tDof, int s, double amg, const double *__restrict__ Ad,
+                         const double *__restrict__ Yg, double *__restrict__ Rd) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 3 * nNo; t += gridDim.x * blockDim.x) {
+    const int a = t / 3, i = t - 3 * a;
+    Rd[t] = amg * Ad[t] - Yg[(size_t)a * tDof + s + i];
+  }
+}
+__global__ void k_ust_kdrd(int nNo, const int *__restrict__ rowPtr, const int *__restrict__ colPtr,
+                           const double *__restrict__ Kd, const double *__restrict__ Rd, double ami,
+                           double *__restrict__ R) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x) {
+    double KU[4] = {0, 0, 0, 0};
+    for (int j = rowPtr[a]; j < rowPtr[a + 1]; j++) {
+      const size_t c = colPtr[j];
+      const double *kd = Kd + (size_t)j * 12;
+      const double r0 = Rd[c * 3], r1 = Rd[c * 3 + 1], r2 = Rd[c * 3 + 2];
+#pragma unroll
+      for (int r = 0; r < 4; r++) KU[r] += kd[3 * r] * r0 + kd[3 * r + 1] * r1 + kd[3 * r + 2] * r2;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) R[(size_t)a * 4 + r] -= ami * KU[r];
+  }
+}
+
+// PICC for ustruct (Code/Source/svFSI/PIC.f:185-196): An -= R, Yn -= R
+// gam dt; dU = Rd / am + R(1:3) af gam dt / am, Ad -= dU, Dn -= dU gam dt
+__global__ void k_picc_ust(int nNo, int tDof, int s, double c1, double c3, double c4,
+                           const double *__restrict__ R, const double *__restrict__ Rd,
+                           double *__restrict__ An, double *__restrict__ Yn,
+                           double *__restrict__ Dn, double *__restrict__ Ad) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x) {
+    for (int c = 0; c < 4; c++) {
+      const size_t k = (size_t)a * tDof + s + c;
+      const double r = R[(size_t)a * 4 + c];
+      An[k] = An[k] - r;
+      Yn[k] = Yn[k] - r * c1;
+    }
+    for (int i = 0; i < 3; i++) {
+      const double dU = Rd[(size_t)a * 3 + i] * c3 + R[(size_t)a * 4 + i] * c4;
+      Ad[(size_t)a * 3 + i] = Ad[(size_t)a * 3 + i] - dU;
+      const size_t k = (size_t)a * tDof + s + i;
+      Dn[k] = Dn[k] - dU * c1;
+    }
+  }
+}
+
 // Aliev-Panfilov right-hand side (AP_GETF, Code/Source/svFSI/CEPMOD_AP.f:
 // 255-267) with the parameters of PARAMS_AP.f:53-86, in precision T.
 template <class T>
@@ -385,6 +461,21 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
   if (p->eparam && (rc = mesh_set_eparam(mesh, p->eparam)) != GSLS_OK) {
     delete eq;
     return rc;
+  }
+  if (p->phys == GSLS_PHYS_USTRUCT) {
+    if (p->dof != 4) {
+      delete eq;
+      return GSLS_ERR_ARG;
+    }
+    eq->ust = true;
+    if ((rc = eq->Ad.alloc(sizeof(double) * 3 * (size_t)eq->nNo)) != GSLS_OK ||
+        (rc = eq->Rd.alloc(sizeof(double) * 3 * (size_t)eq->nNo)) != GSLS_OK ||
+        (rc = eq->Kd.alloc(sizeof(double) * 12 * (size_t)eq->nnz)) != GSLS_OK) {
+      delete eq;
+      return rc;
+    }
+    cudaMemsetAsync(eq->Ad.p, 0, sizeof(double) * 3 * (size_t)eq->nNo, eq->lhs->stream);
+    cudaMemsetAsync(eq->Rd.p, 0, sizeof(double) * 3 * (size_t)eq->nNo, eq->lhs->stream);
   }
   cudaEventCreate(&eq->e0);
   cudaEventCreate(&eq->e1);
@@ -678,6 +769,10 @@ static int restart_fields(const gsls_eq *eq, int stamp[7], size_t *nstate) {
 
 int gsls_eq_write_restart(gsls_eq *eq, const char *path, int cTS, double cpu_time) {
   if (!eq || !path) return GSLS_ERR_ARG;
+  if (eq->ust) {
+    set_error("restart: the USTRUCT record (with Ad, INITIALIZE.f:158) is not built");
+    return GSLS_ERR_UNSUPPORTED;
+  }
   int stamp[7];
   size_t ns;
   restart_fields(eq, stamp, &ns);
@@ -711,6 +806,10 @@ int gsls_eq_write_restart(gsls_eq *eq, const char *path, int cTS, double cpu_tim
 
 int gsls_eq_read_restart(gsls_eq *eq, const char *path, int *cTS, double *cpu_time) {
   if (!eq || !path) return GSLS_ERR_ARG;
+  if (eq->ust) {
+    set_error("restart: the USTRUCT record (with Ad, INITIALIZE.f:158) is not built");
+    return GSLS_ERR_UNSUPPORTED;
+  }
   int stamp[7], ts[7], c = 0;
   size_t ns;
   restart_fields(eq, stamp, &ns);
@@ -845,12 +944,22 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
   k_picp<<<nblk(nr), kT, 0, st>>>(nNo, tD, p.s, dof, coef, eq->dFlag ? 1 : 0, p.dt, c2p, Ao, Yo,
                                   Do, An, Yn, Dn);
   GSLS_CHECK_LAUNCH();
+  if (eq->ust) {  // Ad = Ad (gam - 1)/gam, Dn = Do (PIC.f:111-116)
+    k_scale<<<nblk(3 * (size_t)nNo), kT, 0, st>>>(3 * (size_t)nNo, eq->Ad.as<double>(), coef);
+    GSLS_CHECK_LAUNCH();
+  }
   for (auto *d : eq->dirs) {
     if (d->n == 0) continue;
     k_setbcdir<<<nblk(d->n), kT, 0, st>>>(d->n, d->nodes.as<int>(), d->gx.as<double>(),
                                           d->nV.as<double>(), d->g, d->mask, tD, p.s, dof, An,
                                           Yn);
     GSLS_CHECK_LAUNCH();
+    if (eq->ust) {
+      k_ust_dir<<<nblk(d->n), kT, 0, st>>>(d->n, d->nodes.as<int>(), d->mask, tD, p.s, Yn, Do,
+                                           Dn, eq->Ad.as<double>(), p.gam * p.dt,
+                                           (p.gam - 1.0) * p.dt);
+      GSLS_CHECK_LAUNCH();
+    }
   }
   GSLS_TRY(lhs_update_faces(lhs, nullptr, nullptr));
   int itr = 0;
@@ -861,7 +970,8 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     k_pici<<<nblk(ns), kT, 0, st>>>(ns, p.am, p.af, Ao, An, Yo, Yn, Do, Dn, Ag, Yg, Dg);
     GSLS_CHECK_LAUNCH();
     cudaEventRecord(eq->e0, st);
-    GSLS_TRY(assemble_dev(eq->mesh, &p, Ag, Yg, Dg, eq->R.as<double>(), eq->Val.p, valp));
+    GSLS_TRY(assemble_dev(eq->mesh, &p, Ag, Yg, Dg, eq->R.as<double>(), eq->Val.p, valp,
+                          eq->ust ? eq->Kd.as<double>() : nullptr));
     if (eq->has_trac) {
       k_axpy1<<<nblk(nr), kT, 0, st>>>(nr, eq->R.as<double>(), eq->Ftrac.as<double>());
       GSLS_CHECK_LAUNCH();
@@ -893,6 +1003,20 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
         GSLS_CHECK_LAUNCH();
       }
     }
+    if (eq->ust) {
+      // USTRUCTR (after the boundary terms, as MAIN.f:166 calls it)
+      if (itr == 1) {
+        k_ust_rd<<<nblk(3 * (size_t)nNo), kT, 0, st>>>(nNo, tD, p.s, (p.gam - p.am) / (p.gam - 1.0),
+                                                       eq->Ad.as<double>(), Yg, eq->Rd.as<double>());
+        GSLS_CHECK_LAUNCH();
+        k_ust_kdrd<<<nblk(nNo), kT, 0, st>>>(nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(),
+                                             eq->Kd.as<double>(), eq->Rd.as<double>(), 1.0 / p.am,
+                                             eq->R.as<double>());
+        GSLS_CHECK_LAUNCH();
+      } else {
+        GSLS_CUDA(cudaMemsetAsync(eq->Rd.p, 0, sizeof(double) * 3 * (size_t)nNo, st));
+      }
+    }
     cudaEventRecord(eq->e1, st);
     auto t0 = std::chrono::steady_clock::now();
     int rc = solve_dev(lhs, &eq->ls, dof, eq->R.as<double>(), eq->Val.p, valp, eq->sv.prec, true);
@@ -905,8 +1029,13 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     info->ls_itr_total += eq->ls.RI.itr;
     info->last_suc = eq->ls.RI.suc;
     // PICC
-    k_picc<<<nblk(nr), kT, 0, st>>>(nNo, tD, p.s, dof, p.gam * p.dt, p.beta * p.dt * p.dt,
-                                    eq->R.as<double>(), An, Yn, Dn);
+    if (eq->ust)
+      k_picc_ust<<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, p.gam * p.dt, 1.0 / p.am,
+                                           p.af * p.gam * p.dt / p.am, eq->R.as<double>(),
+                                           eq->Rd.as<double>(), An, Yn, Dn, eq->Ad.as<double>());
+    else
+      k_picc<<<nblk(nr), kT, 0, st>>>(nNo, tD, p.s, dof, p.gam * p.dt, p.beta * p.dt * p.dt,
+                                      eq->R.as<double>(), An, Yn, Dn);
     GSLS_CHECK_LAUNCH();
     // Newton test, Code/Source/svFSI/PIC.f:263-275
     double iN = eq->ls.RI.iNorm;
@@ -934,7 +1063,7 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
   }
   // Ao = An, Yo = Yn and, for equations with displacement, Do = Dn
   // (Code/Source/svFSI/MAIN.f:277-279): swap the buffers
-  for (int k = 0; k < (eq->dFlag ? 3 : 2); k++) {
+  for (int k = 0; k < ((eq->dFlag || eq->ust) ? 3 : 2); k++) {
     std::swap(eq->st[k].p, eq->st[k + 3].p);
     std::swap(eq->st[k].bytes, eq->st[k + 3].bytes);
   }
