@@ -80,9 +80,6 @@ struct KrylovScalars {
   int itr;    // completed iterations
   int mItr;
   int suc;
-  // interleaved-direction CG: the next SpMV takes P as stored (set at the
-  // switch from the CSR batch, cleared by the update kernel)
-  int rp_first, rp_pad;
   // GMRES
   double h_norm;
   double pad1[3];
@@ -120,11 +117,10 @@ struct GraphKey {
   bool fused;
   const void *part, *scal, *w;  // workspace buffers baked into the graph
   const void *sval;             // sliced copy of the matrix (null: CSR SpMV)
-  const void *rp = nullptr;     // interleaved (R, P) buffer (null: separate vectors)
   bool operator==(const GraphKey &o) const {
     return D == o.D && vsz == o.vsz && xsz == o.xsz && val == o.val && x == o.x &&
            batch == o.batch && nNo == o.nNo && tma == o.tma && fused == o.fused &&
-           part == o.part && scal == o.scal && w == o.w && sval == o.sval && rp == o.rp;
+           part == o.part && scal == o.scal && w == o.w && sval == o.sval;
   }
 };
 
@@ -148,7 +144,6 @@ struct Workspace {
   DevBuf ticket;      // unsigned[8]
   DevBuf scal;        // KrylovScalars
   DevBuf vec[6];      // Krylov work vectors (X, P, KP, R32...)
-  DevBuf rp[2];       // interleaved (R, P) node pairs of the sliced CG (FP32, D = 3)
   DevBuf W;           // diag preconditioner (double dof x nNo)
   DevBuf W2;          // RCS second scaling
   DevBuf mask;        // Dirichlet mask (double dof x nNo)

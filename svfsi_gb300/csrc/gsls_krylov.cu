@@ -463,95 +463,6 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_update(size_t n, CgVecs v
   }
 }
 
-// The update kernel of the interleaved-direction path (k_cg_spmv_sell_rp):
-// the same arithmetic, element order and reduction as k_cg_update (FP32, 3
-// components padded to 4), with R read from RP[k mod 2], the direction P_k
-// from RP[(k+1) mod 2] (written by the SpMV) and R_{k+1} written into
-// RP[(k+1) mod 2]; clears rp_first.
-__global__ void __launch_bounds__(kUpdThreads, 2) k_cg_update_rp(size_t n, CgRp v,
-                                                              KrylovScalars *S,
-                                                              double *partials,
-                                                              unsigned *ticket) {
-  cudaGridDependencySynchronize();
-  __shared__ double sh[32];
-  __shared__ float sha[32];
-  const int par = S->itr & 1;
-  const float4 *__restrict__ cur = reinterpret_cast<const float4 *>(v.RP[par]);
-  float4 *__restrict__ nxt = reinterpret_cast<float4 *>(v.RP[par ^ 1]);
-  float4 *__restrict__ X4 = reinterpret_cast<float4 *>(v.X);
-  const float4 *__restrict__ K4 = reinterpret_cast<const float4 *>(v.KP);
-  const size_t n4 = n / 4, t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t nt = (size_t)gridDim.x * blockDim.x;
-  float4 xa = make_float4(0.f, 0.f, 0.f, 0.f), ra = xa, pa = xa, qa = xa;
-  if (t0 < n4) {
-    xa = X4[t0];
-    ra = cur[2 * t0];
-    pa = nxt[2 * t0 + 1];
-    qa = K4[t0];
-  }
-  if (*(volatile int *)&S->done) return;
-  const float alpha = float(S->alpha);
-  float acc = 0.f;
-  for (size_t k = t0; k < n4; k += nt) {
-    float4 x, r, p, q;
-    if (k == t0) {
-      x = xa;
-      r = ra;
-      p = pa;
-      q = qa;
-    } else {
-      x = X4[k];
-      r = cur[2 * k];
-      p = nxt[2 * k + 1];
-      q = K4[k];
-    }
-    x.x = fmaf(alpha, p.x, x.x);
-    x.y = fmaf(alpha, p.y, x.y);
-    x.z = fmaf(alpha, p.z, x.z);
-    x.w = fmaf(alpha, p.w, x.w);
-    r.x = fmaf(-alpha, q.x, r.x);
-    r.y = fmaf(-alpha, q.y, r.y);
-    r.z = fmaf(-alpha, q.z, r.z);
-    r.w = fmaf(-alpha, q.w, r.w);
-    X4[k] = x;
-    nxt[2 * k] = r;
-    acc = fmaf(r.x, r.x, acc);
-    acc = fmaf(r.y, r.y, acc);
-    acc = fmaf(r.z, r.z, acc);
-    acc = fmaf(r.w, r.w, acc);
-  }
-  const float bsa = block_sum_t<float>(acc, sha);
-  double bs = double(bsa);
-  double tot;
-  if (grid_reduce_last1<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
-    S->err = tot;
-    S->beta = tot / S->errO;
-    S->itr += 1;
-    S->rp_first = 0;
-    if (!isfinite(tot))
-      S->done = 3;
-    else if (S->itr >= S->mItr)
-      S->done = 2;
-    else if (S->err < S->eps) {
-      S->done = 1;
-      S->suc = 1;
-    }
-  }
-}
-
-// Switch to the interleaved path after the CSR batch: RP[itr mod 2] =
-// (R, P) with P the direction the batch's last direction kernel formed,
-// which the next SpMV takes as stored (rp_first).
-__global__ void k_rp_init(int nNo, const float4 *__restrict__ R, const float4 *__restrict__ P,
-                          CgRp v, KrylovScalars *S) {
-  float4 *cur = reinterpret_cast<float4 *>(v.RP[S->itr & 1]);
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x) {
-    cur[2 * (size_t)a] = R[a];
-    cur[2 * (size_t)a + 1] = P[a];
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) S->rp_first = 1;
-}
-
 // P = R + beta P (the reference's OMPSUMS/OMPMULS pair, CGRAD.f:172-175),
 // non-fused mode; vectors are L2-resident between the CG kernels.
 template <class XT>
@@ -937,8 +848,7 @@ static int sell_pack(gsls_lhs *lhs, const VT *Val, SellArgs &sa) {
 template <int D, class VT, class XT, bool FUSED>
 static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter, bool prof,
                       int ev_base, const TmaTiles *tt = nullptr, int tma_smem = 0,
-                      int tma_grid = 0, const SellArgs *sa = nullptr,
-                      const CgRp *rp = nullptr) {
+                      int tma_grid = 0, const SellArgs *sa = nullptr) {
   cudaStream_t st = lhs->stream;
   Workspace &ws = lhs->ws;
   const int nNo = lhs->nNo;
@@ -971,13 +881,6 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
     if (tt) {
       k_cg_spmv_tma<D, VT, XT, kTmaWarps, FUSED><<<tma_grid, kTmaWarps * 32, tma_smem, st>>>(
           nNo, lhs->d_rowPtr.as<int>(), lhs->d_colPtr.as<int>(), Val, v, S, part, tk, *tt);
-    } else if (sa && !FUSED && rp) {
-      if constexpr (D == 3 && sizeof(XT) == 4) {
-        static const int Grp = resident_grid(k_cg_spmv_sell_rp<VT, SU>, 1 << 30);
-        cfg.gridDim = dim3(Grp < lhs->grid ? Grp : lhs->grid);
-        cfg.blockDim = dim3(kThreads);
-        GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_spmv_sell_rp<VT, SU>, *sa, *rp, S, part, tk, zz));
-      }
     } else if (sa && !FUSED) {
       cfg.gridDim = dim3(Gsl < lhs->grid ? Gsl : lhs->grid);
       cfg.blockDim = dim3(kThreads);
@@ -995,13 +898,10 @@ static int cg_enqueue(gsls_lhs *lhs, const VT *Val, const CgVecs &v, int n_iter,
     if (prof) cudaEventRecord(prof_event(ev_base + 4 * b + 1), st);
     cfg.gridDim = dim3(G2);
     cfg.blockDim = dim3(kUpdThreads);
-    if (rp && sa)
-      GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_update_rp, nv, *rp, S, part, tk));
-    else
-      GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_update<XT, FUSED>, nv, v, S, part, tk));
+    GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_update<XT, FUSED>, nv, v, S, part, tk));
     GSLS_CHECK_LAUNCH();
     if (prof) cudaEventRecord(prof_event(ev_base + 4 * b + 2), st);
-    if (!FUSED && !(rp && sa)) {
+    if (!FUSED) {
       cfg.gridDim = dim3(G3);
       GSLS_CUDA(cudaLaunchKernelEx(&cfg, k_cg_pupdate<XT>, nv, v, (const KrylovScalars *)S));
       GSLS_CHECK_LAUNCH();
@@ -1053,23 +953,13 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   const bool sell_ok = want_sell && !FUSED && !use_tma;
   SellArgs sa{};
   bool sell_on = false;
-  // interleaved-direction SpMV on the sliced copy (FP32 3-blocks; bitwise
-  // the separate-kernel path; GSLS_CG_RP=0 keeps the direction kernel)
-  static const bool want_rp = [] {
-    const char *e = getenv("GSLS_CG_RP");
-    return !(e && strcmp(e, "0") == 0);
-  }();
-  const bool rp_ok = want_rp && sell_ok && D == 3 && sizeof(XT) == 4;
-  bool rp_on = false;
-  CgRp rpv{};
   // CUDA graph of B iterations, cached per (D, types, Val, workspace,
   // layout); one slot for the CSR batch and one for the sliced batch
   auto graph_for = [&](bool sl, cudaGraphExec_t *&ge) -> int {
     cudaGraphExec_t &gx = sl ? ws.cg_graph_s : ws.cg_graph;
     GraphKey &gk = sl ? ws.cg_key_s : ws.cg_key;
     GraphKey key{D,  (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma,
-                 FUSED, ws.partials.p, ws.scal.p, ws.Wf.p, sl ? sa.sval : nullptr,
-                 (sl && rp_on) ? ws.rp[0].p : nullptr};
+                 FUSED, ws.partials.p, ws.scal.p, ws.Wf.p, sl ? sa.sval : nullptr};
     ge = &gx;
     if (gx && gk == key) return GSLS_OK;
     if (gx) {
@@ -1079,7 +969,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
     cudaGraph_t g;
     GSLS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     int rc = cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, false, 0, ttp, tsmem, tgrid,
-                                          sl ? &sa : nullptr, (sl && rp_on) ? &rpv : nullptr);
+                                          sl ? &sa : nullptr);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc != GSLS_OK) return rc;
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
@@ -1095,31 +985,16 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
       GSLS_TRY(sell_pack<D, VT>(lhs, Val, sa));
       count_launch();
       sell_on = true;
-      if (rp_ok) {
-        const size_t rb = sizeof(float) * 8 * (size_t)nNo;
-        for (int k = 0; k < 2; k++) {
-          GSLS_TRY(ws.rp[k].alloc(rb));
-          GSLS_CUDA(cudaMemsetAsync(ws.rp[k].p, 0, rb, st));
-        }
-        rpv.X = (float *)v.X;
-        rpv.KP = (float *)v.KP;
-        rpv.RP[0] = ws.rp[0].as<float>();
-        rpv.RP[1] = ws.rp[1].as<float>();
-        k_rp_init<<<G, kThreads, 0, st>>>(nNo, (const float4 *)v.R, (const float4 *)v.P0, rpv, S);
-        GSLS_CHECK_LAUNCH();
-        rp_on = true;
-      }
     }
     nbatch++;
     if (prof) {
       GSLS_TRY(cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, true, 0, ttp, tsmem, tgrid,
-                                            sell_on ? &sa : nullptr,
-                                            (sell_on && rp_on) ? &rpv : nullptr));
+                                            sell_on ? &sa : nullptr));
     } else {
       cudaGraphExec_t *ge = nullptr;
       GSLS_TRY(graph_for(sell_on, ge));
       GSLS_CUDA(cudaGraphLaunch(*ge, st));
-      count_launch_n(((FUSED || (sell_on && rp_on)) ? 2 : 3) * B - 1);
+      count_launch_n((FUSED ? 2 : 3) * B - 1);
     }
     GSLS_TRY(wait_scalars(lhs));
     if (prof) {

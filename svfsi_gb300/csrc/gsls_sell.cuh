@@ -127,113 +127,4 @@ __global__ void __launch_bounds__(kThreads, sizeof(VT) == 4 ? (U > 4 ? 4 : 6) : 
   }
 }
 
-// The same SpMV with the direction update of CGRAD.f:172-175 (P = R +
-// beta P) taken into the gathers, for FP32 vectors of 3-blocks: R and the
-// previous direction of a node sit side by side (RP: float4 R, float4 P,
-// one 32-byte sector), so the gather of the new direction at a column is
-// one sector, as the gather of P alone was, and the separate direction
-// kernel goes away.  Iteration k reads RP[k mod 2] = (R_k, P_{k-1}) and
-// writes its own rows' P_k into RP[(k+1) mod 2]'s P slots (no block
-// gathers from that buffer during the launch); the update kernel then
-// fills the R slots of RP[(k+1) mod 2].  Every P_k value is fmaf(beta,
-// P_{k-1}, R_k), the direction kernel's expression, so the iterates are
-// the separate-kernel path's bit for bit.  rp_first: the first launch
-// after the CSR batch takes P as stored (it already holds P_k).
-struct CgRp {
-  float *X, *KP;
-  float *RP[2];
-};
-template <class VT, int U>
-__global__ void __launch_bounds__(kThreads, U > 4 ? 4 : 6)
-    k_cg_spmv_sell_rp(SellArgs A, CgRp v, KrylovScalars *S, double *partials, unsigned *ticket,
-                      int zz) {
-  cudaGridDependencySynchronize();  // launched with programmatic serialization
-  if (*(volatile int *)&S->done) return;
-  constexpr int D = 3, RPW = 32 / D, DD = D * D, CH = RPW * DD;
-  __shared__ double sh[32];
-  __shared__ float sha[32];
-  const VT *__restrict__ sval = (const VT *)A.sval;
-  const int par = S->itr & 1;
-  const float4 *__restrict__ cur = reinterpret_cast<const float4 *>(v.RP[par]);
-  float *__restrict__ nxt = v.RP[par ^ 1];
-  const bool first = S->rp_first != 0;
-  const float beta = float(S->beta);
-  float *__restrict__ KP = v.KP;
-  const int lane = threadIdx.x & 31, g = lane / D, r = lane - g * D;
-  const bool act = g < RPW;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  float dot = 0.f;
-  const bool rev = zz && (S->itr & 1);
-  auto dir = [&](int col, float out[D]) {
-    const float4 rr = __ldg(cur + 2 * (size_t)col), pp = __ldg(cur + 2 * (size_t)col + 1);
-    if (first) {
-      out[0] = pp.x;
-      out[1] = pp.y;
-      out[2] = pp.z;
-    } else {
-      out[0] = fmaf(beta, pp.x, rr.x);
-      out[1] = fmaf(beta, pp.y, rr.y);
-      out[2] = fmaf(beta, pp.z, rr.z);
-    }
-  };
-  for (int s0 = warp; s0 < A.nS; s0 += nwarps) {
-    const int s = rev ? A.nS - 1 - s0 : s0;
-    const int t0 = __ldg(A.off + s), t1 = __ldg(A.off + s + 1);
-    const int row = act ? __ldg(A.slotRow + s * RPW + g) : -1;
-    float acc0 = 0.f, acc1 = 0.f;
-    int cn[U];
-#pragma unroll
-    for (int u = 0; u < U; u++)
-      cn[u] = (act && t0 + u < t1) ? __ldg(A.scol + (size_t)(t0 + u) * RPW + g) : -1;
-    for (int t = t0; t < t1; t += U) {
-      int cc[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        cc[u] = cn[u];
-        cn[u] = (act && t + U + u < t1) ? __ldg(A.scol + (size_t)(t + U + u) * RPW + g) : -1;
-      }
-      float a[U][D], xg[U][D];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        if (cc[u] >= 0) {
-          const VT *p = sval + (size_t)(t + u) * CH + g * D + r;
-#pragma unroll
-          for (int c = 0; c < D; c++) a[u][c] = float(__ldg(p + c * (RPW * D)));
-          dir(cc[u], xg[u]);
-        } else {
-#pragma unroll
-          for (int c = 0; c < D; c++) a[u][c] = xg[u][c] = 0.f;
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; u++)
-#pragma unroll
-        for (int c = 0; c < D; c++) {
-          if (u & 1)
-            acc1 = fmaf(a[u][c], xg[u][c], acc1);
-          else
-            acc0 = fmaf(a[u][c], xg[u][c], acc0);
-        }
-    }
-    if (row >= 0) {
-      const float y = acc0 + acc1;
-      const float *cr = reinterpret_cast<const float *>(cur) + (size_t)row * 8;
-      const float pk = first ? cr[4 + r] : fmaf(beta, cr[4 + r], cr[r]);
-      nxt[(size_t)row * 8 + 4 + r] = pk;
-      KP[(size_t)row * 4 + r] = y;
-      dot = fmaf(pk, y, dot);
-    }
-  }
-  const float bsa = block_sum_t<float>(dot, sha);
-  double bs = double(bsa);
-  double tot;
-  if (grid_reduce_last1<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) {
-    S->errO = S->err;
-    S->dot = tot;
-    S->alpha = S->errO / tot;
-    if (!isfinite(S->alpha)) S->done = 3;
-  }
-}
-
 }  // namespace gsls

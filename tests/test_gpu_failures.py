@@ -9,6 +9,8 @@ RI%suc = .FALSE. (CGRAD.f:146-182) and takes W = 1 for a zero diagonal
 entry in PRECONDDIAG (PRECOND.f:104-109); the library returns a status
 instead of stopping (include/gsls.h).
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -173,12 +175,14 @@ def test_inconsistent_nnz_is_rejected(gsls, orc):
     _solve_ok_after(gsls, orc, q, R0, V0)
 
 
-def test_grid_barrier_timeout_returns_cleanly(gsls, orc):
+@pytest.mark.parametrize("mixed", [False, True])
+def test_grid_barrier_timeout_returns_cleanly(gsls, orc, mixed):
     """The persistent Schur-complement CG of the NS solver waits on a grid
-    barrier between its phases.  With the poll limit cut to 2 the waits run
-    out on a healthy launch: every block leaves, the solve returns
-    GSLS_ERR_CUDA, and with the default limit back the same solve matches
-    the oracle (the context is intact)."""
+    barrier between its phases (FP64 and FP32 inner vectors).  With the
+    poll limit cut to 2 the waits run out on a healthy launch: every block
+    leaves, the solve returns GSLS_ERR_CUDA, and with the default limit back
+    the same solve repeats the result of a solve made before the failure bit
+    for bit and matches the oracle (the context is intact)."""
     p = problems.fluid_cylinder(h=0.1, nsteps=1)
     rng = np.random.default_rng(3)
     Y = np.zeros((p.nNo, 4))
@@ -195,13 +199,24 @@ def test_grid_barrier_timeout_returns_cleanly(gsls, orc):
             fsils.FSILS_BC_CREATE(lhs, k + 1, nodes.size, 3, fsils.BC_TYPE_DIR, nodes + 1,
                                   np.zeros((nodes.size, 3)))
         ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_NS, dimKry=100)
-        R, Val = R0.copy(), V0.copy()
         try:
-            fsils.FSILS_SOLVE(lhs, ls, 4, R, Val, fsils.PRECOND_RCS)
+            if mixed:
+                import torch
+                dR = torch.tensor(R0, dtype=torch.float64, device="cuda")
+                dV = torch.tensor(V0, dtype=torch.float32, device="cuda")
+                torch.cuda.synchronize()
+                _lib.check(gsls.gsls_solve_dev(lhs.h, C.byref(ls), 4, C.c_void_p(dR.data_ptr()),
+                                               C.c_void_p(dV.data_ptr()), _lib.PREC_MIXED,
+                                               fsils.PRECOND_RCS, None, None), "gsls_solve_dev")
+                R = dR.cpu().numpy()
+            else:
+                R, Val = R0.copy(), V0.copy()
+                fsils.FSILS_SOLVE(lhs, ls, 4, R, Val, fsils.PRECOND_RCS)
         finally:
             lhs.free()
         return ls, R
 
+    ls0, R_before = solve()
     try:
         _lib.check(gsls.gsls_set_wait_limit(2), "gsls_set_wait_limit")
         with pytest.raises(_lib.GslsError) as exc:
@@ -217,5 +232,12 @@ def test_grid_barrier_timeout_returns_cleanly(gsls, orc):
     ols = orc.ls_create(orc.LS_TYPE_NS, sD=100)
     Ro, Vo = R0.copy(), V0.copy()
     s.solve(ols, 4, Ro, Vo, orc.PRECOND_RCS)
-    assert ls.RI.suc == ols.RI.suc and ls.RI.itr == ols.RI.itr
-    assert rel(R, Ro) < 1e-8
+    # the solve after the failure repeats the one before it bit for bit
+    assert np.array_equal(R, R_before) and ls.RI.itr == ls0.RI.itr
+    if mixed:
+        # FP32 inner solves: the outer NS iteration stops within one
+        # iteration of the oracle's
+        assert ls.RI.suc == ols.RI.suc and abs(ls.RI.itr - ols.RI.itr) <= 1
+    else:
+        assert ls.RI.suc == ols.RI.suc and ls.RI.itr == ols.RI.itr
+        assert rel(R, Ro) < 1e-8

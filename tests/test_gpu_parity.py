@@ -459,32 +459,3 @@ def test_next_equation_on_the_same_lhs_claims_the_freed_faces(gsls):
             eq3.add_dirichlet(d.nodes, d.g, d.gx, d.mask, d.nV)
     eq3.free()
     eq2.free()
-
-
-def test_interleaved_direction_cg_is_bitwise_the_separate_kernel_path(gsls):
-    """The sliced CG SpMV that forms the direction P = R + beta P in its
-    gathers (interleaved R/P, FP32 3-blocks) gives the same bits as the path
-    with the separate direction kernel (GSLS_CG_RP=0): two mixed-precision
-    steps of a beam, in two fresh processes."""
-    import os
-    import subprocess
-    import sys
-    from pathlib import Path
-    root = Path(__file__).resolve().parents[1]
-    code = ("import hashlib, numpy as np\n"
-            "from svfsi_gb300 import _lib, fsils, problems\n"
-            "L = _lib.load(); _lib.check(L.gsls_init(0))\n"
-            "p = problems.struct_beam(24, 6, 6, nsteps=2)\n"
-            "lhs, mesh, eq = problems.build_equation(p, precision=fsils.PREC_MIXED)\n"
-            "its = [eq.step().ls_itr_total for _ in range(2)]\n"
-            "A, Y, D = eq.get_state()\n"
-            "print(its, hashlib.sha256(np.ascontiguousarray(D).tobytes()).hexdigest())\n")
-    outs = []
-    for rp in ("1", "0"):
-        env = dict(os.environ, GSLS_CG_RP=rp, PYTHONPATH=str(root))
-        r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
-                           text=True, timeout=600)
-        assert r.returncode == 0, r.stderr[-2000:]
-        outs.append(r.stdout.strip().splitlines()[-1])
-    assert outs[0] == outs[1], outs
-    assert int(outs[0].split("]")[0].split(",")[0].strip("[")) > 16   # the sliced path ran
