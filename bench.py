@@ -402,15 +402,14 @@ def run_gsls(args):
     for _ in range(W):
         eq.set_state(*hv)
         eq.step()
-        hv[0][:], hv[1][:], hv[2][:] = eq.get_state()
+        eq.get_state(out=hv)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(K):
         eq.set_state(*hv)
         eq.step()
-        Ao, Yo, Do = eq.get_state()
-        hv[0][:], hv[1][:], hv[2][:] = Ao, Yo, Do
+        eq.get_state(out=hv)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0) / K
     eq.free()
@@ -587,11 +586,13 @@ def config_legs(L, problems, fsils, torch):
     (h 0.027, 1,225,440 tets).  For each, the oracle's first n_par implicit
     steps from the initial state beside the FP64 and mixed GPU steps (error
     of each against the oracle, Newton counts), then n_time more GPU steps
-    per precision timed with CUDA events on the library's stream."""
+    per precision timed with CUDA events on the library's stream.  The slab
+    and the cylinder run their configured step counts (5,000 and 20 steps)
+    per precision; the heat cube its 10 steps twice."""
     threads = os.cpu_count() or 1
     legs = [("heats_cube_20", lambda: problems.heats_cube(20, nsteps=20), 10, 10),
-            ("cep_slab_135x135x27", lambda: problems.cep_slab(nsteps=100, A=-52.0), 20, 50),
-            ("fluid_cylinder_h0.027", lambda: problems.fluid_cylinder(h=0.027, nsteps=4), 1, 3)]
+            ("cep_slab_135x135x27", lambda: problems.cep_slab(nsteps=5000, A=-52.0), 20, 4980),
+            ("fluid_cylinder_h0.027", lambda: problems.fluid_cylinder(h=0.027, nsteps=20), 1, 19)]
     res = {}
     for name, make, n_par, n_time in legs:
         p = make()

@@ -13,8 +13,12 @@
 // block by block: for each node pair (a,b) the 16 entries of lK and the 12
 // of lKd (the displacement tangent, USTRUCT_DOASSEM's Kd) are summed over
 // the points and scattered, so no 4x4x16 element array is held.  Residual
-// and both tangents are formed in FP64; Val is written in VT, Kd in FP64
-// (it enters USTRUCTR's FP64 residual correction).
+// and the kinematics are formed in FP64; the 16 blocks of both tangents in
+// the tangent's precision VT (FP64 for the drop-in; FP32 for the mixed path,
+// whose FP32 tangent needs no FP64 arithmetic -- the FP64 form kept the
+// FP64 pipe 88 % busy).  Kd is stored in FP64 either way: it enters
+// USTRUCTR's FP64 residual correction on the first Newton iteration only,
+// whose error the later iterations (Rd = 0, exact FP64 residual) remove.
 #pragma once
 
 namespace gsls {
@@ -264,129 +268,178 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_ustruct(AsmArgs A, double *
     for (int i = 0; i < 4; i++) A.R[(size_t)n4[a] * 4 + i] += r[i];
   }
 
-  // ---- tangents, block by block
+  // ---- tangents, block by block, in the tangent's precision
+  using TT = VT;
+  TT tN[4][4], tNx[3][4], tNxFi[3][4], tDdNx[3][4], tVxNx[3][4];
+  TT tF[3][3], tSiso[3][3], tVxFi[3][3], tDm[6][6];
+  TT tro[4], tbt[4], tdro[4], tdbt[4], tvd[4][3], tpdg[4], tRc[4], trCl[4], trM[4][3];
+#pragma unroll
+  for (int g = 0; g < 4; g++) {
+#pragma unroll
+    for (int a = 0; a < 4; a++) tN[g][a] = TT(c_rule.N[g][a]);
+    tro[g] = TT(vol[g].ro);
+    tbt[g] = TT(vol[g].bt);
+    tdro[g] = TT(vol[g].dro);
+    tdbt[g] = TT(vol[g].dbt);
+    tpdg[g] = TT(pdg[g]);
+    tRc[g] = TT(rC[g]);
+    trCl[g] = TT(rCl[g]);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      tvd[g][i] = TT(vd[g][i]);
+      trM[g][i] = TT(rM[g][i]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      tNx[i][a] = TT(Nx[i][a]);
+      tNxFi[i][a] = TT(NxFi[i][a]);
+      tDdNx[i][a] = TT(DdNx[i][a]);
+      tVxNx[i][a] = TT(VxNx[i][a]);
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      tF[i][j] = TT(F[i][j]);
+      tSiso[i][j] = TT(Siso[i][j]);
+      tVxFi[i][j] = TT(VxFi[i][j]);
+    }
+  }
+#pragma unroll
+  for (int I = 0; I < 6; I++)
+#pragma unroll
+    for (int K = 0; K < 6; K++) tDm[I][K] = TT(Dm[I][K]);
+  const TT tw = TT(w), tW = TT(W), tJ = TT(J), tmu = TT(mu), tam = TT(am), taf = TT(af);
+  const TT tafm = TT(afm), ttauC = TT(tauC), ttauMc = TT(tauMc);
+  const TT tr13 = TT(r13), tr23 = TT(r23), one = TT(1);
+  TT tPxFi[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) tPxFi[i] = TT(PxFi[i]);
+
   VT *Val = reinterpret_cast<VT *>(A.Val);
   for (int a = 0; a < 4; a++) {
     const int4 m4 = A.map[(size_t)e * 4 + a];
     const int pos[4] = {m4.x, m4.y, m4.z, m4.w};
     for (int b = 0; b < 4; b++) {
-      double k16[16], k12[12];
-      double NxSNx = 0.0;
+      TT k16[16], k12[12];
+      TT NxSNx = TT(0);
 #pragma unroll
       for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int j = 0; j < 3; j++) NxSNx += Nx[i][a] * Siso[i][j] * Nx[j][b];
-      const double NxNx = NxFi[0][a] * NxFi[0][b] + NxFi[1][a] * NxFi[1][b] + NxFi[2][a] * NxFi[2][b];
+        for (int j = 0; j < 3; j++) NxSNx += tNx[i][a] * tSiso[i][j] * tNx[j][b];
+      const TT NxNx = tNxFi[0][a] * tNxFi[0][b] + tNxFi[1][a] * tNxFi[1][b] + tNxFi[2][a] * tNxFi[2][b];
       // point sums that recur below (each includes the weight w)
-      double sRoNN = 0.0, sRo = 0.0, sRcl = 0.0, sRoVdN[3] = {0, 0, 0};
+      TT sRoNN = TT(0), sRo = TT(0), sRcl = TT(0), sRoVdN[3] = {TT(0), TT(0), TT(0)};
 #pragma unroll
       for (int g = 0; g < 4; g++) {
-        const double Na = c_rule.N[g][a], Nb = c_rule.N[g][b];
-        sRoNN += w * vol[g].ro * Na * Nb;
-        sRo += w * vol[g].ro;
-        sRcl += w * rCl[g];
+        const TT Na = tN[g][a], Nb = tN[g][b];
+        sRoNN += tw * tro[g] * Na * Nb;
+        sRo += tw * tro[g];
+        sRcl += tw * trCl[g];
 #pragma unroll
-        for (int r = 0; r < 3; r++) sRoVdN[r] += w * vol[g].ro * vd[g][r] * Na;
+        for (int r = 0; r < 3; r++) sRoVdN[r] += tw * tro[g] * tvd[g][r] * Na;
       }
       // Bm(:, :, a), Bm(:, :, b) and DBm = Dm Bm(:, :, b)
-      double Bb[6][3], Ba[6][3];
+      TT Bb[6][3], Ba[6][3];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        Bb[0][c] = Nx[0][b] * F[c][0];
-        Bb[1][c] = Nx[1][b] * F[c][1];
-        Bb[2][c] = Nx[2][b] * F[c][2];
-        Bb[3][c] = Nx[0][b] * F[c][1] + F[c][0] * Nx[1][b];
-        Bb[4][c] = Nx[1][b] * F[c][2] + F[c][1] * Nx[2][b];
-        Bb[5][c] = Nx[2][b] * F[c][0] + F[c][2] * Nx[0][b];
-        Ba[0][c] = Nx[0][a] * F[c][0];
-        Ba[1][c] = Nx[1][a] * F[c][1];
-        Ba[2][c] = Nx[2][a] * F[c][2];
-        Ba[3][c] = Nx[0][a] * F[c][1] + F[c][0] * Nx[1][a];
-        Ba[4][c] = Nx[1][a] * F[c][2] + F[c][1] * Nx[2][a];
-        Ba[5][c] = Nx[2][a] * F[c][0] + F[c][2] * Nx[0][a];
+        Bb[0][c] = tNx[0][b] * tF[c][0];
+        Bb[1][c] = tNx[1][b] * tF[c][1];
+        Bb[2][c] = tNx[2][b] * tF[c][2];
+        Bb[3][c] = tNx[0][b] * tF[c][1] + tF[c][0] * tNx[1][b];
+        Bb[4][c] = tNx[1][b] * tF[c][2] + tF[c][1] * tNx[2][b];
+        Bb[5][c] = tNx[2][b] * tF[c][0] + tF[c][2] * tNx[0][b];
+        Ba[0][c] = tNx[0][a] * tF[c][0];
+        Ba[1][c] = tNx[1][a] * tF[c][1];
+        Ba[2][c] = tNx[2][a] * tF[c][2];
+        Ba[3][c] = tNx[0][a] * tF[c][1] + tF[c][0] * tNx[1][a];
+        Ba[4][c] = tNx[1][a] * tF[c][2] + tF[c][1] * tNx[2][a];
+        Ba[5][c] = tNx[2][a] * tF[c][0] + tF[c][2] * tNx[0][a];
       }
-      double DBm[6][3];
+      TT DBm[6][3];
 #pragma unroll
       for (int I = 0; I < 6; I++)
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          double s = 0.0;
+          TT sm = TT(0);
 #pragma unroll
-          for (int K = 0; K < 6; K++) s += Dm[I][K] * Bb[K][c];
-          DBm[I][c] = s;
+          for (int K = 0; K < 6; K++) sm += tDm[I][K] * Bb[K][c];
+          DBm[I][c] = sm;
         }
       // momentum rows, USTRUCT3D_M
 #pragma unroll
       for (int r = 0; r < 3; r++)
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          double BtDB = 0.0;
+          TT BtDB = TT(0);
 #pragma unroll
           for (int I = 0; I < 6; I++) BtDB += Ba[I][r] * DBm[I][c];
-          const double T1 = J * sRoVdN[r] * NxFi[c][b];
-          const double T2 = -tauC * J * NxFi[r][a] * VxNx[c][b];
-          const double T3 = (r == c) ? 0.0 : J * sRcl * (NxFi[r][a] * NxFi[c][b] - NxFi[c][a] * NxFi[r][b]);
-          const double Tv = (2.0 * (DdNx[r][a] * NxFi[c][b] - DdNx[r][b] * NxFi[c][a]) -
-                             (NxNx * VxFi[r][c] + NxFi[r][b] * VxNx[c][a] - r23 * NxFi[r][a] * VxNx[c][b])) *
-                            mu * J;
-          const double Ku = af * (T1 + T3 + W * (T2 + Tv + BtDB + ((r == c) ? NxSNx : 0.0)));
+          const TT T1 = tJ * sRoVdN[r] * tNxFi[c][b];
+          const TT T2 = -ttauC * tJ * tNxFi[r][a] * tVxNx[c][b];
+          const TT T3 = (r == c) ? TT(0)
+                                 : tJ * sRcl * (tNxFi[r][a] * tNxFi[c][b] - tNxFi[c][a] * tNxFi[r][b]);
+          const TT Tv = (TT(2) * (tDdNx[r][a] * tNxFi[c][b] - tDdNx[r][b] * tNxFi[c][a]) -
+                         (NxNx * tVxFi[r][c] + tNxFi[r][b] * tVxNx[c][a] -
+                          tr23 * tNxFi[r][a] * tVxNx[c][b])) *
+                        tmu * tJ;
+          const TT Ku = taf * (T1 + T3 + tW * (T2 + Tv + BtDB + ((r == c) ? NxSNx : TT(0))));
           k12[3 * r + c] = Ku;
-          double kv;
+          TT kv;
           if (r == c)
-            kv = am * J * sRoNN + af * J * tauC * sRo * NxFi[r][a] * NxFi[r][b] +
-                 W * af * mu * J * (r13 * NxFi[r][a] * NxFi[r][b] + NxNx);
+            kv = tam * tJ * sRoNN + taf * tJ * ttauC * sRo * tNxFi[r][a] * tNxFi[r][b] +
+                 tW * taf * tmu * tJ * (tr13 * tNxFi[r][a] * tNxFi[r][b] + NxNx);
           else
-            kv = af * J * tauC * sRo * NxFi[r][a] * NxFi[c][b] +
-                 W * af * mu * J * (NxFi[c][a] * NxFi[r][b] - r23 * NxFi[r][a] * NxFi[c][b]);
-          k16[4 * r + c] = kv + afm * Ku;
+            kv = taf * tJ * ttauC * sRo * tNxFi[r][a] * tNxFi[c][b] +
+                 tW * taf * tmu * tJ * (tNxFi[c][a] * tNxFi[r][b] - tr23 * tNxFi[r][a] * tNxFi[c][b]);
+          k16[4 * r + c] = kv + tafm * Ku;
         }
       // dM/dP
 #pragma unroll
       for (int r = 0; r < 3; r++) {
-        double s = 0.0;
+        TT sm = TT(0);
 #pragma unroll
         for (int g = 0; g < 4; g++) {
-          const double T1 = am * tauC * vol[g].bt + af * (tauC * vol[g].dbt * pdg[g] - 1.0);
-          s += w * J * (T1 * NxFi[r][a] * c_rule.N[g][b] +
-                        af * vol[g].dro * vd[g][r] * c_rule.N[g][a] * c_rule.N[g][b]);
+          const TT T1 = tam * ttauC * tbt[g] + taf * (ttauC * tdbt[g] * tpdg[g] - one);
+          sm += tw * tJ * (T1 * tNxFi[r][a] * tN[g][b] + taf * tdro[g] * tvd[g][r] * tN[g][a] * tN[g][b]);
         }
-        k16[4 * r + 3] = s;
+        k16[4 * r + 3] = sm;
       }
       // continuity row, USTRUCT3D_C
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        double Ku = 0.0, kv = 0.0;
+        TT Ku = TT(0), kv = TT(0);
 #pragma unroll
         for (int g = 0; g < 4; g++) {
-          const double Na = c_rule.N[g][a], Nb = c_rule.N[g][b];
-          const double rMNqa = rM[g][0] * NxFi[0][a] + rM[g][1] * NxFi[1][a] + rM[g][2] * NxFi[2][a];
-          const double rMNwb = rM[g][0] * NxFi[0][b] + rM[g][1] * NxFi[1][b] + rM[g][2] * NxFi[2][b];
-          const double T1 = Na * (rC[g] * NxFi[c][b] - VxNx[c][b]);
-          const double T2 = tauMc * (rMNqa * NxFi[c][b] - rMNwb * NxFi[c][a]);
-          const double T3 = -tauMc * NxNx * PxFi[c];
-          Ku += w * af * J * (T1 + T2 + T3);
-          kv += w * J * ((am * tauMc * vol[g].ro) * NxFi[c][a] * Nb + af * Na * NxFi[c][b]);
+          const TT Na = tN[g][a], Nb = tN[g][b];
+          const TT rMNqa = trM[g][0] * tNxFi[0][a] + trM[g][1] * tNxFi[1][a] + trM[g][2] * tNxFi[2][a];
+          const TT rMNwb = trM[g][0] * tNxFi[0][b] + trM[g][1] * tNxFi[1][b] + trM[g][2] * tNxFi[2][b];
+          const TT T1 = Na * (tRc[g] * tNxFi[c][b] - tVxNx[c][b]);
+          const TT T2 = ttauMc * (rMNqa * tNxFi[c][b] - rMNwb * tNxFi[c][a]);
+          const TT T3 = -ttauMc * NxNx * tPxFi[c];
+          Ku += tw * taf * tJ * (T1 + T2 + T3);
+          kv += tw * tJ * ((tam * ttauMc * tro[g]) * tNxFi[c][a] * Nb + taf * Na * tNxFi[c][b]);
         }
         k12[9 + c] = Ku;
-        k16[12 + c] = kv + afm * Ku;
+        k16[12 + c] = kv + tafm * Ku;
       }
       {
-        double s = 0.0;
+        TT sm = TT(0);
 #pragma unroll
         for (int g = 0; g < 4; g++) {
-          const double Na = c_rule.N[g][a], Nb = c_rule.N[g][b];
-          const double T1 = (am * vol[g].bt + af * vol[g].dbt * pdg[g]) * Na * Nb;
-          const double T2 = NxFi[0][a] * vd[g][0] + NxFi[1][a] * vd[g][1] + NxFi[2][a] * vd[g][2];
-          s += w * J * (T1 + af * tauMc * (NxNx + vol[g].dro * T2 * Nb));
+          const TT Na = tN[g][a], Nb = tN[g][b];
+          const TT T1 = (tam * tbt[g] + taf * tdbt[g] * tpdg[g]) * Na * Nb;
+          const TT T2 = tNxFi[0][a] * tvd[g][0] + tNxFi[1][a] * tvd[g][1] + tNxFi[2][a] * tvd[g][2];
+          sm += tw * tJ * (T1 + taf * ttauMc * (NxNx + tdro[g] * T2 * Nb));
         }
-        k16[15] = s;
+        k16[15] = sm;
       }
       VT *dv = Val + (size_t)pos[b] * 16;
 #pragma unroll
       for (int k = 0; k < 16; k++) dv[k] += VT(k16[k]);
       double *dk = Kd + (size_t)pos[b] * 12;
 #pragma unroll
-      for (int k = 0; k < 12; k++) dk[k] += k12[k];
+      for (int k = 0; k < 12; k++) dk[k] += double(k12[k]);
     }
   }
 }

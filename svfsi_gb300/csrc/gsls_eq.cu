@@ -15,7 +15,8 @@
 
 namespace gsls {
 int assemble_dev(gsls_mesh *m, const gsls_eq_params *p, const double *Ag, const double *Yg,
-                 const double *Dg, double *R, void *Val, int val_prec, double *Kd = nullptr);
+                 const double *Dg, double *R, void *Val, int val_prec, double *Kd = nullptr,
+                 LinAsm *la = nullptr);
 int mesh_dRdp(gsls_mesh *m, const gsls_eq_params *p, const double *Yg, const double *Dg,
               const double *lam, double *out, double scale);
 int mesh_mass(gsls_mesh *m, const double *zeros, double *R, double *Val);
@@ -62,6 +63,14 @@ struct gsls_eq {
   gsls::DevBuf Ad, Rd, Kd;
   // CEP cell model
   bool has_cep = false, cep_first = true;
+  // HEATS/CEP operator path: the preconditioned tangent W Val W left in Val
+  // by the last full solve, reused by the next Newton iterations and steps
+  // while its key (operators, coefficients), the lhs's preconditioning
+  // serial (no other solve since) and its Dirichlet mask hold
+  gsls::LinAsm pre_key;
+  bool pre_valid = false;
+  unsigned long long pre_serial = 0;
+  unsigned pre_mask = 0;
   gsls_cep_params cep{};
   gsls::DevBuf Xion;   // double 2 x nNo
   gsls::DevBuf stim;   // int per node
@@ -970,8 +979,23 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     k_pici<<<nblk(ns), kT, 0, st>>>(ns, p.am, p.af, Ao, An, Yo, Yn, Do, Dn, Ag, Yg, Dg);
     GSLS_CHECK_LAUNCH();
     cudaEventRecord(eq->e0, st);
+    LinAsm la;
+    // GSLS_LIN_REUSE=0 rebuilds and rescales the tangent every iteration
+    static const bool reuse_on = [] {
+      const char *e = getenv("GSLS_LIN_REUSE");
+      return !(e && strcmp(e, "0") == 0);
+    }();
+    const bool pre_ok = reuse_on && eq->neus.empty() && eq->sv.prec == GSLS_PRECOND_FSILS;
+    if (pre_ok && eq->pre_valid) {
+      GSLS_TRY(lhs_prepare_ws(lhs, dof));
+      GSLS_TRY(build_dir_mask(lhs, dof));
+      if (lhs->ws.pre_serial == eq->pre_serial && lhs->ws.mask_serial == eq->pre_mask) {
+        la = eq->pre_key;
+        la.skip_val = true;
+      }
+    }
     GSLS_TRY(assemble_dev(eq->mesh, &p, Ag, Yg, Dg, eq->R.as<double>(), eq->Val.p, valp,
-                          eq->ust ? eq->Kd.as<double>() : nullptr));
+                          eq->ust ? eq->Kd.as<double>() : nullptr, &la));
     if (eq->has_trac) {
       k_axpy1<<<nblk(nr), kT, 0, st>>>(nr, eq->R.as<double>(), eq->Ftrac.as<double>());
       GSLS_CHECK_LAUNCH();
@@ -1019,12 +1043,24 @@ int gsls_eq_step(gsls_eq *eq, gsls_step_info *info) {
     }
     cudaEventRecord(eq->e1, st);
     auto t0 = std::chrono::steady_clock::now();
-    int rc = solve_dev(lhs, &eq->ls, dof, eq->R.as<double>(), eq->Val.p, valp, eq->sv.prec, true);
+    const bool prescaled = la.used && la.skipped;
+    int rc = solve_dev(lhs, &eq->ls, dof, eq->R.as<double>(), eq->Val.p, valp, eq->sv.prec, true,
+                       prescaled);
     info->t_solve_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     cudaEventElapsedTime(&ms, eq->e0, eq->e1);
     info->t_assembly_ms += ms;
     if (prof_on()) prof_add("assembly", 1, ms);
-    if (rc != GSLS_OK) return rc;
+    if (rc != GSLS_OK) {
+      eq->pre_valid = false;
+      return rc;
+    }
+    if (la.used && !prescaled && pre_ok) {
+      eq->pre_key = la;
+      eq->pre_key.skip_val = false;
+      eq->pre_valid = true;
+      eq->pre_serial = lhs->ws.pre_serial;
+      eq->pre_mask = lhs->ws.mask_serial;
+    }
     GSLS_TRY(mesh_check_error(eq->mesh));
     info->ls_itr_total += eq->ls.RI.itr;
     info->last_suc = eq->ls.RI.suc;

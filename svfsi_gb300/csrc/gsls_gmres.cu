@@ -6,6 +6,10 @@
 // type (FP32 in mixed mode); Hessenberg matrix, Givens data and every
 // cross-block sum in FP64.  The Arnoldi loop runs device-resident: the
 // Givens kernel sets a device flag and the host polls it once per batch.
+// FP32 basis vectors take the norm of the orthogonalised vector explicitly
+// (k_gm_orth_nrm) instead of the Pythagorean difference |v|^2 - sum h_j^2,
+// which cancels catastrophically in FP32 once the new vector lies nearly in
+// the span of the basis.
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -94,24 +98,92 @@ __global__ void __launch_bounds__(kT) k_gm_spmv(int nNo, const int *__restrict__
   }
 }
 
-// h_j = u_j . v, j = 0..nvec-1; warp w of a block owns j = w, w+8, ...; one
-// FP64 partial per (j, block).
+// 16-byte vectors of the Krylov type: four FP32 or two FP64 values.  Basis
+// vectors start on 32-element boundaries (ld), so every vector's 16-byte
+// groups are aligned; the n % L tail is handled element by element.
+template <class XT> struct Vec16;
+template <> struct Vec16<float> {
+  using T = float4;
+  static constexpr int L = 4;
+  static __device__ __forceinline__ float dot(const float4 a, const float4 b, float acc) {
+    acc = fmaf(a.x, b.x, acc);
+    acc = fmaf(a.y, b.y, acc);
+    acc = fmaf(a.z, b.z, acc);
+    return fmaf(a.w, b.w, acc);
+  }
+  static __device__ __forceinline__ void axpy(float h, const float4 u, float4 &acc) {
+    acc.x = fmaf(h, u.x, acc.x);
+    acc.y = fmaf(h, u.y, acc.y);
+    acc.z = fmaf(h, u.z, acc.z);
+    acc.w = fmaf(h, u.w, acc.w);
+  }
+  static __device__ __forceinline__ void scale(float4 &a, float s) {
+    a.x *= s;
+    a.y *= s;
+    a.z *= s;
+    a.w *= s;
+  }
+};
+template <> struct Vec16<double> {
+  using T = double2;
+  static constexpr int L = 2;
+  static __device__ __forceinline__ double dot(const double2 a, const double2 b, double acc) {
+    acc = fma(a.x, b.x, acc);
+    return fma(a.y, b.y, acc);
+  }
+  static __device__ __forceinline__ void axpy(double h, const double2 u, double2 &acc) {
+    acc.x = fma(h, u.x, acc.x);
+    acc.y = fma(h, u.y, acc.y);
+  }
+  static __device__ __forceinline__ void scale(double2 &a, double s) {
+    a.x *= s;
+    a.y *= s;
+  }
+};
+
+// h_j = u_j . v, j = 0..nvec-1; one FP64 partial per (j, block).  Block b
+// owns a contiguous range of 16-byte groups; warp w of a block takes the
+// vector pairs (2w, 2w+1), (2w+16, 2w+17), ..., so that one load of v
+// serves two basis vectors and every lane keeps two independent loads and
+// FMA chains in flight.  The last block adds the n % L tail.
 template <class XT>
 __global__ void __launch_bounds__(kT) k_gm_multidot(size_t n, const XT *__restrict__ basis,
                                                     size_t ld, int nvec, const XT *__restrict__ v,
                                                     double *partials, const GmresCtl *ctl) {
   if (*(volatile const int *)&ctl->done) return;
-  const size_t per = (n + gridDim.x - 1) / gridDim.x;
+  using V = Vec16<XT>;
+  using VT4 = typename V::T;
+  constexpr int L = V::L;
+  const size_t nq = n / L;
+  const size_t per = (nq + gridDim.x - 1) / gridDim.x;
   const size_t s = (size_t)blockIdx.x * per;
-  const size_t e = s + per < n ? s + per : n;
+  const size_t e = s + per < nq ? s + per : nq;
+  const bool tail = blockIdx.x == gridDim.x - 1;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = wid; j < nvec; j += nw) {
-    const XT *__restrict__ u = basis + ld * j;
-    XT acc = XT(0);
-    for (size_t k = s + lane; k < e; k += 32) acc = fma(u[k], v[k], acc);
-    double a = double(acc);
-    a = warp_sum(a);
-    if (lane == 0) partials[(size_t)j * gridDim.x + blockIdx.x] = a;
+  const VT4 *__restrict__ v4 = reinterpret_cast<const VT4 *>(v);
+  for (int j = 2 * wid; j < nvec; j += 2 * nw) {
+    const bool two = j + 1 < nvec;
+    const VT4 *__restrict__ ua = reinterpret_cast<const VT4 *>(basis + ld * j);
+    const VT4 *__restrict__ ub = reinterpret_cast<const VT4 *>(basis + ld * (two ? j + 1 : j));
+    XT acc_a = XT(0), acc_b = XT(0);
+#pragma unroll 4
+    for (size_t k = s + lane; k < e; k += 32) {
+      const VT4 x = v4[k];
+      acc_a = V::dot(ua[k], x, acc_a);
+      if (two) acc_b = V::dot(ub[k], x, acc_b);
+    }
+    if (tail) {
+      for (size_t k = nq * L + lane; k < n; k += 32) {
+        acc_a = fma(basis[ld * j + k], v[k], acc_a);
+        if (two) acc_b = fma(basis[ld * (j + 1) + k], v[k], acc_b);
+      }
+    }
+    const double a = warp_sum(double(acc_a));
+    const double b = warp_sum(double(acc_b));
+    if (lane == 0) {
+      partials[(size_t)j * gridDim.x + blockIdx.x] = a;
+      if (two) partials[(size_t)(j + 1) * gridDim.x + blockIdx.x] = b;
+    }
   }
 }
 
@@ -126,17 +198,19 @@ __global__ void k_gm_colsum(int grid, const double *partials, double *h, const G
   if (threadIdx.x == 0) h[j] = s;
 }
 
-// Pythagorean norm + Givens rotation for column i (1-based), one thread.
-// hraw[0..i] receives the unrotated column for the Gram-Schmidt update.
+// Norm + Givens rotation for column i (1-based), one thread.  pyth: hcol[i]
+// holds v.v and the norm is the Pythagorean sqrt|v.v - sum h_j^2|; else
+// hcol[i] already holds |v - sum h_j u_j|^2.  hraw[0..i] receives the
+// unrotated column for the Gram-Schmidt update.
 __global__ void k_gm_givens(int sD, double *H, const double *hcol, double *hraw, double *c,
-                            double *s, double *err, GmresCtl *ctl) {
+                            double *s, double *err, GmresCtl *ctl, int pyth) {
   if (ctl->done) return;
   const int i = ctl->i;
   double *h = H + (size_t)(i - 1) * (sD + 1);
   for (int j = 0; j <= i; j++) h[j] = hcol[j];
   for (int j = 0; j < i; j++) {
     hraw[j] = h[j];
-    h[i] = h[i] - h[j] * h[j];
+    if (pyth) h[i] = h[i] - h[j] * h[j];
   }
   h[i] = sqrt(fabs(h[i]));
   hraw[i] = h[i];
@@ -166,24 +240,89 @@ __global__ void k_gm_givens(int sD, double *H, const double *hcol, double *hraw,
   if (i >= sD) ctl->done = 1;
 }
 
-// u_{i+1} = (u_{i+1} - sum_j hraw_j u_j) / hraw_i
+// u_{i+1} = (u_{i+1} - sum_j hraw_j u_j) / hraw_i, one 16-byte group per
+// thread and step (the same per-element FMA sequence as an element loop)
 template <class XT>
 __global__ void __launch_bounds__(kT) k_gm_orth(size_t n, XT *__restrict__ basis, size_t ld,
                                                 const double *__restrict__ hraw,
                                                 const GmresCtl *ctl, int i_expected) {
   if (ctl->last_i != i_expected || ctl->nan || hraw[i_expected] == 0.0) return;
+  using V = Vec16<XT>;
+  using VT4 = typename V::T;
+  constexpr int L = V::L;
   const int i = i_expected;
   __shared__ XT hs[512];
-  for (int j = threadIdx.x; j < i && j < 512; j += blockDim.x) hs[j] = XT(hraw[j]);
+  for (int j = threadIdx.x; j < i && j < 512; j += blockDim.x) hs[j] = XT(-hraw[j]);
   __syncthreads();
   XT *__restrict__ v = basis + ld * i;
   const XT inv = XT(1.0 / hraw[i]);
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-       k += (size_t)gridDim.x * blockDim.x) {
+  const size_t nq = n / L;
+  const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t nt = (size_t)gridDim.x * blockDim.x;
+  for (size_t q = t0; q < nq; q += nt) {
+    VT4 acc = reinterpret_cast<const VT4 *>(v)[q];
+#pragma unroll 4
+    for (int j = 0; j < i; j++) V::axpy(hs[j], reinterpret_cast<const VT4 *>(basis + ld * j)[q], acc);
+    V::scale(acc, inv);
+    reinterpret_cast<VT4 *>(v)[q] = acc;
+  }
+  for (size_t k = nq * L + t0; k < n; k += nt) {
     XT acc = v[k];
-    for (int j = 0; j < i; j++) acc = fma(-hs[j], basis[ld * j + k], acc);
+    for (int j = 0; j < i; j++) acc = fma(hs[j], basis[ld * j + k], acc);
     v[k] = acc * inv;
   }
+}
+
+// FP32 basis: u_{i+1} -= sum_{j<i} h_j u_j (h_j from the multi-dot, before
+// the Givens kernel of the step) and |u_{i+1}|^2 -> hcol[i], a deterministic
+// grid sum; each 16-byte group's squares are summed in FP32 and added in
+// FP64.  k_gm_scale_i then divides by the norm once the Givens kernel has
+// accepted the column.
+template <class XT>
+__global__ void __launch_bounds__(kT) k_gm_orth_nrm(size_t n, XT *__restrict__ basis, size_t ld,
+                                                    double *__restrict__ hcol, const GmresCtl *ctl,
+                                                    int i, double *partials, unsigned *ticket) {
+  if (*(volatile const int *)&ctl->done) return;
+  using V = Vec16<XT>;
+  using VT4 = typename V::T;
+  constexpr int L = V::L;
+  __shared__ XT hs[512];
+  __shared__ double sh[32];
+  for (int j = threadIdx.x; j < i && j < 512; j += blockDim.x) hs[j] = XT(-hcol[j]);
+  __syncthreads();
+  XT *__restrict__ v = basis + ld * i;
+  const size_t nq = n / L;
+  const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t nt = (size_t)gridDim.x * blockDim.x;
+  double nrm = 0.0;
+  for (size_t q = t0; q < nq; q += nt) {
+    VT4 acc = reinterpret_cast<const VT4 *>(v)[q];
+#pragma unroll 4
+    for (int j = 0; j < i; j++) V::axpy(hs[j], reinterpret_cast<const VT4 *>(basis + ld * j)[q], acc);
+    reinterpret_cast<VT4 *>(v)[q] = acc;
+    nrm += double(V::dot(acc, acc, XT(0)));
+  }
+  for (size_t k = nq * L + t0; k < n; k += nt) {
+    XT acc = v[k];
+    for (int j = 0; j < i; j++) acc = fma(hs[j], basis[ld * j + k], acc);
+    v[k] = acc;
+    nrm += double(acc) * double(acc);
+  }
+  const double bs = block_sum(nrm, sh);
+  double tot;
+  if (grid_reduce_last<1>(&bs, partials, ticket, &tot, sh) && threadIdx.x == 0) hcol[i] = tot;
+}
+
+// u_{i+1} /= h_{i+1,i} after the Givens kernel of step i (FP32 basis)
+template <class XT>
+__global__ void k_gm_scale_i(size_t n, XT *__restrict__ basis, size_t ld,
+                             const double *__restrict__ hraw, const GmresCtl *ctl, int i) {
+  if (ctl->last_i != i || ctl->nan || hraw[i] == 0.0) return;
+  XT *__restrict__ v = basis + ld * i;
+  const XT inv = XT(1.0 / hraw[i]);
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    v[k] = v[k] * inv;
 }
 
 // Back substitution y = H(1:i,1:i)^-1 err(1:i), one thread.
@@ -267,6 +406,7 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
   }
   const size_t nv = (size_t)nNo * D;
   const size_t ld = (nv + 31) & ~(size_t)31;
+  constexpr bool kExplicitNorm = sizeof(XT) == 4;
   GSLS_TRY(ws.basis.alloc(sizeof(XT) * ld * (size_t)(sD + 1)));
   const int G = lhs->grid;
   const int Gd = num_sms() * 2;
@@ -350,14 +490,29 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
           launch_addbcmul<XT>(lhs, 0, D, ui, ui1, &ctl->done);
           if (ns) launch_addbcmul<XT>(lhs, 1, D, ui1, ui1, &ctl->done);
         }
-        k_gm_multidot<XT><<<Gd, kT, 0, st>>>(nv, basis, ld, i + 1, ui1, part, ctl);
-        GSLS_CHECK_LAUNCH();
-        k_gm_colsum<<<i + 1, kT, 0, st>>>(Gd, part, hcol, ctl);
-        GSLS_CHECK_LAUNCH();
-        k_gm_givens<<<1, 1, 0, st>>>(sD, H, hcol, hraw, cc, ss, err, ctl);
-        GSLS_CHECK_LAUNCH();
-        k_gm_orth<XT><<<G, kT, 0, st>>>(nv, basis, ld, hraw, ctl, i);
-        GSLS_CHECK_LAUNCH();
+        if (kExplicitNorm) {
+          // h_j for j < i, then the orthogonalised vector and its norm
+          k_gm_multidot<XT><<<Gd, kT, 0, st>>>(nv, basis, ld, i, ui1, part, ctl);
+          GSLS_CHECK_LAUNCH();
+          k_gm_colsum<<<i, kT, 0, st>>>(Gd, part, hcol, ctl);
+          GSLS_CHECK_LAUNCH();
+          k_gm_orth_nrm<XT><<<G, kT, 0, st>>>(nv, basis, ld, hcol, ctl, i, part, tk);
+          GSLS_CHECK_LAUNCH();
+          k_gm_givens<<<1, 1, 0, st>>>(sD, H, hcol, hraw, cc, ss, err, ctl, 0);
+          GSLS_CHECK_LAUNCH();
+          k_gm_scale_i<XT><<<G, kT, 0, st>>>(nv, basis, ld, hraw, ctl, i);
+          GSLS_CHECK_LAUNCH();
+        } else {
+          k_gm_multidot<XT><<<Gd, kT, 0, st>>>(nv, basis, ld, i + 1, ui1, part, ctl);
+          GSLS_CHECK_LAUNCH();
+          k_gm_colsum<<<i + 1, kT, 0, st>>>(Gd, part, hcol, ctl);
+          GSLS_CHECK_LAUNCH();
+          k_gm_givens<<<1, 1, 0, st>>>(sD, H, hcol, hraw, cc, ss, err, ctl, 1);
+          GSLS_CHECK_LAUNCH();
+          k_gm_orth<XT><<<G, kT, 0, st>>>(nv, basis, ld, hraw, ctl, i);
+          GSLS_CHECK_LAUNCH();
+        }
+        if (prof) cudaEventRecord(prof_event(2), st);
       }
       GSLS_CUDA(cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, st));
       GSLS_CUDA(cudaStreamSynchronize(st));
@@ -365,6 +520,9 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
         float t = 0.f;
         cudaEventElapsedTime(&t, prof_event(0), prof_event(1));
         prof_add(D == 3 ? "gm_spmv_d3" : "gm_spmv", 1, t);
+        // multi-dot, Givens and Gram-Schmidt update of the same step
+        cudaEventElapsedTime(&t, prof_event(1), prof_event(2));
+        prof_add("gm_orth", 1, t);
       }
       if (hc.done || i_next > sD) inner_done = true;
       if (!prof && batch < 16) batch *= 2;

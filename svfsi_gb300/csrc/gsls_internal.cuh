@@ -135,6 +135,7 @@ struct Workspace {
   GraphKey cg_key{};
   cudaGraphExec_t cg_graph_s = nullptr;    // CG batch on the sliced copy
   GraphKey cg_key_s{};
+  int cg_last_itr = 0;                     // iterations of the last CG solve (first-batch size)
   // sliced block-ELL layout of the CG SpMV (structure per block size D,
   // values per solve): slice offsets, slot rows, columns, CSR block -> slot
   int sell_D = 0, sell_nS = 0, sell_vkey = 0;
@@ -160,6 +161,8 @@ struct Workspace {
   KrylovScalars *h_scal = nullptr;  // pinned host mirror
   int mask_dof = -1;
   std::vector<int> mask_key;
+  unsigned mask_serial = 0;          // bumped by every rebuild of the Dirichlet mask
+  unsigned long long pre_serial = 0; // bumped by every preconditioning (W and W Val W)
 };
 
 }  // namespace gsls
@@ -328,8 +331,22 @@ int lhs_prepare_ws(gsls_lhs *lhs, int dof);
 int lhs_update_faces(gsls_lhs *lhs, const int *incL, const double *res);
 int build_dir_mask(gsls_lhs *lhs, int dof);
 // padded: dVal has >= 16 bytes of slack after its end (enables staged copies)
+// prescaled: dVal already holds W Val W of the diagonal preconditioner and
+// ws.W its W, both from the last preconditioning on this lhs (the caller has
+// checked ws.pre_serial and ws.mask_serial): only R = W R is formed
 int solve_dev(gsls_lhs *lhs, gsls_ls *ls, int dof, double *dRi, void *dVal,
-              int val_prec, int prec, bool padded);
+              int val_prec, int prec, bool padded, bool prescaled = false);
+// The HEATS/CEP operator path of the assembly (R = rho M A + nu K Y - rho s
+// b, Val = cM M + cK K from the mesh's cached operators).  In: a tangent key
+// from an earlier call; if it matches (same operators, same coefficients)
+// and skip_val is set, only R is formed and Val is left as it is.  Out:
+// whether the operator path ran, its key, whether Val was skipped.
+struct LinAsm {
+  bool skip_val = false;
+  unsigned serial = 0;
+  double cM = 0.0, cK = 0.0;
+  bool used = false, skipped = false;
+};
 int spmv_launch(gsls_lhs *lhs, int dof, const void *dVal, int val_prec,
                 const void *dx, void *dy, int xprec);
 // restarted GMRES on the preconditioned system (gsls_gmres.cu)

@@ -953,12 +953,23 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   const bool sell_ok = want_sell && !FUSED && !use_tma;
   SellArgs sa{};
   bool sell_on = false;
-  // CUDA graph of B iterations, cached per (D, types, Val, workspace,
-  // layout); one slot for the CSR batch and one for the sliced batch
-  auto graph_for = [&](bool sl, cudaGraphExec_t *&ge) -> int {
+  // First batch: the smallest power of two that holds the previous solve's
+  // iteration count on this lhs (2..B), so that the short solves of a
+  // Newton sequence (CEP, heat: 3-30 iterations) do not launch a full batch
+  // of iterations that only test the done flag; later batches (sliced copy)
+  // take B.  Powers of two keep the cached graph of the first batch stable.
+  int B1 = B;
+  if (sell_ok && ws.cg_last_itr > 0) {
+    B1 = 2;
+    while (B1 < ws.cg_last_itr && B1 < B) B1 *= 2;
+  }
+  // CUDA graph of a batch of iterations, cached per (D, types, Val,
+  // workspace, layout, batch); one slot for the CSR batch and one for the
+  // sliced batch
+  auto graph_for = [&](bool sl, int nb, cudaGraphExec_t *&ge) -> int {
     cudaGraphExec_t &gx = sl ? ws.cg_graph_s : ws.cg_graph;
     GraphKey &gk = sl ? ws.cg_key_s : ws.cg_key;
-    GraphKey key{D,  (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, B, nNo, use_tma,
+    GraphKey key{D,  (int)sizeof(VT), (int)sizeof(XT), (const void *)Val, v.X, nb, nNo, use_tma,
                  FUSED, ws.partials.p, ws.scal.p, ws.Wf.p, sl ? sa.sval : nullptr};
     ge = &gx;
     if (gx && gk == key) return GSLS_OK;
@@ -968,7 +979,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
     }
     cudaGraph_t g;
     GSLS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int rc = cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, false, 0, ttp, tsmem, tgrid,
+    int rc = cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, nb, false, 0, ttp, tsmem, tgrid,
                                           sl ? &sa : nullptr);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc != GSLS_OK) return rc;
@@ -986,22 +997,23 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
       count_launch();
       sell_on = true;
     }
+    const int nb = nbatch == 0 ? B1 : B;
     nbatch++;
     if (prof) {
-      GSLS_TRY(cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, B, true, 0, ttp, tsmem, tgrid,
+      GSLS_TRY(cg_enqueue<D, VT, XT, FUSED>(lhs, Val, v, nb, true, 0, ttp, tsmem, tgrid,
                                             sell_on ? &sa : nullptr));
     } else {
       cudaGraphExec_t *ge = nullptr;
-      GSLS_TRY(graph_for(sell_on, ge));
+      GSLS_TRY(graph_for(sell_on, nb, ge));
       GSLS_CUDA(cudaGraphLaunch(*ge, st));
-      count_launch_n((FUSED ? 2 : 3) * B - 1);
+      count_launch_n((FUSED ? 2 : 3) * nb - 1);
     }
     GSLS_TRY(wait_scalars(lhs));
     if (prof) {
       // only the launches that did work (one per completed iteration)
       const int worked = ws.h_scal->itr - itr_before;
       double ms = 0.0, mu = 0.0, mp = 0.0;
-      for (int b = 0; b < worked && b < B; b++) {
+      for (int b = 0; b < worked && b < nb; b++) {
         float t = 0.f;
         cudaEventElapsedTime(&t, prof_event(4 * b), prof_event(4 * b + 1));
         ms += t;
@@ -1019,6 +1031,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   GSLS_CHECK_LAUNCH();
   GSLS_CUDA(cudaStreamSynchronize(st));
   const KrylovScalars &h = *ws.h_scal;
+  ws.cg_last_itr = h.itr;
   ls->iNorm = h.iNorm;
   ls->itr = h.itr;
   ls->suc = h.suc;
@@ -1041,13 +1054,21 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
 }
 
 template <int D, class VT, class XT>
-static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, bool padded) {
+static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, bool padded,
+                   bool prescaled) {
   Workspace &ws = lhs->ws;
   double *W = ws.W.as<double>();
-  if (prec == GSLS_PRECOND_FSILS) {
+  if (prescaled && prec == GSLS_PRECOND_FSILS) {
+    // R = W R with the W that scaled Val (the R update of k_diag_w)
+    const size_t n = (size_t)lhs->nNo * D;
+    k_vec_mul<<<blocks_for(n, num_sms() * 8), kThreads, 0, lhs->stream>>>(n, dRi, W);
+    GSLS_CHECK_LAUNCH();
+  } else if (prec == GSLS_PRECOND_FSILS) {
     GSLS_TRY(precond_diag_t<D, VT>(lhs, Val, dRi, W));
+    ws.pre_serial++;
   } else if (prec == GSLS_PRECOND_RCS) {
     GSLS_TRY(precond_rcs_run(lhs, D, sizeof(VT) == 4, Val, dRi, W));
+    ws.pre_serial++;
   } else {
     set_error("This linear solver and preconditioner combination is not supported.");
     return GSLS_ERR_ARG;
@@ -1077,14 +1098,21 @@ static int solve_t(gsls_lhs *lhs, gsls_ls *ls, double *dRi, VT *Val, int prec, b
 }
 
 int solve_dev(gsls_lhs *lhs, gsls_ls *ls, int dof, double *dRi, void *dVal, int val_prec,
-              int prec, bool padded) {
+              int prec, bool padded, bool prescaled) {
   GSLS_TRY(lhs_prepare_ws(lhs, dof));
+  const unsigned mser = lhs->ws.mask_serial;
   GSLS_TRY(build_dir_mask(lhs, dof));
+  if (prescaled && lhs->ws.mask_serial != mser) {
+    set_error("solve: the Dirichlet mask changed under a preconditioned matrix");
+    return GSLS_ERR_ARG;
+  }
   const bool mixed = (val_prec == GSLS_PREC_MIXED);
-#define GSLS_SOLVE_CASE(DV)                                                              \
-  case DV:                                                                               \
-    return mixed ? solve_t<DV, float, float>(lhs, ls, dRi, (float *)dVal, prec, padded)  \
-                 : solve_t<DV, double, double>(lhs, ls, dRi, (double *)dVal, prec, padded);
+#define GSLS_SOLVE_CASE(DV)                                                                   \
+  case DV:                                                                                    \
+    return mixed ? solve_t<DV, float, float>(lhs, ls, dRi, (float *)dVal, prec, padded,       \
+                                             prescaled)                                       \
+                 : solve_t<DV, double, double>(lhs, ls, dRi, (double *)dVal, prec, padded,    \
+                                               prescaled);
   switch (dof) {
     GSLS_SOLVE_CASE(1)
     GSLS_SOLVE_CASE(2)

@@ -295,6 +295,7 @@ int build_dir_mask(gsls_lhs *lhs, int dof) {
   GSLS_CUDA(cudaStreamSynchronize(lhs->stream));
   ws.mask_dof = dof;
   ws.mask_key = key;
+  ws.mask_serial++;
   return GSLS_OK;
 }
 

@@ -196,9 +196,17 @@ class Equation:
                                             _dp(d) if d is not None else None),
               "gsls_eq_set_state")
 
-    def get_state(self):
+    def get_state(self, out=None):
+        """(Ao, Yo, Do) as (nNo, tDof) FP64 arrays; out: three C-contiguous
+        FP64 arrays of that shape to copy into (e.g. pinned host buffers,
+        which the device-to-host copy then reaches directly)."""
         shp = (self.nNo, self.tDof)
-        Ao, Yo, Do = np.zeros(shp), np.zeros(shp), np.zeros(shp)
+        if out is None:
+            out = (np.zeros(shp), np.zeros(shp), np.zeros(shp))
+        for a in out:
+            if a.shape != shp or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError(f"get_state: out arrays must be C-contiguous float64 {shp}")
+        Ao, Yo, Do = out
         check(_lib.load().gsls_eq_get_state(self.h, _dp(Ao), _dp(Yo), _dp(Do)),
               "gsls_eq_get_state")
         return Ao, Yo, Do

@@ -12,8 +12,10 @@ correction solved tightly by restarted GMRES(20) -- the reference's
 classical Gram-Schmidt with the Pythagorean norm stalls near 2e-8 relative
 over long cycles on this system, after which its basis grows without bound
 -- so every iterate is a well-conditioned function of the previous one
-(FP64: 1e-9 on the temperature change; the mixed path's FP32 GMRES
-corrections: 1e-4).
+(FP64, 4 iterations: 1e-9 on the temperature change).  The mixed path's
+FP32 GMRES corrections (relTol 1e-6) are refined by the FP64 residual of
+the next iterations: after the configuration's 10 iterations per step the
+temperature change is within 1e-8 of the oracle's.
 """
 import ctypes as C
 
@@ -80,9 +82,11 @@ def test_heatf_assembly_fp32_tangent(gsls, orc):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_heatf_steps(gsls, orc, precision):
+    nit = 4 if precision == "fp64" else 10
+
     def make():
         q = problems.heatf_cylinder(h=0.1, nsteps=2, u_max=3.0, cond=1.0, T0_linear=True)
-        q.maxItr, q.ls_sD, q.ls_mItr, q.ls_relTol = 4, 20, 20, 1e-12
+        q.maxItr, q.ls_sD, q.ls_mItr, q.ls_relTol = nit, 20, 20, 1e-12
         return q
     p = make()
     if precision == "mixed":
@@ -95,13 +99,13 @@ def test_heatf_steps(gsls, orc, precision):
     for _ in range(p.nsteps):
         gi = eq.step()
         oi = oeq.step()
-        assert gi.newton_itr == oi.newton_itr == 4
+        assert gi.newton_itr == oi.newton_itr <= nit
     _, Y, _ = eq.get_state()
     _, Yo, _ = oeq.state()
     assert np.array_equal(Y[:, :3], Yo[:, :3])  # the flow is carried unchanged
     dT, dTo = Y[:, 4] - q.Y0[:, 4], Yo[:, 4] - q.Y0[:, 4]
     assert np.abs(dTo).max() > 1e-4  # the temperature moved
-    assert rel(dT, dTo) < (1e-9 if precision == "fp64" else 1e-4)
+    assert rel(dT, dTo) < (1e-9 if precision == "fp64" else 1e-8)
 
 
 @pytest.mark.parametrize("u_max,g", [(-3.0, 0.0), (3.0, 0.5)])

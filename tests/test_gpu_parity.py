@@ -459,3 +459,53 @@ def test_next_equation_on_the_same_lhs_claims_the_freed_faces(gsls):
             eq3.add_dirichlet(d.nodes, d.g, d.gx, d.mask, d.nV)
     eq3.free()
     eq2.free()
+
+
+_LIN_REUSE_CODE = r"""
+import hashlib, json, numpy as np
+from svfsi_gb300 import _lib, fsils, problems
+L = _lib.load(); _lib.check(L.gsls_init(0))
+out = {}
+for name, prec in (("fp64", fsils.PREC_FP64), ("mixed", fsils.PREC_MIXED)):
+    p = problems.cep_slab(16, 16, 3, nsteps=9, A=52.0)
+    lhs, mesh, eq = problems.build_equation(p, precision=prec)
+    counts = [(s.newton_itr, s.ls_itr_total) for s in (eq.step() for _ in range(3))]
+    # an unrelated solve on the same lhs overwrites its preconditioner
+    rp, cp = np.asarray(p.rowPtr), np.asarray(p.colPtr)
+    V = np.where(cp == np.repeat(np.arange(p.nNo), np.diff(rp)),
+                 0.5 * np.repeat(np.diff(rp), np.diff(rp)), -0.5)[:, None].astype(float)
+    R = np.random.default_rng(5).standard_normal((p.nNo, 1))
+    fsils.FSILS_SOLVE(lhs, fsils.FSILS_LS_CREATE(fsils.LS_TYPE_CG, relTol=1e-6), 1, R, V,
+                      fsils.PRECOND_FSILS)
+    counts += [(s.newton_itr, s.ls_itr_total) for s in (eq.step() for _ in range(3))]
+    # a new per-element diffusivity rebuilds the conduction operator
+    eq.set_eparam(np.exp(0.2 * np.random.default_rng(6).standard_normal(p.nEl)) * 0.1)
+    counts += [(s.newton_itr, s.ls_itr_total) for s in (eq.step() for _ in range(3))]
+    A, Y, D = eq.get_state()
+    out[name] = dict(counts=counts, h=hashlib.sha256(np.ascontiguousarray(Y).tobytes()).hexdigest())
+print(json.dumps(out))
+"""
+
+
+def test_linear_tangent_reuse_is_bitwise_the_rebuilt_tangent(gsls):
+    """HEATS/CEP: the preconditioned tangent kept from the last full solve
+    (default) against rebuilding and rescaling it every Newton iteration
+    (GSLS_LIN_REUSE=0), in two fresh processes: nine CEP steps in FP64 and
+    mixed precision, with an unrelated solve on the same lhs after step 3
+    (it overwrites the preconditioner) and a new per-element diffusivity
+    after step 6 (it rebuilds the operator).  Same iteration counts, same
+    bits."""
+    import json
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    outs = []
+    for reuse in ("1", "0"):
+        env = dict(os.environ, GSLS_LIN_REUSE=reuse, PYTHONPATH=str(root))
+        r = subprocess.run([sys.executable, "-c", _LIN_REUSE_CODE], cwd=root, env=env,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.append(json.loads(r.stdout.strip().splitlines()[-1]))
+    assert outs[0] == outs[1], outs

@@ -1,6 +1,8 @@
 """USTRUCT (velocity-pressure nonlinear solid, Code/Source/svFSI/USTRUCT.f)
 on the GPU against the oracle: the element assembly into Val and the
-displacement tangent Kd (FP64 1e-12, FP32 tangent 1e-5), and converged
+displacement tangent Kd (FP64 1e-12; the mixed path forms both tangents in
+FP32 arithmetic: Val 1e-5, Kd 1e-6 -- Kd enters only the first Newton
+iteration's right-hand side, which the later iterations refine), and converged
 implicit steps with USTRUCTR's first-iteration correction and the ustruct
 predictor/corrector (FP64 1e-9, mixed 1e-8, equal Newton counts), for the
 compressible ST91 solid and the incompressible one (Kpen = 0)."""
@@ -50,7 +52,7 @@ def test_ustruct_assembly_matches_oracle(gsls, orc, mixed, visc):
         C.c_void_p(dK.data_ptr()), fsils.PREC_MIXED if mixed else fsils.PREC_FP64))
     torch.cuda.synchronize()
     assert rel(dR.cpu().numpy(), R0) < 1e-12
-    assert rel(dK.cpu().numpy(), K0) < 1e-12
+    assert rel(dK.cpu().numpy(), K0) < (1e-6 if mixed else 1e-12)
     assert rel(dV.cpu().numpy().astype(np.float64), V0) < (1e-5 if mixed else 1e-12)
     mesh.free()
     lhs.free()
