@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--only", choices=["all", "mixed", "fp64"], default="all",
                     help="time one precision only (profiling runs)")
     ap.add_argument("--workload",
-                    choices=["struct", "fluid", "cep", "lelas", "heatf", "ustruct", "adjoint"],
+                    choices=["struct", "fluid", "cep", "lelas", "heatf", "ustruct", "heats",
+                             "adjoint"],
                     default="struct")
     ap.add_argument("--fd-dirs", type=int, default=4,
                     help="adjoint workload: random directions of the central-FD check")
@@ -116,6 +117,9 @@ def workload(args):
         return problems.cep_slab(nsteps=args.steps, A=args.cep_amplitude)
     if args.workload == "heatf":
         return problems.heatf_cylinder(h=0.08 if args.small else args.fluid_h, nsteps=args.steps)
+    if args.workload == "heats":
+        # the heat cube: 20^3 hexes, 48,000 tets
+        return problems.heats_cube(8 if args.small else 20, nsteps=args.steps)
     if args.workload == "lelas":
         if args.small:
             return problems.lelas_beam(24, 6, 6, nsteps=args.steps)
@@ -183,6 +187,9 @@ def workload_desc(p):
                 f"conductivity 0.1, T = 1 on the inlet), {p.nEl:,} tet4, {p.nNo:,} nodes, nnz "
                 f"{p.nnz:,}, GMRES+diag, dt 1e-3, {p.maxItr} Newton iterations per step (the "
                 f"discontinuity-capturing fixed point converges linearly)")
+    if is_heats(p):
+        return (f"{p.name}: HEATS3D, conductivity 1, rho 1, T = 1 at x = 0 and 0 at x = 1, "
+                f"{p.nEl:,} tet4, {p.nNo:,} nodes, nnz {p.nnz:,}, CG+diag relTol 1e-10, dt 0.01")
     if is_cep(p):
         return (f"{p.name}: monodomain Aliev-Panfilov (FE reaction step), Diso 0.1, stimulus "
                 f"{p.cep['A']:+g} for 2 ms on the 1x1x2 corner block, {p.nEl:,} tet4, {p.nNo:,} "
@@ -336,7 +343,8 @@ def run_gsls(args):
             acnt, atot = C.c_longlong(), C.c_double()
             L.gsls_profile_read(b"assembly", C.byref(acnt), C.byref(atot))
             prof = {"cg_spmv": (cnt.value, tot.value), "assembly": (acnt.value, atot.value)}
-            for extra in (b"cg_update", b"cg_pupdate", b"schur", b"schur_calls", b"gm_orth"):
+            for extra in (b"cg_update", b"cg_pupdate", b"schur", b"schur_calls", b"gm_orth",
+                          b"cg_persistent"):
                 ec, et = C.c_longlong(), C.c_double()
                 if L.gsls_profile_read(extra, C.byref(ec), C.byref(et)) == 0 and ec.value:
                     prof[extra.decode()] = (ec.value, et.value)
@@ -425,6 +433,26 @@ def run_gsls(args):
     def roofline(prof, s):
         cnt, tot_ms = prof["cg_spmv"]
         t = "float" if s == 4 else "double"
+        if "cg_persistent" in prof:
+            # small systems run each CG solve as one cooperative launch: the
+            # roof is per CG iteration (SpMV + updates), the operator and
+            # vectors L2-resident across iterations
+            it, ms = prof["cg_persistent"]
+            B = p.algorithmic_bytes(s, s)["cg_iter"]
+            it_s = (ms / max(it, 1)) / 1e3
+            ach = B / it_s / 1e9 if it else None
+            r = C.c_double()
+            _lib.check(L.gsls_l2_read_rate(C.byref(r)), "gsls_l2_read_rate")
+            l2 = r.value / 1e9
+            return {"kernel": f"k_cg_persistent<{p.dof},{t},{t}> (every CG iteration of a solve "
+                              "in one cooperative launch, two grid barriers per iteration)",
+                    "bound": "l2", "achieved": ach, "peak": l2, "unit": "GB/s",
+                    "frac": (ach / l2) if ach else None,
+                    "peak_source": "measured L2 read bandwidth (gsls_l2_read_rate)",
+                    "hbm_frac": (ach / peak) if ach else None,
+                    "bytes_per_launch": B, "avg_launch_us": it_s * 1e6, "launches": it,
+                    "note": "per CG iteration: B_cg algorithmic bytes / (launch time / "
+                            "iterations of the launch)", "traffic": None}
         if is_fluid(p):
             B = p.nnz * (9 * s + 4) + 8 * p.nNo + 2 * p.nNo * 3 * s
             kname = f"k_gm_spmv<3,{t},{t}> (block-CSR SpMV on the K block of the NS solver)"
@@ -437,10 +465,10 @@ def run_gsls(args):
             B = p.algorithmic_bytes(s, s)["spmv"]
             kname = f"k_gm_spmv<4,{t},{t}> (block-CSR SpMV of the GMRES Arnoldi step, 4x4 blocks)"
             tkey = f"gm_spmv_d4_f{8 * s}_{p.name}"
-        elif is_cep(p):
+        elif is_cep(p) or is_heats(p):
             B = p.algorithmic_bytes(s, s)["spmv"]
             kname = f"k_cg_spmv<1,{t},{t}> (CSR SpMV + fused P.KP)"
-            tkey = f"cg_spmv_d1_f{8 * s}_cep_slab"
+            tkey = f"cg_spmv_d1_f{8 * s}_{p.name}"
         else:
             B = p.algorithmic_bytes(s, s)["spmv"]
             kname = (f"k_cg_spmv_sell<3,{t},{t},{8 if s == 4 else 4}> (sliced block-ELL SpMV + "
@@ -514,6 +542,7 @@ def run_gsls(args):
         "data": ("synthetic: seeded Delaunay cylinder mesh, no external data"
                  if (is_fluid(p) or is_heatf(p))
                  else "synthetic: Kuhn-split slab mesh, no external data" if is_cep(p)
+                 else "synthetic: Kuhn-split unit-cube mesh, no external data" if is_heats(p)
                  else "synthetic: seeded Kuhn-split beam mesh, no external data"),
         "config": {"workload": workload_desc(p), "precision": "mixed",
                    "l2": l2_note(p),
@@ -586,12 +615,20 @@ def config_legs(L, problems, fsils, torch):
     (h 0.027, 1,225,440 tets).  For each, the oracle's first n_par implicit
     steps from the initial state beside the FP64 and mixed GPU steps (error
     of each against the oracle, Newton counts), then n_time more GPU steps
-    per precision timed with CUDA events on the library's stream.  The slab
-    and the cylinder run their configured step counts (5,000 and 20 steps)
-    per precision; the heat cube its 10 steps twice."""
+    per precision timed with CUDA events on the library's stream.  The
+    cylinder runs its configured 20 steps, the heat cube its 10 steps twice.
+    The slab with the configured stimulus -52 runs 250 steps: it
+    hyperpolarises the corner below -110 mV, where the Aliev-Panfilov
+    recovery term mu1 X2 / (mu2 + X1) has its pole, and on this mesh a node
+    lands close enough to the pole near step 257 that the reference's model
+    state becomes non-finite (the oracle, FP64 and mixed alike).  The
+    configured 5,000 steps are timed with the depolarising stimulus +52 (a
+    propagating front)."""
     threads = os.cpu_count() or 1
     legs = [("heats_cube_20", lambda: problems.heats_cube(20, nsteps=20), 10, 10),
-            ("cep_slab_135x135x27", lambda: problems.cep_slab(nsteps=5000, A=-52.0), 20, 4980),
+            ("cep_slab_135x135x27", lambda: problems.cep_slab(nsteps=250, A=-52.0), 20, 230),
+            ("cep_slab_135x135x27_stim+52", lambda: problems.cep_slab(nsteps=5000, A=52.0), 20,
+             4980),
             ("fluid_cylinder_h0.027", lambda: problems.fluid_cylinder(h=0.027, nsteps=20), 1, 19)]
     res = {}
     for name, make, n_par, n_time in legs:
@@ -599,9 +636,7 @@ def config_legs(L, problems, fsils, torch):
         so, secs, co = oracle_steps(p, n_par, threads)
         ref = compared_field(p, so)
         nref = float(np.linalg.norm(ref))
-        leg = {"workload": workload_desc(p) if (is_fluid(p) or is_cep(p)) else
-               (f"{p.name}: HEATS3D, conductivity 1, rho 1, T = 1 at x = 0 and 0 at x = 1, "
-                f"{p.nEl:,} tet4, {p.nNo:,} nodes, nnz {p.nnz:,}, CG+diag relTol 1e-10, dt 0.01"),
+        leg = {"workload": workload_desc(p),
                "oracle": {"s_per_step": float(sum(secs) / len(secs)), "cores": threads,
                           "steps": n_par, "newton": [c[0] for c in co],
                           "ls_itr": [c[1] for c in co], "kind": "port"}}
@@ -647,7 +682,8 @@ def config_legs(L, problems, fsils, torch):
 
 # implicit steps the oracle runs beside the GPU in the default bench run: the
 # cpu_baseline sample and the full-size error against the oracle's solution
-PARITY_STEPS = {"struct": 2, "lelas": 2, "fluid": 1, "heatf": 2, "cep": 20, "ustruct": 1}
+PARITY_STEPS = {"struct": 2, "lelas": 2, "fluid": 1, "heatf": 2, "cep": 20, "ustruct": 1,
+                "heats": 10}
 
 
 def oracle_steps(p, nsteps, threads, warm=0):
@@ -700,6 +736,7 @@ def run_reference(args):
     data = ("synthetic: seeded Delaunay cylinder mesh, no external data"
             if (is_fluid(p) or is_heatf(p))
             else "synthetic: Kuhn-split slab mesh, no external data" if is_cep(p)
+            else "synthetic: Kuhn-split unit-cube mesh, no external data" if is_heats(p)
             else "synthetic: seeded Kuhn-split beam mesh, no external data")
     out = {"metric": METRIC, "value": v, "unit": "s/step", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,

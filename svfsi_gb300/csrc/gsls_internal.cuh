@@ -76,7 +76,8 @@ struct DevBuf {
 struct KrylovScalars {
   double iNorm, eps, err, errO, alpha, dot, fNorm;
   double beta;
-  int done;   // 0 running, 1 converged, 2 max iterations, 3 breakdown/NaN
+  int done;   // 0 running, 1 converged, 2 max iterations, 3 breakdown/NaN,
+              // 4 grid barrier timed out (persistent CG)
   int itr;    // completed iterations
   int mItr;
   int suc;
@@ -144,6 +145,7 @@ struct Workspace {
   DevBuf partials;    // double[grid * 64]
   DevBuf ticket;      // unsigned[8]
   DevBuf scal;        // KrylovScalars
+  DevBuf cgbar;       // grid barrier of the persistent CG
   DevBuf vec[6];      // Krylov work vectors (X, P, KP, R32...)
   DevBuf W;           // diag preconditioner (double dof x nNo)
   DevBuf W2;          // RCS second scaling

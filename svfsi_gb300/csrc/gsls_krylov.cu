@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "gsls_gridbar.cuh"
 #include "gsls_internal.cuh"
 #include "gsls_spmv.cuh"
 
@@ -504,6 +505,128 @@ __global__ void __launch_bounds__(kUpdThreads, 2) k_cg_pupdate(size_t n, CgVecs 
     P[k] = fma(beta, P[k], R[k]);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent CG for systems whose matrix sits in L2 (the heat cube, the CEP
+// slab): a solve of a few thousand to a few hundred thousand rows spends a
+// three-kernel iteration mostly on launch and drain latency, so every
+// iteration runs inside one cooperative launch.  Iteration k:
+//  1. P_k = R + beta P_{k-1} formed on the fly at every column (and stored
+//     by the owner of each row into the other buffer), KP = K P_k and the
+//     block partials of P_k.KP;
+//  2. after a grid barrier every block sums the partials in block order:
+//     alpha = errO / dot; X += alpha P_k, R -= alpha KP and the partials of
+//     |R|^2;
+//  3. after the second barrier: err, beta = err / errO and CGRAD's stopping
+//     tests in k_cg_update's order.
+// The arithmetic of each entry is that of k_cg_spmv (fused form) and
+// k_cg_update; vectors written inside the launch are read through L2
+// (ld.cg), the matrix through the read-only path.
+template <int D, class XT, class AT, int VD>
+struct GatherDirL2 {
+  const XT *__restrict__ R;
+  const XT *__restrict__ Pold;
+  AT beta;
+  __device__ __forceinline__ void get(int col, AT out[D]) const {
+#pragma unroll
+    for (int c = 0; c < D; c++)
+      out[c] = fma(beta, AT(__ldcg(Pold + (size_t)col * VD + c)), AT(__ldcg(R + (size_t)col * VD + c)));
+  }
+};
+
+constexpr int kCpThreads = 512;
+template <int D, class VT, class XT>
+__global__ void __launch_bounds__(kCpThreads) k_cg_persistent(int nNo,
+                                                              const int *__restrict__ rowPtr,
+                                                              const int *__restrict__ colPtr,
+                                                              const VT *__restrict__ Val, CgVecs v,
+                                                              KrylovScalars *S, double *part,
+                                                              GridBar *bar, unsigned spin) {
+  using AT = typename AccOf<VT>::T;
+  constexpr int VD = VStride<D, XT>::v, RPW = 32 / D;
+  __shared__ double sh[32];
+  __shared__ AT sha[32];
+  __shared__ XT shx[32];
+  const unsigned nblk = gridDim.x;
+  XT *__restrict__ X = (XT *)v.X;
+  XT *__restrict__ R = (XT *)v.R;
+  XT *__restrict__ KP = (XT *)v.KP;
+  double err = S->err, errO = S->errO, alpha = S->alpha, beta = S->beta;
+  const double eps = S->eps;
+  const int mItr = S->mItr;
+  int done = S->done, suc = S->suc, itr = S->itr;
+  unsigned epoch = 0;
+  bool ok = true;
+  const int lane = threadIdx.x & 31, grp = lane / D, r = lane - grp * D;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const size_t n = (size_t)nNo * VD;
+  const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t nt = (size_t)gridDim.x * blockDim.x;
+  while (!done) {
+    XT *__restrict__ Pold = (XT *)((itr & 1) ? v.P1 : v.P0);
+    XT *__restrict__ Pnew = (XT *)((itr & 1) ? v.P0 : v.P1);
+    const AT b = AT(beta);
+    GatherDirL2<D, XT, AT, VD> gd{R, Pold, b};
+    AT dot = AT(0);
+    for (int base = warp * RPW; base < nNo; base += nwarps * RPW) {
+      const int i = base + grp;
+      if (grp < RPW && i < nNo) {
+        const size_t k = (size_t)i * VD + r;
+        const AT y = spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, gd);
+        const AT pn = fma(b, AT(__ldcg(Pold + k)), AT(__ldcg(R + k)));
+        __stcg(Pnew + k, XT(pn));
+        __stcg(KP + k, XT(y));
+        dot = fma(pn, y, dot);
+      }
+    }
+    {
+      const double bs = double(block_sum_t<AT>(dot, sha));
+      if (threadIdx.x == 0) __stcg(part + blockIdx.x, bs);
+    }
+    if (!(ok = grid_bar(bar, nblk, epoch, spin))) break;
+    const double dsum = sum_partials(part, nblk, sh);
+    errO = err;
+    alpha = errO / dsum;
+    if (!isfinite(alpha)) {
+      done = 3;
+      break;
+    }
+    const XT al = XT(alpha);
+    XT acc = XT(0);
+    for (size_t k = t0; k < n; k += nt) {
+      __stcg(X + k, XT(fma(al, __ldcg(Pnew + k), __ldcg(X + k))));
+      const XT rr = XT(fma(-al, __ldcg(KP + k), __ldcg(R + k)));
+      __stcg(R + k, rr);
+      acc = fma(rr, rr, acc);
+    }
+    {
+      const double bs = double(block_sum_t<XT>(acc, shx));
+      if (threadIdx.x == 0) __stcg(part + nblk + blockIdx.x, bs);
+    }
+    if (!(ok = grid_bar(bar, nblk, epoch, spin))) break;
+    err = sum_partials(part + nblk, nblk, sh);
+    beta = err / errO;
+    itr++;
+    if (!isfinite(err))
+      done = 3;
+    else if (itr >= mItr)
+      done = 2;
+    else if (err < eps) {
+      done = 1;
+      suc = 1;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S->err = err;
+    S->errO = errO;
+    S->alpha = alpha;
+    S->beta = beta;
+    S->itr = itr;
+    S->suc = suc;
+    S->done = ok ? done : 4;
+  }
+}
+
 // R_out = W * X (X in node stride VD, R_out packed)
 template <int D, class XT>
 __global__ void k_scale_out(int nNo, double *__restrict__ Rout, const XT *__restrict__ X,
@@ -925,11 +1048,66 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
   unsigned *tk = ws.ticket.as<unsigned>();
   const int G = lhs->grid;
   auto t0 = std::chrono::steady_clock::now();
-  k_cg_init<D, XT, FUSED><<<G, kThreads, 0, st>>>(nNo, R, v, S, ls->absTol, ls->relTol, ls->mItr,
-                                                   part, tk);
+  // Persistent CG (one cooperative launch per solve) when the matrix fits in
+  // L2 with room to spare; GSLS_CG_PERSISTENT=0 never, =1 always
+  static const int cp_mode = [] {
+    const char *e = getenv("GSLS_CG_PERSISTENT");
+    return e ? (strcmp(e, "0") == 0 ? 0 : 1) : -1;
+  }();
+  static const bool env_tma = [] {
+    const char *e = getenv("GSLS_SPMV");
+    return e && strcmp(e, "tma") == 0;
+  }();
+  const size_t vbytes = (size_t)lhs->nnz * D * D * sizeof(VT);
+  const bool persistent =
+      !env_tma && (cp_mode == 1 || (cp_mode == -1 && vbytes <= ((size_t)64 << 20)));
+  if (persistent)
+    k_cg_init<D, XT, true><<<G, kThreads, 0, st>>>(nNo, R, v, S, ls->absTol, ls->relTol,
+                                                    ls->mItr, part, tk);
+  else
+    k_cg_init<D, XT, FUSED><<<G, kThreads, 0, st>>>(nNo, R, v, S, ls->absTol, ls->relTol,
+                                                     ls->mItr, part, tk);
   GSLS_CHECK_LAUNCH();
+  if (persistent) {
+    // co-resident grid: enough warps for one pass over the rows, at most
+    // what the SMs hold at once
+    static const int per_sm = [] {
+      int nb = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cg_persistent<D, VT, XT>, kCpThreads,
+                                                    0);
+      return nb;
+    }();
+    constexpr int RPW = 32 / D, WPB = kCpThreads / 32;
+    const long long warps = ((long long)nNo + RPW - 1) / RPW;
+    long long gp = (warps + WPB - 1) / WPB;
+    const long long gmax = (long long)per_sm * num_sms();
+    if (gp > gmax) gp = gmax;
+    if (gp < 1) gp = 1;
+    if (per_sm < 1) {
+      set_error("CG: the persistent kernel does not fit on an SM");
+      return GSLS_ERR_CUDA;
+    }
+    GSLS_TRY(ws.cgbar.alloc(sizeof(GridBar)));
+    GSLS_CUDA(cudaMemsetAsync(ws.cgbar.p, 0, sizeof(GridBar), st));
+    int nNo_ = nNo;
+    const int *rp = lhs->d_rowPtr.as<int>(), *cp = lhs->d_colPtr.as<int>();
+    GridBar *gb = ws.cgbar.as<GridBar>();
+    unsigned spin = wait_limit();
+    void *args[] = {&nNo_, (void *)&rp, (void *)&cp, (void *)&Val, &v, &S, &part, &gb, &spin};
+    const bool prof_p = prof_on();
+    if (prof_p) cudaEventRecord(prof_event(0), st);
+    GSLS_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_persistent<D, VT, XT>, dim3((int)gp),
+                                          dim3(kCpThreads), args, 0, st));
+    GSLS_CHECK_LAUNCH();
+    if (prof_p) cudaEventRecord(prof_event(1), st);
+  }
   GSLS_TRY(wait_scalars(lhs));
-  const bool prof = prof_on();
+  if (persistent && prof_on()) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, prof_event(0), prof_event(1));
+    prof_add("cg_persistent", ws.h_scal->itr, ms);
+  }
+  const bool prof = prof_on() && !persistent;
   const int B = nv < (1u << 20) ? 8 : 16;
   // TMA-staged SpMV for FP32 values in a buffer with copy slack
   TmaTiles tt{};
@@ -990,7 +1168,7 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
     return GSLS_OK;
   };
   int nbatch = 0;
-  while (ws.h_scal->done == 0) {
+  while (!persistent && ws.h_scal->done == 0) {
     const int itr_before = ws.h_scal->itr;
     if (sell_ok && !sell_on && nbatch >= 1) {
       GSLS_TRY(sell_pack<D, VT>(lhs, Val, sa));
@@ -1045,6 +1223,10 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
       set_error("CG: a staged copy did not complete (bounded mbarrier wait expired)");
       return GSLS_ERR_CUDA;
     }
+  }
+  if (h.done == 4) {
+    set_error("CG: grid barrier of the persistent CG timed out");
+    return GSLS_ERR_CUDA;
   }
   if (h.done == 3) {
     set_error("CG: NaN/Inf or breakdown in Krylov scalars");

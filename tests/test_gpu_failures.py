@@ -241,3 +241,29 @@ def test_grid_barrier_timeout_returns_cleanly(gsls, orc, mixed):
     else:
         assert ls.RI.suc == ols.RI.suc and ls.RI.itr == ols.RI.itr
         assert rel(R, Ro) < 1e-8
+
+
+def test_persistent_cg_barrier_timeout_returns_cleanly(gsls, orc):
+    """Small CG solves run in one cooperative launch whose iterations meet
+    at bounded grid barriers.  With the poll limit cut to 2 the waits run
+    out: the solve returns GSLS_ERR_CUDA, and with the default limit back
+    the library solves correctly (the context is intact)."""
+    # the 20^3 heat cube: ~19 blocks meet at every barrier
+    q = problems.heats_cube(20)
+    rng = np.random.default_rng(4)
+    Rq, Vq = orc.assemble(q, 1e-3 * rng.standard_normal((q.nNo, 1)),
+                          1e-3 * rng.standard_normal((q.nNo, 1)))
+    lhs = _lhs_with_dir(q)
+    ls = fsils.FSILS_LS_CREATE(fsils.LS_TYPE_CG, relTol=1e-10, maxItr=2000)
+    try:
+        _lib.check(gsls.gsls_set_wait_limit(2), "gsls_set_wait_limit")
+        R, Val = Rq.copy(), Vq.copy()
+        with pytest.raises(_lib.GslsError) as exc:
+            fsils.FSILS_SOLVE(lhs, ls, 1, R, Val, fsils.PRECOND_FSILS)
+        assert _status(exc) == GSLS_ERR_CUDA
+        assert "grid barrier" in str(exc.value)
+    finally:
+        _lib.check(gsls.gsls_set_wait_limit(0), "gsls_set_wait_limit")
+        lhs.free()
+    p, R0, V0 = _heat_system(orc)
+    _solve_ok_after(gsls, orc, p, R0, V0)

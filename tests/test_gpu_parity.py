@@ -509,3 +509,25 @@ def test_linear_tangent_reuse_is_bitwise_the_rebuilt_tangent(gsls):
         assert r.returncode == 0, r.stderr[-2000:]
         outs.append(json.loads(r.stdout.strip().splitlines()[-1]))
     assert outs[0] == outs[1], outs
+
+
+def test_batched_cg_path_on_small_systems(gsls):
+    """Small systems take the persistent CG (one cooperative launch per
+    solve); the batched path (CUDA graphs of SpMV/update/direction kernels,
+    sliced copy after the first batch) is what the large ones run.  This
+    re-runs the small-system CG parity tests with the persistent kernel
+    switched off (GSLS_CG_PERSISTENT=0), in a fresh process."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, GSLS_CG_PERSISTENT="0", PYTHONPATH=str(root))
+    sel = ("cg_block_sizes or struct_steps or heats_c1 or heats_mixed or cep_steps or "
+           "iteration_limit or zero_diagonal or deterministic")
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-m", "gpu", "-p", "no:cacheprovider",
+                        "-k", sel, str(root / "tests" / "test_gpu_parity.py"),
+                        str(root / "tests" / "test_gpu_failures.py")],
+                       cwd=root, env=env, capture_output=True, text=True, timeout=1200)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
+    assert " passed" in r.stdout
