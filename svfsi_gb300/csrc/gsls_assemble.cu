@@ -279,12 +279,36 @@ __global__ void __launch_bounds__(256) k_asm_lin(int nNo, const int *__restrict_
   double rM = 0.0, rK = 0.0;
   if (row < nNo) {
     const int j0 = __ldg(rowPtr + row), j1 = __ldg(rowPtr + row + 1);
-    for (int j = j0 + l; j < j1; j += kLinLanes) {
-      const double m = __ldcs(Mg + j), k = __ldcs(Kg + j);
-      const size_t c = (size_t)__ldcs(colPtr + j) * tDof + s;
-      if constexpr (kVal) __stcs(Val + j, cM * __ldcs(Mt + j) + cK * __ldcs(Kt + j));
-      rM = fma(m, __ldg(Ag + c), rM);
-      rK = fma(k, __ldg(Yg + c), rK);
+    // a lane's entries j, j+4, ... are loaded kU at a time (columns and
+    // operator values, then the gathers) so that one pass over a tet4 row
+    // of ~15 entries is one memory round trip; the sums keep the entry order
+    constexpr int kU = 4;
+    for (int j = j0 + l; j < j1; j += kU * kLinLanes) {
+      double m[kU], k[kU], a[kU], y[kU];
+      size_t c[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const int jj = j + u * kLinLanes;
+        const bool ok = jj < j1;
+        m[u] = ok ? __ldcs(Mg + jj) : 0.0;
+        k[u] = ok ? __ldcs(Kg + jj) : 0.0;
+        c[u] = ok ? (size_t)__ldcs(colPtr + jj) * tDof + s : (size_t)s;
+        if constexpr (kVal)
+          if (ok) __stcs(Val + jj, cM * __ldcs(Mt + jj) + cK * __ldcs(Kt + jj));
+      }
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const bool ok = j + u * kLinLanes < j1;
+        a[u] = ok ? __ldg(Ag + c[u]) : 0.0;
+        y[u] = ok ? __ldg(Yg + c[u]) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        if (j + u * kLinLanes < j1) {
+          rM = fma(m[u], a[u], rM);
+          rK = fma(k[u], y[u], rK);
+        }
+      }
     }
   }
 #pragma unroll
