@@ -6,7 +6,10 @@ same initial state, on all host cores (coloured OpenMP assembly).
 * monodomain slab, Aliev-Panfilov: 135x135x27 hexes -> 2,952,450 tet4,
   stimulus -52 (the configured amplitude), 20 steps;
 * cylinder, VMS Navier-Stokes + RCS + NS solver: h 0.027 -> 1,225,440 tet4,
-  1 step.
+  1 step;
+* the beam with linear elasticity (LELAS3D), 2 steps, and the cylinder with
+  heat carried by a Poiseuille flow (HEATF3D, 10 Newton iterations per
+  step), 2 steps.
 
 Bar: identical Newton counts per step; the FP64 GPU state within 1e-10
 relative L2 of the oracle's and the mixed one within 1e-8 (the Newton
@@ -83,3 +86,16 @@ def test_fluid_cylinder_full_size(gsls, orc):
     p = problems.fluid_cylinder(h=0.027, nsteps=1)
     assert p.nEl == 1_225_440
     _check(orc, p, 1, lambda s: s[1])
+
+
+def test_lelas_beam_full_size(gsls, orc):
+    p = problems.lelas_beam(nsteps=2)
+    assert (p.nEl, p.nNo, p.nnz) == (2_044_416, 358_425, 5_233_801)
+    _check(orc, p, 2, lambda s: s[2])
+
+
+def test_heatf_cylinder_full_size(gsls, orc):
+    p = problems.heatf_cylinder(h=0.027, nsteps=2)
+    assert p.nEl == 1_225_440
+    # the temperature column (the velocity is prescribed and carried unchanged)
+    _check(orc, p, 2, lambda s: s[1][:, 4])
