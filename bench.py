@@ -798,46 +798,62 @@ def run_adjoint(args):
         d = D[tip] - target
         return 0.5 * float(np.sum(d * d))
 
-    eq = problems.equation_on(p, mesh)
-    eq.set_eparam(c10)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    tape = eq.adjoint_forward(nsteps, every=5)
-    t1 = time.perf_counter()
-    DN = eq.get_state()[2]
-    bar = np.zeros_like(DN)
-    bar[tip] = DN[tip] - target
-    g_c10 = tape.backward(Dbar=bar)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    tape.free()
-    eq.free()
-    grad_mu = 0.5 * g_c10
+    def adjoint(precision):
+        """forward with checkpoints + backward; (gradient w.r.t. mu, J,
+        forward s, backward s)"""
+        e = problems.equation_on(p, mesh, precision)
+        e.set_eparam(c10)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tape = e.adjoint_forward(nsteps, every=5)
+        t1 = time.perf_counter()
+        DN = e.get_state()[2]
+        bar = np.zeros_like(DN)
+        bar[tip] = DN[tip] - target
+        g_c10 = tape.backward(Dbar=bar)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        tape.free()
+        e.free()
+        return 0.5 * g_c10, J(DN), t1 - t0, t2 - t1
+
+    g64, J64, f64s, b64s = adjoint(fsils.PREC_FP64)
+    gmx, Jmx, fmxs, bmxs = adjoint(fsils.PREC_MIXED)
     h = args.fd_h
-    errs, pairs = [], []
+    errs, errs_mx, pairs = [], [], []
     for k in range(args.fd_dirs):
         r = rng.standard_normal(p.nEl)
         r /= np.linalg.norm(r)
         dmu = mu * r
         fd = (J(forward(0.5 * (mu + h * dmu))) - J(forward(0.5 * (mu - h * dmu)))) / (2 * h)
-        ad = float(grad_mu @ dmu)
+        ad, am = float(g64 @ dmu), float(gmx @ dmu)
         errs.append(abs(fd - ad) / abs(ad))
-        pairs.append([fd, ad])
-        print(f"direction {k}: fd {fd:.10e} adjoint {ad:.10e} rel {errs[-1]:.2e}",
-              file=sys.stderr, flush=True)
+        errs_mx.append(abs(fd - am) / abs(am))
+        pairs.append([fd, ad, am])
+        print(f"direction {k}: fd {fd:.10e} adjoint fp64 {ad:.10e} mixed {am:.10e} "
+              f"rel {errs[-1]:.2e} / {errs_mx[-1]:.2e}", file=sys.stderr, flush=True)
     mesh.free()
     lhs.free()
-    out = {"metric": "adjoint s/step (forward with checkpoints + backward), FP64", "impl": "gsls",
-           "value": (t2 - t0) / nsteps, "unit": "s/step", "n_gpus": 1, "steps": nsteps,
-           "higher_is_better": False, "dtype": "f64", "data": "synthetic: seeded Kuhn-split beam",
+    rms = float(np.sqrt(np.mean([b * b for _, b, _ in pairs]))) if pairs else None
+    out = {"metric": "adjoint s/step (forward with checkpoints + backward), mixed vs FP64",
+           "impl": "gsls", "value": (fmxs + bmxs) / nsteps, "unit": "s/step", "n_gpus": 1,
+           "steps": nsteps, "higher_is_better": False,
+           "dtype": "f32 tangent+inner CG / f64 residual,Newton, refinement of the transpose "
+                    "solves",
+           "data": "synthetic: seeded Kuhn-split beam",
            "config": {"workload": workload_desc(p) + "; per-element mu log-normal sigma 0.2, "
                       "checkpoint every 5, Newton tol 1e-12", "params": p.nEl},
-           "forward_s": t1 - t0, "backward_s": t2 - t1, "J": J(DN),
-           "fd_check": {"directions": args.fd_dirs, "h_rel": h, "rel_errs": errs, "fd_ad": pairs,
-                        "max_rel_err": max(errs) if errs else None,
+           "mixed": {"forward_s": fmxs, "backward_s": bmxs, "J": Jmx},
+           "fp64": {"value": (f64s + b64s) / nsteps, "forward_s": f64s, "backward_s": b64s,
+                    "J": J64},
+           "speedup_mixed_vs_fp64": (f64s + b64s) / (fmxs + bmxs),
+           "grad_rel_l2_mixed_vs_fp64": float(np.linalg.norm(gmx - g64) / np.linalg.norm(g64)),
+           "fd_check": {"directions": args.fd_dirs, "h_rel": h, "fd_ad_fp64_ad_mixed": pairs,
+                        "rel_errs_fp64": errs, "rel_errs_mixed": errs_mx,
                         # FD noise is absolute: normalise by the RMS directional derivative
-                        "max_err_over_rms": (max(abs(a - b) for a, b in pairs) /
-                                             float(np.sqrt(np.mean([b * b for _, b in pairs]))))
+                        "max_err_over_rms_fp64": (max(abs(a - b) for a, b, _ in pairs) / rms)
+                        if pairs else None,
+                        "max_err_over_rms_mixed": (max(abs(a - c) for a, _, c in pairs) / rms)
                         if pairs else None}}
     print(json.dumps(out))
 

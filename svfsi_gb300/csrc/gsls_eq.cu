@@ -420,6 +420,27 @@ __global__ void k_axpy1(size_t n, double *__restrict__ y, const double *__restri
     y[k] += x[k];
 }
 
+// y += c x
+__global__ void k_axpyc(size_t n, double *__restrict__ y, double c, const double *__restrict__ x) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    y[k] += c * x[k];
+}
+
+// r = g - Kx
+__global__ void k_resid(size_t n, double *__restrict__ r, const double *__restrict__ g,
+                        const double *__restrict__ Kx) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    r[k] = g[k] - Kx[k];
+}
+
+__global__ void k_d2f(size_t n, const double *__restrict__ a, float *__restrict__ b) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    b[k] = float(a[k]);
+}
+
 }  // namespace gsls
 
 using namespace gsls;
@@ -1151,6 +1172,7 @@ struct gsls_tape {
   gsls::DevBuf last;    // final state, restored after the backward pass
   gsls::DevBuf M, Mz;   // mass CSR values; zeros / scratch (nNo)
   gsls::DevBuf ValK, Val0, Rk;
+  gsls::DevBuf ValK32, ir;  // mixed refinement: FP32 tangent; r, d, K lambda (3 x nr)
   gsls::DevBuf cot, lam, tmp;  // cotangents (3 x nr), lambda, M lambda / K lambda
   gsls::DevBuf grad;    // per-element gradient (colour order)
   ~gsls_tape() {
@@ -1279,6 +1301,66 @@ static int adj_solve_at(gsls_tape *t, const double *Ao, const double *Yo, const 
   ls.RI.absTol = 1e-300;
   if (ls.RI.mItr < 20000 && ls.LS_type == GSLS_LS_TYPE_CG) ls.RI.mItr = 20000;
   GSLS_TRY(lhs_update_faces(lhs, nullptr, nullptr));
+  if (eq->sv.precision == GSLS_PREC_MIXED && ls.LS_type == GSLS_LS_TYPE_CG &&
+      eq->sv.prec == GSLS_PRECOND_FSILS) {
+    // Mixed precision: iterative refinement of the same solve.  Each sweep
+    // solves K d = r / |r| with the FP32 tangent and FP32 CG to relTol 1e-4
+    // (the right-hand side normalised: the residuals of later sweeps are far
+    // below FP32's range once squared; the first sweep preconditions the FP32
+    // copy, the later ones reuse it and its W), adds |r| d to lambda and forms
+    // r = g - K lambda with the unscaled FP64 tangent; it stops when the
+    // preconditioned residual |W r| is below 1e-12 |W g|, the FP64 solve's
+    // own stopping point.
+    GSLS_TRY(t->ValK32.alloc(sizeof(float) * vk + 64));
+    GSLS_TRY(t->ir.alloc(sizeof(double) * 3 * nr));
+    double *r = t->ir.as<double>(), *d = r + nr, *Kx = d + nr;
+    k_d2f<<<nblk(vk), kT, 0, st>>>(vk, t->ValK.as<double>(), t->ValK32.as<float>());
+    GSLS_CHECK_LAUNCH();
+    GSLS_CUDA(cudaMemsetAsync(lam, 0, sizeof(double) * nr, st));
+    GSLS_CUDA(cudaMemcpyAsync(r, g, sizeof(double) * nr, cudaMemcpyDeviceToDevice, st));
+    double n0 = 0.0;
+    bool conv = false;
+    for (int sweep = 0; sweep < 16 && !conv; sweep++) {
+      double rn = 0.0;
+      GSLS_TRY(gsls_norm_dev(lhs, p.dof, r, &rn));
+      if (!(rn > 0.0)) {
+        conv = rn == 0.0;  // lambda is exact (or the residual is not finite)
+        break;
+      }
+      GSLS_CUDA(cudaMemcpyAsync(d, r, sizeof(double) * nr, cudaMemcpyDeviceToDevice, st));
+      k_scale<<<nblk(nr), kT, 0, st>>>(nr, d, 1.0 / rn);
+      GSLS_CHECK_LAUNCH();
+      gsls_ls l32 = ls;
+      l32.RI.relTol = 1e-4;
+      l32.RI.absTol = sweep == 0 ? 1e-300 : 1e-12 * n0 / rn;
+      GSLS_TRY(solve_dev(lhs, &l32, p.dof, d, t->ValK32.p, GSLS_PREC_MIXED, eq->sv.prec, true,
+                         sweep > 0));
+      if (sweep == 0) n0 = l32.RI.iNorm * rn;
+      if (sweep > 0 && l32.RI.itr == 0 && l32.RI.suc) {
+        conv = true;  // |W r| <= 1e-12 |W g| before this sweep
+        break;
+      }
+      if (!l32.RI.suc) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "adjoint: refinement sweep %d did not converge (%d iterations, |Wr| %.3e of "
+                 "%.3e, final %.3e)",
+                 sweep, l32.RI.itr, l32.RI.iNorm, n0, l32.RI.fNorm);
+        set_error(msg);
+        return GSLS_ERR_NAN;
+      }
+      k_axpyc<<<nblk(nr), kT, 0, st>>>(nr, lam, rn, d);
+      GSLS_CHECK_LAUNCH();
+      GSLS_TRY(spmv_launch(lhs, p.dof, t->Val0.p, GSLS_PREC_FP64, lam, Kx, GSLS_PREC_FP64));
+      k_resid<<<nblk(nr), kT, 0, st>>>(nr, r, g, Kx);
+      GSLS_CHECK_LAUNCH();
+    }
+    if (!conv) {
+      set_error("adjoint: mixed-precision refinement did not reach 1e-12");
+      return GSLS_ERR_NAN;
+    }
+    return GSLS_OK;
+  }
   GSLS_TRY(solve_dev(lhs, &ls, p.dof, lam, t->ValK.p, GSLS_PREC_FP64, eq->sv.prec, true));
   if (!ls.RI.suc) {
     set_error("adjoint: transpose solve did not converge");

@@ -50,26 +50,42 @@ def _J(u, sel, target):
     return 0.5 * float(np.sum(d * d))
 
 
+def _adjoint_grad(p, ep, sel, field, target, precision):
+    lhs, mesh, eq = problems.build_equation(p, precision=precision)
+    eq.set_eparam(ep)
+    tape = eq.adjoint_forward(p.nsteps, every=4)
+    st = eq.get_state()
+    uN = st[field]
+    bar = np.zeros_like(uN)
+    bar[sel] = uN[sel] - target
+    grad = tape.backward(Dbar=bar) if field == 2 else tape.backward(Ybar=bar)
+    tape.free()
+    # the equation is left at step N
+    assert np.allclose(eq.get_state()[field], uN, rtol=0, atol=0)
+    return uN, grad
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("case", ["struct", "heats"])
-def test_adjoint_gradient_matches_central_fd(gsls, case):
+def test_adjoint_gradient_matches_central_fd(gsls, case, precision):
+    """The mixed path runs the forward and recomputed steps with the FP32
+    tangent and inner CG, and each transpose solve as iterative refinement
+    (FP32 CG sweeps on FP64 residuals, to the FP64 solve's 1e-12): its
+    gradient matches the FP64 adjoint's to 1e-8 and the same central
+    differences to 1e-5."""
     p, ep, sel = _struct() if case == "struct" else _heats()
     field = 2 if case == "struct" else 1  # D (struct) or T = Y (heats)
     u0 = _final(p, ep, field)
     rng = np.random.default_rng(21)
     target = u0[sel] * (1.0 + 0.1 * rng.standard_normal(u0[sel].shape))
-    # adjoint
-    lhs, mesh, eq = problems.build_equation(p)
-    eq.set_eparam(ep)
-    tape = eq.adjoint_forward(p.nsteps, every=4)
-    st = eq.get_state()
-    uN = st[field]
-    assert np.allclose(uN, u0, rtol=0, atol=1e-12 * np.abs(u0).max())
-    bar = np.zeros_like(uN)
-    bar[sel] = uN[sel] - target
-    grad = tape.backward(Dbar=bar) if case == "struct" else tape.backward(Ybar=bar)
-    tape.free()
-    # the equation is left at step N
-    assert np.allclose(eq.get_state()[field], uN, rtol=0, atol=0)
+    prec = fsils.PREC_FP64 if precision == "fp64" else fsils.PREC_MIXED
+    uN, grad = _adjoint_grad(p, ep, sel, field, target, prec)
+    # the FP64 forward is u0 to rounding; the mixed one within the contract
+    tol = 1e-12 if precision == "fp64" else 1e-9
+    assert np.allclose(uN, u0, rtol=0, atol=tol * np.abs(u0).max())
+    if precision == "mixed":
+        _, g64 = _adjoint_grad(p, ep, sel, field, target, fsils.PREC_FP64)
+        assert np.linalg.norm(grad - g64) <= 1e-8 * np.linalg.norm(g64)
     for k in range(3):
         r = rng.standard_normal(p.nEl)
         r /= np.linalg.norm(r)
