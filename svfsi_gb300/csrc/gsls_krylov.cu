@@ -534,7 +534,11 @@ struct GatherDirL2 {
 };
 
 constexpr int kCpThreads = 512;
-template <int D, class VT, class XT>
+// LN: lanes per scalar row (D = 1 only; 4 when the co-resident grid covers
+// every row in one pass, so a row is one round of dependent loads; 1 for
+// larger systems, where the passes dominate and fewer registers keep more
+// blocks resident)
+template <int D, class VT, class XT, int LN = 1>
 __global__ void __launch_bounds__(kCpThreads) k_cg_persistent(int nNo,
                                                               const int *__restrict__ rowPtr,
                                                               const int *__restrict__ colPtr,
@@ -568,15 +572,57 @@ __global__ void __launch_bounds__(kCpThreads) k_cg_persistent(int nNo,
     const AT b = AT(beta);
     GatherDirL2<D, XT, AT, VD> gd{R, Pold, b};
     AT dot = AT(0);
-    for (int base = warp * RPW; base < nNo; base += nwarps * RPW) {
-      const int i = base + grp;
-      if (grp < RPW && i < nNo) {
-        const size_t k = (size_t)i * VD + r;
-        const AT y = spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, gd);
-        const AT pn = fma(b, AT(__ldcg(Pold + k)), AT(__ldcg(R + k)));
-        __stcg(Pnew + k, XT(pn));
-        __stcg(KP + k, XT(y));
-        dot = fma(pn, y, dot);
+    if constexpr (D == 1 && LN == 4) {
+      // scalar rows (~15 entries on tet4 meshes): 4 lanes per row, entries
+      // strided by 4 and loaded 4 at a time, so a row is one round of
+      // dependent loads; the lane sums by a fixed shuffle tree
+      constexpr int RW = 32 / LN, UL = 4;
+      const int sub = lane & (LN - 1), rg = lane / LN;
+      for (int base = warp * RW; base < nNo; base += nwarps * RW) {
+        const int i = base + rg;
+        AT y = AT(0);
+        if (i < nNo) {
+          const int j0 = __ldg(rowPtr + i), j1 = __ldg(rowPtr + i + 1);
+          for (int j = j0 + sub; j < j1; j += LN * UL) {
+            int cc[UL];
+            AT a[UL], x[UL];
+#pragma unroll
+            for (int u = 0; u < UL; u++) {
+              const int jj = j + u * LN;
+              cc[u] = jj < j1 ? __ldg(colPtr + jj) : -1;
+              a[u] = jj < j1 ? AT(__ldg(Val + jj)) : AT(0);
+            }
+#pragma unroll
+            for (int u = 0; u < UL; u++) {
+              AT xv[1] = {AT(0)};
+              if (cc[u] >= 0) gd.get(cc[u], xv);
+              x[u] = xv[0];
+            }
+#pragma unroll
+            for (int u = 0; u < UL; u++) y = fma(a[u], x[u], y);
+          }
+        }
+        y += __shfl_xor_sync(0xffffffffu, y, 1);
+        y += __shfl_xor_sync(0xffffffffu, y, 2);
+        if (i < nNo && sub == 0) {
+          const size_t k = (size_t)i * VD;
+          const AT pn = fma(b, AT(__ldcg(Pold + k)), AT(__ldcg(R + k)));
+          __stcg(Pnew + k, XT(pn));
+          __stcg(KP + k, XT(y));
+          dot = fma(pn, y, dot);
+        }
+      }
+    } else {
+      for (int base = warp * RPW; base < nNo; base += nwarps * RPW) {
+        const int i = base + grp;
+        if (grp < RPW && i < nNo) {
+          const size_t k = (size_t)i * VD + r;
+          const AT y = spmv_row_comp<D, VT, AT>(i, r, rowPtr, colPtr, Val, gd);
+          const AT pn = fma(b, AT(__ldcg(Pold + k)), AT(__ldcg(R + k)));
+          __stcg(Pnew + k, XT(pn));
+          __stcg(KP + k, XT(y));
+          dot = fma(pn, y, dot);
+        }
       }
     }
     {
@@ -1077,13 +1123,22 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
                                                     0);
       return nb;
     }();
-    constexpr int RPW = 32 / D, WPB = kCpThreads / 32;
+    static const int per_sm4 = [] {
+      int nb = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cg_persistent<D, VT, XT, 4>,
+                                                    kCpThreads, 0);
+      return nb;
+    }();
+    constexpr int WPB = kCpThreads / 32;
+    // scalar rows: 4 lanes per row when one pass covers them all
+    const bool four = D == 1 && (long long)per_sm4 * num_sms() * WPB * 8 >= nNo;
+    const int RPW = four ? 8 : 32 / D;  // rows per warp
     const long long warps = ((long long)nNo + RPW - 1) / RPW;
     long long gp = (warps + WPB - 1) / WPB;
-    const long long gmax = (long long)per_sm * num_sms();
+    const long long gmax = (long long)(four ? per_sm4 : per_sm) * num_sms();
     if (gp > gmax) gp = gmax;
     if (gp < 1) gp = 1;
-    if (per_sm < 1) {
+    if ((four ? per_sm4 : per_sm) < 1) {
       set_error("CG: the persistent kernel does not fit on an SM");
       return GSLS_ERR_CUDA;
     }
@@ -1096,8 +1151,9 @@ static int cg_t(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, double *R, const 
     void *args[] = {&nNo_, (void *)&rp, (void *)&cp, (void *)&Val, &v, &S, &part, &gb, &spin};
     const bool prof_p = prof_on();
     if (prof_p) cudaEventRecord(prof_event(0), st);
-    GSLS_CUDA(cudaLaunchCooperativeKernel((const void *)k_cg_persistent<D, VT, XT>, dim3((int)gp),
-                                          dim3(kCpThreads), args, 0, st));
+    const void *kfn = four ? (const void *)k_cg_persistent<D, VT, XT, 4>
+                           : (const void *)k_cg_persistent<D, VT, XT>;
+    GSLS_CUDA(cudaLaunchCooperativeKernel(kfn, dim3((int)gp), dim3(kCpThreads), args, 0, st));
     GSLS_CHECK_LAUNCH();
     if (prof_p) cudaEventRecord(prof_event(1), st);
   }
