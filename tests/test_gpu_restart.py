@@ -6,14 +6,17 @@ Code/Source/svFSI/OUTPUT.f:132-232, INITIALIZE.f:152-163 and 508-621):
   IKIND*(1+7) + RKIND*(2 + nEq + nX + i*tnNo);
 * a run interrupted by write/read continues bit for bit as the
   uninterrupted run (state, time, Newton normalisation and cell state
-  restored);
+  restored), in FP64 and in mixed precision (whose solver caches -- the kept
+  linear tangent, the first CG batch size -- change no arithmetic);
 * a file of another problem is rejected, naming the stamp field.
 """
 import numpy as np
 import pytest
 
-from svfsi_gb300 import problems
+from svfsi_gb300 import fsils, problems
 from svfsi_gb300._lib import GslsError
+
+PRECS = {"fp64": fsils.PREC_FP64, "mixed": fsils.PREC_MIXED}
 
 pytestmark = pytest.mark.gpu
 
@@ -39,13 +42,14 @@ def _parse(path, nNo, tDof, dFlag, nxion=0):
     return out
 
 
-def test_struct_restart_layout_and_bitwise_resume(gsls, tmp_path):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_struct_restart_layout_and_bitwise_resume(gsls, tmp_path, precision):
     p = problems.struct_beam(8, 2, 2, nsteps=4)
-    _, _, ref = problems.build_equation(p)
+    _, _, ref = problems.build_equation(p, precision=PRECS[precision])
     for _ in range(4):
         ref.step()
     Ar, Yr, Dr = ref.get_state()
-    _, _, eq = problems.build_equation(p)
+    _, _, eq = problems.build_equation(p, precision=PRECS[precision])
     for _ in range(2):
         eq.step()
     f = tmp_path / "stFile_last.bin"
@@ -58,7 +62,7 @@ def test_struct_restart_layout_and_bitwise_resume(gsls, tmp_path):
     assert rec["iNorm"] > 0
     assert np.array_equal(rec["Y"], Y2) and np.array_equal(rec["A"], A2)
     assert np.array_equal(rec["D"], D2)
-    _, _, res = problems.build_equation(p)
+    _, _, res = problems.build_equation(p, precision=PRECS[precision])
     cts, cpu = res.read_restart(f)
     assert (cts, cpu) == (2, 1.5)
     for _ in range(2):
@@ -67,20 +71,21 @@ def test_struct_restart_layout_and_bitwise_resume(gsls, tmp_path):
     assert np.array_equal(A, Ar) and np.array_equal(Y, Yr) and np.array_equal(D, Dr)
 
 
-def test_cep_restart_carries_the_cell_state(gsls, tmp_path):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cep_restart_carries_the_cell_state(gsls, tmp_path, precision):
     p = problems.cep_slab(6, 6, 2, nsteps=6, A=52.0)
-    _, _, ref = problems.build_equation(p)
+    _, _, ref = problems.build_equation(p, precision=PRECS[precision])
     for _ in range(6):
         ref.step()
     Yr = ref.get_state()[1]
-    _, _, eq = problems.build_equation(p)
+    _, _, eq = problems.build_equation(p, precision=PRECS[precision])
     for _ in range(3):
         eq.step()
     f = tmp_path / "cep.bin"
     eq.write_restart(f, 3)
     rec = _parse(f, p.nNo, 1, False, nxion=2)
     assert rec["stamp"] == [1, 1, 1, p.nNo, 0, 1, 0]
-    _, _, res = problems.build_equation(p)
+    _, _, res = problems.build_equation(p, precision=PRECS[precision])
     res.read_restart(f)
     for _ in range(3):
         res.step()
