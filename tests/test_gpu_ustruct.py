@@ -82,6 +82,38 @@ def test_ustruct_steps_match_oracle(gsls, orc, nu, precision):
     assert np.abs(D[:, :3]).max() > 1e-3          # the beam did bend
 
 
+def test_ustruct_medium_beam_matches_oracle(gsls, orc):
+    """The 66x16x16-hex beam (101,376 tets) at the benchmark's settings (the
+    reference's default GMRES, Newton tol 1e-8 and limit 10): one step in
+    FP64 and mixed precision against the oracle's step on all host cores
+    (coloured OpenMP assembly), equal Newton counts, FP64 1e-10 and mixed
+    1e-8 on the displacement and the pressure."""
+    import os
+    p = problems.ustruct_beam(66, 16, 16, nsteps=1)
+    assert p.nEl == 101_376
+    orc.set_threads(os.cpu_count() or 1)
+    try:
+        oeq = orc.OracleEquation(p, colored=True)
+        oeq.set_state(*p.initial_state())
+        no = oeq.step().newton_itr
+    finally:
+        orc.set_threads(1)
+    Ao, Yo, Do = oeq.state()
+    for precision, tol in (("fp64", 1e-10), ("mixed", 1e-8)):
+        prec = fsils.PREC_FP64 if precision == "fp64" else fsils.PREC_MIXED
+        lhs, mesh, eq = problems.build_equation(p, precision=prec)
+        gi = eq.step()
+        A, Y, D = eq.get_state()
+        eq.free()
+        mesh.free()
+        lhs.free()
+        print(f"ustruct 66x16x16 {precision}: newton {gi.newton_itr} (oracle {no}); rel D "
+              f"{rel(D[:, :3], Do[:, :3]):.2e} p {rel(Y[:, 3], Yo[:, 3]):.2e}")
+        assert gi.newton_itr == no
+        assert rel(D[:, :3], Do[:, :3]) < tol
+        assert rel(Y[:, 3], Yo[:, 3]) < tol
+
+
 def test_ustruct_restart_is_rejected(gsls, tmp_path):
     p = problems.ustruct_beam(4, 2, 2, nsteps=1)
     lhs, mesh, eq = problems.build_equation(p)
