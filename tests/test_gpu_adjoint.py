@@ -228,20 +228,35 @@ def _cep_T_oracle(orc, p, ep):
     return T
 
 
-def test_cep_activation_adjoint_matches_fd(gsls, orc):
-    p, ep = _cep()
-    rng = np.random.default_rng(31)
-    Tstar = _cep_T_gpu(p, ep * np.exp(0.05 * rng.standard_normal(p.nEl)))
-    lhs, mesh, eq = problems.build_equation(p)
+def _cep_adjoint(p, ep, Tstar, precision):
+    lhs, mesh, eq = problems.build_equation(p, precision=precision)
     eq.set_eparam(ep)
     T, tape = eq.cep_adjoint_forward(p.nsteps, every=25, vth=CEP_VTH, vw=CEP_VW)
-    # the front crossed part of the slab: activation times spread over the run
-    assert T.min() < 2.0 and np.percentile(T, 50) < 0.9 * p.nsteps * p.params["dt"]
-    assert np.allclose(T, _cep_T_gpu(p, ep), rtol=0, atol=1e-12 * T.max())
     YN = eq.get_state()[1].copy()
     grad = tape.backward(T - Tstar)
     tape.free()
     assert np.array_equal(eq.get_state()[1], YN)       # left at step N
+    return T, grad
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cep_activation_adjoint_matches_fd(gsls, orc, precision):
+    """FP64: the gradient against central differences of the GPU's and the
+    oracle's activation times.  Mixed (FP32 tangent and CG in the steps,
+    refined transpose solves): against the FP64 gradient to 1e-8 and the
+    same central differences."""
+    p, ep = _cep()
+    rng = np.random.default_rng(31)
+    Tstar = _cep_T_gpu(p, ep * np.exp(0.05 * rng.standard_normal(p.nEl)))
+    prec = fsils.PREC_FP64 if precision == "fp64" else fsils.PREC_MIXED
+    T, grad = _cep_adjoint(p, ep, Tstar, prec)
+    # the front crossed part of the slab: activation times spread over the run
+    assert T.min() < 2.0 and np.percentile(T, 50) < 0.9 * p.nsteps * p.params["dt"]
+    tol_T = 1e-12 if precision == "fp64" else 1e-9
+    assert np.allclose(T, _cep_T_gpu(p, ep), rtol=0, atol=tol_T * T.max())
+    if precision == "mixed":
+        _, g64 = _cep_adjoint(p, ep, Tstar, fsils.PREC_FP64)
+        assert np.linalg.norm(grad - g64) <= 1e-8 * np.linalg.norm(g64)
 
     def J(Tx):
         d = Tx - Tstar
@@ -255,8 +270,9 @@ def test_cep_activation_adjoint_matches_fd(gsls, orc):
         fd = (J(_cep_T_gpu(p, ep + FD_H * dp)) - J(_cep_T_gpu(p, ep - FD_H * dp))) / (2 * FD_H)
         ad = float(grad @ dp)
         errs.append(abs(fd - ad) / abs(ad))
-        print(f"CEP adjoint direction {k}: fd {fd:.12e} adjoint {ad:.12e} rel {errs[-1]:.2e}")
-        if k == 0:
+        print(f"CEP adjoint ({precision}) direction {k}: fd {fd:.12e} adjoint {ad:.12e} "
+              f"rel {errs[-1]:.2e}")
+        if k == 0 and precision == "fp64":
             # and against finite differences of the oracle's own steps
             fdo = (J(_cep_T_oracle(orc, p, ep + FD_H * dp)) -
                    J(_cep_T_oracle(orc, p, ep - FD_H * dp))) / (2 * FD_H)
