@@ -409,7 +409,7 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
   constexpr bool kExplicitNorm = sizeof(XT) == 4;
   GSLS_TRY(ws.basis.alloc(sizeof(XT) * ld * (size_t)(sD + 1)));
   const int G = lhs->grid;
-  const int Gd = num_sms() * 2;
+  const int Gd = num_sms() * 4;  // multi-dot grid: 4 co-resident blocks per SM
   const size_t hbytes = sizeof(double) * ((size_t)(sD + 1) * sD + 6 * (sD + 2)) + 64;
   GSLS_TRY(ws.hcol.alloc(hbytes + sizeof(GmresCtl) + 64));
   GSLS_TRY(ws.partials.alloc(sizeof(double) * (size_t)(sD + 2) * (Gd > G ? Gd : G) + 64));

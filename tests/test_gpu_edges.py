@@ -37,11 +37,11 @@ def _lhs(p):
     return lhs
 
 
-def _oracle_solve(orc, p, lt, mitr, R, V):
+def _oracle_solve(orc, p, lt, mitr, R, V, rtol):
     s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
     dirn = p.dirichlet[0].nodes
     s.bc_create(1, dirn, 3, 0, np.zeros((dirn.size, 3)))
-    ls = orc.ls_create(lt, relTol=1e-8, mItr=mitr)
+    ls = orc.ls_create(lt, relTol=rtol, mItr=mitr)
     s.solve(ls, 1, R, V, orc.PRECOND_FSILS)
     return ls
 
@@ -53,23 +53,35 @@ def test_degenerate_solves_match_oracle(gsls, orc, lstype, case):
     BiCGStab report success after no iteration; GMRES returns before its
     first restart with suc false).  maxItr = 1: one CG / BiCGStab iteration
     (suc false) or one GMRES restart (it converges inside it); counts,
-    flags and solution as the oracle's."""
+    flags and solution as the oracle's.
+
+    GMRES's stop test and its fNorm read the Givens residual estimate
+    |err(i+1)| (GMRES.f:161), and the Pythagorean norm sqrt|v.v - sum
+    h_j^2| resolves h_{i+1,i} only to about sqrt(eps)|v|.  On this system
+    the oracle's estimates after 7..12 inner iterations are 3.4e-5, 5.5e-6,
+    9.4e-7, 1.6e-7, 2.1e-8 and 9.1e-9 of the initial norm; from the 11th on
+    they are at that resolution (the GPU, summing the dot products in
+    another order, reads 3.0e-9 at the 11th), so the count and fNorm at a
+    1e-8 threshold depend on rounding.  The GMRES restart therefore stops
+    at 2.5e-6, after the 9th iteration, with the iterations either side a
+    factor 2 or more from the threshold."""
     p, R0, V0 = _system(orc)
     t = {"cg": fsils.LS_TYPE_CG, "gmres": fsils.LS_TYPE_GMRES, "bicgs": fsils.LS_TYPE_BICGS}[lstype]
     mitr = 1 if case == "one_iteration" else 500
+    rtol = 2.5e-6 if (lstype, case) == ("gmres", "one_iteration") else 1e-8
     Rin = np.zeros_like(R0) if case == "zero" else R0.copy()
     lhs = _lhs(p)
-    ls = fsils.FSILS_LS_CREATE(t, relTol=1e-8, maxItr=mitr)
+    ls = fsils.FSILS_LS_CREATE(t, relTol=rtol, maxItr=mitr)
     R, V = Rin.copy(), V0.copy()
     fsils.FSILS_SOLVE(lhs, ls, 1, R, V, fsils.PRECOND_FSILS)
     Ro = Rin.copy()
-    ols = _oracle_solve(orc, p, t, mitr, Ro, V0.copy())
+    ols = _oracle_solve(orc, p, t, mitr, Ro, V0.copy(), rtol)
     assert (ls.RI.itr, ls.RI.suc) == (ols.RI.itr, ols.RI.suc)
     if case == "zero":
         assert np.all(R == 0.0) and ls.RI.iNorm == 0.0
     else:
         # GMRES's classical Gram-Schmidt with the Pythagorean norm is
-        # rounding-sensitive near convergence (its restart ends at 1e-8)
+        # rounding-sensitive near convergence
         tol = 1e-8 if lstype == "gmres" else 1e-10
         assert abs(ls.RI.fNorm - ols.RI.fNorm) <= tol * ols.RI.iNorm
         assert rel(R, Ro) < tol
