@@ -10,8 +10,8 @@
 //   lR_a += w (N_a (Td + u.Tx) + nu_g Nx_a.Tx + tauM (u.Nx_a)(Td + u.Tx))
 //   lK_ab += w T1 (nu_g Nx_a.Nx_b + (N_a + tauM u.Nx_a)(amd N_b + u.Nx_b))
 // with ks = xiX^T xiX from the geometry table and T1 = af gam dt.  The
-// point quantities are FP64 (the residual), the 16 tangent entries are
-// accumulated in VT.
+// point quantities are FP64 (the residual); the tangent's factors are
+// rounded to VT and its 16 entries formed and accumulated in VT.
 #pragma once
 
 namespace gsls {
@@ -25,13 +25,8 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
   const int4 nd = A.ien[e];
   const int n4[4] = {nd.x, nd.y, nd.z, nd.w};
   const int tD = A.tDof, s0 = A.s;
-  double Nx[3][4], K[3][3];
+  double Nx[3][4];
   const double w = c_rule.w * load_geo(A, e, Nx);
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++)
-      K[i][j] = Nx[i][0] * Nx[j][0] + Nx[i][1] * Nx[j][1] + Nx[i][2] * Nx[j][2];
   double y[4][3], Ty[4], Ta[4];
 #pragma unroll
   for (int a = 0; a < 4; a++) {
@@ -41,20 +36,33 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
     Ty[a] = __ldg(A.Yg + b + s0);
     Ta[a] = __ldg(A.Ag + b + s0);
   }
+  // ks = xiX^T xiX (GNN, NN.f:1539-1547); on a tet4 the rows of xiX are the
+  // gradients of the first three shape functions, so ks = sum_{a<3} Nx_a
+  // Nx_a^T.  The element runs on the FP64 pipe, so its quadratic forms are
+  // taken through those gradients, x.ks.x = sum_{a<3} (Nx_a.x)^2 (u.ks.u
+  // and Tx.ks.Tx), and ks:ks from the six distinct entries of the symmetric
+  // ks: the reference's quantities, rounded differently.
+  double k00 = 0, k01 = 0, k02 = 0, k11 = 0, k12 = 0, k22 = 0;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    k00 += Nx[0][a] * Nx[0][a];
+    k01 += Nx[0][a] * Nx[1][a];
+    k02 += Nx[0][a] * Nx[2][a];
+    k11 += Nx[1][a] * Nx[1][a];
+    k12 += Nx[1][a] * Nx[2][a];
+    k22 += Nx[2][a] * Nx[2][a];
+  }
+  const double kS = k00 * k00 + k11 * k11 + k22 * k22 + 2.0 * (k01 * k01 + k02 * k02 + k12 * k12);
   double Tx[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) Tx[i] = Nx[i][0] * Ty[0] + Nx[i][1] * Ty[1] + Nx[i][2] * Ty[2] + Nx[i][3] * Ty[3];
-  double kS = 0.0;
+  double NxTx[4];  // Nx_a . Tx (constant on a tet4)
 #pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) kS += K[i][j] * K[i][j];
-  double nTx = K[0][0] * Tx[0] * Tx[0] + K[1][1] * Tx[1] * Tx[1] + K[2][2] * Tx[2] * Tx[2] +
-               (K[0][1] + K[1][0]) * Tx[0] * Tx[1] + (K[0][2] + K[2][0]) * Tx[0] * Tx[2] +
-               (K[1][2] + K[2][1]) * Tx[1] * Tx[2];
+  for (int a = 0; a < 4; a++) NxTx[a] = Nx[0][a] * Tx[0] + Nx[1][a] * Tx[1] + Nx[2][a] * Tx[2];
+  double nTx = NxTx[0] * NxTx[0] + NxTx[1] * NxTx[1] + NxTx[2] * NxTx[2];  // Tx.ks.Tx
   // ISZERO (MATFUN.f:763-780): |x| < eps^2
   if (fabs(nTx) < 4.930380657631324e-32) nTx = 2.220446049250313e-16;
-  const double rnTx = 0.5 / sqrt(nTx);
+  const double rnTx = 0.5 * rsqrt(nTx);
   const double dt = A.dt, T1 = A.af * A.gam * dt, amd = A.am / T1;
   const double kT = 4.0 / (dt * dt);
   double lR[4] = {0, 0, 0, 0};
@@ -63,13 +71,24 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
   for (int a = 0; a < 4; a++)
 #pragma unroll
     for (int b = 0; b < 4; b++) lK[a][b] = VT(0);
-  VT NxN[4][4];  // Nx_a . Nx_b
+  // Nx_a . Nx_b in the tangent's precision (symmetric: 10 entries)
+  VT NxN[4][4];
+  {
+    VT nx[3][4];
 #pragma unroll
-  for (int a = 0; a < 4; a++)
+    for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int b = 0; b < 4; b++)
-      NxN[a][b] = VT(Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b]);
+      for (int a = 0; a < 4; a++) nx[i][a] = VT(Nx[i][a]);
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = a; b < 4; b++) {
+        NxN[a][b] = nx[0][a] * nx[0][b] + nx[1][a] * nx[1][b] + nx[2][a] * nx[2][b];
+        NxN[b][a] = NxN[a][b];
+      }
+  }
   const double wl = w * T1;
+  const VT wlv = VT(wl), amdv = VT(amd);
 #pragma unroll 1
   for (int g = 0; g < 4; g++) {
     double N[4];
@@ -80,28 +99,24 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
     for (int i = 0; i < 3; i++) u[i] = N[0] * y[0][i] + N[1] * y[1][i] + N[2] * y[2][i] + N[3] * y[3][i];
 #pragma unroll
     for (int a = 0; a < 4; a++) Td += N[a] * Ta[a];
-    double kU = 0.0;
+    double udNx[4];  // u . Nx_a
 #pragma unroll
-    for (int j = 0; j < 3; j++)
-#pragma unroll
-      for (int i = 0; i < 3; i++) kU += u[i] * u[j] * K[i][j];
+    for (int a = 0; a < 4; a++) udNx[a] = u[0] * Nx[0][a] + u[1] * Nx[1][a] + u[2] * Nx[2][a];
+    const double kU = udNx[0] * udNx[0] + udNx[1] * udNx[1] + udNx[2] * udNx[2];  // u.ks.u
     const double udTx = u[0] * Tx[0] + u[1] * Tx[1] + u[2] * Tx[2];
     const double r = Td + udTx;
     const double nu = A.cond + fabs(r) * rnTx;
-    const double tauM = 1.0 / sqrt(kT + kU + 3.0 * nu * nu * kS);
-    double udNx[4];
+    const double tauM = rsqrt(kT + kU + 3.0 * nu * nu * kS);
+    const double tr = tauM * r;
 #pragma unroll
-    for (int a = 0; a < 4; a++) udNx[a] = u[0] * Nx[0][a] + u[1] * Nx[1][a] + u[2] * Nx[2][a];
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-      lR[a] += w * (N[a] * r + (Nx[0][a] * Tx[0] + Nx[1][a] * Tx[1] + Nx[2][a] * Tx[2]) * nu +
-                    udNx[a] * tauM * r);
-    const VT wn = VT(wl * nu);
+    for (int a = 0; a < 4; a++) lR[a] += N[a] * r + NxTx[a] * nu + udNx[a] * tr;
+    const VT wn = VT(wl * nu), tv = VT(tauM);
     VT ta[4], tb[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-      ta[a] = VT(wl * (N[a] + tauM * udNx[a]));
-      tb[a] = VT(N[a] * amd + udNx[a]);
+      const VT un = VT(udNx[a]), na = VT(N[a]);
+      ta[a] = wlv * (na + tv * un);
+      tb[a] = na * amdv + un;
     }
 #pragma unroll
     for (int a = 0; a < 4; a++)
@@ -112,7 +127,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
   asm_colour_scatter();
 #pragma unroll
   for (int a = 0; a < 4; a++) {
-    A.R[n4[a]] += lR[a];
+    A.R[n4[a]] += w * lR[a];
     const int4 mp = A.map[(size_t)e * 4 + a];
     const int pos[4] = {mp.x, mp.y, mp.z, mp.w};
 #pragma unroll

@@ -87,13 +87,11 @@ __global__ void __launch_bounds__(kAsmThreads, sizeof(VT) == 4 ? 3 : 1) k_asm_st
   }
   double Fi[3][3];
   const double J = adj_det3(F, Fi);
-  {
-    const double iJ = 1.0 / J;
+  const double iJ = 1.0 / J;  // one FP64 division, also the ST91 pressure's 1/J
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+  for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int j = 0; j < 3; j++) Fi[i][j] *= iJ;
-  }
+    for (int j = 0; j < 3; j++) Fi[i][j] *= iJ;
   // Ci = C^-1 = Fi Fi^T, trC = |F|^2
   double Ci[3][3];
 #pragma unroll
@@ -114,7 +112,7 @@ __global__ void __launch_bounds__(kAsmThreads, sizeof(VT) == 4 ? 3 : 1) k_asm_st
   const double J2d = jm23(J);
   double p = 0.0, pl = 0.0;
   if (A.Kpen != 0.0) {
-    p = 0.5 * A.Kpen * (J - 1.0 / J);
+    p = 0.5 * A.Kpen * (J - iJ);
     pl = A.Kpen * J;
   }
   const double r1 = J2d * g1 * trC / 3.0;
