@@ -63,8 +63,7 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
   // ISZERO (MATFUN.f:763-780): |x| < eps^2
   if (fabs(nTx) < 4.930380657631324e-32) nTx = 2.220446049250313e-16;
   const double rnTx = 0.5 * rsqrt(nTx);
-  const double dt = A.dt, T1 = A.af * A.gam * dt, amd = A.am / T1;
-  const double kT = 4.0 / (dt * dt);
+  const double T1 = A.af * A.gam * A.dt, amd = A.hf_amd, kT = A.hf_kT;
   double lR[4] = {0, 0, 0, 0};
   VT lK[4][4];
 #pragma unroll
