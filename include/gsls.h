@@ -227,6 +227,16 @@ typedef struct {
                        (MATMODELS.f:1020-1070): 0 quadratic, 1 ST91, 2 M94;
                        USTRUCT also reads rho, C10 (neo-Hookean), Kpen
                        (0: incompressible), visc, fb, elM, nu, ctM, ctC */
+  /* CEP fibres (CEP3D without electromechanical coupling,
+     Code/Source/svFSI/CEP.f:136-266): the diffusion tensor of element e is
+     D_e = Diso I + sum_i Dani[i] f_i f_i^T with the fibre directions
+     f_i = fN[e*3*nFn + 3*i + (0..2)] used as given (lM%fN).  The reference
+     repeats its last configured Dani for further mesh fibres (CEP.f:
+     158-165); here Dani holds one value per fibre.  nFn = 0: isotropic
+     (fN NULL).  Other physics take no fibres (GSLS_ERR_ARG). */
+  int nFn;          /* fibre families per element, 0..3 */
+  double Dani[3];   /* anisotropic diffusivity of each family */
+  const double *fN; /* host, 3*nFn per element (original order), or NULL */
 } gsls_eq_params;
 
 #define GSLS_VISC_CONST 0

@@ -42,7 +42,8 @@ class EqP(C.Structure):
                 ("ctC", C.c_double), ("eparam", c_double_p), ("elM", C.c_double),
                 ("nu", C.c_double), ("viscType", C.c_int), ("mu_o", C.c_double),
                 ("vlam", C.c_double), ("va", C.c_double), ("vn", C.c_double),
-                ("bstab", C.c_double), ("volType", C.c_int)]
+                ("bstab", C.c_double), ("volType", C.c_int), ("nFn", C.c_int),
+                ("Dani", C.c_double * 3), ("fN", c_double_p)]
 
 
 class DirBC(C.Structure):
@@ -178,14 +179,21 @@ def lhsa(nNo, ien):
 
 
 def eqp_from(problem, eparam=None) -> EqP:
+    """The problem's parameters; its CEP fibres (nEl x 3 nFn, original
+    element order) are held by the returned structure."""
     p = EqP()
     p.phys, p.dof, p.tDof, p.s = problem.phys, problem.dof, problem.tDof, getattr(problem, "s", 0)
     for k, v in problem.params.items():
-        if k == "fb":
-            for i in range(3):
-                p.fb[i] = v[i]
+        if k in ("fb", "Dani"):
+            for i, vi in enumerate(v):
+                getattr(p, k)[i] = vi
         else:
             setattr(p, k, v)
+    fib = getattr(problem, "fibers", None)
+    if fib is not None:
+        p._fib = f64(fib)
+        p.nFn = p._fib.shape[1] // 3
+        p.fN = dp(p._fib)
     return p
 
 
@@ -301,7 +309,10 @@ class OracleEquation:
             return a
 
         eq = Eq()
-        eq.p = eqp_from(p)
+        ep_ = eqp_from(p)
+        if hasattr(ep_, "_fib"):
+            keep(ep_._fib)  # eq.p is a copy: the fibre array must outlive it
+        eq.p = ep_
         ep = eparam if eparam is not None else p.eparam
         if ep is not None:
             eq.p.eparam = dp(keep(f64(ep)))

@@ -131,6 +131,9 @@ typedef struct {
   double mu_o, vlam, va, vn;   /* mu_o, lam, a, n of the model (mu_i = mu_f) */
   double bstab;                /* FLUID backflow_stab (F/READFILES.f:1089-1091) */
   int volType;                 /* USTRUCT volumetric penalty: 0 Quad, 1 ST91, 2 M94 */
+  int nFn;                     /* CEP fibre families per element (lM%nFn), 0..3 */
+  double Dani[3];              /* CEP anisotropic diffusivity per family (cep%Dani) */
+  const double *fN;            /* CEP fibre directions, 3*nFn per element (lM%fN) */
 } orc_eqp;
 
 int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
@@ -177,8 +180,10 @@ void orc_bfluid(const orc_eqp *p, int nFel, const int *fIEN, double g, int nEl,
 /* node of each face's parent element that is off the face (-1: none) */
 void orc_face_inner(int nFel, const int *fIEN, int nEl, const int *IEN, int *inner);
 
-/* CEP3D with isotropic diffusivity, F/CEP.f:136-266 (no fibres) */
-void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12],
+/* CEP3D, F/CEP.f:136-266 without electromechanical coupling: D = Diso I +
+   sum_i Dani_i f_i f_i^T with the element's fibres fN_e (3*p->nFn, or
+   NULL: isotropic) */
+void orc_elem_cep(const orc_eqp *p, double Diso, const double *fN_e, const double xl[12],
                   const double *al, const double *yl, double lR[4], double lK[16]);
 
 /* Aliev-Panfilov cell model (F/CEPMOD_AP.f, F/PARAMS_AP.f:53-86) and the

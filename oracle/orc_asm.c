@@ -537,10 +537,12 @@ void orc_elem_heatf(const orc_eqp *p, const double xl[12], const double *al,
   }
 }
 
-/* CEP3D, F/CEP.f:136-266, isotropic D = Diso I (no fibres, no
-   electromechanical coupling), one tet4 element. */
-void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12], const double *al,
-                  const double *yl, double lR[4], double lK[16]) {
+/* CEP3D, F/CEP.f:136-266 without electromechanical coupling (ecCpld
+   false: fl = fN, F/CEP.f:213-218), one tet4 element.  The diffusion
+   tensor D = Diso I plus Dani(i) fl(:,i) fl(:,i)^T per fibre
+   (F/CEP.f:221-233); fN_e NULL or p->nFn = 0: isotropic. */
+void orc_elem_cep(const orc_eqp *p, double Diso, const double *fN_e, const double xl[12],
+                  const double *al, const double *yl, double lR[4], double lK[16]) {
   double w4[4], N4[4][4], Nx[3][4], Jac;
   tet4_gauss(w4, N4);
   gnn3(xl, Nx, &Jac);
@@ -550,6 +552,12 @@ void orc_elem_cep(const orc_eqp *p, double Diso, const double xl[12], const doub
   const double amd = p->am / T1;
   const int i = p->s, tD = p->tDof;
   double D[3][3] = {{Diso, 0, 0}, {0, Diso, 0}, {0, 0, Diso}};
+  if (fN_e)
+    for (int f = 0; f < p->nFn; f++) {
+      const double *fl = fN_e + 3 * f;
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) D[r][c] = D[r][c] + p->Dani[f] * fl[r] * fl[c];
+    }
   for (int g = 0; g < 4; g++) {
     const double w = w4[g] * Jac, wl = w * T1;
     const double *N = N4[g];
@@ -849,7 +857,9 @@ int orc_assemble(const orc_eqp *p, int nNo, int nEl, const int *IEN,
       orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
     } else if (p->phys == 3) {
       double lR[4], lK[16];
-      orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso, xl, al, yl, lR, lK);
+      orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso,
+                   (p->fN && p->nFn > 0) ? p->fN + (size_t)e * 3 * p->nFn : NULL, xl, al, yl,
+                   lR, lK);
       orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
     } else if (p->phys == 4) {
       double lR[16], lK[256];
@@ -909,7 +919,9 @@ int orc_assemble_colored(const orc_eqp *p, int nNo, int nEl, const int *IEN,
         orc_doassem(3, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
       } else if (p->phys == 3) {
         double lR[4], lK[16];
-        orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso, xl, al, yl, lR, lK);
+        orc_elem_cep(p, p->eparam ? p->eparam[e] : p->Diso,
+                     (p->fN && p->nFn > 0) ? p->fN + (size_t)e * 3 * p->nFn : NULL, xl, al,
+                     yl, lR, lK);
         orc_doassem(1, 4, ptr, lK, lR, rowPtr, colPtr, R, Val);
       } else if (p->phys == 4) {
         double lR[16], lK[256];

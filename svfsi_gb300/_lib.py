@@ -45,7 +45,8 @@ class EqParams(C.Structure):
                 ("eparam", c_double_p), ("elM", C.c_double), ("nu", C.c_double),
                 ("viscType", C.c_int), ("mu_o", C.c_double), ("vlam", C.c_double),
                 ("va", C.c_double), ("vn", C.c_double), ("bstab", C.c_double),
-                ("volType", C.c_int)]
+                ("volType", C.c_int), ("nFn", C.c_int), ("Dani", C.c_double * 3),
+                ("fN", c_double_p)]
 
 
 class EqSolver(C.Structure):

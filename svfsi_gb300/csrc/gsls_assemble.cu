@@ -33,6 +33,8 @@ struct gsls_mesh {
   bool bad_jac = false;           // a zero or non-finite element Jacobian
   const double *eparam_src = nullptr;
   bool has_eparam = false;
+  gsls::DevBuf d_fib;             // CEP fibres, SoA: fib[(i*3 + k) * nEl + e] (colour order)
+  int nFn = 0;                    // fibre families in d_fib (0: none)
   // HEATS/CEP operators (built on the first heat/CEP assembly, rebuilt after
   // a new per-element parameter): the assembled mass sum_e w M_ab, the
   // assembled conduction sum_e W nu_e Nx_a.Nx_b (nu_e = 1 without a
@@ -41,6 +43,7 @@ struct gsls_mesh {
   gsls::DevBuf d_linM32, d_linK32;  // FP32 copies for the mixed-precision tangent
   bool lin_ready = false;
   unsigned lin_serial = 0;  // bumped by every build of the operators
+  double lin_key[5] = {0, 0, 0, 0, 0};  // the diffusivities the conduction operator holds
 };
 
 namespace gsls {
@@ -93,6 +96,10 @@ struct AsmArgs {
   double mu_o, vlam, va, vn;
   double E_s, nu_s;      // USTRUCT elasticity modulus and Poisson ratio (GETTAU)
   int volType;           // USTRUCT volumetric penalty (GVOLPEN)
+  double hf_amd, hf_kT;  // HEATF am / (af gam dt) and 4 / dt^2, formed once on the host
+  const double *fib;     // CEP fibre table (SoA, colour order) or null
+  int nFn;               // fibre families in fib
+  double Dani[3];        // their anisotropic diffusivities
   const int4 *ien;
   const int4 *map;  // 4 int4 per element: map[e*4 + a] = (b0..b3)
   const double *x;
@@ -171,6 +178,27 @@ __global__ void k_geo_tet4(int nEl, const int4 *__restrict__ ien, const double *
 //   lK(a,b) = wl (amd M_ab + 4 nu Nx_a . Nx_b)
 // (the reference's per-point sums, reordered).  Geometry from the per-mesh
 // table; residual FP64, tangent in VT.
+// CEP fibres (CEP3D, CEP.f:221-233): with D_e = nu I + sum_i Dani_i f_i f_i^T,
+// Nx_a . D_e Nx_b = nu Nx_a.Nx_b + sum_i Dani_i (f_i.Nx_a)(f_i.Nx_b).  fNx
+// receives f_i.Nx_a pre-scaled by Dani_i (zero past nFn).
+__device__ __forceinline__ void fibre_proj(const AsmArgs &A, int e, const double Nx[3][4],
+                                           double dfNx[3][4], double fNx[3][4]) {
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    double f[3] = {0.0, 0.0, 0.0};
+    const double d = i < A.nFn ? A.Dani[i] : 0.0;
+    if (i < A.nFn) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) f[k] = __ldg(A.fib + (size_t)(i * 3 + k) * A.nElAll + e);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      fNx[i][a] = f[0] * Nx[0][a] + f[1] * Nx[1][a] + f[2] * Nx[2][a];
+      dfNx[i][a] = d * fNx[i][a];
+    }
+  }
+}
+
 template <class VT>
 __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -200,18 +228,30 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int a = 0; a < 4; a++) Nxa[i][a] = VT(Nx[i][a]);
+  double dfNx[3][4], fNx[3][4], fTx[3] = {0.0, 0.0, 0.0};
+  if (A.nFn > 0) {
+    fibre_proj(A, e, Nx, dfNx, fNx);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      fTx[i] = fNx[i][0] * yl[0] + fNx[i][1] * yl[1] + fNx[i][2] * yl[2] + fNx[i][3] * yl[3];
+  }
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     double m = -A.src * c_rule.Ns[a];
 #pragma unroll
     for (int b = 0; b < 4; b++) m += c_rule.M[a][b] * al[b];
-    A.R[n4[a]] += w * A.rho * m + W * nu * (Nx[0][a] * Tx[0] + Nx[1][a] * Tx[1] + Nx[2][a] * Tx[2]);
+    double dx = nu * (Nx[0][a] * Tx[0] + Nx[1][a] * Tx[1] + Nx[2][a] * Tx[2]);
+    if (A.nFn > 0) dx += dfNx[0][a] * fTx[0] + dfNx[1][a] * fTx[1] + dfNx[2][a] * fTx[2];
+    A.R[n4[a]] += w * A.rho * m + W * dx;
     const int4 mp = A.map[(size_t)e * 4 + a];
     const int pos[4] = {mp.x, mp.y, mp.z, mp.w};
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       const VT dd = Nxa[0][a] * Nxa[0][b] + Nxa[1][a] * Nxa[1][b] + Nxa[2][a] * Nxa[2][b];
-      Val[pos[b]] += wl * (kM * VT(c_rule.M[a][b]) + kS * dd);
+      VT v = kM * VT(c_rule.M[a][b]) + kS * dd;
+      if (A.nFn > 0)
+        v += VT(4.0 * (dfNx[0][a] * fNx[0][b] + dfNx[1][a] * fNx[1][b] + dfNx[2][a] * fNx[2][b]));
+      Val[pos[b]] += wl * v;
     }
   }
 }
@@ -227,7 +267,10 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heats(AsmArgs A) {
 // each, k_lin_build), and every Newton assembly is one row-parallel pass:
 //   R = rho Mg Ag + nu Kg Yg - rho s b,   Val = am rho Mg + T1 nu Kg
 // (k_asm_lin).  The sums are regrouped, not changed: FP64 results agree
-// with the element-by-element loop to rounding.
+// with the element-by-element loop to rounding.  With CEP fibres the
+// conduction operator holds the whole tensor, Kg = sum_e W Nx_a . D_e Nx_b
+// with D_e = nu_e I + sum_i Dani_i f_i f_i^T (nu_e the element's parameter
+// or Diso), and the assembly passes nu = 1.
 __global__ void __launch_bounds__(kAsmThreads) k_lin_build(AsmArgs A, double *Mg, double *Kg,
                                                            double *Bg) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -238,7 +281,9 @@ __global__ void __launch_bounds__(kAsmThreads) k_lin_build(AsmArgs A, double *Mg
   double Nx[3][4];
   const double Jac = load_geo(A, e, Nx);
   const double w = c_rule.w * Jac;
-  const double Wn = 4.0 * w * (A.eparam ? A.eparam[e] : 1.0);
+  const double Wn = 4.0 * w * (A.eparam ? A.eparam[e] : (A.nFn > 0 ? A.cond : 1.0));
+  double dfNx[3][4], fNx[3][4];
+  if (A.nFn > 0) fibre_proj(A, e, Nx, dfNx, fNx);
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     Bg[n4[a]] += w * c_rule.Ns[a];
@@ -247,7 +292,10 @@ __global__ void __launch_bounds__(kAsmThreads) k_lin_build(AsmArgs A, double *Mg
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       Mg[pos[b]] += w * c_rule.M[a][b];
-      Kg[pos[b]] += Wn * (Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b]);
+      double k = Wn * (Nx[0][a] * Nx[0][b] + Nx[1][a] * Nx[1][b] + Nx[2][a] * Nx[2][b]);
+      if (A.nFn > 0)
+        k += 4.0 * w * (dfNx[0][a] * fNx[0][b] + dfNx[1][a] * fNx[1][b] + dfNx[2][a] * fNx[2][b]);
+      Kg[pos[b]] += k;
     }
   }
 }
@@ -326,7 +374,14 @@ __global__ void k_f64_to_f32(size_t n, const double *__restrict__ a, float *__re
 }
 
 static int lin_prepare(gsls_mesh *m, AsmArgs A) {
+  // the diffusivities the conduction operator holds: none without fibres
+  // (Kg = sum W nu_e k_e, nu_e = 1 or the element parameter), the fibre
+  // diffusivities and, without an element parameter, Diso with fibres
+  const double key[5] = {(double)A.nFn, A.Dani[0], A.Dani[1], A.Dani[2],
+                         (A.nFn > 0 && !A.eparam) ? A.cond : 0.0};
+  if (m->lin_ready && memcmp(key, m->lin_key, sizeof(key)) != 0) m->lin_ready = false;
   if (m->lin_ready) return GSLS_OK;
+  memcpy(m->lin_key, key, sizeof(key));
   gsls_lhs *lhs = m->lhs;
   cudaStream_t st = lhs->stream;
   GSLS_TRY(m->d_linM.alloc(sizeof(double) * (size_t)lhs->nnz));
@@ -448,6 +503,11 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
   A.E_s = p->elM;
   A.nu_s = p->nu;
   A.volType = p->volType;
+  A.hf_amd = p->am / (p->af * p->gam * p->dt);
+  A.hf_kT = 4.0 / (p->dt * p->dt);
+  A.nFn = (p->phys == GSLS_PHYS_CEP) ? m->nFn : 0;  // only CEP reads the mesh's fibres
+  A.fib = A.nFn > 0 ? m->d_fib.as<double>() : nullptr;
+  for (int i = 0; i < 3; i++) A.Dani[i] = i < A.nFn ? p->Dani[i] : 0.0;
   if (p->phys == GSLS_PHYS_USTRUCT &&
       (p->dof != 4 || p->s + 4 > p->tDof || !Dg || !Kd || !(p->am > 0.0) ||
        !(p->rho > 0.0) || !(p->elM > 0.0) || p->volType < 0 || p->volType > 2 ||
@@ -478,7 +538,8 @@ static int launch_assembly(gsls_mesh *m, const gsls_eq_params *p, const double *
     if (dof != 1) return GSLS_ERR_ARG;
     GSLS_TRY(lin_prepare(m, A));
     const double T1 = A.af * A.gam * A.dt;
-    const double nu = A.eparam ? 1.0 : A.cond;  // a per-element nu is inside Kg
+    // a per-element nu, or the whole tensor with fibres, is inside Kg
+    const double nu = (A.eparam || A.nFn > 0) ? 1.0 : A.cond;
     const long long nt = (long long)lhs->nNo * kLinLanes;
     const int nb = (int)((nt + 255) / 256);
     const int *rp = lhs->d_rowPtr.as<int>(), *cp = lhs->d_colPtr.as<int>();
@@ -748,6 +809,36 @@ int mesh_set_eparam(gsls_mesh *m, const double *eparam) {
   return GSLS_OK;
 }
 
+// CEP fibres in original element order (3*nFn per element) -> the colour-
+// ordered SoA table; nFn = 0 clears them
+int mesh_set_fibers(gsls_mesh *m, int nFn, const double *fN) {
+  if (nFn < 0 || nFn > 3 || (nFn > 0 && !fN)) {
+    set_error("fibres: nFn must be 0..3 with 3*nFn directions per element");
+    return GSLS_ERR_ARG;
+  }
+  m->lin_ready = false;  // the conduction operator holds the fibres
+  m->nFn = nFn;
+  if (nFn == 0) return GSLS_OK;
+  const size_t nE = (size_t)m->nEl;
+  std::vector<double> v(nE * 3 * nFn);
+  for (size_t i = 0; i < nE; i++) {
+    const double *f = fN + (size_t)m->perm[i] * 3 * nFn;
+    for (int k = 0; k < 3 * nFn; k++) {
+      if (!std::isfinite(f[k])) {
+        m->nFn = 0;
+        set_error("fibres: a non-finite fibre direction");
+        return GSLS_ERR_ARG;
+      }
+      v[(size_t)k * nE + i] = f[k];
+    }
+  }
+  GSLS_TRY(m->d_fib.alloc(sizeof(double) * v.size()));
+  GSLS_CUDA(cudaMemcpyAsync(m->d_fib.p, v.data(), sizeof(double) * v.size(),
+                            cudaMemcpyHostToDevice, m->lhs->stream));
+  GSLS_CUDA(cudaStreamSynchronize(m->lhs->stream));
+  return GSLS_OK;
+}
+
 int assemble_dev(gsls_mesh *m, const gsls_eq_params *p, const double *Ag, const double *Yg,
                  const double *Dg, double *R, void *Val, int val_prec, double *Kd,
                  LinAsm *la = nullptr) {
@@ -923,7 +1014,12 @@ int gsls_assemble_dev(gsls_mesh *m, const gsls_eq_params *p, const double *dAg,
                       const double *dYg, const double *dDg, double *dR, void *dVal,
                       int val_prec) {
   if (!m || !p || !dAg || !dYg || !dR || !dVal) return GSLS_ERR_ARG;
+  if (p->nFn != 0 && p->phys != GSLS_PHYS_CEP) {
+    set_error("assembly: fibres are read by CEP only");
+    return GSLS_ERR_ARG;
+  }
   GSLS_TRY(mesh_set_eparam(m, p->eparam));
+  if (p->phys == GSLS_PHYS_CEP) GSLS_TRY(mesh_set_fibers(m, p->nFn, p->fN));
   GSLS_TRY(assemble_dev(m, p, dAg, dYg, dDg, dR, dVal, val_prec, nullptr));
   GSLS_CUDA(cudaStreamSynchronize(m->lhs->stream));
   return mesh_check_error(m);
@@ -933,7 +1029,7 @@ int gsls_assemble_ustruct_dev(gsls_mesh *m, const gsls_eq_params *p, const doubl
                               const double *dYg, const double *dDg, double *dR, void *dVal,
                               double *dKd, int val_prec) {
   if (!m || !p || !dAg || !dYg || !dDg || !dR || !dVal || !dKd ||
-      p->phys != GSLS_PHYS_USTRUCT)
+      p->phys != GSLS_PHYS_USTRUCT || p->nFn != 0)
     return GSLS_ERR_ARG;
   GSLS_TRY(assemble_dev(m, p, dAg, dYg, dDg, dR, dVal, val_prec, dKd));
   GSLS_CUDA(cudaStreamSynchronize(m->lhs->stream));

@@ -23,6 +23,7 @@ int mesh_mass(gsls_mesh *m, const double *zeros, double *R, double *Val);
 const int *mesh_perm(gsls_mesh *m, int *nEl);
 int mesh_host_geometry(gsls_mesh *m, const int **ien, int *nEl, std::vector<double> &x);
 int mesh_set_eparam(gsls_mesh *m, const double *eparam);
+int mesh_set_fibers(gsls_mesh *m, int nFn, const double *fN);
 int mesh_check_error(gsls_mesh *m);
 gsls_lhs *mesh_lhs(gsls_mesh *m);
 int mesh_coords_host(gsls_mesh *m, double *x);
@@ -451,6 +452,10 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
                    const gsls_eq_solver *sv) {
   if (!out || !mesh || !p || !sv) return GSLS_ERR_ARG;
   if (p->dof < 1 || p->dof > 4 || p->s < 0 || p->s + p->dof > p->tDof) return GSLS_ERR_ARG;
+  if (p->nFn != 0 && p->phys != GSLS_PHYS_CEP) {
+    set_error("gsls_eq_create: fibres are read by CEP only");
+    return GSLS_ERR_ARG;
+  }
   if (sv->precision != GSLS_PREC_FP64 && sv->precision != GSLS_PREC_MIXED) return GSLS_ERR_ARG;
   gsls_eq *eq = new gsls_eq();
   eq->mesh = mesh;
@@ -458,6 +463,7 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
   lhs_attach(eq->lhs, &eq->lhs);
   eq->p = *p;
   eq->p.eparam = nullptr;
+  eq->p.fN = nullptr;
   eq->sv = *sv;
   if (eq->sv.maxItr <= 0) eq->sv.maxItr = 5;
   if (eq->sv.minItr <= 0) eq->sv.minItr = 1;
@@ -489,6 +495,10 @@ int gsls_eq_create(gsls_eq **out, gsls_mesh *mesh, const gsls_eq_params *p,
     return rc;
   }
   if (p->eparam && (rc = mesh_set_eparam(mesh, p->eparam)) != GSLS_OK) {
+    delete eq;
+    return rc;
+  }
+  if (p->phys == GSLS_PHYS_CEP && (rc = mesh_set_fibers(mesh, p->nFn, p->fN)) != GSLS_OK) {
     delete eq;
     return rc;
   }

@@ -48,6 +48,9 @@ MODULE GSLS_C
      REAL(C_DOUBLE) :: mu_o, vlam, va, vn
      REAL(C_DOUBLE) :: bstab
      INTEGER(C_INT) :: volType
+     INTEGER(C_INT) :: nFn = 0
+     REAL(C_DOUBLE) :: Dani(3) = 0.0_C_DOUBLE
+     TYPE(C_PTR) :: fN = C_NULL_PTR
   END TYPE gsls_eq_params
 
   INTERFACE

@@ -68,6 +68,8 @@ CONTAINS
     INTEGER(C_INT) :: istat
     INTEGER(C_INT), ALLOCATABLE :: ien(:,:)
     REAL(C_DOUBLE), ALLOCATABLE :: xx(:,:)
+    REAL(C_DOUBLE), ALLOCATABLE, TARGET, SAVE :: fib(:,:)
+    INTEGER :: i
 
     IF (.NOT. C_ASSOCIATED(gslsMesh(iM))) THEN
        ien = INT(lM%IEN, C_INT)
@@ -77,6 +79,20 @@ CONTAINS
        IF (istat .NE. GSLS_OK) err = "gsls_mesh_create: "//TRIM(gsls_error_text())
     END IF
     CALL GSLS_PARAMS(p)
+    IF (p%phys .EQ. GSLS_PHYS_CEP .AND. ALLOCATED(lM%fN)) THEN
+       ! CEP3D's fibres (F/CEP.f:89-93) and one Dani per family, the last
+       ! configured value repeated (F/CEP.f:158-165)
+       fib = REAL(lM%fN, C_DOUBLE)
+       p%nFn = INT(MIN(lM%nFn, 3), C_INT)
+       DO i = 1, p%nFn
+          IF (i .LE. eq(cEq)%dmn(1)%cep%nFn) THEN
+             p%Dani(i) = eq(cEq)%dmn(1)%cep%Dani(i)
+          ELSE IF (i .GT. 1) THEN
+             p%Dani(i) = p%Dani(i-1)
+          END IF
+       END DO
+       p%fN = C_LOC(fib)
+    END IF
     istat = gsls_assemble(gslsMesh(iM), p, Ag, Yg, Dg, R, Val)
     IF (istat .NE. GSLS_OK) err = "gsls_assemble: "//TRIM(gsls_error_text())
   END SUBROUTINE GSLS_GLOBALEQASSEM

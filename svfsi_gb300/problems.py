@@ -18,6 +18,7 @@ Poiseuille flow in the fluid cylinder.
 """
 from __future__ import annotations
 
+import ctypes as C
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -86,6 +87,7 @@ class Problem:
     absTol: float = 1e-15
     nsteps: int = 10
     eparam: np.ndarray | None = None
+    fibers: np.ndarray | None = None  # CEP fibre directions, nEl x 3 nFn (params: Dani)
     cep: dict | None = None         # cell model and stimulus (CEP only)
     stim: np.ndarray | None = None  # per-node stimulus flag (CEP only)
     s: int = 0                      # first unknown of this equation in the state
@@ -104,14 +106,20 @@ class Problem:
         return int(self.colPtr.size)
 
     def eq_params(self) -> EqParams:
+        """gsls_eq_params of the problem; the fibre array its fN points to
+        is held by the returned structure."""
         p = EqParams()
         p.phys, p.dof, p.tDof, p.s = self.phys, self.dof, self.tDof, self.s
         for k, v in self.params.items():
-            if k == "fb":
-                for i in range(3):
-                    p.fb[i] = v[i]
+            if k in ("fb", "Dani"):
+                for i, vi in enumerate(v):
+                    getattr(p, k)[i] = vi
             else:
                 setattr(p, k, v)
+        if self.fibers is not None:
+            p._fib = np.ascontiguousarray(self.fibers, dtype=np.float64)
+            p.nFn = p._fib.shape[1] // 3
+            p.fN = p._fib.ctypes.data_as(C.POINTER(C.c_double))
         return p
 
     def eq_solver(self, precision=PREC_FP64) -> EqSolver:
@@ -236,24 +244,46 @@ def ustruct_beam(nx: int = 24, ny: int = 6, nz: int = 6, nsteps: int = 10,
                    nsteps=nsteps)
 
 
+def slab_fibers(x: np.ndarray, ien: np.ndarray, nFn: int, depth: float = 2.0,
+                angles=(-60.0, 60.0)) -> np.ndarray:
+    """Synthetic myocardial fibre field on a slab, per element (nEl x 3 nFn):
+    family 1 lies in the x-y plane at an angle turning linearly through the
+    thickness (the element centroid's z) from angles[0] to angles[1]
+    degrees; family 2, when asked for, is the in-plane direction normal to
+    it; family 3 is z."""
+    zc = x[ien, 2].mean(axis=1)
+    th = np.deg2rad(angles[0] + (angles[1] - angles[0]) * np.clip(zc / depth, 0.0, 1.0))
+    fam = [np.stack([np.cos(th), np.sin(th), np.zeros_like(th)], axis=1),
+           np.stack([-np.sin(th), np.cos(th), np.zeros_like(th)], axis=1),
+           np.tile([0.0, 0.0, 1.0], (th.size, 1))]
+    return np.ascontiguousarray(np.concatenate(fam[:nFn], axis=1))
+
+
 def cep_slab(nx: int = 135, ny: int = 135, nz: int = 27, nsteps: int = 5000,
-             A: float = -52.0, ode: int = 0, Diso: float = 0.1) -> Problem:
+             A: float = -52.0, ode: int = 0, Diso: float = 0.1, nFn: int = 0,
+             Dani=(0.4, 0.05, 0.02)) -> Problem:
     """Config: monodomain electrophysiology (Aliev-Panfilov) on a 10x10x2
     slab (135x135x27 hexes -> 2,952,450 tets at full size), isotropic
     diffusivity 0.1, stimulus amplitude A for 2 ms from t = 0 on the nodes
     of the 1x1x2 corner block x <= 1, y <= 1, dt = 0.01, CG + diagonal
     preconditioner.  The reference applies a stimulus per domain; here the
-    corner block is the explicit stimulated node set."""
+    corner block is the explicit stimulated node set.  nFn > 0 adds that
+    many fibre families (slab_fibers) with anisotropic diffusivities
+    Dani[:nFn] (CEP3D's D = Diso I + sum Dani f f^T)."""
     x, ien = meshgen.kuhn_box(nx, ny, nz, 10.0, 10.0, 2.0)
     rp, cp = meshgen.csr_from_ien(x.shape[0], ien)
     am, af, beta, gam = genalpha(0.2, second_order=False)
     params = dict(am=am, af=af, beta=beta, gam=gam, dt=0.01, Diso=Diso)
+    fib = None
+    if nFn > 0:
+        params["Dani"] = tuple(Dani[:nFn])
+        fib = slab_fibers(x, ien, nFn)
     stim = ((x[:, 0] <= 1.0 + 1e-12) & (x[:, 1] <= 1.0 + 1e-12)).astype(np.int32)
     cep = dict(ode=ode, dt_ode=0.01, A=A, Ts=0.0, Td=2.0, CL=1e9, V0=-80.0, X20=1e-3)
-    return Problem(name=f"cep_slab_{nx}x{ny}x{nz}", x=x, ien=ien, rowPtr=rp, colPtr=cp,
-                   phys=PHYS_CEP, dof=1, tDof=1, params=params, LS_type=LS_TYPE_CG,
-                   prec=PRECOND_FSILS, minItr=1, maxItr=5, tol=1e-6, nsteps=nsteps,
-                   cep=cep, stim=stim)
+    return Problem(name=f"cep_slab_{nx}x{ny}x{nz}" + (f"_fib{nFn}" if nFn else ""), x=x,
+                   ien=ien, rowPtr=rp, colPtr=cp, phys=PHYS_CEP, dof=1, tDof=1, params=params,
+                   LS_type=LS_TYPE_CG, prec=PRECOND_FSILS, minItr=1, maxItr=5, tol=1e-6,
+                   nsteps=nsteps, cep=cep, stim=stim, fibers=fib)
 
 
 VISC_CONST, VISC_CY, VISC_CASSON = 0, 1, 2

@@ -684,6 +684,52 @@ def test_bheatf_uniform_state_kat(orc):
         assert np.allclose(rows[[0, 1, 3]], area / 3.0 * T1 * (-udn), rtol=1e-14, atol=1e-16)
 
 
+def _one_tet_cep(nFn, Dani, fib):
+    import dataclasses
+    base = problems.cep_slab(2, 2, 1, nsteps=1)
+    x = np.array([[0.1, 0.0, 0.0], [1.3, 0.2, 0.1], [0.2, 0.9, 0.3], [0.3, 0.2, 1.1]])
+    ien = np.array([[0, 1, 2, 3]], dtype=np.int32)
+    rp, cp = meshgen.csr_from_ien(4, ien)
+    params = dict(base.params)
+    if nFn:
+        params["Dani"] = tuple(Dani[:nFn])
+    return dataclasses.replace(base, x=x, ien=ien, rowPtr=rp, colPtr=cp, params=params,
+                               fibers=fib, stim=np.zeros(4, np.int32))
+
+
+@pytest.mark.parametrize("nFn", [1, 2])
+def test_cep_fibre_diffusion_kat(orc, nFn):
+    """CEP3D's anisotropic part (F/CEP.f:221-266): against the isotropic
+    element, the tangent gains T1 V sum_i Dani_i (f_i.grad N_a)(f_i.grad N_b)
+    and the residual V sum_i Dani_i (f_i.grad N_a)(f_i.grad V), with V the
+    tet's volume and grad N from the inverse Jacobian (numpy)."""
+    rng = np.random.default_rng(11)
+    f = rng.standard_normal((nFn, 3))
+    f /= np.linalg.norm(f, axis=1, keepdims=True)
+    Dani = (0.4, 0.05, 0.02)
+    p1 = _one_tet_cep(nFn, Dani, f.reshape(1, -1))
+    p0 = _one_tet_cep(0, Dani, None)
+    A = rng.standard_normal((4, 1))
+    Y = rng.standard_normal((4, 1))
+    R1, V1 = orc.assemble(p1, A, Y)
+    R0, V0 = orc.assemble(p0, A, Y)
+    x = p1.x
+    J = np.stack([x[k] - x[3] for k in range(3)], axis=1)  # dx/dxi
+    G = np.linalg.inv(J).T @ np.array([[1, 0, 0, -1], [0, 1, 0, -1], [0, 0, 1, -1]], float)
+    vol = np.linalg.det(J) / 6.0
+    fG = f @ G                            # (nFn, 4): f_i . grad N_a
+    d = np.array(Dani[:nFn])
+    K = vol * (fG.T * d) @ fG
+    T1 = p1.params["af"] * p1.params["gam"] * p1.params["dt"]
+    gradV = G @ Y[:, 0]
+    dR = vol * (fG.T * d) @ (f @ gradV)
+    # the single element's CSR rows hold columns 0..3 in order
+    assert np.array_equal(p1.colPtr, np.tile(np.arange(4), 4))
+    assert np.allclose((V1 - V0)[:, 0].reshape(4, 4), T1 * K, rtol=1e-12, atol=1e-15)
+    assert np.allclose((R1 - R0)[:, 0], dR, rtol=1e-12, atol=1e-14)
+    assert np.abs(K).max() > 1e-2
+
+
 def test_oracle_ctypes_mirrors_match_its_header(orc, tmp_path):
     """The oracle's ctypes structures have the size and field offsets that a
     C compiler gives oracle/orc.h (gcc probe)."""
