@@ -1444,52 +1444,114 @@ __global__ void k_act_src(int nNo, int tDof, int s, const double *__restrict__ Y
   }
 }
 
-// Reverse of the forward-Euler cell step of k_cep_ionic at (V, X2) =
-// (Yin or Xin(1) on the first pass, Xin(2)): Ybar (cotangent of V' on
-// entry, of V on exit) and X2bar (of X2' on entry, of X2 on exit).  With
-// X0 = (V - Voffset)/Vscale, each substep X <- X + h f(X) has the Jacobian
-// I + h df/dX of AP_GETF's right-hand side
+// Reverse of the cell step of k_cep_ionic at (V, X2) = (Yin or Xin(1) on
+// the first pass, Xin(2)): Ybar (cotangent of V' on entry, of V on exit)
+// and X2bar (of X2' on entry, of X2 on exit).  With X0 = (V - Voffset)/
+// Vscale, the Jacobian of AP_GETF's right-hand side
 //   f0 = X0 (c (X0 - alpha)(1 - X0) - X1) + fext,
-//   f1 = (a + mu1 X1/(mu2 + X0)) (-X1 - c X0 (X0 - b - 1)).
+//   f1 = (a + mu1 X1/(mu2 + X0)) (-X1 - c X0 (X0 - b - 1))
+// enters transposed: a forward-Euler substep X <- X + h f(X) (AP_INTEGFE)
+// maps B to (I + h J(X))^T B; an RK4 substep (AP_INTEGRK) with stages
+// X, Xb = X + h/2 k1, Xc = X + h/2 k2, Xd = X + h k3 and X' = X + h/6 (k1 +
+// 2 k2 + 2 k3 + k4) is reversed stage by stage (k4, k3, k2, k1), each
+// stage cotangent picking up J^T at its stage state.  The substep start
+// states are recomputed from the stored pre-step state, in the forward
+// kernel's order of operations.
 constexpr int kCepMaxSub = 32;
+__device__ __forceinline__ void ap_jt(double X0, double X1, double b0, double b1, double &o0,
+                                      double &o1) {
+  const double c = 8.0, alpha = 1e-2, aa = 2e-3, b = 0.15, mu1 = 0.2, mu2 = 0.3;
+  const double d00 = c * (X0 - alpha) * (1.0 - X0) - X1 + c * X0 * (1.0 + alpha - 2.0 * X0);
+  const double d01 = -X0;
+  const double gg = aa + mu1 * X1 / (mu2 + X0);
+  const double q = -X1 - c * X0 * (X0 - b - 1.0);
+  const double dg0 = -mu1 * X1 / ((mu2 + X0) * (mu2 + X0)), dg1 = mu1 / (mu2 + X0);
+  const double dq0 = -c * (2.0 * X0 - b - 1.0), dq1 = -1.0;
+  const double d10 = dg0 * q + gg * dq0, d11 = dg1 * q + gg * dq1;
+  o0 = d00 * b0 + d10 * b1;
+  o1 = d01 * b0 + d11 * b1;
+}
+
 __global__ void k_cep_ionic_rev(int nNo, int tDof, int s, const double *__restrict__ Yin,
                                 const double *__restrict__ Xin, const int *__restrict__ stim,
-                                int first, int nt, double dt_ode, double t1, double Ts, double Te,
-                                double A, double *__restrict__ Ybar, double *__restrict__ X2bar) {
+                                int first, int ode, int nt, double dt_ode, double t1, double Ts,
+                                double Te, double A, double *__restrict__ Ybar,
+                                double *__restrict__ X2bar) {
   const double Vscale = 100.0, Tscale = 12.9, Voffset = -80.0;
-  const double c = 8.0, alpha = 1e-2, aa = 2e-3, b = 0.15, mu1 = 0.2, mu2 = 0.3;
   const double eps = 2.220446049250313e-16;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nNo; a += gridDim.x * blockDim.x) {
     const double V = first ? Xin[2 * (size_t)a] : Yin[(size_t)a * tDof + s];
     const bool st = stim && stim[a];
     const double h = dt_ode / Tscale;
-    double X0s[kCepMaxSub], X1s[kCepMaxSub];
+    double X0s[kCepMaxSub], X1s[kCepMaxSub], Fx[kCepMaxSub];
     double x0 = V, x1 = Xin[2 * (size_t)a + 1];
     for (int i = 0; i < nt; i++) {
       const double t = t1 + (double)i * dt_ode;
       const double Istim = (st && t >= Ts - eps && t <= Te + eps) ? A : 0.0;
       const double fext = Istim * Tscale / Vscale;
-      double X0 = (x0 - Voffset) / Vscale, X1 = x1, f0, f1;
+      double X0 = (x0 - Voffset) / Vscale, X1 = x1;
       X0s[i] = X0;
       X1s[i] = X1;
-      ap_f<double>(X0, X1, fext, f0, f1);
-      x0 = (X0 + h * f0) * Vscale + Voffset;
-      x1 = X1 + h * f1;
+      Fx[i] = fext;
+      if (ode == 0) {
+        double f0, f1;
+        ap_f<double>(X0, X1, fext, f0, f1);
+        X0 = X0 + h * f0;
+        X1 = X1 + h * f1;
+      } else {
+        double k0[4], k1[4];
+        ap_f<double>(X0, X1, fext, k0[0], k1[0]);
+        ap_f<double>(X0 + 0.5 * h * k0[0], X1 + 0.5 * h * k1[0], fext, k0[1], k1[1]);
+        ap_f<double>(X0 + 0.5 * h * k0[1], X1 + 0.5 * h * k1[1], fext, k0[2], k1[2]);
+        ap_f<double>(X0 + h * k0[2], X1 + h * k1[2], fext, k0[3], k1[3]);
+        const double h6 = h / 6.0;
+        X0 = X0 + h6 * (k0[0] + 2.0 * (k0[1] + k0[2]) + k0[3]);
+        X1 = X1 + h6 * (k1[0] + 2.0 * (k1[1] + k1[2]) + k1[3]);
+      }
+      x0 = X0 * Vscale + Voffset;
+      x1 = X1;
     }
     double B0 = Ybar[a] * Vscale, B1 = X2bar[a];
     for (int i = nt - 1; i >= 0; i--) {
       const double X0 = X0s[i], X1 = X1s[i];
-      const double d00 = c * (X0 - alpha) * (1.0 - X0) - X1 + c * X0 * (1.0 + alpha - 2.0 * X0);
-      const double d01 = -X0;
-      const double gg = aa + mu1 * X1 / (mu2 + X0);
-      const double q = -X1 - c * X0 * (X0 - b - 1.0);
-      const double dg0 = -mu1 * X1 / ((mu2 + X0) * (mu2 + X0)), dg1 = mu1 / (mu2 + X0);
-      const double dq0 = -c * (2.0 * X0 - b - 1.0), dq1 = -1.0;
-      const double d10 = dg0 * q + gg * dq0, d11 = dg1 * q + gg * dq1;
-      const double n0 = B0 * (1.0 + h * d00) + B1 * h * d10;
-      const double n1 = B0 * h * d01 + B1 * (1.0 + h * d11);
-      B0 = n0;
-      B1 = n1;
+      if (ode == 0) {
+        double j0, j1;
+        ap_jt(X0, X1, B0, B1, j0, j1);
+        B0 += h * j0;
+        B1 += h * j1;
+      } else {
+        // stage states of the forward substep
+        const double fext = Fx[i];
+        double a0, a1, b0, b1, c0, c1;
+        ap_f<double>(X0, X1, fext, a0, a1);
+        const double Xb0 = X0 + 0.5 * h * a0, Xb1 = X1 + 0.5 * h * a1;
+        ap_f<double>(Xb0, Xb1, fext, b0, b1);
+        const double Xc0 = X0 + 0.5 * h * b0, Xc1 = X1 + 0.5 * h * b1;
+        ap_f<double>(Xc0, Xc1, fext, c0, c1);
+        const double Xd0 = X0 + h * c0, Xd1 = X1 + h * c1;
+        const double h6 = h / 6.0, h3 = h / 3.0;
+        double k4b0 = h6 * B0, k4b1 = h6 * B1, k3b0 = h3 * B0, k3b1 = h3 * B1;
+        double k2b0 = h3 * B0, k2b1 = h3 * B1, k1b0 = h6 * B0, k1b1 = h6 * B1;
+        double xb0 = B0, xb1 = B1, j0, j1;
+        ap_jt(Xd0, Xd1, k4b0, k4b1, j0, j1);  // k4 = f(Xd), Xd = X + h k3
+        xb0 += j0;
+        xb1 += j1;
+        k3b0 += h * j0;
+        k3b1 += h * j1;
+        ap_jt(Xc0, Xc1, k3b0, k3b1, j0, j1);  // k3 = f(Xc), Xc = X + h/2 k2
+        xb0 += j0;
+        xb1 += j1;
+        k2b0 += 0.5 * h * j0;
+        k2b1 += 0.5 * h * j1;
+        ap_jt(Xb0, Xb1, k2b0, k2b1, j0, j1);  // k2 = f(Xb), Xb = X + h/2 k1
+        xb0 += j0;
+        xb1 += j1;
+        k1b0 += 0.5 * h * j0;
+        k1b1 += 0.5 * h * j1;
+        ap_jt(X0, X1, k1b0, k1b1, j0, j1);  // k1 = f(X)
+        B0 = xb0 + j0;
+        B1 = xb1 + j1;
+      }
     }
     // on the first pass V came from Xion(1), not from the state
     Ybar[a] = first ? 0.0 : B0 / Vscale;
@@ -1506,8 +1568,8 @@ static int adj_check(gsls_eq *eq, bool cep = false) {
                     "gsls_cep_adjoint_forward/backward)");
     return GSLS_ERR_UNSUPPORTED;
   }
-  if (cep && (!eq->has_cep || eq->cep.ode != 0)) {
-    set_error("adjoint: CEP needs gsls_eq_set_cep with the forward-Euler cell step");
+  if (cep && !eq->has_cep) {
+    set_error("adjoint: CEP needs gsls_eq_set_cep (the cell model)");
     return GSLS_ERR_UNSUPPORTED;
   }
   if (p.s != 0 || p.tDof != p.dof) {
@@ -1774,8 +1836,8 @@ int gsls_cep_adjoint_backward(gsls_tape *t, const double *Tbar, double *grad) {
       // the diffusion step, then the cell step, in reverse
       GSLS_TRY(adj_reverse_step(t, so, sn));
       k_cep_ionic_rev<<<nblk(nNo), kT, 0, st>>>(nNo, tD, p.s, sp + ns, segX + (size_t)(k - 1) * nx,
-                                                eq->stim.as<int>(), first, nt, c.dt_ode, t1, Ts,
-                                                Te, c.A, Yb, t->x2bar.as<double>());
+                                                eq->stim.as<int>(), first, c.ode, nt, c.dt_ode, t1,
+                                                Ts, Te, c.A, Yb, t->x2bar.as<double>());
       GSLS_CHECK_LAUNCH();
     }
   }
