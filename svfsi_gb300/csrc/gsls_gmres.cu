@@ -409,7 +409,12 @@ static int gmres_loop(gsls_lhs *lhs, gsls_sub_ls *ls, const VT *Val, const XT *R
   constexpr bool kExplicitNorm = sizeof(XT) == 4;
   GSLS_TRY(ws.basis.alloc(sizeof(XT) * ld * (size_t)(sD + 1)));
   const int G = lhs->grid;
-  const int Gd = num_sms() * 4;  // multi-dot grid: 4 co-resident blocks per SM
+  // multi-dot grid: 4 co-resident blocks per SM for vectors of >= 2^20
+  // unknowns (USTRUCT beam, 1.43M: 0.324 -> 0.282 ms per Arnoldi step),
+  // else 2: shorter vectors, e.g. the NS solver's momentum block of the
+  // cylinder (645k), are bound by the per-block reductions, and 4 per SM
+  // made that fluid step 5 % slower
+  const int Gd = num_sms() * (nv >= ((size_t)1 << 20) ? 4 : 2);
   const size_t hbytes = sizeof(double) * ((size_t)(sD + 1) * sD + 6 * (sD + 2)) + 64;
   GSLS_TRY(ws.hcol.alloc(hbytes + sizeof(GmresCtl) + 64));
   GSLS_TRY(ws.partials.alloc(sizeof(double) * (size_t)(sD + 2) * (Gd > G ? Gd : G) + 64));
