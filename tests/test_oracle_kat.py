@@ -730,6 +730,23 @@ def test_cep_fibre_diffusion_kat(orc, nFn):
     assert np.abs(K).max() > 1e-2
 
 
+def test_slab_fibre_field():
+    """The synthetic fibre field: unit directions, family 1 at -60 degrees
+    at the bottom of the slab and +60 at the top (in the x-y plane), family
+    2 orthogonal to it in the plane, family 3 along z; element order."""
+    x, ien = meshgen.kuhn_box(4, 4, 4, 10.0, 10.0, 2.0)
+    f = problems.slab_fibers(x, ien, 3)
+    assert f.shape == (ien.shape[0], 9)
+    fam = f.reshape(-1, 3, 3)
+    assert np.allclose(np.linalg.norm(fam, axis=2), 1.0, atol=1e-15)
+    assert np.allclose(np.einsum("ei,ei->e", fam[:, 0], fam[:, 1]), 0.0, atol=1e-15)
+    assert np.allclose(fam[:, 2], [0.0, 0.0, 1.0])
+    zc = x[ien, 2].mean(axis=1)
+    ang = np.rad2deg(np.arctan2(fam[:, 0, 1], fam[:, 0, 0]))
+    assert np.allclose(ang, -60.0 + 120.0 * zc / 2.0, atol=1e-12)
+    assert np.allclose(problems.slab_fibers(x, ien, 1), f[:, :3])
+
+
 def test_oracle_ctypes_mirrors_match_its_header(orc, tmp_path):
     """The oracle's ctypes structures have the size and field offsets that a
     C compiler gives oracle/orc.h (gcc probe)."""
