@@ -351,6 +351,64 @@ def load_mesh(vtu_path, faces: dict | None = None) -> SvMesh:
     return SvMesh(v.points[:, :3].copy(), v.cells.astype(np.int32), out)
 
 
+def _fibre_block(piece: VtkPiece, name: str, nEl: int, src) -> np.ndarray:
+    a = piece.cell_data.get(name)
+    if a is None:
+        raise VtkError(f"{src}: no cell array {name}")
+    a = np.asarray(a, np.float64).reshape(piece.cells.shape[0], -1)
+    if a.shape[0] != nEl:
+        raise VtkError(f"{src}: {a.shape[0]} cells for {name}, the mesh has {nEl} elements")
+    out = np.zeros((nEl, 3))
+    k = min(3, a.shape[1])
+    out[:, :k] = a[:, :k]
+    return out
+
+
+def load_fibers(nEl: int, file=None, files=None, directions=None,
+                nFn: int | None = None) -> np.ndarray | None:
+    """Per-element fibre directions (the reference's lM%fN), nEl x 3 nFn in
+    element order, from the first of the reference's three sources that
+    gives fibres (Code/Source/svFSI/READMSH.f:336-420):
+
+    * ``file``: one .vtu whose cell arrays FIB_DIR1, FIB_DIR2, ... hold the
+      families (READFIBNFSF, READMSH.f:895-965); ``nFn`` families, or as
+      many as the largest index among the FIB_DIR<i> names (one digit, as
+      the reference parses it);
+    * ``files``: one .vtu per family, each with the cell array FIB_DIR
+      (READFIBNFF, READMSH.f:968-1003);
+    * ``directions``: one constant vector per family ("Fiber direction").
+
+    Every direction is normalised to unit length unless its length is zero
+    (ISZERO), as READMSH does after reading.  None when no source gives a
+    family.  The result is what ``gsls_eq_params.fN`` expects."""
+    fN = None
+    if file is not None:
+        v = read_vtu(file)
+        n = nFn or 0
+        if not n:
+            for name in v.cell_data:
+                if name.startswith("FIB_DIR") and len(name) >= 8:
+                    if not name[7].isdigit():
+                        raise VtkError(f"{file}: cannot read the fibre index of {name}")
+                    n = max(n, int(name[7]))
+        if n:
+            fN = np.concatenate([_fibre_block(v, f"FIB_DIR{i}", nEl, file)
+                                 for i in range(1, n + 1)], axis=1)
+    if fN is None and files:
+        fN = np.concatenate([_fibre_block(read_vtu(p), "FIB_DIR", nEl, p) for p in files], axis=1)
+    if fN is None and directions is not None and len(directions):
+        d = np.asarray(directions, np.float64).reshape(-1, 3)
+        fN = np.tile(d.ravel(), (nEl, 1))
+    if fN is None:
+        return None
+    fam = fN.reshape(nEl, -1, 3)
+    nrm = np.linalg.norm(fam, axis=2, keepdims=True)
+    # ISZERO: |x| / max(|x|, eps) < eps, i.e. |x| < eps^2, is zero
+    ok = nrm >= np.finfo(np.float64).eps ** 2
+    fam = np.where(ok, fam / np.where(ok, nrm, 1.0), fam)
+    return np.ascontiguousarray(fam.reshape(nEl, -1))
+
+
 def pack_struct_header(hdr_type: str, nblocks: int, bs: int, last: int, sizes) -> bytes:
     """vtkZLibDataCompressor block header (for tests and writers)."""
     c = "Q" if hdr_type == "UInt64" else "I"

@@ -1,8 +1,9 @@
 """VTK XML mesh I/O (READVTU / READVTP, Code/Source/svFSI/VTKXML.f:39-150):
 hand-written ASCII fixtures (tests/golden/two_tets.vtu, two_tets_face.vtp,
-written from the VTK XML format description), a zlib-compressed inline
-array encoded independently in the test, and round trips through the
-writer in every format / header / compression combination."""
+two_tets_fibers.vtu, written from the VTK XML format description), a
+zlib-compressed inline array encoded independently in the test, round
+trips through the writer in every format / header / compression
+combination, and the three fibre sources of READMSH."""
 import base64
 import struct
 import zlib
@@ -122,3 +123,36 @@ def test_rejects_non_tet_volume(tmp_path):
     vtkio.write_vtu(f, np.zeros((8, 3)), np.arange(8).reshape(1, 8), cell_type=12, fmt="ascii")
     with pytest.raises(vtkio.VtkError):
         vtkio.load_mesh(f)
+
+
+def test_fibres_from_one_file_fixture():
+    """READFIBNFSF: FIB_DIR1, FIB_DIR2 cell arrays, the family count from the
+    names, each direction normalised, a zero direction left zero."""
+    f = vtkio.load_fibers(2, file=GOLD / "two_tets_fibers.vtu")
+    assert f.shape == (2, 6)
+    assert np.allclose(f, [[1, 0, 0, 0, 0, 1], [0, 0.6, 0.8, 0, 0, 0]], atol=1e-15)
+    f1 = vtkio.load_fibers(2, file=GOLD / "two_tets_fibers.vtu", nFn=1)
+    assert np.array_equal(f1, f[:, :3])
+
+
+def test_fibres_from_one_file_per_family_and_uniform(tmp_path):
+    x, ien = meshgen.kuhn_box(2, 2, 1, 1.0, 1.0, 1.0)
+    rng = np.random.default_rng(3)
+    fams = [rng.standard_normal((ien.shape[0], 3)) for _ in range(2)]
+    paths = []
+    for i, a in enumerate(fams):
+        p = tmp_path / f"fib{i}.vtu"
+        vtkio.write_vtu(p, x, ien, cell_data={"FIB_DIR": a})
+        paths.append(p)
+    f = vtkio.load_fibers(ien.shape[0], files=paths)
+    want = np.concatenate([a / np.linalg.norm(a, axis=1, keepdims=True) for a in fams], axis=1)
+    assert np.allclose(f, want, atol=1e-15)
+    # a file without FIB_DIR<i> arrays gives no fibres: the next source is read
+    plain = tmp_path / "plain.vtu"
+    vtkio.write_vtu(plain, x, ien)
+    assert np.allclose(vtkio.load_fibers(ien.shape[0], file=plain, files=paths), want, atol=1e-15)
+    u = vtkio.load_fibers(ien.shape[0], directions=[[0, 0, 2.0], [1, 1, 0]])
+    assert np.allclose(u, np.tile([0, 0, 1, 2 ** -0.5, 2 ** -0.5, 0], (ien.shape[0], 1)))
+    assert vtkio.load_fibers(ien.shape[0]) is None
+    with pytest.raises(vtkio.VtkError):
+        vtkio.load_fibers(ien.shape[0] + 1, files=paths)
