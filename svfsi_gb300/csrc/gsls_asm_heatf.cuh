@@ -64,7 +64,6 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
   if (fabs(nTx) < 4.930380657631324e-32) nTx = 2.220446049250313e-16;
   const double rnTx = 0.5 * rsqrt(nTx);
   const double T1 = A.af * A.gam * A.dt, amd = A.hf_amd, kT = A.hf_kT;
-  double lR[4] = {0, 0, 0, 0};
   VT lK[4][4];
 #pragma unroll
   for (int a = 0; a < 4; a++)
@@ -86,18 +85,24 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
         NxN[b][a] = NxN[a][b];
       }
   }
+  // The tet4 rule's shape values are N_a(g) = t + (s - t) delta_ag (NN.f:
+  // 268-275), so the point values are u_g = t sum_a y_a + (s - t) y_g (and
+  // Td likewise), and the N_a r_g part of lR_a sums to t sum_g r_g +
+  // (s - t) r_a: the reference's sums, regrouped.
+  const double rt = c_rule.N[0][1], rd = c_rule.N[0][0] - c_rule.N[0][1];
+  double ys[3], Tas = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) ys[i] = rt * (y[0][i] + y[1][i] + y[2][i] + y[3][i]);
+  Tas = rt * (Ta[0] + Ta[1] + Ta[2] + Ta[3]) - A.src;
   const double wl = w * T1;
-  const VT wlv = VT(wl), amdv = VT(amd);
-#pragma unroll 1
+  const VT wlv = VT(wl), amdv = VT(amd), ntv = VT(rt), nsv = VT(c_rule.N[0][0]);
+  double rg[4], rsum = 0.0, nusum = 0.0, lRu[4] = {0, 0, 0, 0};
+#pragma unroll
   for (int g = 0; g < 4; g++) {
-    double N[4];
+    double u[3];
 #pragma unroll
-    for (int a = 0; a < 4; a++) N[a] = c_rule.N[g][a];
-    double u[3], Td = -A.src;
-#pragma unroll
-    for (int i = 0; i < 3; i++) u[i] = N[0] * y[0][i] + N[1] * y[1][i] + N[2] * y[2][i] + N[3] * y[3][i];
-#pragma unroll
-    for (int a = 0; a < 4; a++) Td += N[a] * Ta[a];
+    for (int i = 0; i < 3; i++) u[i] = ys[i] + rd * y[g][i];
+    const double Td = Tas + rd * Ta[g];
     double udNx[4];  // u . Nx_a
 #pragma unroll
     for (int a = 0; a < 4; a++) udNx[a] = u[0] * Nx[0][a] + u[1] * Nx[1][a] + u[2] * Nx[2][a];
@@ -107,13 +112,16 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
     const double nu = A.cond + fabs(r) * rnTx;
     const double tauM = rsqrt(kT + kU + 3.0 * nu * nu * kS);
     const double tr = tauM * r;
+    rg[g] = r;
+    rsum += r;
+    nusum += nu;
 #pragma unroll
-    for (int a = 0; a < 4; a++) lR[a] += N[a] * r + NxTx[a] * nu + udNx[a] * tr;
+    for (int a = 0; a < 4; a++) lRu[a] += udNx[a] * tr;
     const VT wn = VT(wl * nu), tv = VT(tauM);
     VT ta[4], tb[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-      const VT un = VT(udNx[a]), na = VT(N[a]);
+      const VT un = VT(udNx[a]), na = a == g ? nsv : ntv;
       ta[a] = wlv * (na + tv * un);
       tb[a] = na * amdv + un;
     }
@@ -122,6 +130,9 @@ __global__ void __launch_bounds__(kAsmThreads) k_asm_heatf(AsmArgs A) {
 #pragma unroll
       for (int b = 0; b < 4; b++) lK[a][b] += wn * NxN[a][b] + ta[a] * tb[b];
   }
+  double lR[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) lR[a] = rt * rsum + rd * rg[a] + NxTx[a] * nusum + lRu[a];
   VT *Val = reinterpret_cast<VT *>(A.Val);
   asm_colour_scatter();
 #pragma unroll
