@@ -190,8 +190,8 @@ def test_adjoint_solve_and_dRdp_building_blocks(gsls):
 CEP_VTH, CEP_VW = -30.0, 5.0
 
 
-def _cep(nsteps=120, ode=0):
-    p = problems.cep_slab(24, 24, 2, nsteps=nsteps, A=52.0, Diso=1.0)
+def _cep(nsteps=120, ode=0, nFn=0, Dani=(0.5, 0.1)):
+    p = problems.cep_slab(24, 24, 2, nsteps=nsteps, A=52.0, Diso=1.0, nFn=nFn, Dani=Dani)
     p.stim = (p.x[:, 0] <= 1.5).astype(np.int32)
     p.params["dt"] = 0.1
     p.cep["dt_ode"] = 0.1
@@ -241,14 +241,16 @@ def _cep_adjoint(p, ep, Tstar, precision):
     return T, grad
 
 
-@pytest.mark.parametrize("precision,ode", [("fp64", 0), ("mixed", 0), ("fp64", 1)])
-def test_cep_activation_adjoint_matches_fd(gsls, orc, precision, ode):
+@pytest.mark.parametrize("precision,ode,nFn", [("fp64", 0, 0), ("mixed", 0, 0), ("fp64", 1, 0),
+                                               ("fp64", 0, 2)])
+def test_cep_activation_adjoint_matches_fd(gsls, orc, precision, ode, nFn):
     """FP64: the gradient against central differences of the GPU's and the
     oracle's activation times.  Mixed (FP32 tangent and CG in the steps,
     refined transpose solves): against the FP64 gradient to 1e-8 and the
     same central differences.  ode = 1: the RK4 cell step (two substeps
-    per step) reversed stage by stage."""
-    p, ep = _cep(ode=ode)
+    per step) reversed stage by stage.  nFn = 2: two fibre families on top
+    of the per-element isotropic diffusivity being differentiated."""
+    p, ep = _cep(ode=ode, nFn=nFn)
     rng = np.random.default_rng(31)
     Tstar = _cep_T_gpu(p, ep * np.exp(0.05 * rng.standard_normal(p.nEl)))
     prec = fsils.PREC_FP64 if precision == "fp64" else fsils.PREC_MIXED
@@ -273,7 +275,8 @@ def test_cep_activation_adjoint_matches_fd(gsls, orc, precision, ode):
         fd = (J(_cep_T_gpu(p, ep + FD_H * dp)) - J(_cep_T_gpu(p, ep - FD_H * dp))) / (2 * FD_H)
         ad = float(grad @ dp)
         errs.append(abs(fd - ad) / abs(ad))
-        print(f"CEP adjoint ({precision}, ode {ode}) direction {k}: fd {fd:.12e} adjoint {ad:.12e} "
+        print(f"CEP adjoint ({precision}, ode {ode}, nFn {nFn}) direction {k}: fd {fd:.12e} "
+              f"adjoint {ad:.12e} "
               f"rel {errs[-1]:.2e}")
         if k == 0 and precision == "fp64":
             # and against finite differences of the oracle's own steps

@@ -60,6 +60,25 @@ def test_cep_fibre_assembly_fp64(gsls, orc, nFn):
     lhs.free()
 
 
+def test_cep_fibre_assembly_with_element_diffusivity(gsls, orc):
+    """Fibres with a per-element Diso (the parameter of the CEP adjoint):
+    D_e = Diso_e I + sum_i Dani_i f_i f_i^T, FP64 1e-12."""
+    p = problems.cep_slab(8, 8, 3, nsteps=1, nFn=2)
+    ep = np.exp(0.3 * np.random.default_rng(4).standard_normal(p.nEl)) * 0.1
+    A, Y = _state(p, 5)
+    R0, V0 = orc.assemble(p, A, Y, eparam=ep)
+    lhs = _lhs(p)
+    mesh = fsils.Mesh(lhs, p.ien, p.x)
+    prm = p.eq_params()
+    epc = np.ascontiguousarray(ep)
+    prm.eparam = epc.ctypes.data_as(C.POINTER(C.c_double))
+    R, Val = mesh.assemble(prm, A, Y, np.zeros_like(Y), p.dof)
+    assert rel(R, R0) < 1e-12
+    assert rel(Val, V0) < 1e-12
+    mesh.free()
+    lhs.free()
+
+
 def test_cep_fibre_assembly_fp32_tangent(gsls, orc):
     torch = pytest.importorskip("torch")
     p = problems.cep_slab(8, 8, 3, nsteps=1, nFn=2)
@@ -96,7 +115,7 @@ def test_cep_fibres_on_the_element_loop(gsls):
                         "-k", "fibre_assembly or fibre_steps", str(Path(__file__).resolve())],
                        cwd=root, env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
-    assert "5 passed" in r.stdout, r.stdout[-500:]
+    assert "6 passed" in r.stdout, r.stdout[-500:]
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
