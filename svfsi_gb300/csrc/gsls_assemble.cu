@@ -300,16 +300,17 @@ __global__ void __launch_bounds__(kAsmThreads) k_lin_build(AsmArgs A, double *Mg
   }
 }
 
-// 4 lanes per CSR row (tet4 rows hold ~15 entries), entries strided by 4,
-// the row sums by a fixed two-step shuffle tree: deterministic.  GB300 runs
-// FP64 at ~1/74 of the FP32 rate, so a pass over the operators is FP64-bound
+// 2 lanes per CSR row (tet4 rows hold ~15 entries), entries strided by 2,
+// the row sums by one fixed shuffle step: deterministic.  GB300 runs FP64
+// at ~1/74 of the FP32 rate, so a pass over the operators is FP64-bound
 // before it is HBM-bound: the residual takes two FP64 FMAs per entry
-// (rM = sum m Ag, rK = sum k Yg; R = rho rM + nu rK - rs b), the lane sums
-// 2 x 2 FP64 adds per lane (16 lanes per row spent 8x that in the tree and
+// (rM = sum m Ag, rK = sum k Yg; R = rho rM + nu rK - rs b) and the lane
+// sums 2 FP64 adds per lane (4 lanes spent 4 per lane, 30 % more FP64 work
+// per row, and took 63.8 against 53.0 us per pass on the CEP slab; 16 lanes
 // ran 4x slower), and the FP32 tangent is formed from FP32 copies of the
 // operators (Val = cM m + cK k in VT; the FP64 tangent from the FP64
 // operators).
-constexpr int kLinLanes = 4;
+constexpr int kLinLanes = 2;
 template <class VT, bool kVal = true>
 __global__ void __launch_bounds__(256) k_asm_lin(int nNo, const int *__restrict__ rowPtr,
                                                  const int *__restrict__ colPtr,
