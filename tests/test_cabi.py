@@ -99,3 +99,58 @@ def test_ctypes_mirrors_match_the_header_layout(tmp_path):
     assert len(got) == len(expect)
     for (py, f, off), g in zip(expect, got):
         assert off == int(g), (py, f, off, g)
+
+
+def _fortran_bind_c_types(path):
+    """(name -> [(field, kind, count)]) of the BIND(C) derived types of a
+    free-form Fortran source: kind C_INT / C_DOUBLE / C_PTR or the name of a
+    nested type, count the array extent (1 for scalars)."""
+    import re
+    types, cur = {}, None
+    for raw in Path(path).read_text().splitlines():
+        line = raw.split("!")[0].strip()
+        m = re.match(r"TYPE\s*,\s*BIND\(C\)\s*::\s*(\w+)", line, re.I)
+        if m:
+            cur = types.setdefault(m.group(1).lower(), [])
+            continue
+        if cur is not None and re.match(r"END\s*TYPE", line, re.I):
+            cur = None
+            continue
+        if cur is None or "::" not in line:
+            continue
+        decl, names = line.split("::", 1)
+        m = re.match(r"(INTEGER|REAL)\s*\(\s*(C_\w+)\s*\)|TYPE\s*\(\s*(\w+)\s*\)", decl.strip(), re.I)
+        assert m, raw
+        kind = (m.group(2) or m.group(3)).upper()
+        for item in re.sub(r"=\s*[^,]+", "", names).split(","):
+            item = item.strip()
+            a = re.match(r"(\w+)\s*(?:\((\d+)\))?", item)
+            cur.append((a.group(1).lower(), kind, int(a.group(2) or 1)))
+    return types
+
+
+def test_fortran_interop_types_mirror_the_header():
+    """The Fortran module's BIND(C) types (svfsi_gb300/fortran/gsls_c.f90)
+    declare the header's structs field for field: same order, same
+    interoperable kinds and array extents as the ctypes mirror, whose
+    offsets the probe above pins to include/gsls.h.  (No Fortran compiler
+    here: this reads the declarations.)"""
+    from svfsi_gb300 import _lib
+    ft = _fortran_bind_c_types(ROOT / "svfsi_gb300" / "fortran" / "gsls_c.f90")
+    pairs = {"gsls_sub_ls": _lib.SubLs, "gsls_ls": _lib.Ls, "gsls_eq_params": _lib.EqParams}
+    names = {_lib.SubLs: "GSLS_SUB_LS"}
+    for fname, cls in pairs.items():
+        assert fname in ft, fname
+        want = []
+        for f, t in cls._fields_:
+            if t is C.c_int:
+                want.append((f.lower(), "C_INT", 1))
+            elif t is C.c_double:
+                want.append((f.lower(), "C_DOUBLE", 1))
+            elif isinstance(t, type) and issubclass(t, C.Array) and t._type_ is C.c_double:
+                want.append((f.lower(), "C_DOUBLE", t._length_))
+            elif isinstance(t, type) and issubclass(t, C._Pointer):
+                want.append((f.lower(), "C_PTR", 1))
+            else:
+                want.append((f.lower(), names[t], 1))
+        assert ft[fname] == want, (fname, ft[fname], want)
