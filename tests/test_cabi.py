@@ -154,3 +154,16 @@ def test_fortran_interop_types_mirror_the_header():
             else:
                 want.append((f.lower(), names[t], 1))
         assert ft[fname] == want, (fname, ft[fname], want)
+
+
+def test_fortran_bindings_name_exported_symbols(libpath):
+    """Every C entry point the Fortran module binds (BIND(C, NAME=...)) is
+    declared in include/gsls.h and exported by the library."""
+    import re
+    src = (ROOT / "svfsi_gb300" / "fortran" / "gsls_c.f90").read_text()
+    bound = sorted(set(re.findall(r'BIND\(C,\s*NAME="(\w+)"\)', src)))
+    assert "gsls_solve" in bound and "gsls_assemble" in bound
+    declared = set(declared_functions())
+    lib = C.CDLL(str(libpath))
+    assert [n for n in bound if n not in declared] == []
+    assert [n for n in bound if not hasattr(lib, n)] == []
