@@ -404,7 +404,10 @@ int gsls_l2_read_rate(double *bytes_per_s);
    mu/2, HEATS conductivity), through every implicit step: transpose solve
    on the assembled tangent, element kernel for dR/dp, checkpoint every
    `every` steps and recompute of each segment on the way back.  New
-   capability (the reference has no adjoint); FP64 throughout. */
+   capability (the reference has no adjoint).  An FP64 equation runs FP64
+   throughout; a GSLS_PREC_MIXED equation takes its forward and recomputed
+   steps on the mixed path and refines each transpose solve (FP32 solves of
+   the normalised FP64 residual) to the FP64 tolerance. */
 typedef struct gsls_tape gsls_tape;
 /* Take nsteps steps of eq (as gsls_eq_step), storing checkpoints. */
 int gsls_adjoint_forward(gsls_eq *eq, int nsteps, int every, gsls_tape **tape);
@@ -414,8 +417,9 @@ int gsls_adjoint_backward(gsls_tape *tape, const double *Abar, const double *Yba
                           const double *Dbar, double *grad);
 int gsls_tape_free(gsls_tape *tape);
 
-/* Activation-time adjoint of a CEP equation (monodomain, forward-Euler
-   cell step; config: per-element diffusivity by gsls_eq_set_eparam).  The
+/* Activation-time adjoint of a CEP equation (monodomain, forward-Euler or
+   RK4 cell step, isotropic or with fibres; per-element isotropic
+   diffusivity by gsls_eq_set_eparam).  The
    smoothed activation time of node a over the nsteps steps is
      T_a = sum_n dt (1 - s(V_n(a))),  s(V) = 1 / (1 + exp(-(V - vth) / vw))
    (vw > 0; T_a tends to the first crossing of vth as vw -> 0 for a node
@@ -425,7 +429,8 @@ int gsls_tape_free(gsls_tape *tape);
    takes dJ/dT (host, nNo) and writes dJ/dDiso_e (host, nEl, original
    element order): each reverse step adds dJ/dV_n, reverses the diffusion
    solve (transpose solve + dR/dDiso) and the cell step's substeps.  eq is
-   left at step N.  New capability (the reference has no adjoint); FP64. */
+   left at step N.  New capability (the reference has no adjoint); the
+   precision follows the equation's, as for gsls_adjoint_forward. */
 int gsls_cep_adjoint_forward(gsls_eq *eq, int nsteps, int every, double vth, double vw,
                              double *T, gsls_tape **tape);
 int gsls_cep_adjoint_backward(gsls_tape *tape, const double *Tbar, double *grad);
