@@ -730,6 +730,41 @@ def test_cep_fibre_diffusion_kat(orc, nFn):
     assert np.abs(K).max() > 1e-2
 
 
+def test_precond_diag_kat(orc):
+    """PRECONDDIAG (L/PRECOND.f:50-145) against numpy on a 3-dof block CSR:
+    W = 1/sqrt|diag| per node and component, W = 1 where the diagonal is
+    zero, then Val <- W Val W blockwise and R <- W R.  (The Dirichlet mask
+    multiplies W only for the faces FSILS_SOLVE flags as included,
+    SOLVE.f:70-84; it is compared through the solves.)"""
+    p = problems.struct_beam(4, 2, 2, nsteps=1)
+    rng = np.random.default_rng(21)
+    d = 3
+    Val = rng.standard_normal((p.nnz, d * d))
+    rows = np.repeat(np.arange(p.nNo), np.diff(p.rowPtr))
+    diag = np.nonzero(p.colPtr == rows)[0]
+    for j in diag:
+        Val[j, [0, 4, 8]] = rng.uniform(0.5, 3.0, 3) * rng.choice([-1.0, 1.0], 3)
+    Val[diag[5], 4] = 0.0  # a zero diagonal entry: W = 1 there
+    R = rng.standard_normal((p.nNo, d))
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
+    L = orc.load()
+    L.orc_precond_diag.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    Vo, Ro, W = Val.copy(), R.copy(), np.zeros((p.nNo, d))
+    L.orc_precond_diag(C.c_void_p(s.h), d, orc.dp(Vo), orc.dp(Ro), orc.dp(W))
+    dg = Val[diag].reshape(p.nNo, d, d)[:, [0, 1, 2], [0, 1, 2]]
+    We = 1.0 / np.sqrt(np.abs(np.where(dg == 0.0, 1.0, dg)))
+    assert W[5, 1] == 1.0
+    assert np.allclose(W, We, rtol=1e-15, atol=0)
+    Ve = (We[rows][:, :, None] * Val.reshape(-1, d, d) * We[p.colPtr][:, None, :]).reshape(-1, d * d)
+    assert np.allclose(Vo, Ve, rtol=1e-14, atol=1e-300)
+    assert np.allclose(Ro, We * R, rtol=1e-15, atol=1e-300)
+    # the scaled diagonal is +-1 wherever the original was nonzero
+    sd = Vo[diag].reshape(p.nNo, d, d)[:, [0, 1, 2], [0, 1, 2]]
+    nz = dg != 0.0
+    assert np.allclose(np.abs(sd[nz]), 1.0, rtol=1e-14)
+
+
 def test_slab_fibre_field():
     """The synthetic fibre field: unit directions, family 1 at -60 degrees
     at the bottom of the slab and +60 at the top (in the x-y plane), family
