@@ -765,6 +765,48 @@ def test_precond_diag_kat(orc):
     assert np.allclose(np.abs(sd[nz]), 1.0, rtol=1e-14)
 
 
+def test_precond_rcs_kat(orc):
+    """PRECONDRCS (L/PRECOND.f:150-368, no Dirichlet face flagged) against a
+    dense numpy restatement: passes of row and column scaling by
+    1/sqrt(max |a|) over every scalar row and column, the stop test
+    max|1 - max| < 2 over rows and columns taken before each pass's scaling,
+    at most 10 passes; W1, W2, Val <- W1 Val W2 and R <- W1 R."""
+    p = problems.struct_beam(4, 2, 2, nsteps=1)
+    rng = np.random.default_rng(22)
+    d = 3
+    Val = rng.standard_normal((p.nnz, d * d)) * np.exp(3.0 * rng.standard_normal((p.nnz, 1)))
+    R = rng.standard_normal((p.nNo, d))
+    rows = np.repeat(np.arange(p.nNo), np.diff(p.rowPtr))
+    n = p.nNo * d
+    Ad = np.zeros((n, n))
+    for j in range(p.nnz):
+        Ad[rows[j] * d:(rows[j] + 1) * d, p.colPtr[j] * d:(p.colPtr[j] + 1) * d] = Val[j].reshape(d, d)
+    pattern = Ad != 0.0
+    W1, W2 = np.ones(n), np.ones(n)
+    for it in range(1, 11):
+        wr, wc = np.abs(Ad).max(axis=1), np.abs(Ad).max(axis=0)
+        stop = it >= 10 or (np.abs(1 - wr).max() < 2.0 and np.abs(1 - wc).max() < 2.0)
+        wr, wc = 1 / np.sqrt(wr), 1 / np.sqrt(wc)
+        Ad = wr[:, None] * Ad * wc[None, :]
+        W1 *= wr
+        W2 *= wc
+        if stop:
+            break
+    s = orc.OracleSolver(p.nNo, p.rowPtr, p.colPtr, 1)
+    L = orc.load()
+    L.orc_precond_rcs.argtypes = [C.c_void_p, C.c_int] + [C.POINTER(C.c_double)] * 4
+    Vo, Ro = Val.copy(), R.copy()
+    w1, w2 = np.zeros((p.nNo, d)), np.zeros((p.nNo, d))
+    L.orc_precond_rcs(C.c_void_p(s.h), d, orc.dp(Vo), orc.dp(Ro), orc.dp(w1), orc.dp(w2))
+    assert it > 1  # the matrix needed more than one pass
+    assert np.allclose(w1.ravel(), W1, rtol=1e-13) and np.allclose(w2.ravel(), W2, rtol=1e-13)
+    got = np.zeros((n, n))
+    for j in range(p.nnz):
+        got[rows[j] * d:(rows[j] + 1) * d, p.colPtr[j] * d:(p.colPtr[j] + 1) * d] = Vo[j].reshape(d, d)
+    assert np.allclose(got[pattern], Ad[pattern], rtol=1e-12)
+    assert np.allclose(Ro.ravel(), W1 * R.ravel(), rtol=1e-13)
+
+
 def test_slab_fibre_field():
     """The synthetic fibre field: unit directions, family 1 at -60 degrees
     at the bottom of the slab and +60 at the top (in the x-y plane), family
