@@ -807,6 +807,24 @@ def test_precond_rcs_kat(orc):
     assert np.allclose(Ro.ravel(), W1 * R.ravel(), rtol=1e-13)
 
 
+def test_isotropic_cep_is_heats(orc):
+    """Without fibres CEP3D (F/CEP.f:136-266) is HEATS3D (F/HEATS.f:116-159)
+    with unit density, no source and conductivity Diso: the oracle's two
+    assemblies agree on a slab (and so CEP inherits the P1 and patch-test
+    pinning of HEATS)."""
+    import dataclasses
+    pc = problems.cep_slab(5, 4, 2, nsteps=1, Diso=0.37)
+    ph = problems.heats_cube(2, nsteps=1)
+    ph = dataclasses.replace(ph, x=pc.x, ien=pc.ien, rowPtr=pc.rowPtr, colPtr=pc.colPtr,
+                             params=dict(pc.params, rho=1.0, cond=0.37, src=0.0))
+    rng = np.random.default_rng(23)
+    A, Y = rng.standard_normal((pc.nNo, 1)), rng.standard_normal((pc.nNo, 1))
+    Rc, Vc = orc.assemble(pc, A, Y)
+    Rh, Vh = orc.assemble(ph, A, Y)
+    assert np.allclose(Rc, Rh, rtol=1e-13, atol=1e-13 * np.abs(Rh).max())
+    assert np.allclose(Vc, Vh, rtol=1e-13, atol=1e-13 * np.abs(Vh).max())
+
+
 def test_slab_fibre_field():
     """The synthetic fibre field: unit directions, family 1 at -60 degrees
     at the bottom of the slab and +60 at the top (in the x-y plane), family
