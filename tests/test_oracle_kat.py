@@ -825,6 +825,29 @@ def test_isotropic_cep_is_heats(orc):
     assert np.allclose(Vc, Vh, rtol=1e-13, atol=1e-13 * np.abs(Vh).max())
 
 
+def test_parabolic_inflow_profile():
+    """BCINI's parabolic profile (F/BAFINI.f:362-403) on the cylinder's
+    circular inlet: zero on the perimeter, 1 - r^2/R^2 inside (the centre is
+    the area-weighted centroid, 0 here by symmetry, and each node is scaled
+    by the perimeter node along its direction: exact for nodes on a ray
+    through a perimeter node, within the perimeter's angular spacing
+    otherwise)."""
+    R, h = 0.5, 0.1
+    x, ien, info = meshgen.cylinder(R, 5.0, h)
+    inlet, wall = info["inlet"], info["wall"]
+    perim = np.intersect1d(inlet, wall)
+    gx = meshgen.parabolic_profile(x, info["inlet_faces"], inlet, perim)
+    r2 = (x[inlet, 0] ** 2 + x[inlet, 1] ** 2) / R ** 2
+    on_rim = np.isin(inlet, perim)
+    assert np.allclose(gx[on_rim], 0.0, atol=1e-12)
+    assert np.all(gx >= -1e-12) and np.all(gx <= 1.0 + 1e-12)
+    # the perimeter polygon's vertices are spaced ~h apart on the circle:
+    # the scaling radius is R cos(dphi/2) at worst
+    dphi = 2.0 * np.pi / perim.size
+    assert np.max(np.abs(gx - (1.0 - r2))) <= 1.0 - np.cos(dphi) + 1e-12
+    assert gx.max() > 0.95
+
+
 def test_slab_fibre_field():
     """The synthetic fibre field: unit directions, family 1 at -60 degrees
     at the bottom of the slab and +60 at the top (in the x-y plane), family
